@@ -1,0 +1,686 @@
+// K1: one persistent launch that integrates every element of every type and
+// scatters K, M (structure), K_f / rho, M_f / rho (fluid) and the coupling
+// (-ori)(C + C^T) into w-independent CSR value arrays.
+//
+// The reference integrates K - w^2 M per element at every frequency
+// (analysis/frequency/analysisfrequencybasic.cpp:281-304). Every term of
+// A(w) is a fixed w-dependent multiple of one of these arrays, so the
+// integration runs once per model and the per-w work becomes an HBM-bound
+// combine (numeric.cu).
+//
+// Element arithmetic follows (paths inside elpasoCore/source/):
+//  Brick8  element/structure/linear/brick/elementstructurebrick.cpp:281-554
+//          (B(6x24) with engineering shear rows xy, yz, xz; C from
+//          material/.../materialstructureisotrop.cpp:130-148), written in the
+//          closed form K_ab = lam P + mu P^T + mu tr(P) I,
+//          P = sum_gp wdJ grad N_a grad N_b^T (same quantity, fewer flops);
+//  DSG4    element/structure/linear/plate/elementstructuremindlindsg4.cpp:37-211
+//          (bending Bb, DSG shear Bs, tau = 1/(1 + 0.12 hk^2 / t^2) with hk
+//          the longest of edges 0-1, 1-2, 2-3 -- edge 3-0 is not measured),
+//          mass elementstructuremindlin.cpp:299-366;
+//  Fluid8  element/fluid/elementfluid3d.cpp:54-167 (M carries 1/c^2),
+//          divided by rho as in element/fluid/elementfluid.cpp:58-77;
+//  InterfaceMindlin element/interface/elementinterfacemindlin.cpp:80-181,
+//          scaled by -ori into C and C^T (elementinterfacestructural.cpp:209-237).
+// Shape tables and the 15-digit Gauss constants follow shape/shapefunctions.cpp,
+// shape/shapehex8.cpp:49-90, shape/shapequad4.cpp:48-73, misc/gausspoints.h:27-43;
+// 3D Gauss points are numbered x fastest, 2D points y fastest
+// (misc/gausspoints.cpp:76-87, 165-195).
+#include <cstdio>
+#include <cstring>
+
+#include "device.cuh"
+
+namespace elp {
+
+// ---------------------------------------------------------------- tables
+__constant__ double c_hex[4][8][8];    // [fun, xi, eta, zeta][node][gp]
+__constant__ double c_quad[3][4][4];   // [fun, xi, eta][node][gp]
+__constant__ unsigned char c_pair_a[36], c_pair_b[36];
+
+static const double kGp2 = 0.577350269189626;  // misc/gausspoints.h gp4[1]
+
+static double lagrange_hex8(int k, int deriv, const double g[3]) {
+  static const int sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+  static const int sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+  static const int sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+  double fx = 1. + sx[k] * g[0], fy = 1. + sy[k] * g[1], fz = 1. + sz[k] * g[2];
+  switch (deriv) {
+    case 0: return fx * fy * fz * 0.125;
+    case 1: return sx[k] * fy * fz * 0.125;
+    case 2: return sy[k] * fx * fz * 0.125;
+    default: return sz[k] * fx * fy * 0.125;
+  }
+}
+static double lagrange_quad4(int k, int deriv, const double g[2]) {
+  static const int sx[4] = {-1, 1, 1, -1};
+  static const int sy[4] = {-1, -1, 1, 1};
+  double fx = 1. + sx[k] * g[0], fy = 1. + sy[k] * g[1];
+  switch (deriv) {
+    case 0: return 0.25 * fx * fy;
+    case 1: return 0.25 * sx[k] * fy;
+    default: return 0.25 * sy[k] * fx;
+  }
+}
+
+void shape_tables(double hex[4][8][8], double quad[3][4][4]) {
+  const double pts[2] = {kGp2, -kGp2};
+  for (int n = 0; n < 8; ++n) {
+    // gausspoints.cpp:76-87: x fastest
+    int x = n % 2, y = (n / 2) % 2, z = n / 4;
+    double g[3] = {pts[x], pts[y], pts[z]};
+    for (int k = 0; k < 8; ++k)
+      for (int dv = 0; dv < 4; ++dv) hex[dv][k][n] = lagrange_hex8(k, dv, g);
+  }
+  for (int n = 0; n < 4; ++n) {
+    // gausspoints.cpp:165-195: y fastest
+    int y = n % 2, x = n / 2;
+    double g[2] = {pts[x], pts[y]};
+    for (int k = 0; k < 4; ++k)
+      for (int dv = 0; dv < 3; ++dv) quad[dv][k][n] = lagrange_quad4(k, dv, g);
+  }
+}
+
+// ---------------------------------------------------------------- helpers
+// CSR index of (row, col); the pattern guarantees presence.
+__device__ __forceinline__ int find_col(const int32_t* __restrict__ row_ptr,
+                                        const int32_t* __restrict__ col_idx, int row, int col) {
+  int lo = row_ptr[row], hi = row_ptr[row + 1];
+  while (hi - lo > 8) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(col_idx + mid) <= col) lo = mid; else hi = mid;
+  }
+  for (int p = lo; p < hi; ++p)
+    if (__ldg(col_idx + p) == col) return p;
+  return -1;
+}
+
+__device__ __forceinline__ void add_at(double* v, int p, double x) {
+  if (p >= 0 && x != 0.0) atomicAdd(v + p, x);
+}
+
+struct AsmArgs {
+  const double* coords;
+  const int32_t *row_ptr, *col_idx;
+  double *VK, *VM, *VKg;
+  int64_t nnz;
+  const int32_t *brick_conn, *plate_conn, *fluid_conn;
+  const int16_t *brick_mat, *plate_mat, *fluid_mat;
+  const int32_t *nr_brick, *nr_plate, *nr_fluid;
+  const ElemMaterial* mats;
+  const int32_t* iface_rows;
+  const double* iface_scale;
+  const int32_t* iface_geom;
+  int64_t n_brick, n_plate, n_fluid, n_iface;
+  int64_t items_brick, items_fluid, items_plate, items_iface;
+  int* flags;
+};
+
+constexpr int kThreads = 288;   // 8 hexes x 36 node pairs
+constexpr int kHexPerItem = 8;
+
+// 3D Jacobian, determinant and inverse exactly as elementfem.cpp:158-210.
+__device__ __forceinline__ double jac3(const double* x, int gp, double inv[3][3]) {
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      double d = c_hex[i + 1][k][gp];
+      J[i][0] += d * x[3 * k + 0];
+      J[i][1] += d * x[3 * k + 1];
+      J[i][2] += d * x[3 * k + 2];
+    }
+  }
+  double det = J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] +
+               J[0][2] * J[1][0] * J[2][1] - J[0][2] * J[1][1] * J[2][0] -
+               J[0][0] * J[1][2] * J[2][1] - J[0][1] * J[1][0] * J[2][2];
+  inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+  inv[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) / det;
+  inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+  inv[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) / det;
+  inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+  inv[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) / det;
+  inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+  inv[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) / det;
+  inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+  return det;
+}
+
+// ---------------------------------------------------------------- hex items
+// kind 0 = Brick8, 1 = Fluid8
+template <int kKind>
+__device__ void hex_item(const AsmArgs& A, int64_t item, double (*sg)[8][8][3], double (*sw)[8],
+                         int (*srow)[8], int* smat) {
+  const int t = threadIdx.x;
+  const int64_t e0 = item * kHexPerItem;
+  const int64_t ne = kKind == 0 ? A.n_brick : A.n_fluid;
+  const int32_t* conn = kKind == 0 ? A.brick_conn : A.fluid_conn;
+  if (t < 64) {
+    int el = t >> 3, gp = t & 7;
+    int64_t e = e0 + el;
+    if (e < ne) {
+      double x[24];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        int v = __ldg(conn + e * 8 + k);
+        x[3 * k + 0] = __ldg(A.coords + 3 * (int64_t)v + 0);
+        x[3 * k + 1] = __ldg(A.coords + 3 * (int64_t)v + 1);
+        x[3 * k + 2] = __ldg(A.coords + 3 * (int64_t)v + 2);
+      }
+      double inv[3][3];
+      double det = jac3(x, gp, inv);
+      if (det <= 0.0) atomicAdd(A.flags + 0, 1);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        double a = c_hex[1][k][gp], b = c_hex[2][k][gp], c = c_hex[3][k][gp];
+        sg[el][gp][k][0] = inv[0][0] * a + inv[0][1] * b + inv[0][2] * c;
+        sg[el][gp][k][1] = inv[1][0] * a + inv[1][1] * b + inv[1][2] * c;
+        sg[el][gp][k][2] = inv[2][0] * a + inv[2][1] * b + inv[2][2] * c;
+      }
+      sw[el][gp] = 1.0 * det;  // level-2 weights are 1 x 1 x 1
+    }
+  } else if (t < 128) {
+    int el = (t - 64) >> 3, k = (t - 64) & 7;
+    int64_t e = e0 + el;
+    if (e < ne) {
+      int v = __ldg(conn + e * 8 + k);
+      srow[el][k] = kKind == 0 ? __ldg(A.nr_brick + v) : __ldg(A.nr_fluid + v);
+      if (k == 0) smat[el] = kKind == 0 ? A.brick_mat[e] : A.fluid_mat[e];
+    }
+  }
+  __syncthreads();
+  if (t < kHexPerItem * 36) {
+    int el = t / 36, pr = t % 36;
+    int64_t e = e0 + el;
+    if (e < ne) {
+      const int a = c_pair_a[pr], b = c_pair_b[pr];
+      const ElemMaterial& mt = A.mats[smat[el]];
+      const int ra = srow[el][a], rb = srow[el][b];
+      if (kKind == 0) {
+        double P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        double mm = 0.0;
+#pragma unroll
+        for (int gp = 0; gp < 8; ++gp) {
+          double w = sw[el][gp];
+          double wa0 = w * sg[el][gp][a][0], wa1 = w * sg[el][gp][a][1], wa2 = w * sg[el][gp][a][2];
+          double gb0 = sg[el][gp][b][0], gb1 = sg[el][gp][b][1], gb2 = sg[el][gp][b][2];
+          P[0][0] += wa0 * gb0; P[0][1] += wa0 * gb1; P[0][2] += wa0 * gb2;
+          P[1][0] += wa1 * gb0; P[1][1] += wa1 * gb1; P[1][2] += wa1 * gb2;
+          P[2][0] += wa2 * gb0; P[2][1] += wa2 * gb1; P[2][2] += wa2 * gb2;
+          mm += w * c_hex[0][a][gp] * c_hex[0][b][gp];
+        }
+        const double tr = P[0][0] + P[1][1] + P[2][2];
+        double Kb[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) Kb[i][j] = mt.lam * P[i][j] + mt.mu * P[j][i] + (i == j ? mt.mu * tr : 0.0);
+        const double mv = mt.rho * mm;
+        double* VKt = mt.group == 0 ? A.VK : A.VKg + (int64_t)(mt.group - 1) * A.nnz;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          int p = find_col(A.row_ptr, A.col_idx, ra + i, rb);
+#pragma unroll
+          for (int j = 0; j < 3; ++j) add_at(VKt, p + j, Kb[i][j]);
+          add_at(A.VM, p + i, mv);
+        }
+        if (a != b) {
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            int p = find_col(A.row_ptr, A.col_idx, rb + j, ra);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) add_at(VKt, p + i, Kb[i][j]);
+            add_at(A.VM, p + j, mv);
+          }
+        }
+      } else {
+        double kk = 0.0, mm = 0.0;
+#pragma unroll
+        for (int gp = 0; gp < 8; ++gp) {
+          double w = sw[el][gp];
+          kk += w * (sg[el][gp][a][0] * sg[el][gp][b][0] + sg[el][gp][a][1] * sg[el][gp][b][1] +
+                     sg[el][gp][a][2] * sg[el][gp][b][2]);
+          mm += mt.inv_c2 * c_hex[0][a][gp] * c_hex[0][b][gp] * w;
+        }
+        const double ir = 1.0 / mt.rho;
+        int p = find_col(A.row_ptr, A.col_idx, ra, rb);
+        add_at(A.VK, p, kk * ir);
+        add_at(A.VM, p, mm * ir);
+        if (a != b) {
+          p = find_col(A.row_ptr, A.col_idx, rb, ra);
+          add_at(A.VK, p, kk * ir);
+          add_at(A.VM, p, mm * ir);
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- DSG4 plate
+__device__ void plate_element(const AsmArgs& A, int64_t e) {
+  double x[4], y[4], z[4];
+  int rows[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    int v = __ldg(A.plate_conn + e * 4 + k);
+    x[k] = A.coords[3 * (int64_t)v + 0];
+    y[k] = A.coords[3 * (int64_t)v + 1];
+    z[k] = A.coords[3 * (int64_t)v + 2];
+    rows[k] = A.nr_plate[v];
+  }
+  const ElemMaterial& mt = A.mats[A.plate_mat[e]];
+  const double thick = mt.t;
+  // Lyly-Stenberg: hk = max edge over the pairs (1,0), (2,1), (3,2)
+  double hk = 0.0;
+  const int seq[5] = {0, 1, 2, 3, 0};
+#pragma unroll
+  for (int i = 1; i < 4; ++i) {
+    int p = seq[i], q = seq[i - 1];
+    double dx = x[p] - x[q], dy = y[p] - y[q], dz = z[p] - z[q];
+    double dd = sqrt(dx * dx + dy * dy + dz * dz);
+    hk = hk > dd ? hk : dd;
+  }
+  const double tau = 1.0 / (1.0 + 0.12 * hk * hk / (thick * thick));
+  const double Bm = mt.Db;                 // E t^3 / (12 (1 - nu^2))
+  const double Cb00 = Bm, Cb01 = Bm * mt.nu, Cb22 = mt.Gt;  // Gt holds G t^3 / 12
+  const double Cs = mt.lam * tau;          // lam holds G t Ks for plates
+  const double m1 = mt.rho * thick, m2 = mt.rho * (thick * thick * thick / 12.0);
+  double K[78];
+  double M[16];
+#pragma unroll
+  for (int i = 0; i < 78; ++i) K[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) M[i] = 0.0;
+  for (int n = 0; n < 4; ++n) {
+    double J00 = 0, J01 = 0, J10 = 0, J11 = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      J00 += c_quad[1][k][n] * x[k];
+      J01 += c_quad[1][k][n] * y[k];
+      J10 += c_quad[2][k][n] * x[k];
+      J11 += c_quad[2][k][n] * y[k];
+    }
+    const double det = J00 * J11 - J01 * J10;
+    if (det <= 0.0) atomicAdd(A.flags + 1, 1);
+    const double a = J00, b = J01, d = J10, c = J11;
+    const double wdJ = 1.0 * det;
+    double Bb[3][12], Bs[2][12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) { Bb[0][i] = Bb[1][i] = Bb[2][i] = 0.0; }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      double dNdx = (c * c_quad[1][k][n] - b * c_quad[2][k][n]) / det;
+      double dNdy = (-d * c_quad[1][k][n] + a * c_quad[2][k][n]) / det;
+      Bb[0][k * 3 + 2] = dNdx;
+      Bb[1][k * 3 + 1] = -dNdy;
+      Bb[2][k * 3 + 2] = dNdy;
+      Bb[2][k * 3 + 1] = -dNdx;
+    }
+    const double Nx1 = c_quad[1][1][n], Nx2 = c_quad[1][2][n];
+    const double Ne2 = c_quad[2][2][n], Ne3 = c_quad[2][3][n];
+    Bs[0][0] = -c * Nx1 + b * Ne3;
+    Bs[0][1] = -b * c * Nx1 + b * c * Ne3;
+    Bs[0][2] = a * c * Nx1 - b * d * Ne3;
+    Bs[1][0] = d * Nx1 - a * Ne3;
+    Bs[1][1] = -a * c * Ne3 + b * d * Nx1;
+    Bs[1][2] = a * d * Ne3 - a * d * Nx1;
+    Bs[0][3] = c * Nx1 + b * Ne2;
+    Bs[0][4] = -b * c * Nx1 + b * c * Ne2;
+    Bs[0][5] = a * c * Nx1 - b * d * Ne2;
+    Bs[1][3] = -a * Ne2 - d * Nx1;
+    Bs[1][4] = -a * c * Ne2 + b * d * Nx1;
+    Bs[1][5] = a * d * Ne2 - a * d * Nx1;
+    Bs[0][6] = c * Nx2 - b * Ne2;
+    Bs[0][7] = -b * c * Nx2 + b * c * Ne2;
+    Bs[0][8] = a * c * Nx2 - b * d * Ne2;
+    Bs[1][6] = a * Ne2 - d * Nx2;
+    Bs[1][7] = -a * c * Ne2 + b * d * Nx2;
+    Bs[1][8] = a * d * Ne2 - a * d * Nx2;
+    Bs[0][9] = -c * Nx2 - b * Ne3;
+    Bs[0][10] = -b * c * Nx2 + b * c * Ne3;
+    Bs[0][11] = a * c * Nx2 - b * d * Ne3;
+    Bs[1][9] = a * Ne3 + d * Nx2;
+    Bs[1][10] = -a * c * Ne3 + b * d * Nx2;
+    Bs[1][11] = a * d * Ne3 - a * d * Nx2;
+    const double idet = 1. / det;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) { Bs[0][i] *= idet; Bs[1][i] *= idet; }
+    // K += Bb^T Cb Bb wdJ + Bs^T (tau Cs) Bs wdJ (upper triangle)
+    double CB[3][12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+      CB[0][j] = Cb00 * Bb[0][j] + Cb01 * Bb[1][j];
+      CB[1][j] = Cb01 * Bb[0][j] + Cb00 * Bb[1][j];
+      CB[2][j] = Cb22 * Bb[2][j];
+    }
+    int idx = 0;
+#pragma unroll
+    for (int i = 0; i < 12; ++i)
+#pragma unroll
+      for (int j = i; j < 12; ++j) {
+        double s = Bb[0][i] * CB[0][j] + Bb[1][i] * CB[1][j] + Bb[2][i] * CB[2][j];
+        s += Cs * (Bs[0][i] * Bs[0][j] + Bs[1][i] * Bs[1][j]);
+        K[idx++] += s * wdJ;
+      }
+#pragma unroll
+    for (int zz = 0; zz < 4; ++zz)
+#pragma unroll
+      for (int ss = 0; ss < 4; ++ss) M[zz * 4 + ss] += c_quad[0][zz][n] * c_quad[0][ss][n] * wdJ;
+  }
+  double* VKt = mt.group == 0 ? A.VK : A.VKg + (int64_t)(mt.group - 1) * A.nnz;
+  // scatter: row (node zz, dof i), col (node ss, dof j)
+  for (int zz = 0; zz < 4; ++zz)
+    for (int i = 0; i < 3; ++i) {
+      const int gi = zz * 3 + i;
+      const int r = rows[zz] + i;
+      for (int ss = 0; ss < 4; ++ss) {
+        int p = find_col(A.row_ptr, A.col_idx, r, rows[ss]);
+        for (int j = 0; j < 3; ++j) {
+          const int gj = ss * 3 + j;
+          const int lo = gi < gj ? gi : gj, hi = gi < gj ? gj : gi;
+          const int u = lo * 12 - (lo * (lo - 1)) / 2 + (hi - lo);
+          add_at(VKt, p + j, K[u]);
+        }
+        const double mv = M[zz * 4 + ss] * (i == 0 ? m1 : m2);
+        add_at(A.VM, p + i, mv);
+      }
+    }
+}
+
+// ---------------------------------------------------------------- interface
+__device__ void interface_quad(const AsmArgs& A, int64_t q) {
+  double x[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    int v = A.iface_geom[q * 4 + k];
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) x[k][dd] = A.coords[3 * (int64_t)v + dd];
+  }
+  double C[4][4];  // C(3z+2, s)
+#pragma unroll
+  for (int zz = 0; zz < 4; ++zz)
+#pragma unroll
+    for (int ss = 0; ss < 4; ++ss) C[zz][ss] = 0.0;
+  for (int n = 0; n < 4; ++n) {
+    double a1[3] = {0, 0, 0}, a2[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) {
+        a1[dd] += c_quad[1][k][n] * x[k][dd];
+        a2[dd] += c_quad[2][k][n] * x[k][dd];
+      }
+    double n1 = a1[0] * a1[0] + a1[1] * a1[1] + a1[2] * a1[2];
+    double n2 = a2[0] * a2[0] + a2[1] * a2[1] + a2[2] * a2[2];
+    double d12 = a1[0] * a2[0] + a1[1] * a2[1] + a1[2] * a2[2];
+    double det = sqrt(n1 * n2 - d12 * d12);
+#pragma unroll
+    for (int zz = 0; zz < 4; ++zz)
+#pragma unroll
+      for (int ss = 0; ss < 4; ++ss) C[zz][ss] += c_quad[0][zz][n] * c_quad[0][ss][n] * 1.0 * det;
+  }
+  const int32_t* rows = A.iface_rows + q * 16;  // 12 structure rows then 4 fluid rows
+  const double sc = A.iface_scale[q];
+  // shell transformation (elementinterfacemindlin.cpp:131-181) when the
+  // structure node carries x1: rows 3n, 3n+1 get normal components.
+  double Cf[12][4];
+  const bool transform = rows[0] >= 0;
+#pragma unroll
+  for (int zz = 0; zz < 4; ++zz)
+#pragma unroll
+    for (int ss = 0; ss < 4; ++ss) { Cf[3 * zz][ss] = 0.0; Cf[3 * zz + 1][ss] = 0.0; Cf[3 * zz + 2][ss] = C[zz][ss]; }
+  if (transform) {
+    const double xi[4] = {-1., 1., 1., -1.}, et[4] = {-1., -1., 1., 1.};
+    for (int nn = 0; nn < 4; ++nn) {
+      double g[2] = {xi[nn], et[nn]};
+      double a1[3] = {0, 0, 0}, a2[3] = {0, 0, 0};
+      const int sx[4] = {-1, 1, 1, -1}, sy[4] = {-1, -1, 1, 1};
+      for (int k = 0; k < 4; ++k) {
+        double nxi = 0.25 * sx[k] * (1. + sy[k] * g[1]);
+        double net = 0.25 * sy[k] * (1. + sx[k] * g[0]);
+        for (int dd = 0; dd < 3; ++dd) { a1[dd] += nxi * x[k][dd]; a2[dd] += net * x[k][dd]; }
+      }
+      double nv[3] = {a1[1] * a2[2] - a1[2] * a2[1], a1[2] * a2[0] - a1[0] * a2[2], a1[0] * a2[1] - a1[1] * a2[0]};
+      double nrm = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+      for (int dd = 0; dd < 3; ++dd) nv[dd] *= 1. / nrm;
+      for (int ss = 0; ss < 4; ++ss) {
+        double cz = Cf[3 * nn + 2][ss];
+        Cf[3 * nn][ss] = nv[0] * cz;
+        Cf[3 * nn + 1][ss] = nv[1] * cz;
+        Cf[3 * nn + 2][ss] = nv[2] * cz;
+      }
+    }
+  }
+  for (int zi = 0; zi < 12; ++zi) {
+    const int r = rows[zi];
+    if (r < 0) continue;
+    for (int ss = 0; ss < 4; ++ss) {
+      const int f = rows[12 + ss];
+      if (f < 0) continue;
+      const double v = sc * Cf[zi][ss];
+      add_at(A.VK, find_col(A.row_ptr, A.col_idx, r, f), v);
+      add_at(A.VK, find_col(A.row_ptr, A.col_idx, f, r), v);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- kernel
+__global__ void __launch_bounds__(kThreads) assemble_kernel(AsmArgs A) {
+  __shared__ double sg[kHexPerItem][8][8][3];
+  __shared__ double sw[kHexPerItem][8];
+  __shared__ int srow[kHexPerItem][8];
+  __shared__ int smat[kHexPerItem];
+  const int64_t total = A.items_brick + A.items_fluid + A.items_plate + A.items_iface;
+  for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
+    int64_t r = it;
+    if (r < A.items_brick) { hex_item<0>(A, r, sg, sw, srow, smat); continue; }
+    r -= A.items_brick;
+    if (r < A.items_fluid) { hex_item<1>(A, r, sg, sw, srow, smat); continue; }
+    r -= A.items_fluid;
+    if (r < A.items_plate) {
+      int64_t e = r * kThreads + threadIdx.x;
+      if (e < A.n_plate) plate_element(A, e);
+      continue;
+    }
+    r -= A.items_plate;
+    int64_t q = r * kThreads + threadIdx.x;
+    if (q < A.n_iface) interface_quad(A, q);
+  }
+}
+
+// ---------------------------------------------------------------- host
+static bool g_tables_done[64] = {false};
+
+static int upload_tables(int dev) {
+  if (dev < 0 || dev >= 64) return ELP_OK;
+  if (g_tables_done[dev]) return ELP_OK;
+  double hex[4][8][8], quad[3][4][4];
+  shape_tables(hex, quad);
+  unsigned char pa[36], pb[36];
+  int k = 0;
+  for (int a = 0; a < 8; ++a)
+    for (int b = a; b < 8; ++b) { pa[k] = (unsigned char)a; pb[k] = (unsigned char)b; ++k; }
+  ELP_CUDA(cudaMemcpyToSymbol(c_hex, hex, sizeof(hex)));
+  ELP_CUDA(cudaMemcpyToSymbol(c_quad, quad, sizeof(quad)));
+  ELP_CUDA(cudaMemcpyToSymbol(c_pair_a, pa, sizeof(pa)));
+  ELP_CUDA(cudaMemcpyToSymbol(c_pair_b, pb, sizeof(pb)));
+  g_tables_done[dev] = true;
+  return ELP_OK;
+}
+
+int device_upload_model(Model& m) {
+  if (!m.dev) m.dev.reset(new DeviceModel());
+  DeviceModel& D = *m.dev;
+  ELP_CUDA(cudaGetDevice(&D.device));
+  int rc = upload_tables(D.device);
+  if (rc) return rc;
+  ELP_CUDA(D.coords.upload(m.coords));
+  ELP_CUDA(D.row_ptr.upload(m.row_ptr));
+  ELP_CUDA(D.col_idx.upload(m.col_idx));
+  ELP_CUDA(D.diag_idx.upload(m.diag_idx));
+  ELP_CUDA(D.cls.upload(m.cls));
+  std::vector<double> rhs(2 * m.n);
+  for (int64_t i = 0; i < m.n; ++i) { rhs[2 * i] = m.rhs[i].real(); rhs[2 * i + 1] = m.rhs[i].imag(); }
+  ELP_CUDA(D.rhs.upload(rhs));
+  ELP_CUDA(D.bc_rows.upload(m.bc_rows));
+  // element lists per type
+  std::vector<int32_t> bc, pc, fc;
+  std::vector<int16_t> bm, pm, fm;
+  for (auto& blk : m.blocks) {
+    std::vector<int32_t>* c = blk.type == ELP_BRICK8 ? &bc : blk.type == ELP_DSG4 ? &pc : &fc;
+    std::vector<int16_t>* mm = blk.type == ELP_BRICK8 ? &bm : blk.type == ELP_DSG4 ? &pm : &fm;
+    c->insert(c->end(), blk.conn.begin(), blk.conn.end());
+    mm->insert(mm->end(), blk.n_elements, (int16_t)blk.material);
+  }
+  if (m.materials.size() > 32767) { set_error("too many materials"); return ELP_ERR_ARG; }
+  D.n_brick = (int64_t)bm.size();
+  D.n_plate = (int64_t)pm.size();
+  D.n_fluid = (int64_t)fm.size();
+  ELP_CUDA(D.brick_conn.upload(bc));
+  ELP_CUDA(D.plate_conn.upload(pc));
+  ELP_CUDA(D.fluid_conn.upload(fc));
+  ELP_CUDA(D.brick_mat.upload(bm));
+  ELP_CUDA(D.plate_mat.upload(pm));
+  ELP_CUDA(D.fluid_mat.upload(fm));
+  std::vector<int32_t> nb(m.n_nodes, -1), np(m.n_nodes, -1), nf(m.n_nodes, -1);
+  for (int64_t v = 0; v < m.n_nodes; ++v) {
+    const int32_t* g = &m.global_rows[(size_t)v * ELP_NUM_KNOWN_DOFS];
+    nb[v] = g[ELP_DOF_X1];
+    np[v] = g[ELP_DOF_X3];
+    nf[v] = g[ELP_DOF_FLUID];
+  }
+  ELP_CUDA(D.node_row_brick.upload(nb));
+  ELP_CUDA(D.node_row_plate.upload(np));
+  ELP_CUDA(D.node_row_fluid.upload(nf));
+  std::vector<ElemMaterial> em(m.materials.size());
+  for (size_t i = 0; i < m.materials.size(); ++i) {
+    const elp_material& mt = m.materials[i];
+    ElemMaterial& e = em[i];
+    memset(&e, 0, sizeof(e));
+    e.rho = mt.rho;
+    e.group = m.material_group[i] < 0 ? 0 : m.material_group[i];
+    if (mt.kind == ELP_AF_LIN_UAF_ISO_DIR) {
+      e.inv_c2 = 1.0 / (mt.c * mt.c);
+    } else {
+      // Lame constants of setupC with real E (the group coefficient carries eta)
+      double f = mt.E / (1.0 + mt.nu) / (1.0 - 2.0 * mt.nu);
+      e.mu = f * (1.0 - 2.0 * mt.nu) / 2.0;
+      double diag = f * (1. - mt.nu);
+      e.lam = diag - 2.0 * e.mu;
+      // plate constants (setupCb / setupCs): lam slot reused for G t Ks
+      bool plate_material = false;
+      for (auto& blk : m.blocks)
+        if (blk.material == (int)i && blk.type == ELP_DSG4) plate_material = true;
+      if (plate_material) {
+        double h = mt.t;
+        e.Db = mt.E * h * h * h / (12. * (1. - mt.nu * mt.nu));
+        double G = mt.E / (2. * (1. + mt.nu));
+        e.Gt = G * h * h * h / 12.;
+        e.lam = mt.E / (2. * (1. + mt.nu)) * h * (5. / 6.);
+        e.nu = mt.nu;
+        e.t = h;
+        for (auto& blk : m.blocks)
+          if (blk.material == (int)i && blk.type == ELP_BRICK8) {
+            set_error("a material used by both Brick8 and DSG4 blocks is not supported");
+            return ELP_ERR_ARG;
+          }
+      }
+    }
+  }
+  ELP_CUDA(D.materials.upload(em));
+  // interfaces
+  D.n_iface = (int64_t)m.interfaces.size();
+  std::vector<int32_t> ir(16 * D.n_iface), ig(4 * D.n_iface);
+  std::vector<double> isc(D.n_iface);
+  for (int64_t q = 0; q < D.n_iface; ++q) {
+    const elp_interface_quad& Q = m.interfaces[q];
+    for (int k = 0; k < 4; ++k) {
+      for (int d3 = 0; d3 < 3; ++d3)
+        ir[16 * q + 3 * k + d3] = m.global_rows[(size_t)Q.structure_nodes[k] * ELP_NUM_KNOWN_DOFS + d3];
+      ir[16 * q + 12 + k] = m.global_rows[(size_t)Q.fluid_nodes[k] * ELP_NUM_KNOWN_DOFS + ELP_DOF_FLUID];
+      ig[4 * q + k] = Q.fluid_nodes[k];
+    }
+    // transformC is applied when the first structure node has x1 active
+    if (m.global_rows[(size_t)Q.structure_nodes[0] * ELP_NUM_KNOWN_DOFS + ELP_DOF_X1] < 0)
+      for (int k = 0; k < 4; ++k) { ir[16 * q + 3 * k] = -1; ir[16 * q + 3 * k + 1] = -1; }
+    isc[q] = -1.0 * Q.ori;
+  }
+  ELP_CUDA(D.iface_rows.upload(ir));
+  ELP_CUDA(D.iface_geom.upload(ig));
+  ELP_CUDA(D.iface_scale.upload(isc));
+  ELP_CUDA(D.VK.alloc(m.nnz));
+  ELP_CUDA(D.VM.alloc(m.nnz));
+  if (m.groups.size() > 1) ELP_CUDA(D.VKg.alloc((m.groups.size() - 1) * (size_t)m.nnz));
+  ELP_CUDA(D.flags.alloc(4));
+  return ELP_OK;
+}
+
+int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms) {
+  DeviceModel& D = *m.dev;
+  ELP_CUDA(cudaMemsetAsync(D.VK.p, 0, sizeof(double) * m.nnz, stream));
+  ELP_CUDA(cudaMemsetAsync(D.VM.p, 0, sizeof(double) * m.nnz, stream));
+  if (D.VKg.p) ELP_CUDA(cudaMemsetAsync(D.VKg.p, 0, sizeof(double) * D.VKg.n, stream));
+  ELP_CUDA(cudaMemsetAsync(D.flags.p, 0, sizeof(int) * 4, stream));
+  AsmArgs A;
+  A.coords = D.coords.p;
+  A.row_ptr = D.row_ptr.p;
+  A.col_idx = D.col_idx.p;
+  A.VK = D.VK.p;
+  A.VM = D.VM.p;
+  A.VKg = D.VKg.p;
+  A.nnz = m.nnz;
+  A.brick_conn = D.brick_conn.p;
+  A.plate_conn = D.plate_conn.p;
+  A.fluid_conn = D.fluid_conn.p;
+  A.brick_mat = D.brick_mat.p;
+  A.plate_mat = D.plate_mat.p;
+  A.fluid_mat = D.fluid_mat.p;
+  A.nr_brick = D.node_row_brick.p;
+  A.nr_plate = D.node_row_plate.p;
+  A.nr_fluid = D.node_row_fluid.p;
+  A.mats = D.materials.p;
+  A.iface_rows = D.iface_rows.p;
+  A.iface_scale = D.iface_scale.p;
+  A.iface_geom = D.iface_geom.p;
+  A.n_brick = D.n_brick;
+  A.n_plate = D.n_plate;
+  A.n_fluid = D.n_fluid;
+  A.n_iface = D.n_iface;
+  A.items_brick = (D.n_brick + kHexPerItem - 1) / kHexPerItem;
+  A.items_fluid = (D.n_fluid + kHexPerItem - 1) / kHexPerItem;
+  A.items_plate = (D.n_plate + kThreads - 1) / kThreads;
+  A.items_iface = (D.n_iface + kThreads - 1) / kThreads;
+  A.flags = D.flags.p;
+  const int64_t total = A.items_brick + A.items_fluid + A.items_plate + A.items_iface;
+  int sms = 0, per_sm = 0;
+  ELP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D.device));
+  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, assemble_kernel, kThreads, 0));
+  if (per_sm < 1) per_sm = 1;
+  int64_t grid = (int64_t)sms * per_sm;
+  if (grid > total) grid = total;
+  cudaEvent_t e0, e1;
+  ELP_CUDA(cudaEventCreate(&e0));
+  ELP_CUDA(cudaEventCreate(&e1));
+  ELP_CUDA(cudaEventRecord(e0, stream));
+  if (grid > 0) assemble_kernel<<<(unsigned)grid, kThreads, 0, stream>>>(A);
+  ELP_CUDA(cudaGetLastError());
+  ELP_CUDA(cudaEventRecord(e1, stream));
+  ELP_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  ELP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (kernel_ms) *kernel_ms = ms;
+  D.assembly_ms = ms;
+  int flags[4];
+  ELP_CUDA(cudaMemcpy(flags, D.flags.p, sizeof(flags), cudaMemcpyDeviceToHost));
+  if (flags[1] > 0) {
+    set_error("detJac <= 0 in a DSG4 element: check orientation of the elements");
+    return ELP_ERR_GEOMETRY;
+  }
+  return ELP_OK;
+}
+
+}  // namespace elp

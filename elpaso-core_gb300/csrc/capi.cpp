@@ -1,0 +1,259 @@
+// extern "C" entry points of libelpaso_gb300.so (declared in
+// include/elpaso_gb300.h). Every call returns an int status and never
+// aborts; the text of the last error is per thread.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "device.cuh"
+#include "numeric.cuh"
+#include "symbolic.hpp"
+
+using namespace elp;
+
+struct elp_model {
+  Model m;
+};
+
+namespace elp {
+Model::Model() = default;
+Model::~Model() = default;
+}  // namespace elp
+
+#define GUARD_BEGIN try {
+#define GUARD_END                                   \
+  }                                                 \
+  catch (const std::bad_alloc&) {                   \
+    set_error("host allocation failed");            \
+    return ELP_ERR_NOMEM;                           \
+  }                                                 \
+  catch (const std::exception& ex) {                \
+    set_error(std::string("exception: ") + ex.what()); \
+    return ELP_ERR_ARG;                             \
+  }
+
+static int check_cuda_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device: this library has no CPU path");
+    return ELP_ERR_CUDA;
+  }
+  return ELP_OK;
+}
+
+extern "C" {
+
+const char* elp_last_error(void) { return get_error().c_str(); }
+
+int elp_model_create(const elp_model_desc* desc, elp_model** out) {
+  GUARD_BEGIN
+  if (!out) { set_error("null output handle"); return ELP_ERR_ARG; }
+  *out = nullptr;
+  elp_model* h = new elp_model();
+  std::string err;
+  int rc = build_model(desc, h->m, err);
+  if (rc) {
+    set_error(err);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_destroy(elp_model* m) {
+  GUARD_BEGIN
+  delete m;
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_assemble(elp_model* h) {
+  GUARD_BEGIN
+  if (!h) { set_error("null model"); return ELP_ERR_ARG; }
+  int rc = check_cuda_device();
+  if (rc) return rc;
+  Model& m = h->m;
+  if (!m.dev) {
+    rc = device_upload_model(m);
+    if (rc) return rc;
+  }
+  float ms = 0.f;
+  rc = device_assemble(m, 0, &ms);
+  if (rc) return rc;
+  m.assembled = true;
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_time_assembly(elp_model* h, int repeats, double* ms_per_assembly, double* ms_kernel_only) {
+  GUARD_BEGIN
+  if (!h || !h->m.assembled) { set_error("assemble the model first"); return ELP_ERR_STATE; }
+  if (repeats < 1) repeats = 1;
+  double tot = 0.0, best = 1e300;
+  for (int r = 0; r < repeats; ++r) {
+    float ms = 0.f;
+    int rc = device_assemble(h->m, 0, &ms);
+    if (rc) return rc;
+    tot += ms;
+    best = std::min(best, (double)ms);
+  }
+  if (ms_per_assembly) *ms_per_assembly = tot / repeats;
+  if (ms_kernel_only) *ms_kernel_only = best;
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_analyse(elp_model* h) {
+  GUARD_BEGIN
+  if (!h) { set_error("null model"); return ELP_ERR_ARG; }
+  int rc = check_cuda_device();
+  if (rc) return rc;
+  Model& m = h->m;
+  if (m.analysed) return ELP_OK;
+  m.sym.reset(new Symbolic());
+  rc = symbolic_analyse(m, *m.sym, 128);
+  if (rc) return rc;
+  rc = device_upload_symbolic(m);
+  if (rc) return rc;
+  m.analysed = true;
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_get_info(const elp_model* h, elp_model_info* info) {
+  GUARD_BEGIN
+  if (!h || !info) { set_error("null argument"); return ELP_ERR_ARG; }
+  const Model& m = h->m;
+  memset(info, 0, sizeof(*info));
+  info->n_dofs = m.n;
+  info->nnz = m.nnz;
+  info->n_elements = m.n_elements_total;
+  info->n_struct_groups = (int)m.groups.size();
+  if (m.sym) {
+    info->n_fronts = (int64_t)m.sym->fronts.size();
+    info->factor_entries = m.sym->arena;
+    info->factor_flops = m.sym->flops;
+    info->n_levels = m.sym->n_levels;
+    info->max_front = m.sym->max_front;
+  }
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_pattern(const elp_model* h, int32_t* row_ptr, int32_t* col_idx, int64_t* nnz) {
+  GUARD_BEGIN
+  if (!h) { set_error("null model"); return ELP_ERR_ARG; }
+  const Model& m = h->m;
+  if (nnz) *nnz = m.nnz;
+  if (row_ptr) memcpy(row_ptr, m.row_ptr.data(), sizeof(int32_t) * (m.n + 1));
+  if (col_idx) memcpy(col_idx, m.col_idx.data(), sizeof(int32_t) * m.nnz);
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_global_rows(const elp_model* h, int32_t* rows_out) {
+  GUARD_BEGIN
+  if (!h || !rows_out) { set_error("null argument"); return ELP_ERR_ARG; }
+  memcpy(rows_out, h->m.global_rows.data(), sizeof(int32_t) * h->m.global_rows.size());
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_rhs(const elp_model* h, double* f_out) {
+  GUARD_BEGIN
+  if (!h || !f_out) { set_error("null argument"); return ELP_ERR_ARG; }
+  const Model& m = h->m;
+  for (int64_t i = 0; i < m.n; ++i) { f_out[2 * i] = m.rhs[i].real(); f_out[2 * i + 1] = m.rhs[i].imag(); }
+  return ELP_OK;
+  GUARD_END
+}
+
+int elp_model_system_values(elp_model* h, double omega, double* values_out) {
+  GUARD_BEGIN
+  if (!h || !values_out) { set_error("null argument"); return ELP_ERR_ARG; }
+  Model& m = h->m;
+  if (!m.assembled) { set_error("assemble the model first"); return ELP_ERR_STATE; }
+  if (!(omega > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
+  DevBuf<double2> out;
+  ELP_CUDA(out.alloc(m.nnz));
+  int rc = numeric_system_values(m, omega, out.p);
+  if (rc) return rc;
+  ELP_CUDA(cudaMemcpy(values_out, out.p, sizeof(double2) * m.nnz, cudaMemcpyDeviceToHost));
+  return ELP_OK;
+  GUARD_END
+}
+
+static int prepare(elp_model* h) {
+  if (!h) { set_error("null model"); return ELP_ERR_ARG; }
+  int rc = ELP_OK;
+  if (!h->m.assembled) rc = elp_model_assemble(h);
+  if (rc) return rc;
+  if (!h->m.analysed) rc = elp_model_analyse(h);
+  return rc;
+}
+
+int elp_solve_device(elp_model* h, const double* omegas, int n_omega, int precision, const double* f_dev,
+                     double* x_dev, elp_solve_info* info, double tol, void* stream) {
+  GUARD_BEGIN
+  int rc = prepare(h);
+  if (rc) return rc;
+  if (precision != ELP_FP64_PLAIN && precision != ELP_MIXED) { set_error("unknown precision"); return ELP_ERR_ARG; }
+  if (n_omega < 0 || (n_omega > 0 && (!omegas || !x_dev))) { set_error("bad solve arguments"); return ELP_ERR_ARG; }
+  if (!(tol > 0.0)) tol = 1e-10;
+  Model& m = h->m;
+  const int64_t n = m.n;
+  // batch size: as many frequencies as fit a quarter of free memory, <= kMaxSlots
+  size_t freeb = 0, totb = 0;
+  ELP_CUDA(cudaMemGetInfo(&freeb, &totb));
+  const size_t elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
+  const size_t per_slot = (size_t)m.dsym->arena * elem + (size_t)n * (3 * sizeof(double2) + 24 + elem) +
+                          (size_t)m.dsym->cb_total * elem;
+  int slots = (int)std::min<size_t>((size_t)kMaxSlots, std::max<size_t>(1, (freeb / 2) / std::max<size_t>(1, per_slot)));
+  if (m.ws[precision] && m.ws[precision]->slots > 0) slots = std::max(slots, std::min(m.ws[precision]->slots, kMaxSlots));
+  slots = std::min(slots, std::max(1, n_omega));
+  int worst = ELP_OK;
+  for (int s0 = 0; s0 < n_omega; s0 += slots) {
+    int cnt = std::min(slots, n_omega - s0);
+    rc = numeric_solve_batch(m, precision, omegas + s0, cnt,
+                             f_dev ? reinterpret_cast<const double2*>(f_dev) + (size_t)s0 * n : nullptr,
+                             reinterpret_cast<double2*>(x_dev) + (size_t)s0 * n, info ? info + s0 : nullptr, tol,
+                             (cudaStream_t)stream);
+    if (rc == ELP_ERR_NOCONV) worst = rc;
+    else if (rc) return rc;
+  }
+  if (worst) set_error("iterative refinement did not reach the requested relative residual");
+  return worst;
+  GUARD_END
+}
+
+int elp_solve(elp_model* h, const double* omegas, int n_omega, int precision, const double* f_or_null,
+              double* x_out, elp_solve_info* info, double tol) {
+  GUARD_BEGIN
+  int rc = prepare(h);
+  if (rc) return rc;
+  if (n_omega < 0 || (n_omega > 0 && (!omegas || !x_out))) { set_error("bad solve arguments"); return ELP_ERR_ARG; }
+  if (n_omega == 0) return ELP_OK;
+  Model& m = h->m;
+  const int64_t n = m.n;
+  DevBuf<double2> fd, xd;
+  if (f_or_null) {
+    ELP_CUDA(fd.alloc((size_t)n * n_omega));
+    ELP_CUDA(cudaMemcpy(fd.p, f_or_null, sizeof(double2) * n * n_omega, cudaMemcpyHostToDevice));
+  }
+  ELP_CUDA(xd.alloc((size_t)n * n_omega));
+  rc = elp_solve_device(h, omegas, n_omega, precision, f_or_null ? reinterpret_cast<double*>(fd.p) : nullptr,
+                        reinterpret_cast<double*>(xd.p), info, tol, nullptr);
+  if (rc && rc != ELP_ERR_NOCONV) return rc;
+  ELP_CUDA(cudaMemcpy(x_out, xd.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToHost));
+  return rc;
+  GUARD_END
+}
+
+}  // extern "C"

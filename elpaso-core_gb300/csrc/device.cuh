@@ -1,0 +1,87 @@
+// Device-resident arrays of a model and shared CUDA helpers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "model.hpp"
+
+namespace elp {
+
+#define ELP_CUDA(call)                                                            \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) {                                                      \
+      set_error(std::string("CUDA: ") + cudaGetErrorString(e_) + " at " __FILE__); \
+      return ELP_ERR_CUDA;                                                        \
+    }                                                                             \
+  } while (0)
+
+// Per-element material constants for the assembly kernel (real E: the
+// loss factor is a per-w coefficient of the group's stiffness array).
+struct ElemMaterial {
+  double lam, mu;      // Brick8: Lame constants from E, nu (setupC)
+  double rho;          // structure density / fluid density
+  double Db, nu;       // DSG4: E t^3 / (12 (1 - nu^2)), nu
+  double Gt, t;        // DSG4: E / (2 (1 + nu)) * t * 5/6 (setupCs), thickness
+  double inv_c2;       // Fluid8: 1 / c^2
+  int group;           // structure loss-factor group
+  int pad;
+};
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    release();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void**)&p, count * sizeof(T));
+  }
+  cudaError_t upload(const T* h, size_t count) {
+    cudaError_t e = alloc(count);
+    if (e != cudaSuccess || count == 0) return e;
+    return cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice);
+  }
+  cudaError_t upload(const std::vector<T>& v) { return upload(v.data(), v.size()); }
+};
+
+struct DeviceModel {
+  int device = 0;
+  DevBuf<double> coords;           // 3 N
+  DevBuf<int32_t> row_ptr, col_idx, diag_idx;
+  DevBuf<uint8_t> cls;
+  DevBuf<double> VK, VM;           // nnz each
+  DevBuf<double> VKg;              // (G - 1) x nnz extra structure groups
+  DevBuf<double> rhs;              // 2 n
+  DevBuf<int32_t> bc_rows;
+  // element work lists
+  DevBuf<int32_t> brick_conn, plate_conn, fluid_conn;   // 8 / 4 / 8 node indices
+  DevBuf<int16_t> brick_mat, plate_mat, fluid_mat;      // index into materials
+  DevBuf<int32_t> node_row_brick, node_row_plate, node_row_fluid;  // first row of the type's dofs
+  DevBuf<ElemMaterial> materials;
+  DevBuf<int32_t> iface_rows;      // per quad: 12 structure rows + 4 fluid rows
+  DevBuf<double> iface_scale;      // per quad: -ori
+  DevBuf<int32_t> iface_geom;      // per quad: 4 fluid node indices (geometry)
+  DevBuf<int> flags;               // [0] 3D non-positive detJ count, [1] 2D count
+  int64_t n_brick = 0, n_plate = 0, n_fluid = 0, n_iface = 0;
+  double assembly_ms = 0.0;
+};
+
+// assemble.cu
+int device_upload_model(Model& m);
+int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms);
+
+}  // namespace elp

@@ -1,0 +1,351 @@
+// Host-side model construction: DOF numbering, CSR pattern, entry classes,
+// Dirichlet rows and the nodal-force right-hand side.
+//
+// Reference behaviour restated (paths inside elpasoCore/source/):
+//  - numbering: nodes in ascending id (std::map, fedata/mesh.h:49), per node
+//    the active DOFs in enum order 0..20 each take the next row
+//    (analysis/analysis.cpp:499-518); inactive DOFs keep row -1
+//    (fedata/dof.cpp:24-26);
+//  - active DOFs are the union of getDofs() of the elements touching the
+//    node (analysis.cpp:480-490); interface elements activate nothing;
+//  - pattern: every element's dense DOF block (analysis.cpp:815-823, values
+//    inserted with ADD_VALUES incl. explicit zeros, :1238-1246), every
+//    interface's C (structure rows x fluid cols) and C^T block
+//    (analysis.cpp:826-866), negative indices dropped, diagonal always
+//    present (analysis.cpp:791); Dirichlet rows keep their pattern
+//    (MAT_KEEP_NONZERO_PATTERN, analysis.cpp:802);
+//  - BC rows: nodes in id order, each BC of the node, DOFs 0..20 that are
+//    active and fixed (analysis.cpp:366-414); MatZeroRows(diag = 1) and
+//    F[row] = value (analysis.cpp:419-454);
+//  - nodal forces add F on active x1, x2, x3 rows (analysis.cpp:171-279).
+#include "model.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <numeric>
+#include <stdexcept>
+#include <unordered_map>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace elp {
+
+static thread_local std::string g_error;
+void set_error(const std::string& s) { g_error = s; }
+const std::string& get_error() { return g_error; }
+
+int nodes_per_element(int type) {
+  switch (type) {
+    case ELP_BRICK8: return 8;
+    case ELP_DSG4: return 4;
+    case ELP_FLUID8: return 8;
+  }
+  return 0;
+}
+int dofs_per_node(int type) {
+  switch (type) {
+    case ELP_BRICK8: return 3;
+    case ELP_DSG4: return 3;
+    case ELP_FLUID8: return 1;
+  }
+  return 0;
+}
+static const int kBrickDofs[3] = {ELP_DOF_X1, ELP_DOF_X2, ELP_DOF_X3};
+static const int kPlateDofs[3] = {ELP_DOF_X3, ELP_DOF_W1, ELP_DOF_W2};
+static const int kFluidDofs[1] = {ELP_DOF_FLUID};
+const int* element_dofs(int type) {
+  switch (type) {
+    case ELP_BRICK8: return kBrickDofs;
+    case ELP_DSG4: return kPlateDofs;
+    case ELP_FLUID8: return kFluidDofs;
+  }
+  return nullptr;
+}
+
+cplx group_coefficient(const StructGroup& g, double w) {
+  if (g.visco_type == 1) return cplx(1.0, g.eta);
+  if (g.visco_type == 2) return cplx(1.0, w * g.eta);
+  return cplx(1.0, 0.0);
+}
+
+static bool is_structure_type(int t) { return t == ELP_BRICK8 || t == ELP_DSG4; }
+
+int build_model(const elp_model_desc* d, Model& m, std::string& err) {
+  if (!d) { err = "null model description"; return ELP_ERR_ARG; }
+  if (d->n_nodes <= 0 || !d->coords || !d->node_ids) { err = "model has no nodes"; return ELP_ERR_ARG; }
+  if (d->n_nodes >= (int64_t)1 << 30) { err = "too many nodes"; return ELP_ERR_ARG; }
+  m.n_nodes = d->n_nodes;
+  m.node_ids.assign(d->node_ids, d->node_ids + d->n_nodes);
+  m.coords.assign(d->coords, d->coords + 3 * d->n_nodes);
+  if (d->n_materials < 0 || (d->n_materials > 0 && !d->materials)) { err = "bad materials"; return ELP_ERR_ARG; }
+  m.materials.assign(d->materials, d->materials + d->n_materials);
+  for (auto& mt : m.materials) {
+    if (mt.kind != ELP_STR_LIN_ELA_ISO_DIR && mt.kind != ELP_STR_LIN_VIS_ISO_DIR &&
+        mt.kind != ELP_AF_LIN_UAF_ISO_DIR) { err = "unknown material kind"; return ELP_ERR_ARG; }
+    if (mt.kind == ELP_STR_LIN_VIS_ISO_DIR && mt.visco_type != 1 && mt.visco_type != 2)
+      { err = "visco_type must be 1 or 2"; return ELP_ERR_ARG; }
+    if (mt.kind == ELP_AF_LIN_UAF_ISO_DIR && (!(mt.c > 0) || !(mt.rho > 0)))
+      { err = "fluid material needs c > 0 and rho > 0"; return ELP_ERR_ARG; }
+  }
+  for (int b = 0; b < d->n_blocks; ++b) {
+    const elp_element_block& eb = d->blocks[b];
+    int npe = nodes_per_element(eb.type);
+    if (!npe) { err = "unknown element type"; return ELP_ERR_ARG; }
+    if (eb.material < 0 || eb.material >= d->n_materials) { err = "element block material out of range"; return ELP_ERR_ARG; }
+    int mk = m.materials[eb.material].kind;
+    if (is_structure_type(eb.type) == (mk == ELP_AF_LIN_UAF_ISO_DIR))
+      { err = "element type / material kind mismatch"; return ELP_ERR_ARG; }
+    if (eb.n_elements < 0 || (eb.n_elements > 0 && !eb.connectivity)) { err = "bad connectivity"; return ELP_ERR_ARG; }
+    Block blk;
+    blk.type = eb.type;
+    blk.material = eb.material;
+    blk.n_elements = eb.n_elements;
+    blk.conn.assign(eb.connectivity, eb.connectivity + (size_t)npe * eb.n_elements);
+    for (int32_t v : blk.conn)
+      if (v < 0 || v >= d->n_nodes) { err = "connectivity node index out of range"; return ELP_ERR_ARG; }
+    m.n_elements_total += eb.n_elements;
+    m.blocks.push_back(std::move(blk));
+  }
+  if (d->n_interfaces > 0) {
+    if (!d->interfaces) { err = "bad interfaces"; return ELP_ERR_ARG; }
+    m.interfaces.assign(d->interfaces, d->interfaces + d->n_interfaces);
+    for (auto& q : m.interfaces)
+      for (int k = 0; k < 4; ++k)
+        if (q.structure_nodes[k] < 0 || q.structure_nodes[k] >= d->n_nodes || q.fluid_nodes[k] < 0 ||
+            q.fluid_nodes[k] >= d->n_nodes) { err = "interface node index out of range"; return ELP_ERR_ARG; }
+  }
+  if (d->n_fixed > 0) {
+    if (!d->fixed) { err = "bad fixed dofs"; return ELP_ERR_ARG; }
+    m.fixed.assign(d->fixed, d->fixed + d->n_fixed);
+    for (auto& f : m.fixed)
+      if (f.node < 0 || f.node >= d->n_nodes || f.dof < 0 || f.dof >= ELP_NUM_KNOWN_DOFS)
+        { err = "fixed dof out of range"; return ELP_ERR_ARG; }
+  }
+  if (d->n_forces > 0) {
+    if (!d->forces) { err = "bad forces"; return ELP_ERR_ARG; }
+    m.forces.assign(d->forces, d->forces + d->n_forces);
+    for (auto& f : m.forces)
+      if (f.node < 0 || f.node >= d->n_nodes) { err = "force node out of range"; return ELP_ERR_ARG; }
+  }
+
+  const int64_t N = m.n_nodes;
+  // ---- node order by ascending id, duplicate ids rejected
+  m.order.resize(N);
+  std::iota(m.order.begin(), m.order.end(), 0);
+  std::sort(m.order.begin(), m.order.end(),
+            [&](int32_t a, int32_t b) { return m.node_ids[a] < m.node_ids[b]; });
+  for (int64_t i = 1; i < N; ++i)
+    if (m.node_ids[m.order[i]] == m.node_ids[m.order[i - 1]]) { err = "duplicate node id"; return ELP_ERR_ARG; }
+
+  // ---- active DOFs (bitset of 21 per node)
+  std::vector<uint32_t> active(N, 0u);
+  for (auto& blk : m.blocks) {
+    int npe = nodes_per_element(blk.type), ndn = dofs_per_node(blk.type);
+    const int* dofs = element_dofs(blk.type);
+    uint32_t mask = 0;
+    for (int k = 0; k < ndn; ++k) mask |= 1u << dofs[k];
+    for (size_t i = 0; i < blk.conn.size(); ++i) active[blk.conn[i]] |= mask;
+    (void)npe;
+  }
+  m.global_rows.assign((size_t)N * ELP_NUM_KNOWN_DOFS, -1);
+  int64_t row = 0;
+  for (int64_t r = 0; r < N; ++r) {
+    int32_t v = m.order[r];
+    for (int k = 0; k < ELP_NUM_KNOWN_DOFS; ++k)
+      if (active[v] & (1u << k)) m.global_rows[(size_t)v * ELP_NUM_KNOWN_DOFS + k] = (int32_t)row++;
+  }
+  if (row >= ((int64_t)1 << 31) - 1) { err = "too many dofs"; return ELP_ERR_ARG; }
+  m.n = row;
+  const int64_t n = m.n;
+  if (n == 0) { err = "model has no active degrees of freedom"; return ELP_ERR_ARG; }
+  m.dof_node.resize(n);
+  m.dof_kind.resize(n);
+  for (int64_t v = 0; v < N; ++v)
+    for (int k = 0; k < ELP_NUM_KNOWN_DOFS; ++k) {
+      int32_t g = m.global_rows[(size_t)v * ELP_NUM_KNOWN_DOFS + k];
+      if (g >= 0) {
+        m.dof_node[g] = (int32_t)v;
+        m.dof_kind[g] = (k == ELP_DOF_FLUID) ? 1 : 0;
+      }
+    }
+  auto grow = [&](int32_t node, int dof) -> int32_t {
+    return m.global_rows[(size_t)node * ELP_NUM_KNOWN_DOFS + dof];
+  };
+
+  // ---- structure loss-factor groups
+  m.material_group.assign(m.materials.size(), -1);
+  {
+    std::vector<int64_t> count;
+    for (size_t i = 0; i < m.materials.size(); ++i) {
+      const elp_material& mt = m.materials[i];
+      if (mt.kind == ELP_AF_LIN_UAF_ISO_DIR) continue;
+      StructGroup g{mt.kind == ELP_STR_LIN_VIS_ISO_DIR ? mt.visco_type : 0,
+                    mt.kind == ELP_STR_LIN_VIS_ISO_DIR ? mt.eta : 0.0};
+      if (g.visco_type != 0 && g.eta == 0.0) g.visco_type = 0;
+      int found = -1;
+      for (size_t j = 0; j < m.groups.size(); ++j)
+        if (m.groups[j].visco_type == g.visco_type && m.groups[j].eta == g.eta) found = (int)j;
+      if (found < 0) { found = (int)m.groups.size(); m.groups.push_back(g); count.push_back(0); }
+      m.material_group[i] = found;
+    }
+    // elements per group; the most used group becomes group 0 (array VK)
+    for (auto& blk : m.blocks)
+      if (m.material_group[blk.material] >= 0) count[m.material_group[blk.material]] += blk.n_elements;
+    if (m.groups.size() > 1) {
+      size_t best = std::max_element(count.begin(), count.end()) - count.begin();
+      if (best != 0) {
+        std::swap(m.groups[0], m.groups[best]);
+        for (auto& g : m.material_group) {
+          if (g == 0) g = (int)best;
+          else if (g == (int)best) g = 0;
+        }
+      }
+    }
+    if (m.groups.empty()) m.groups.push_back(StructGroup{0, 0.0});
+  }
+
+  // ---- node -> incident elements (per block), CSR
+  std::vector<int64_t> ne_ptr(N + 1, 0);
+  for (auto& blk : m.blocks)
+    for (int32_t v : blk.conn) ne_ptr[v + 1]++;
+  for (int64_t v = 0; v < N; ++v) ne_ptr[v + 1] += ne_ptr[v];
+  struct ERef { int32_t block; int64_t elem; };
+  std::vector<ERef> ne_list(ne_ptr[N]);
+  {
+    std::vector<int64_t> fill(ne_ptr.begin(), ne_ptr.end() - 1);
+    for (int32_t b = 0; b < (int32_t)m.blocks.size(); ++b) {
+      auto& blk = m.blocks[b];
+      int npe = nodes_per_element(blk.type);
+      for (int64_t e = 0; e < blk.n_elements; ++e)
+        for (int k = 0; k < npe; ++k) {
+          int32_t v = blk.conn[(size_t)e * npe + k];
+          // an element lists each node once; repeated nodes would add twice
+          ne_list[fill[v]++] = ERef{b, e};
+        }
+    }
+  }
+  // ---- interface contributions per row: struct row -> fluid cols, fluid row -> struct cols
+  std::vector<std::vector<int32_t>> extra;  // sparse: only rows touched by interfaces
+  std::unordered_map<int32_t, int32_t> extra_slot;
+  for (auto& q : m.interfaces) {
+    int32_t srows[12], fcols[4];
+    for (int k = 0; k < 4; ++k) {
+      for (int d3 = 0; d3 < 3; ++d3) srows[k * 3 + d3] = grow(q.structure_nodes[k], d3);
+      fcols[k] = grow(q.fluid_nodes[k], ELP_DOF_FLUID);
+    }
+    auto add = [&](int32_t r, int32_t c) {
+      if (r < 0 || c < 0) return;
+      auto it = extra_slot.find(r);
+      int32_t s;
+      if (it == extra_slot.end()) { s = (int32_t)extra.size(); extra_slot[r] = s; extra.emplace_back(); }
+      else s = it->second;
+      extra[s].push_back(c);
+    };
+    for (int z = 0; z < 12; ++z)
+      for (int s = 0; s < 4; ++s) { add(srows[z], fcols[s]); add(fcols[s], srows[z]); }
+  }
+
+  // ---- per-row column lists (parallel over nodes)
+  std::vector<std::vector<int32_t>> rowcols(n);
+  const int64_t nnodes = N;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t v = 0; v < nnodes; ++v) {
+    std::vector<int32_t> cols;
+    for (int k = 0; k < ELP_NUM_KNOWN_DOFS; ++k) {
+      int32_t r = grow((int32_t)v, k);
+      if (r < 0) continue;
+      cols.clear();
+      for (int64_t p = ne_ptr[v]; p < ne_ptr[v + 1]; ++p) {
+        const Block& blk = m.blocks[ne_list[p].block];
+        const int* dofs = element_dofs(blk.type);
+        int ndn = dofs_per_node(blk.type), npe = nodes_per_element(blk.type);
+        bool has = false;
+        for (int q = 0; q < ndn; ++q) has |= (dofs[q] == k);
+        if (!has) continue;
+        const int32_t* en = &blk.conn[(size_t)ne_list[p].elem * npe];
+        for (int a = 0; a < npe; ++a)
+          for (int q = 0; q < ndn; ++q) {
+            int32_t c = grow(en[a], dofs[q]);
+            if (c >= 0) cols.push_back(c);
+          }
+      }
+      cols.push_back(r);  // diagonal always present
+      auto it = extra_slot.find(r);
+      if (it != extra_slot.end()) cols.insert(cols.end(), extra[it->second].begin(), extra[it->second].end());
+      std::sort(cols.begin(), cols.end());
+      cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+      rowcols[r] = cols;
+    }
+  }
+  m.row_ptr.assign(n + 1, 0);
+  int64_t nnz = 0;
+  for (int64_t r = 0; r < n; ++r) {
+    nnz += (int64_t)rowcols[r].size();
+    if (nnz >= ((int64_t)1 << 31) - 1) { err = "nnz exceeds int32 CSR range"; return ELP_ERR_ARG; }
+    m.row_ptr[r + 1] = (int32_t)nnz;
+  }
+  m.nnz = nnz;
+  m.col_idx.resize(nnz);
+  m.diag_idx.resize(n);
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < n; ++r) {
+    std::copy(rowcols[r].begin(), rowcols[r].end(), m.col_idx.begin() + m.row_ptr[r]);
+    auto it = std::lower_bound(rowcols[r].begin(), rowcols[r].end(), (int32_t)r);
+    m.diag_idx[r] = m.row_ptr[r] + (int32_t)(it - rowcols[r].begin());
+    std::vector<int32_t>().swap(rowcols[r]);
+  }
+
+  // ---- BC rows in reference order (analysis.cpp:376-413)
+  std::vector<std::vector<int32_t>> node_bcs(N);
+  for (size_t i = 0; i < m.fixed.size(); ++i) node_bcs[m.fixed[i].node].push_back((int32_t)i);
+  m.is_bc_row.assign(n, 0);
+  for (int64_t r = 0; r < N; ++r) {
+    int32_t v = m.order[r];
+    for (int32_t bi : node_bcs[v]) {
+      const elp_fixed_dof& f = m.fixed[bi];
+      int32_t g = grow(v, f.dof);
+      if (g < 0) continue;  // the dof does not exist at the node
+      m.bc_rows.push_back(g);
+      m.bc_values.push_back(cplx(f.value_re, f.value_im));
+      m.is_bc_row[g] = 1;
+    }
+  }
+
+  // ---- entry classes
+  m.cls.resize(nnz);
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < n; ++r) {
+    for (int32_t p = m.row_ptr[r]; p < m.row_ptr[r + 1]; ++p) {
+      int32_t c = m.col_idx[p];
+      uint8_t k;
+      if (m.is_bc_row[r]) k = (c == r) ? CLS_BC_DIAG : CLS_BC_OFF;
+      else if (m.dof_kind[r] == 0 && m.dof_kind[c] == 0) k = CLS_STRUCT;
+      else if (m.dof_kind[r] == 1 && m.dof_kind[c] == 1) k = CLS_FLUID;
+      else k = CLS_COUPLE;
+      m.cls[p] = k;
+    }
+  }
+
+  // ---- right-hand side: nodal forces (ADD) then BC values (set)
+  m.rhs.assign(n, cplx(0.0, 0.0));
+  {
+    // forces are applied per node in id order (analysis.cpp:187-276)
+    std::vector<std::vector<int32_t>> node_forces(N);
+    for (size_t i = 0; i < m.forces.size(); ++i) node_forces[m.forces[i].node].push_back((int32_t)i);
+    for (int64_t r = 0; r < N; ++r) {
+      int32_t v = m.order[r];
+      for (int32_t fi : node_forces[v])
+        for (int d3 = 0; d3 < 3; ++d3) {
+          int32_t g = grow(v, d3);
+          if (g >= 0) m.rhs[g] += cplx(m.forces[fi].f[d3], 0.0);
+        }
+    }
+    for (size_t i = 0; i < m.bc_rows.size(); ++i) m.rhs[m.bc_rows[i]] = m.bc_values[i];
+  }
+  return ELP_OK;
+}
+
+}  // namespace elp

@@ -1,0 +1,111 @@
+// Internal model state of the GB300 frequency-response path.
+//
+// A model owns (host) the copied description, the DOF numbering, the CSR
+// pattern and per-entry physics class, and (device) the w-independent value
+// arrays produced by the assembly kernel plus the symbolic factorisation.
+#pragma once
+#include <complex>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/elpaso_gb300.h"
+
+namespace elp {
+
+using cplx = std::complex<double>;
+
+// Physics class of a CSR entry. The per-w coefficient of each value array
+// depends only on this class (and on the structure loss-factor group):
+//   A(w) = a_cls(w) * VK + b_cls(w) * VM + sum_g c_g(w) * VKg
+enum EntryClass : uint8_t {
+  CLS_STRUCT = 0,   // structure-structure: a = c_0(w) (1, 1+i eta, 1+i w eta), b = -w^2
+  CLS_FLUID = 1,    // fluid-fluid, VK = K_f/rho, VM = M_f/rho: a = 1/w^2, b = -1
+  CLS_COUPLE = 2,   // structure-fluid coupling (-ori)(C + C^T): a = 1, b = 0
+  CLS_BC_OFF = 3,   // off-diagonal of a Dirichlet row: 0
+  CLS_BC_DIAG = 4,  // diagonal of a Dirichlet row: 1 (MatZeroRows diag = 1)
+};
+
+// Loss-factor group of the structure stiffness: coefficient c_g(w).
+struct StructGroup {
+  int visco_type;  // 0 elastic, 1: 1 + i eta, 2: 1 + i w eta
+  double eta;
+};
+
+int nodes_per_element(int type);
+int dofs_per_node(int type);
+// reference getDofs(): Brick8 {x1,x2,x3}, DSG4 {x3,w1,w2}, Fluid8 {fluid}
+const int* element_dofs(int type);
+
+struct Block {
+  int type = 0;
+  int material = 0;
+  int64_t n_elements = 0;
+  std::vector<int32_t> conn;
+};
+
+struct DeviceModel;   // device arrays, defined in device.cuh
+struct Symbolic;      // host symbolic factorisation, symbolic.hpp
+struct DeviceSymbolic;
+struct Workspace;
+
+struct Model {
+  // ---- copied description
+  int64_t n_nodes = 0;
+  std::vector<int64_t> node_ids;
+  std::vector<double> coords;
+  std::vector<elp_material> materials;
+  std::vector<Block> blocks;
+  std::vector<elp_interface_quad> interfaces;
+  std::vector<elp_fixed_dof> fixed;
+  std::vector<elp_nodal_force> forces;
+
+  // ---- numbering (analysis.cpp:475-520)
+  std::vector<int32_t> order;        // node indices by ascending id
+  std::vector<int32_t> global_rows;  // n_nodes x 21, -1 inactive
+  int64_t n = 0;
+  std::vector<int32_t> dof_node;     // node index of each dof
+  std::vector<uint8_t> dof_kind;     // 0 structure, 1 fluid
+
+  // ---- pattern (analysis.cpp:806-867)
+  std::vector<int32_t> row_ptr;      // n + 1   (nnz < 2^31 checked)
+  std::vector<int32_t> col_idx;      // nnz
+  std::vector<uint8_t> cls;          // nnz
+  std::vector<int32_t> diag_idx;     // n: CSR index of (i, i)
+  int64_t nnz = 0;
+
+  // ---- BC rows and right-hand side (analysis.cpp:171-279, 366-454)
+  std::vector<int32_t> bc_rows;
+  std::vector<cplx> bc_values;
+  std::vector<uint8_t> is_bc_row;    // n
+  std::vector<cplx> rhs;             // n
+
+  // ---- structure loss-factor groups
+  std::vector<StructGroup> groups;   // groups[0] -> VK, groups[g>0] -> VKg[g-1]
+  std::vector<int> material_group;   // per material, -1 for fluid
+
+  int64_t n_elements_total = 0;
+  bool assembled = false;
+  bool analysed = false;
+
+  std::unique_ptr<DeviceModel> dev;
+  std::unique_ptr<Symbolic> sym;
+  std::unique_ptr<DeviceSymbolic> dsym;
+  std::unique_ptr<Workspace> ws[2];  // per precision
+
+  Model();
+  ~Model();
+};
+
+// host-side construction (model.cpp)
+int build_model(const elp_model_desc* d, Model& m, std::string& err);
+
+// coefficient of group g at angular frequency w
+cplx group_coefficient(const StructGroup& g, double w);
+
+// thread-local error text
+void set_error(const std::string& s);
+const std::string& get_error();
+
+}  // namespace elp

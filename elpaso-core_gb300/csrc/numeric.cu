@@ -1,0 +1,1007 @@
+// K3 (per-w combine), K4/K7 (multifrontal numeric LU), K5 (triangular
+// solves) and K6 (FP64 residual + refinement) for the complex dynamic
+// stiffness system A(w) u = f.
+//
+// The reference solves each w with MUMPS (KSPPREONLY + PCLU,
+// analysis/analysis.cpp:1159-1169, 1293-1332) on m_K after
+// MatZeroRows(diag = 1) (analysis.cpp:419-454). Here:
+//  - A(w) is formed on the device from the w-independent arrays (entry
+//    classes, model.hpp), BC rows included, and scaled symmetrically by
+//    D = diag(1/sqrt|a_ii|) so that pivots are O(1) in FP32 and FP64 alike;
+//  - fronts are factorised level by level (all fronts of a level, and all
+//    frequencies of a batch, in the same launches) with a right-looking
+//    blocked LU: panel (partial pivoting restricted to the fully summed
+//    rows, static-pivot floor for tiny pivots), border rows of the panel
+//    (L21), pivot block row (U12), and the Schur update of the trailing
+//    matrix -- complex GEMM, precision of the fronts;
+//  - the Schur complement is extend-added into the parent, one child slot at
+//    a time so the summation order is fixed (results do not depend on the
+//    batch a frequency lands in);
+//  - the residual r = f - A(w) x is always FP64 from the FP64 value arrays,
+//    the correction is solved with the front-precision factors, and x is
+//    updated in FP64 until ||r||/||f|| <= tol.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "numeric.cuh"
+
+namespace elp {
+
+// ------------------------------------------------------------- complex ops
+template <class R> struct Vec2;
+template <> struct Vec2<double> { using T = double2; };
+template <> struct Vec2<float> { using T = float2; };
+
+__device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ float2 mkf(float a, float b) { return make_float2(a, b); }
+template <class V> __device__ __forceinline__ V cmk(double a, double b);
+template <> __device__ __forceinline__ double2 cmk<double2>(double a, double b) { return make_double2(a, b); }
+template <> __device__ __forceinline__ float2 cmk<float2>(double a, double b) { return make_float2((float)a, (float)b); }
+
+template <class V> __device__ __forceinline__ V cadd(V a, V b) { a.x += b.x; a.y += b.y; return a; }
+template <class V> __device__ __forceinline__ V csub(V a, V b) { a.x -= b.x; a.y -= b.y; return a; }
+template <class V> __device__ __forceinline__ V cmul(V a, V b) {
+  V r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+// a - b * c
+template <class V> __device__ __forceinline__ V cfms(V a, V b, V c) {
+  a.x -= b.x * c.x - b.y * c.y;
+  a.y -= b.x * c.y + b.y * c.x;
+  return a;
+}
+template <class V> __device__ __forceinline__ auto cabs2(V a) -> decltype(a.x) { return a.x * a.x + a.y * a.y; }
+template <class V> __device__ __forceinline__ V cinv(V a) {
+  auto d = a.x * a.x + a.y * a.y;
+  V r;
+  r.x = a.x / d;
+  r.y = -a.y / d;
+  return r;
+}
+
+// ------------------------------------------------------------- combine
+struct CombineArgs {
+  const double* VK;
+  const double* VM;
+  const double* VKg;
+  const uint8_t* cls;
+  int64_t nnz;
+  int ngroups;
+};
+
+__device__ __forceinline__ double2 combine(const CombineArgs& A, const Coef& c, int64_t q) {
+  const uint8_t k = A.cls[q];
+  if (k == CLS_BC_DIAG) return make_double2(1.0, 0.0);
+  if (k == CLS_BC_OFF) return make_double2(0.0, 0.0);
+  const double vk = A.VK[q], vm = A.VM[q];
+  double2 v;
+  v.x = c.a[k].x * vk + c.b[k] * vm;
+  v.y = c.a[k].y * vk;
+  if (k == CLS_STRUCT)
+    for (int g = 1; g < A.ngroups; ++g) {
+      double e = A.VKg[(int64_t)(g - 1) * A.nnz + q];
+      v.x += c.g[g].x * e;
+      v.y += c.g[g].y * e;
+    }
+  return v;
+}
+
+__global__ void k_dscale(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ diag,
+                         int64_t n, double* __restrict__ dscale) {
+  const int s = blockIdx.y;
+  const Coef c = coef[s];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double2 v = combine(A, c, diag[i]);
+    double a = sqrt(v.x * v.x + v.y * v.y);
+    dscale[s * n + i] = a > 0.0 ? 1.0 / sqrt(a) : 1.0;
+  }
+}
+
+// A(w) values on the pattern (unscaled), for parity checks
+__global__ void k_values(CombineArgs A, const Coef* __restrict__ coef, double2* __restrict__ out) {
+  const Coef c = coef[0];
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < A.nnz; q += (int64_t)gridDim.x * blockDim.x)
+    out[q] = combine(A, c, q);
+}
+
+template <class V>
+__global__ void k_scatter(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ row_ptr,
+                          const int32_t* __restrict__ col_idx, const int64_t* __restrict__ entry_off,
+                          const double* __restrict__ dscale, int64_t n, V* __restrict__ arena,
+                          int64_t arena_size, unsigned long long* __restrict__ stats) {
+  const int s = blockIdx.y;
+  const Coef c = coef[s];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double* d = dscale + s * n;
+  V* F = arena + s * arena_size;
+  double amax = 0.0;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    const double di = d[i];
+    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
+      double2 v = combine(A, c, q);
+      double sc = di * d[col_idx[q]];
+      v.x *= sc;
+      v.y *= sc;
+      amax = fmax(amax, sqrt(v.x * v.x + v.y * v.y));
+      F[entry_off[q]] = cmk<V>(v.x, v.y);
+    }
+  }
+  for (int o = 16; o; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  if (lane == 0) atomicMax(stats + 4 * s + 3, (unsigned long long)__double_as_longlong(amax));
+}
+
+// ------------------------------------------------------------- panel
+struct LevelArgs {
+  const int32_t* list;      // fronts of the level (offset applied)
+  int count;
+  const int32_t *fp, *fb, *piv_off;
+  const int64_t* foff;
+  int64_t arena_size;
+  int64_t n;
+};
+
+template <class R, int NB>
+__global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T* __restrict__ arena,
+                                               int32_t* __restrict__ perm, int step, R tiny,
+                                               unsigned long long* __restrict__ stats) {
+  using V = typename Vec2<R>::T;
+  const int f = L.list[blockIdx.x];
+  const int s = blockIdx.y;
+  const int p = L.fp[f], m = p + L.fb[f];
+  const int k0 = step * NB;
+  if (k0 >= p) return;
+  const int w = min(NB, p - k0);
+  V* F = arena + s * L.arena_size + L.foff[f];
+  int32_t* pv = perm + s * L.n + L.piv_off[f];
+  __shared__ R red_v[8];
+  __shared__ int red_i[8];
+  __shared__ V prow[NB];
+  __shared__ int s_piv;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  int nstatic = 0;
+  R pmax = 0, pmin = (R)1e30;
+  for (int j = k0; j < k0 + w; ++j) {
+    // ---- pivot search over the fully summed rows j..p-1
+    R best = -1;
+    int bi = 0x7fffffff;
+    for (int r = j + tid; r < p; r += blockDim.x) {
+      R a = cabs2(F[(int64_t)j * m + r]);
+      if (a > best) { best = a; bi = r; }
+    }
+    for (int o = 16; o; o >>= 1) {
+      R ob = __shfl_xor_sync(0xffffffffu, best, o);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) { red_v[wid] = best; red_i[wid] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      R b0 = red_v[0];
+      int i0 = red_i[0];
+      for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+        if (red_v[q] > b0 || (red_v[q] == b0 && red_i[q] < i0)) { b0 = red_v[q]; i0 = red_i[q]; }
+      s_piv = i0;
+      pv[j] = i0;
+    }
+    __syncthreads();
+    const int pr = s_piv;
+    if (pr != j)
+      for (int c = tid; c < m; c += blockDim.x) {
+        V t = F[(int64_t)c * m + j];
+        F[(int64_t)c * m + j] = F[(int64_t)c * m + pr];
+        F[(int64_t)c * m + pr] = t;
+      }
+    __syncthreads();
+    V d = F[(int64_t)j * m + j];
+    R ad = sqrt(cabs2(d));
+    if (!(ad >= tiny)) {  // static pivot floor (also catches NaN)
+      d = cmk<V>((double)tiny, 0.0);
+      ad = tiny;
+      ++nstatic;
+      __syncthreads();
+      if (tid == 0) F[(int64_t)j * m + j] = d;
+    }
+    pmax = ad > pmax ? ad : pmax;
+    pmin = ad < pmin ? ad : pmin;
+    for (int c = j + 1 + tid; c < k0 + w; c += blockDim.x) prow[c - k0] = F[(int64_t)c * m + j];
+    __syncthreads();
+    const V inv = cinv(d);
+    for (int r = j + 1 + tid; r < p; r += blockDim.x) {
+      V l = cmul(F[(int64_t)j * m + r], inv);
+      F[(int64_t)j * m + r] = l;
+      for (int c = j + 1; c < k0 + w; ++c) F[(int64_t)c * m + r] = cfms(F[(int64_t)c * m + r], l, prow[c - k0]);
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (nstatic) atomicAdd(stats + 4 * s + 0, (unsigned long long)nstatic);
+    atomicMax(stats + 4 * s + 1, (unsigned long long)__double_as_longlong((double)pmax));
+    // min |u_jj| stored as bits of 1/|u_jj| max
+    atomicMax(stats + 4 * s + 2, (unsigned long long)__double_as_longlong(1.0 / (double)pmin));
+  }
+}
+
+// L21 of the panel: rows p..m-1, panel columns (row-wise triangular solve with U of the panel)
+template <class R, int NB>
+__global__ void __launch_bounds__(128) k_border(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
+  using V = typename Vec2<R>::T;
+  const int f = L.list[blockIdx.x];
+  const int s = blockIdx.y;
+  const int p = L.fp[f], b = L.fb[f], m = p + b;
+  const int k0 = step * NB;
+  if (k0 >= p) return;
+  const int w = min(NB, p - k0);
+  V* F = arena + s * L.arena_size + L.foff[f];
+  __shared__ V U[NB][NB + 1];
+  __shared__ V dinv[NB];
+  for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
+    int i = t % w, j = t / w;
+    if (i <= j) U[i][j] = F[(int64_t)(k0 + j) * m + k0 + i];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < w; j += blockDim.x) dinv[j] = cinv(U[j][j]);
+  __syncthreads();
+  for (int r = p + blockIdx.z * blockDim.x + threadIdx.x; r < m; r += gridDim.z * blockDim.x) {
+    V v[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+      if (j < w) v[j] = F[(int64_t)(k0 + j) * m + r];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      if (j < w) {
+        V t = v[j];
+#pragma unroll
+        for (int i = 0; i < NB; ++i)
+          if (i < j) t = cfms(t, v[i], U[i][j]);
+        v[j] = cmul(t, dinv[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+      if (j < w) F[(int64_t)(k0 + j) * m + r] = v[j];
+  }
+}
+
+// U12 of the panel rows: columns k0+w..m-1, unit-lower solve with L of the panel
+template <class R, int NB>
+__global__ void __launch_bounds__(128) k_urow(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
+  using V = typename Vec2<R>::T;
+  const int f = L.list[blockIdx.x];
+  const int s = blockIdx.y;
+  const int p = L.fp[f], m = p + L.fb[f];
+  const int k0 = step * NB;
+  if (k0 >= p) return;
+  const int w = min(NB, p - k0);
+  V* F = arena + s * L.arena_size + L.foff[f];
+  __shared__ V Lp[NB][NB + 1];
+  for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
+    int i = t % w, j = t / w;
+    if (i > j) Lp[i][j] = F[(int64_t)(k0 + j) * m + k0 + i];
+  }
+  __syncthreads();
+  for (int c = k0 + w + blockIdx.z * blockDim.x + threadIdx.x; c < m; c += gridDim.z * blockDim.x) {
+    V v[NB];
+    V* col = F + (int64_t)c * m + k0;
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+      if (j < w) v[j] = col[j];
+#pragma unroll
+    for (int j = 1; j < NB; ++j) {
+      if (j < w) {
+        V t = v[j];
+#pragma unroll
+        for (int i = 0; i < NB; ++i)
+          if (i < j) t = cfms(t, Lp[j][i], v[i]);
+        v[j] = t;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+      if (j < w) col[j] = v[j];
+  }
+}
+
+// trailing update F22 -= L(:, panel) U(panel, :) on rows/cols k0+w..m-1
+template <class R, int NB>
+__global__ void __launch_bounds__(256) k_gemm(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
+  using V = typename Vec2<R>::T;
+  constexpr int TM = 64, TN = 64;
+  const int f = L.list[blockIdx.x];
+  const int s = blockIdx.y;
+  const int p = L.fp[f], m = p + L.fb[f];
+  const int k0 = step * NB;
+  if (k0 >= p) return;
+  const int w = min(NB, p - k0);
+  const int t0 = k0 + w;
+  const int mt = m - t0;
+  if (mt <= 0) return;
+  const int tiles_r = (mt + TM - 1) / TM;
+  const int ntiles = tiles_r * tiles_r;
+  V* F = arena + s * L.arena_size + L.foff[f];
+  constexpr int KC = 16;  // k chunk staged in shared memory
+  __shared__ R As_re[KC][TM], As_im[KC][TM];
+  __shared__ R Bs_re[KC][TN], Bs_im[KC][TN];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads, 4 x 4 outputs each
+  for (int tile = blockIdx.z; tile < ntiles; tile += gridDim.z) {
+    const int r0 = t0 + (tile % tiles_r) * TM;
+    const int c0 = t0 + (tile / tiles_r) * TN;
+    R acc_re[4][4], acc_im[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b2 = 0; b2 < 4; ++b2) { acc_re[a][b2] = 0; acc_im[a][b2] = 0; }
+    for (int kc = 0; kc < w; kc += KC) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < KC * TM; t += blockDim.x) {
+        int k = t / TM, i = t % TM;
+        V a = (kc + k < w && r0 + i < m) ? F[(int64_t)(k0 + kc + k) * m + r0 + i] : cmk<V>(0.0, 0.0);
+        As_re[k][i] = a.x;
+        As_im[k][i] = a.y;
+        int j = t / KC, kk = t % KC;
+        V bv = (kc + kk < w && c0 + j < m) ? F[(int64_t)(c0 + j) * m + k0 + kc + kk] : cmk<V>(0.0, 0.0);
+        Bs_re[kk][j] = bv.x;
+        Bs_im[kk][j] = bv.y;
+      }
+      __syncthreads();
+      const int kend = min(KC, w - kc);
+      for (int k = 0; k < kend; ++k) {
+        R ar[4], ai[4], br[4], bi[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) { ar[a] = As_re[k][ty + 16 * a]; ai[a] = As_im[k][ty + 16 * a]; }
+#pragma unroll
+        for (int b2 = 0; b2 < 4; ++b2) { br[b2] = Bs_re[k][tx + 16 * b2]; bi[b2] = Bs_im[k][tx + 16 * b2]; }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b2 = 0; b2 < 4; ++b2) {
+            acc_re[a][b2] += ar[a] * br[b2] - ai[a] * bi[b2];
+            acc_im[a][b2] += ar[a] * bi[b2] + ai[a] * br[b2];
+          }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b2 = 0; b2 < 4; ++b2) {
+        int r = r0 + ty + 16 * a, c = c0 + tx + 16 * b2;
+        if (r < m && c < m) {
+          V* dst = F + (int64_t)c * m + r;
+          V v = *dst;
+          v.x -= acc_re[a][b2];
+          v.y -= acc_im[a][b2];
+          *dst = v;
+        }
+      }
+  }
+}
+
+// extend-add of children's Schur complements into their parents
+template <class R>
+__global__ void __launch_bounds__(256) k_extend_add(const int32_t* __restrict__ list, const int32_t* __restrict__ fp,
+                                                    const int32_t* __restrict__ fb, const int32_t* __restrict__ fparent,
+                                                    const int32_t* __restrict__ map_off, const int64_t* __restrict__ foff,
+                                                    const int32_t* __restrict__ pmap, typename Vec2<R>::T* __restrict__ arena,
+                                                    int64_t arena_size) {
+  using V = typename Vec2<R>::T;
+  const int c = list[blockIdx.x];
+  const int s = blockIdx.y;
+  const int pc = fp[c], bc = fb[c], mc = pc + bc;
+  const int P = fparent[c];
+  const int mP = fp[P] + fb[P];
+  const V* C = arena + s * arena_size + foff[c];
+  V* PF = arena + s * arena_size + foff[P];
+  const int32_t* mp = pmap + map_off[c];
+  for (int j = blockIdx.z; j < bc; j += gridDim.z) {
+    const int64_t pcol = (int64_t)mp[j] * mP;
+    const V* src = C + (int64_t)(pc + j) * mc + pc;
+    for (int i = threadIdx.x; i < bc; i += blockDim.x) {
+      V* d = PF + pcol + mp[i];
+      *d = cadd(*d, src[i]);
+    }
+  }
+}
+
+// ------------------------------------------------------------- solves
+struct SolveArgs {
+  const int32_t* list;
+  int count;
+  const int32_t *fp, *fb, *idx_off, *map_off, *cb_off, *piv_off, *child_ptr, *child_list;
+  const int64_t* foff;
+  const int32_t* dofs;
+  const int32_t* pmap;
+  int64_t arena_size, n, cb_total;
+  const int* active;
+};
+
+template <class R>
+__global__ void __launch_bounds__(256) k_forward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
+                                                 const int32_t* __restrict__ perm, typename Vec2<R>::T* __restrict__ z,
+                                                 typename Vec2<R>::T* __restrict__ cb) {
+  using V = typename Vec2<R>::T;
+  extern __shared__ unsigned char smraw[];
+  V* w = reinterpret_cast<V*>(smraw);
+  const int f = S.list[blockIdx.x];
+  const int s = blockIdx.y;
+  if (!S.active[s]) return;
+  const int p = S.fp[f], b = S.fb[f], m = p + b;
+  const V* F = arena + s * S.arena_size + S.foff[f];
+  const int32_t* I = S.dofs + S.idx_off[f];
+  V* zs = z + s * S.n;
+  V* cbs = cb + s * S.cb_total;
+  const int tid = threadIdx.x;
+  for (int k = tid; k < m; k += blockDim.x) w[k] = k < p ? zs[I[k]] : cmk<V>(0.0, 0.0);
+  __syncthreads();
+  for (int q = S.child_ptr[f]; q < S.child_ptr[f + 1]; ++q) {
+    const int c = S.child_list[q];
+    const int bc = S.fb[c];
+    const int32_t* mp = S.pmap + S.map_off[c];
+    const V* src = cbs + S.cb_off[c];
+    for (int i = tid; i < bc; i += blockDim.x) w[mp[i]] = cadd(w[mp[i]], src[i]);
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const int32_t* pv = perm + s * S.n + S.piv_off[f];
+    for (int j = 0; j < p; ++j) {
+      int r = pv[j];
+      if (r != j) { V t = w[j]; w[j] = w[r]; w[r] = t; }
+    }
+  }
+  __syncthreads();
+  const int lane = tid & 31, wid = tid >> 5;
+  for (int j0 = 0; j0 < p; j0 += 32) {
+    const int jw = min(32, p - j0);
+    if (wid == 0) {
+      V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
+      for (int jj = 0; jj < jw; ++jj) {
+        V x;
+        x.x = __shfl_sync(0xffffffffu, val.x, jj);
+        x.y = __shfl_sync(0xffffffffu, val.y, jj);
+        if (lane > jj && lane < jw) val = cfms(val, F[(int64_t)(j0 + jj) * m + j0 + lane], x);
+      }
+      if (lane < jw) w[j0 + lane] = val;
+    }
+    __syncthreads();
+    for (int r = j0 + jw + tid; r < m; r += blockDim.x) {
+      V t = w[r];
+      for (int jj = 0; jj < jw; ++jj) t = cfms(t, F[(int64_t)(j0 + jj) * m + r], w[j0 + jj]);
+      w[r] = t;
+    }
+    __syncthreads();
+  }
+  for (int k = tid; k < m; k += blockDim.x) {
+    if (k < p) zs[I[k]] = w[k];
+    else cbs[S.cb_off[f] + k - p] = w[k];
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_backward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
+                                                  typename Vec2<R>::T* __restrict__ z) {
+  using V = typename Vec2<R>::T;
+  extern __shared__ unsigned char smraw[];
+  V* w = reinterpret_cast<V*>(smraw);
+  const int f = S.list[blockIdx.x];
+  const int s = blockIdx.y;
+  if (!S.active[s]) return;
+  const int p = S.fp[f], b = S.fb[f], m = p + b;
+  const V* F = arena + s * S.arena_size + S.foff[f];
+  const int32_t* I = S.dofs + S.idx_off[f];
+  V* zs = z + s * S.n;
+  const int tid = threadIdx.x;
+  for (int k = tid; k < m; k += blockDim.x) w[k] = zs[I[k]];
+  __syncthreads();
+  // t = y - U12 x_border
+  for (int r = tid; r < p; r += blockDim.x) {
+    V t = w[r];
+    for (int i = 0; i < b; ++i) t = cfms(t, F[(int64_t)(p + i) * m + r], w[p + i]);
+    w[r] = t;
+  }
+  __syncthreads();
+  const int lane = tid & 31, wid = tid >> 5;
+  for (int jend = p; jend > 0; jend -= 32) {
+    const int j0 = max(0, jend - 32);
+    const int jw = jend - j0;
+    if (wid == 0) {
+      V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
+      for (int jj = jw - 1; jj >= 0; --jj) {
+        if (lane == jj) val = cmul(val, cinv(F[(int64_t)(j0 + jj) * m + j0 + jj]));
+        V x;
+        x.x = __shfl_sync(0xffffffffu, val.x, jj);
+        x.y = __shfl_sync(0xffffffffu, val.y, jj);
+        if (lane < jj) val = cfms(val, F[(int64_t)(j0 + jj) * m + j0 + lane], x);
+      }
+      if (lane < jw) w[j0 + lane] = val;
+    }
+    __syncthreads();
+    for (int r = tid; r < j0; r += blockDim.x) {
+      V t = w[r];
+      for (int jj = 0; jj < jw; ++jj) t = cfms(t, F[(int64_t)(j0 + jj) * m + r], w[j0 + jj]);
+      w[r] = t;
+    }
+    __syncthreads();
+  }
+  for (int k = tid; k < p; k += blockDim.x) zs[I[k]] = w[k];
+}
+
+// ------------------------------------------------------------- refinement (FP64)
+// r = f - A x (unscaled A, BC rows included); partial sums of |r|^2 and |f|^2
+__global__ void k_residual(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ row_ptr,
+                           const int32_t* __restrict__ col_idx, int64_t n, const double2* __restrict__ x,
+                           const double2* __restrict__ f, double2* __restrict__ r, double* __restrict__ partial,
+                           int nparts, const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  const Coef c = coef[s];
+  const int lane = threadIdx.x & 31;
+  const double2* xs = x + s * n;
+  double rr = 0.0, ff = 0.0;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    double sx = 0.0, sy = 0.0;
+    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
+      double2 a = combine(A, c, q);
+      double2 v = xs[col_idx[q]];
+      sx += a.x * v.x - a.y * v.y;
+      sy += a.x * v.y + a.y * v.x;
+    }
+    for (int o = 16; o; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    }
+    if (lane == 0) {
+      double2 fi = f[s * n + i];
+      double2 ri = make_double2(fi.x - sx, fi.y - sy);
+      r[s * n + i] = ri;
+      rr += ri.x * ri.x + ri.y * ri.y;
+      ff += fi.x * fi.x + fi.y * fi.y;
+    }
+  }
+  __shared__ double red[2][32];
+  const int wid = threadIdx.x >> 5;
+  if (lane == 0) { red[0][wid] = rr; red[1][wid] = ff; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a += red[0][q]; b += red[1][q]; }
+    partial[(s * (int64_t)nparts + blockIdx.x) * 2 + 0] = a;
+    partial[(s * (int64_t)nparts + blockIdx.x) * 2 + 1] = b;
+  }
+}
+
+__global__ void k_norms(const double* __restrict__ partial, int nparts, double* __restrict__ norms,
+                        const int* __restrict__ active) {
+  const int s = blockIdx.x;
+  if (!active[s]) return;
+  __shared__ double a[256], b[256];
+  double x = 0, y = 0;
+  for (int q = threadIdx.x; q < nparts; q += blockDim.x) {
+    x += partial[(s * (int64_t)nparts + q) * 2];
+    y += partial[(s * (int64_t)nparts + q) * 2 + 1];
+  }
+  a[threadIdx.x] = x;
+  b[threadIdx.x] = y;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) { a[threadIdx.x] += a[threadIdx.x + o]; b[threadIdx.x] += b[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { norms[2 * s] = a[0]; norms[2 * s + 1] = b[0]; }
+}
+
+// z = D r in front precision
+template <class V>
+__global__ void k_rhs(const double2* __restrict__ r, const double* __restrict__ dscale, int64_t n, V* __restrict__ z,
+                      const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double d = dscale[s * n + i];
+    double2 v = r[s * n + i];
+    z[s * n + i] = cmk<V>(v.x * d, v.y * d);
+  }
+}
+
+// x += D z
+template <class V>
+__global__ void k_update(double2* __restrict__ x, const double* __restrict__ dscale, int64_t n, const V* __restrict__ z,
+                         const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double d = dscale[s * n + i];
+    V v = z[s * n + i];
+    double2 t = x[s * n + i];
+    t.x += d * (double)v.x;
+    t.y += d * (double)v.y;
+    x[s * n + i] = t;
+  }
+}
+
+// ------------------------------------------------------------- host side
+Workspace::~Workspace() {
+  if (h_coef) cudaFreeHost(h_coef);
+  if (h_norms) cudaFreeHost(h_norms);
+  if (h_active) cudaFreeHost(h_active);
+  if (h_stats) cudaFreeHost(h_stats);
+  if (stream) {
+    for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+    cudaStreamDestroy(stream);
+  }
+}
+
+void make_coef(const Model& m, double w, Coef& c) {
+  memset(&c, 0, sizeof(c));
+  cplx c0 = group_coefficient(m.groups[0], w);
+  c.a[CLS_STRUCT] = make_double2(c0.real(), c0.imag());
+  c.b[CLS_STRUCT] = -w * w;
+  c.a[CLS_FLUID] = make_double2(1.0 / (w * w), 0.0);
+  c.b[CLS_FLUID] = -1.0;
+  c.a[CLS_COUPLE] = make_double2(1.0, 0.0);
+  c.b[CLS_COUPLE] = 0.0;
+  for (size_t g = 1; g < m.groups.size() && g < (size_t)kMaxGroups; ++g) {
+    cplx cg = group_coefficient(m.groups[g], w);
+    c.g[g] = make_double2(cg.real(), cg.imag());
+  }
+}
+
+int device_upload_symbolic(Model& m) {
+  const Symbolic& S = *m.sym;
+  if (!m.dsym) m.dsym.reset(new DeviceSymbolic());
+  DeviceSymbolic& D = *m.dsym;
+  const int T = (int)S.fronts.size();
+  std::vector<int32_t> p(T), b(T), par(T), io(T), mo(T), co(T), po(T);
+  std::vector<int64_t> off(T);
+  std::vector<std::vector<int32_t>> kids(T);
+  for (int t = 0; t < T; ++t) {
+    const FrontInfo& F = S.fronts[t];
+    p[t] = F.p; b[t] = F.b; par[t] = F.parent; io[t] = F.idx_off; mo[t] = F.map_off;
+    co[t] = F.cb_off; po[t] = F.piv_off; off[t] = F.off;
+    if (F.parent >= 0) kids[F.parent].push_back(t);
+  }
+  std::vector<int32_t> cptr(T + 1, 0), clist;
+  for (int t = 0; t < T; ++t) {
+    std::sort(kids[t].begin(), kids[t].end(), [&](int a, int c) { return S.fronts[a].child_slot < S.fronts[c].child_slot; });
+    cptr[t + 1] = cptr[t] + (int32_t)kids[t].size();
+    clist.insert(clist.end(), kids[t].begin(), kids[t].end());
+  }
+  ELP_CUDA(D.f_p.upload(p));
+  ELP_CUDA(D.f_b.upload(b));
+  ELP_CUDA(D.f_parent.upload(par));
+  ELP_CUDA(D.f_idx_off.upload(io));
+  ELP_CUDA(D.f_map_off.upload(mo));
+  ELP_CUDA(D.f_cb_off.upload(co));
+  ELP_CUDA(D.f_piv_off.upload(po));
+  ELP_CUDA(D.f_off.upload(off));
+  ELP_CUDA(D.front_dofs.upload(S.front_dofs));
+  ELP_CUDA(D.parent_map.upload(S.parent_map));
+  ELP_CUDA(D.child_ptr.upload(cptr));
+  ELP_CUDA(D.child_list.upload(clist));
+  ELP_CUDA(D.entry_off.upload(S.entry_off));
+  std::vector<int32_t> ll, ea;
+  D.levels.assign(S.n_levels, DeviceSymbolic::Level());
+  int maxc = std::max(1, S.max_children);
+  for (int l = 0; l < S.n_levels; ++l) {
+    auto& L = D.levels[l];
+    L.start = (int)ll.size();
+    L.count = (int)S.level_fronts[l].size();
+    for (int t : S.level_fronts[l]) {
+      ll.push_back(t);
+      L.max_p = std::max(L.max_p, p[t]);
+      L.max_b = std::max(L.max_b, b[t]);
+      L.max_m = std::max(L.max_m, p[t] + b[t]);
+    }
+    L.ea_start.assign(maxc, 0);
+    L.ea_count.assign(maxc, 0);
+    for (int k = 0; k < maxc; ++k) {
+      L.ea_start[k] = (int)ea.size();
+      for (int t : S.level_fronts[l])
+        if (par[t] >= 0 && S.fronts[t].child_slot == k && b[t] > 0) {
+          ea.push_back(t);
+          L.ea_max_b = std::max(L.ea_max_b, b[t]);
+        }
+      L.ea_count[k] = (int)ea.size() - L.ea_start[k];
+    }
+  }
+  ELP_CUDA(D.level_list.upload(ll));
+  ELP_CUDA(D.ea_list.upload(ea));
+  D.n_fronts = T;
+  D.arena = S.arena;
+  D.cb_total = S.cb_total;
+  D.max_front = S.max_front;
+  return ELP_OK;
+}
+
+int workspace_ensure(Model& m, int precision, int slots) {
+  std::unique_ptr<Workspace>& W = m.ws[precision];
+  if (W && W->slots >= slots) return ELP_OK;
+  W.reset(new Workspace());
+  Workspace& w = *W;
+  w.precision = precision;
+  w.slots = slots;
+  w.elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
+  const DeviceSymbolic& D = *m.dsym;
+  const int64_t n = m.n;
+  cudaError_t e = w.arena.alloc((size_t)slots * D.arena * w.elem);
+  if (e != cudaSuccess) {
+    W.reset();
+    cudaGetLastError();
+    set_error("front arena does not fit in device memory");
+    return ELP_ERR_NOMEM;
+  }
+  ELP_CUDA(w.cb.alloc((size_t)slots * std::max<int64_t>(1, D.cb_total) * w.elem));
+  ELP_CUDA(w.z.alloc((size_t)slots * n * w.elem));
+  ELP_CUDA(w.perm.alloc((size_t)slots * n));
+  ELP_CUDA(w.dscale.alloc((size_t)slots * n));
+  ELP_CUDA(w.x.alloc((size_t)slots * n));
+  ELP_CUDA(w.r.alloc((size_t)slots * n));
+  ELP_CUDA(w.f.alloc((size_t)slots * n));
+  ELP_CUDA(w.coef.alloc(slots));
+  ELP_CUDA(w.norms.alloc(2 * (size_t)slots));
+  w.nparts = (int)std::min<int64_t>(1024, (n + 255) / 256);
+  ELP_CUDA(w.partial.alloc((size_t)slots * w.nparts * 2));
+  ELP_CUDA(w.active.alloc(slots));
+  ELP_CUDA(w.stats.alloc(4 * (size_t)slots));
+  ELP_CUDA(cudaMallocHost((void**)&w.h_coef, sizeof(Coef) * slots));
+  ELP_CUDA(cudaMallocHost((void**)&w.h_norms, sizeof(double) * 2 * slots));
+  ELP_CUDA(cudaMallocHost((void**)&w.h_active, sizeof(int) * slots));
+  ELP_CUDA(cudaMallocHost((void**)&w.h_stats, sizeof(unsigned long long) * 4 * slots));
+  ELP_CUDA(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
+  for (int i = 0; i < 8; ++i) ELP_CUDA(cudaEventCreate(&w.ev[i]));
+  return ELP_OK;
+}
+
+static CombineArgs combine_args(const Model& m) {
+  CombineArgs A;
+  A.VK = m.dev->VK.p;
+  A.VM = m.dev->VM.p;
+  A.VKg = m.dev->VKg.p;
+  A.cls = m.dev->cls.p;
+  A.nnz = m.nnz;
+  A.ngroups = (int)std::min<size_t>(m.groups.size(), kMaxGroups);
+  return A;
+}
+
+int numeric_system_values(Model& m, double omega, double2* out_dev) {
+  DevBuf<Coef> c;
+  Coef h;
+  make_coef(m, omega, h);
+  ELP_CUDA(c.upload(&h, 1));
+  CombineArgs A = combine_args(m);
+  k_values<<<1024, 256>>>(A, c.p, out_dev);
+  ELP_CUDA(cudaGetLastError());
+  ELP_CUDA(cudaDeviceSynchronize());
+  return ELP_OK;
+}
+
+template <class R>
+static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st) {
+  using V = typename Vec2<R>::T;
+  constexpr int NB = sizeof(R) == 8 ? 32 : 32;
+  DeviceSymbolic& D = *m.dsym;
+  DeviceModel& G = *m.dev;
+  const int64_t n = m.n;
+  V* arena = reinterpret_cast<V*>(w.arena.p);
+  CombineArgs A = combine_args(m);
+  ELP_CUDA(cudaMemsetAsync(w.stats.p, 0, sizeof(unsigned long long) * 4 * S_used, st));
+  {
+    dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 4096), S_used);
+    k_dscale<<<g, 256, 0, st>>>(A, w.coef.p, G.diag_idx.p, n, w.dscale.p);
+  }
+  ELP_CUDA(cudaMemsetAsync(w.arena.p, 0, (size_t)S_used * D.arena * sizeof(V), st));
+  {
+    dim3 g((unsigned)std::min<int64_t>((n + 7) / 8, 8192), S_used);
+    k_scatter<V><<<g, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, D.entry_off.p, w.dscale.p, n, arena,
+                                    D.arena, w.stats.p);
+  }
+  ELP_CUDA(cudaGetLastError());
+  LevelArgs L;
+  L.fp = D.f_p.p;
+  L.fb = D.f_b.p;
+  L.piv_off = D.f_piv_off.p;
+  L.foff = D.f_off.p;
+  L.arena_size = D.arena;
+  L.n = n;
+  const R tiny = sizeof(R) == 8 ? (R)1e-10 : (R)1e-6;
+  for (size_t l = 0; l < D.levels.size(); ++l) {
+    const auto& LV = D.levels[l];
+    L.list = D.level_list.p + LV.start;
+    L.count = LV.count;
+    const int steps = (LV.max_p + NB - 1) / NB;
+    for (int k = 0; k < steps; ++k) {
+      dim3 g1(LV.count, S_used);
+      k_panel<R, NB><<<g1, 256, 0, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p);
+      if (LV.max_b > 0) {
+        dim3 g2(LV.count, S_used, (unsigned)std::min(65535, (LV.max_b + 127) / 128));
+        k_border<R, NB><<<g2, 128, 0, st>>>(L, arena, k);
+      }
+      const int rest = LV.max_m - k * NB - 1;
+      if (rest > 0) {
+        dim3 g3(LV.count, S_used, (unsigned)std::min(65535, (rest + 127) / 128));
+        k_urow<R, NB><<<g3, 128, 0, st>>>(L, arena, k);
+        const int tr = (rest + 63) / 64;
+        dim3 g4(LV.count, S_used, (unsigned)std::min(65535, tr * tr));
+        k_gemm<R, NB><<<g4, 256, 0, st>>>(L, arena, k);
+      }
+    }
+    for (size_t k = 0; k < LV.ea_count.size(); ++k) {
+      if (!LV.ea_count[k]) continue;
+      dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, LV.ea_max_b));
+      k_extend_add<R><<<g5, 256, 0, st>>>(D.ea_list.p + LV.ea_start[k], D.f_p.p, D.f_b.p, D.f_parent.p, D.f_map_off.p,
+                                          D.f_off.p, D.parent_map.p, arena, D.arena);
+    }
+  }
+  ELP_CUDA(cudaGetLastError());
+  return ELP_OK;
+}
+
+template <class R>
+static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st) {
+  using V = typename Vec2<R>::T;
+  DeviceSymbolic& D = *m.dsym;
+  SolveArgs S;
+  S.fp = D.f_p.p;
+  S.fb = D.f_b.p;
+  S.idx_off = D.f_idx_off.p;
+  S.map_off = D.f_map_off.p;
+  S.cb_off = D.f_cb_off.p;
+  S.piv_off = D.f_piv_off.p;
+  S.child_ptr = D.child_ptr.p;
+  S.child_list = D.child_list.p;
+  S.foff = D.f_off.p;
+  S.dofs = D.front_dofs.p;
+  S.pmap = D.parent_map.p;
+  S.arena_size = D.arena;
+  S.n = m.n;
+  S.cb_total = std::max<int64_t>(1, D.cb_total);
+  S.active = w.active.p;
+  const V* arena = reinterpret_cast<const V*>(w.arena.p);
+  V* z = reinterpret_cast<V*>(w.z.p);
+  V* cb = reinterpret_cast<V*>(w.cb.p);
+  for (size_t l = 0; l < D.levels.size(); ++l) {
+    const auto& LV = D.levels[l];
+    S.list = D.level_list.p + LV.start;
+    S.count = LV.count;
+    size_t sm = (size_t)LV.max_m * sizeof(V);
+    k_forward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, w.perm.p, z, cb);
+  }
+  for (int l = (int)D.levels.size() - 1; l >= 0; --l) {
+    const auto& LV = D.levels[l];
+    S.list = D.level_list.p + LV.start;
+    S.count = LV.count;
+    size_t sm = (size_t)LV.max_m * sizeof(V);
+    k_backward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, z);
+  }
+  ELP_CUDA(cudaGetLastError());
+  return ELP_OK;
+}
+
+template <class R>
+static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_iter, cudaStream_t st,
+                     int* iters, float* ms) {
+  using V = typename Vec2<R>::T;
+  const int64_t n = m.n;
+  DeviceModel& G = *m.dev;
+  CombineArgs A = combine_args(m);
+  const size_t smem_need = (size_t)m.dsym->max_front * sizeof(V);
+  if (smem_need > 48 * 1024) {
+    ELP_CUDA(cudaFuncSetAttribute(k_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+    ELP_CUDA(cudaFuncSetAttribute(k_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+  }
+  if (smem_need > 227 * 1024) {
+    set_error("front larger than the shared-memory solve buffer (max 227 KB)");
+    return ELP_ERR_NOMEM;
+  }
+  for (int s = 0; s < S_used; ++s) w.h_active[s] = 1;
+  ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+  ELP_CUDA(cudaEventRecord(w.ev[0], st));
+  int rc = factor_and_setup<R>(m, w, S_used, st);
+  if (rc) return rc;
+  ELP_CUDA(cudaEventRecord(w.ev[1], st));
+  ELP_CUDA(cudaMemsetAsync(w.x.p, 0, sizeof(double2) * S_used * n, st));
+  const dim3 gv((unsigned)std::min<int64_t>((n + 255) / 256, 4096), S_used);
+  const dim3 gr((unsigned)w.nparts, S_used);
+  int it = 0;
+  float solve_ms = 0.f, refine_ms = 0.f;
+  // initial residual r = f (x = 0)
+  k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p, w.r.p, w.partial.p,
+                                 w.nparts, w.active.p);
+  for (it = 0; it < max_iter; ++it) {
+    ELP_CUDA(cudaEventRecord(w.ev[2], st));
+    k_rhs<V><<<gv, 256, 0, st>>>(w.r.p, w.dscale.p, n, reinterpret_cast<V*>(w.z.p), w.active.p);
+    rc = solve_sweep<R>(m, w, S_used, st);
+    if (rc) return rc;
+    k_update<V><<<gv, 256, 0, st>>>(w.x.p, w.dscale.p, n, reinterpret_cast<const V*>(w.z.p), w.active.p);
+    ELP_CUDA(cudaEventRecord(w.ev[3], st));
+    k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p, w.r.p, w.partial.p,
+                                   w.nparts, w.active.p);
+    k_norms<<<S_used, 256, 0, st>>>(w.partial.p, w.nparts, w.norms.p, w.active.p);
+    ELP_CUDA(cudaMemcpyAsync(w.h_norms, w.norms.p, sizeof(double) * 2 * S_used, cudaMemcpyDeviceToHost, st));
+    ELP_CUDA(cudaEventRecord(w.ev[4], st));
+    ELP_CUDA(cudaEventSynchronize(w.ev[4]));
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, w.ev[2], w.ev[3]);
+    cudaEventElapsedTime(&b, w.ev[3], w.ev[4]);
+    solve_ms += a;
+    refine_ms += b;
+    bool all = true, changed = false;
+    for (int s = 0; s < S_used; ++s) {
+      if (!w.h_active[s]) continue;
+      double fn = w.h_norms[2 * s + 1];
+      double rel = fn > 0 ? std::sqrt(w.h_norms[2 * s] / fn) : std::sqrt(w.h_norms[2 * s]);
+      if (rel <= tol || !std::isfinite(rel)) { w.h_active[s] = 0; changed = true; }
+      else all = false;
+    }
+    if (all) { ++it; break; }
+    if (changed) ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+  }
+  float fms = 0.f;
+  cudaEventElapsedTime(&fms, w.ev[0], w.ev[1]);
+  ms[0] = fms;
+  ms[1] = solve_ms;
+  ms[2] = refine_ms;
+  *iters = it;
+  return ELP_OK;
+}
+
+int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega, const double2* f_dev,
+                        double2* x_dev, elp_solve_info* info, double tol, cudaStream_t user_stream) {
+  if (n_omega <= 0) return ELP_OK;
+  if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
+  for (int s = 0; s < n_omega; ++s)
+    if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
+  int rc = workspace_ensure(m, precision, n_omega);
+  if (rc) return rc;
+  Workspace& w = *m.ws[precision];
+  cudaStream_t st = user_stream ? user_stream : w.stream;
+  const int64_t n = m.n;
+  for (int s = 0; s < n_omega; ++s) make_coef(m, omegas[s], w.h_coef[s]);
+  ELP_CUDA(cudaMemcpyAsync(w.coef.p, w.h_coef, sizeof(Coef) * n_omega, cudaMemcpyHostToDevice, st));
+  for (int s = 0; s < n_omega; ++s) {
+    const double2* src = f_dev ? f_dev + (size_t)s * n : reinterpret_cast<const double2*>(m.dev->rhs.p);
+    ELP_CUDA(cudaMemcpyAsync(w.f.p + (size_t)s * n, src, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+  }
+  int iters = 0;
+  float ms[3] = {0, 0, 0};
+  const int max_iter = precision == ELP_MIXED ? 40 : 8;
+  if (precision == ELP_MIXED) rc = run_batch<float>(m, w, n_omega, tol, max_iter, st, &iters, ms);
+  else rc = run_batch<double>(m, w, n_omega, tol, max_iter, st, &iters, ms);
+  if (rc) return rc;
+  ELP_CUDA(cudaMemcpyAsync(x_dev, w.x.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToDevice, st));
+  ELP_CUDA(cudaMemcpyAsync(w.h_stats, w.stats.p, sizeof(unsigned long long) * 4 * n_omega, cudaMemcpyDeviceToHost, st));
+  ELP_CUDA(cudaStreamSynchronize(st));
+  bool ok = true;
+  for (int s = 0; s < n_omega; ++s) {
+    double fn = w.h_norms[2 * s + 1];
+    double rel = fn > 0 ? std::sqrt(w.h_norms[2 * s] / fn) : std::sqrt(w.h_norms[2 * s]);
+    if (!(rel <= tol)) ok = false;
+    if (info) {
+      elp_solve_info& I = info[s];
+      I.rel_residual = rel;
+      double umax, amax;
+      unsigned long long b1 = w.h_stats[4 * s + 1], b3 = w.h_stats[4 * s + 3];
+      memcpy(&umax, &b1, 8);
+      memcpy(&amax, &b3, 8);
+      I.growth = amax > 0 ? umax / amax : 0.0;
+      I.iterations = iters;
+      I.static_pivots = (int)w.h_stats[4 * s + 0];
+      I.converged = rel <= tol ? 1 : 0;
+      I.ms_factor = ms[0] / n_omega;
+      I.ms_solve = ms[1] / n_omega;
+      I.ms_refine = ms[2] / n_omega;
+      I.ms_combine = 0.0;
+    }
+  }
+  if (!ok) {
+    set_error("iterative refinement did not reach the requested relative residual");
+    return ELP_ERR_NOCONV;
+  }
+  return ELP_OK;
+}
+
+}  // namespace elp

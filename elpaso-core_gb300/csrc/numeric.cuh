@@ -1,0 +1,74 @@
+// Numeric multifrontal factorisation and solve: device structures.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "device.cuh"
+#include "symbolic.hpp"
+
+namespace elp {
+
+constexpr int kMaxGroups = 8;    // structure loss-factor groups supported per model
+constexpr int kMaxSlots = 64;    // frequencies factorised together
+
+// per-slot coefficients of the value arrays
+struct Coef {
+  double2 a[3];                  // CLS_STRUCT, CLS_FLUID, CLS_COUPLE coefficient of VK
+  double b[3];                   // coefficient of VM
+  double2 g[kMaxGroups];         // coefficient of VKg[g - 1] (g >= 1) on structure entries
+};
+
+struct DeviceSymbolic {
+  DevBuf<int32_t> f_p, f_b, f_parent, f_idx_off, f_map_off, f_cb_off, f_piv_off;
+  DevBuf<int64_t> f_off;
+  DevBuf<int32_t> front_dofs, parent_map, child_ptr, child_list;
+  DevBuf<int64_t> entry_off;
+  DevBuf<int32_t> level_list;     // fronts grouped by level
+  DevBuf<int32_t> ea_list;        // per (level, child slot): fronts to extend-add
+  struct Level {
+    int start = 0, count = 0;
+    int max_p = 0, max_m = 0, max_b = 0;
+    std::vector<int> ea_start, ea_count;   // per child slot
+    int ea_max_b = 0;
+  };
+  std::vector<Level> levels;
+  int n_fronts = 0;
+  int64_t arena = 0, cb_total = 0;
+  int max_front = 0;
+};
+
+struct Workspace {
+  int precision = 0;              // ELP_FP64_PLAIN / ELP_MIXED
+  int slots = 0;                  // capacity in frequencies
+  size_t elem = 0;                // bytes of one complex front entry
+  DevBuf<char> arena;             // slots x arena complex entries
+  DevBuf<char> cb;                // slots x cb_total complex (solve contributions)
+  DevBuf<char> z;                 // slots x n complex (solve vector, front precision)
+  DevBuf<int32_t> perm;           // slots x n local pivot rows
+  DevBuf<double> dscale;          // slots x n symmetric diagonal scaling
+  DevBuf<double2> x, r, f;        // slots x n FP64 solution, residual, rhs
+  DevBuf<Coef> coef;              // slots
+  DevBuf<double> norms;           // slots x 2 (||r||^2, ||f||^2)
+  DevBuf<double> partial;         // reduction partials
+  DevBuf<int> active;             // slots
+  DevBuf<unsigned long long> stats;  // slots x 4: static pivots, max|u_jj| bits, min|u_jj| bits, max|a|
+  Coef* h_coef = nullptr;         // pinned host staging
+  double* h_norms = nullptr;
+  int* h_active = nullptr;
+  unsigned long long* h_stats = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8];
+  int nparts = 0;
+  ~Workspace();
+};
+
+int device_upload_symbolic(Model& m);
+int workspace_ensure(Model& m, int precision, int slots);
+int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega,
+                        const double2* f_dev, double2* x_dev, elp_solve_info* info, double tol,
+                        cudaStream_t user_stream);
+int numeric_system_values(Model& m, double omega, double2* out_dev);
+void make_coef(const Model& m, double w, Coef& c);
+
+}  // namespace elp

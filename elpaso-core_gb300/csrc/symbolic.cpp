@@ -1,0 +1,338 @@
+// Symbolic multifrontal analysis.
+//
+// The reference hands this to MUMPS (KSPPREONLY + PCLU + MUMPS,
+// analysis/analysis.cpp:1071-1226): ordering, elimination tree and front
+// sizes are computed inside the library. Here they are project code:
+//
+//  1. node graph from the CSR pattern (two nodes are adjacent when any of
+//     their DOFs share an entry; this includes the FSI coupling);
+//  2. geometric nested dissection: recursive median bisection along the
+//     longest axis of the node coordinates; the vertex separator is the
+//     boundary layer of one side (the smaller one) and becomes the parent
+//     front of the two halves; subsets at or below `leaf_dofs` DOFs are
+//     leaf fronts;
+//  3. fronts in postorder; front s holds its pivots (the separator's DOFs)
+//     followed by its border: every later-eliminated DOF adjacent to a pivot
+//     or in a child's border, sorted by elimination position;
+//  4. per CSR entry, the arena offset of its slot in the front that owns it
+//     (the front of whichever of row/column is eliminated first);
+//  5. per border DOF, its position in the parent front (extend-add map).
+#include "symbolic.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <functional>
+#include <numeric>
+
+namespace elp {
+
+namespace {
+
+struct NodeGraph {
+  std::vector<int64_t> ptr;
+  std::vector<int32_t> adj;
+};
+
+struct Builder {
+  const Model& m;
+  const NodeGraph& g;
+  std::vector<int32_t> first_row, ndof;
+  std::vector<int32_t> mark;    // per node: stamp * 4 + side
+  int32_t stamp = 0;
+  int leaf_dofs;
+  std::vector<std::vector<int32_t>> tnodes;     // tree node -> graph nodes (pivots)
+  std::vector<std::vector<int32_t>> tchildren;  // tree node -> children
+
+  Builder(const Model& mm, const NodeGraph& gg, int leaf) : m(mm), g(gg), leaf_dofs(leaf) {}
+
+  int64_t dofs_of(const std::vector<int32_t>& set) const {
+    int64_t s = 0;
+    for (int32_t v : set) s += ndof[v];
+    return s;
+  }
+
+  int make_node(std::vector<int32_t>&& nodes, std::vector<int32_t>&& children) {
+    tnodes.push_back(std::move(nodes));
+    tchildren.push_back(std::move(children));
+    return (int)tnodes.size() - 1;
+  }
+
+  // returns the roots of the subtree built over `set`
+  std::vector<int32_t> nd(std::vector<int32_t>& set) {
+    std::vector<int32_t> roots;
+    if (set.empty()) return roots;
+    if (dofs_of(set) <= leaf_dofs || set.size() <= 2) {
+      roots.push_back(make_node(std::move(set), {}));
+      return roots;
+    }
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int32_t v : set)
+      for (int d = 0; d < 3; ++d) {
+        double x = m.coords[3 * (size_t)v + d];
+        lo[d] = std::min(lo[d], x);
+        hi[d] = std::max(hi[d], x);
+      }
+    int axis = 0;
+    for (int d = 1; d < 3; ++d)
+      if (hi[d] - lo[d] > hi[axis] - lo[axis]) axis = d;
+    std::vector<int32_t> left, right;
+    if (hi[axis] - lo[axis] > 0.0) {
+      std::vector<double> vals(set.size());
+      for (size_t i = 0; i < set.size(); ++i) vals[i] = m.coords[3 * (size_t)set[i] + axis];
+      std::nth_element(vals.begin(), vals.begin() + vals.size() / 2, vals.end());
+      double xm = vals[vals.size() / 2];
+      for (int32_t v : set) (m.coords[3 * (size_t)v + axis] < xm ? left : right).push_back(v);
+      if (left.empty() || right.empty()) {
+        left.clear();
+        right.clear();
+        for (int32_t v : set) (m.coords[3 * (size_t)v + axis] <= xm ? left : right).push_back(v);
+      }
+    }
+    if (left.empty() || right.empty()) {
+      // coincident coordinates: split by index
+      left.assign(set.begin(), set.begin() + set.size() / 2);
+      right.assign(set.begin() + set.size() / 2, set.end());
+    }
+    ++stamp;
+    for (int32_t v : left) mark[v] = stamp * 4 + 1;
+    for (int32_t v : right) mark[v] = stamp * 4 + 2;
+    auto boundary = [&](const std::vector<int32_t>& side, int other) {
+      std::vector<int32_t> sep;
+      for (int32_t v : side) {
+        for (int64_t q = g.ptr[v]; q < g.ptr[v + 1]; ++q)
+          if (mark[g.adj[q]] == stamp * 4 + other) { sep.push_back(v); break; }
+      }
+      return sep;
+    };
+    std::vector<int32_t> sepL = boundary(left, 2), sepR = boundary(right, 1);
+    bool takeL = dofs_of(sepL) < dofs_of(sepR);
+    std::vector<int32_t>& sep = takeL ? sepL : sepR;
+    std::vector<int32_t>& side = takeL ? left : right;
+    if (!sep.empty()) {
+      ++stamp;
+      for (int32_t v : sep) mark[v] = stamp * 4 + 3;
+      std::vector<int32_t> rest;
+      rest.reserve(side.size());
+      for (int32_t v : side)
+        if (mark[v] != stamp * 4 + 3) rest.push_back(v);
+      side.swap(rest);
+    }
+    std::vector<int32_t> sep_nodes(sep.begin(), sep.end());
+    std::vector<int32_t> r1 = nd(left);
+    std::vector<int32_t> r2 = nd(right);
+    std::vector<int32_t> children(r1);
+    children.insert(children.end(), r2.begin(), r2.end());
+    if (sep_nodes.empty()) return children;  // disconnected halves: a forest
+    roots.push_back(make_node(std::move(sep_nodes), std::move(children)));
+    return roots;
+  }
+};
+
+}  // namespace
+
+int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
+  const int64_t N = m.n_nodes, n = m.n;
+  // ---- per node dof range (a node's active dofs have consecutive rows)
+  std::vector<int32_t> first_row(N, -1), ndof(N, 0);
+  for (int64_t r = 0; r < n; ++r) {
+    int32_t v = m.dof_node[r];
+    if (first_row[v] < 0) first_row[v] = (int32_t)r;
+    ndof[v]++;
+  }
+  // ---- node graph from the pattern
+  NodeGraph g;
+  g.ptr.assign(N + 1, 0);
+  std::vector<std::vector<int32_t>> nb(N);
+#pragma omp parallel for schedule(dynamic, 512)
+  for (int64_t v = 0; v < N; ++v) {
+    if (ndof[v] == 0) continue;
+    std::vector<int32_t>& L = nb[v];
+    for (int32_t r = first_row[v]; r < first_row[v] + ndof[v]; ++r)
+      for (int32_t q = m.row_ptr[r]; q < m.row_ptr[r + 1]; ++q) {
+        int32_t u = m.dof_node[m.col_idx[q]];
+        if (u != v) L.push_back(u);
+      }
+    std::sort(L.begin(), L.end());
+    L.erase(std::unique(L.begin(), L.end()), L.end());
+  }
+  for (int64_t v = 0; v < N; ++v) g.ptr[v + 1] = g.ptr[v] + (int64_t)nb[v].size();
+  g.adj.resize(g.ptr[N]);
+  for (int64_t v = 0; v < N; ++v) {
+    std::copy(nb[v].begin(), nb[v].end(), g.adj.begin() + g.ptr[v]);
+    std::vector<int32_t>().swap(nb[v]);
+  }
+
+  // ---- nested dissection
+  Builder B(m, g, leaf_dofs);
+  B.first_row = first_row;
+  B.ndof = ndof;
+  B.mark.assign(N, 0);
+  std::vector<int32_t> all;
+  for (int64_t v = 0; v < N; ++v)
+    if (ndof[v] > 0) all.push_back((int32_t)v);
+  std::vector<int32_t> roots = B.nd(all);
+  const int T = (int)B.tnodes.size();
+
+  // ---- elimination order
+  std::vector<int32_t> snode(N, -1), node_rank(N, -1);
+  S.elim_dof.clear();
+  S.elim_dof.reserve(n);
+  std::vector<int32_t> dof_pos(n, -1);
+  int32_t rank = 0;
+  for (int t = 0; t < T; ++t)
+    for (int32_t v : B.tnodes[t]) {
+      snode[v] = t;
+      node_rank[v] = rank++;
+      for (int32_t r = first_row[v]; r < first_row[v] + ndof[v]; ++r) {
+        dof_pos[r] = (int32_t)S.elim_dof.size();
+        S.elim_dof.push_back(r);
+      }
+    }
+  if ((int64_t)S.elim_dof.size() != n) { set_error("ordering lost degrees of freedom"); return ELP_ERR_ARG; }
+
+  // ---- parents, levels, borders
+  std::vector<int32_t> parent(T, -1), level(T, 0), slot(T, 0);
+  int maxc = 0;
+  for (int t = 0; t < T; ++t) {
+    int c = 0;
+    for (int32_t ch : B.tchildren[t]) {
+      parent[ch] = t;
+      slot[ch] = c++;
+      level[t] = std::max(level[t], level[ch] + 1);
+    }
+    maxc = std::max(maxc, c);
+  }
+  std::vector<std::vector<int32_t>> border(T);
+  std::vector<int32_t> seen(N, -1);
+  for (int t = 0; t < T; ++t) {
+    std::vector<int32_t> cand;
+    auto consider = [&](int32_t u) {
+      if (snode[u] > t && seen[u] != t) { seen[u] = t; cand.push_back(u); }
+    };
+    for (int32_t v : B.tnodes[t])
+      for (int64_t q = g.ptr[v]; q < g.ptr[v + 1]; ++q) consider(g.adj[q]);
+    for (int32_t ch : B.tchildren[t]) {
+      for (int32_t u : border[ch]) consider(u);
+    }
+    std::sort(cand.begin(), cand.end(), [&](int32_t a, int32_t b) { return node_rank[a] < node_rank[b]; });
+    border[t].swap(cand);
+  }
+
+  // ---- fronts
+  S.fronts.assign(T, FrontInfo());
+  S.front_dofs.clear();
+  int64_t arena = 0, cbt = 0;
+  double flops = 0.0;
+  int32_t piv = 0;
+  int maxm = 0;
+  for (int t = 0; t < T; ++t) {
+    FrontInfo& F = S.fronts[t];
+    F.parent = parent[t];
+    F.level = level[t];
+    F.child_slot = slot[t];
+    F.idx_off = (int32_t)S.front_dofs.size();
+    int p = 0, b = 0;
+    for (int32_t v : B.tnodes[t])
+      for (int32_t r = first_row[v]; r < first_row[v] + ndof[v]; ++r) { S.front_dofs.push_back(r); ++p; }
+    for (int32_t v : border[t])
+      for (int32_t r = first_row[v]; r < first_row[v] + ndof[v]; ++r) { S.front_dofs.push_back(r); ++b; }
+    F.p = p;
+    F.b = b;
+    F.piv_off = piv;
+    piv += p;
+    F.off = arena;
+    const int64_t mm = (int64_t)p + b;
+    arena += mm * mm;
+    F.cb_off = (int32_t)cbt;
+    cbt += b;
+    maxm = std::max<int>(maxm, (int)mm);
+    for (int k = 0; k < p; ++k) {
+      double r = (double)(mm - k - 1);
+      flops += 8.0 * r * r + 8.0 * r;
+    }
+    if (S.front_dofs.size() > (size_t)INT32_MAX) { set_error("front index lists too large"); return ELP_ERR_NOMEM; }
+  }
+  S.arena = arena;
+  S.cb_total = cbt;
+  S.flops = flops;
+  S.max_front = maxm;
+  S.max_children = maxc;
+
+  // ---- extend-add maps
+  std::vector<int32_t> loc(n, -1);
+  S.parent_map.clear();
+  for (int t = 0; t < T; ++t) S.fronts[t].map_off = 0;
+  {
+    // map offsets in front order
+    int32_t mo = 0;
+    for (int t = 0; t < T; ++t) { S.fronts[t].map_off = mo; mo += S.fronts[t].b; }
+    S.parent_map.assign(mo, -1);
+  }
+  for (int t = 0; t < T; ++t) {
+    const FrontInfo& P = S.fronts[t];
+    const int mP = P.p + P.b;
+    for (int k = 0; k < mP; ++k) loc[S.front_dofs[P.idx_off + k]] = k;
+    for (int32_t ch : B.tchildren[t]) {
+      const FrontInfo& C = S.fronts[ch];
+      for (int k = 0; k < C.b; ++k) {
+        int32_t d = S.front_dofs[C.idx_off + C.p + k];
+        int32_t pos = loc[d];
+        if (pos < 0) { set_error("extend-add map: border dof missing in parent"); return ELP_ERR_ARG; }
+        S.parent_map[C.map_off + k] = pos;
+      }
+    }
+    for (int k = 0; k < mP; ++k) loc[S.front_dofs[P.idx_off + k]] = -1;
+  }
+  for (int t = 0; t < T; ++t)
+    if (S.fronts[t].parent < 0 && S.fronts[t].b != 0) { set_error("root front with a border"); return ELP_ERR_ARG; }
+
+  // ---- per-entry arena offsets (bucket entries by owner front)
+  const int64_t nnz = m.nnz;
+  std::vector<int32_t> owner(nnz);
+  std::vector<int64_t> cnt(T + 1, 0);
+  std::vector<int32_t> front_of_pos(n);
+  for (int t = 0; t < T; ++t)
+    for (int k = 0; k < S.fronts[t].p; ++k) front_of_pos[S.fronts[t].piv_off + k] = t;
+  for (int64_t r = 0; r < n; ++r)
+    for (int32_t q = m.row_ptr[r]; q < m.row_ptr[r + 1]; ++q) {
+      int32_t c = m.col_idx[q];
+      int32_t pmin = std::min(dof_pos[r], dof_pos[c]);
+      owner[q] = front_of_pos[pmin];
+      cnt[owner[q] + 1]++;
+    }
+  for (int t = 0; t < T; ++t) cnt[t + 1] += cnt[t];
+  std::vector<int64_t> bucket(nnz), rowof(nnz);
+  {
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    for (int64_t r = 0; r < n; ++r)
+      for (int32_t q = m.row_ptr[r]; q < m.row_ptr[r + 1]; ++q) {
+        int64_t at = fill[owner[q]]++;
+        bucket[at] = q;
+        rowof[at] = r;
+      }
+  }
+  S.entry_off.assign(nnz, -1);
+  for (int t = 0; t < T; ++t) {
+    const FrontInfo& F = S.fronts[t];
+    const int mm = F.p + F.b;
+    for (int k = 0; k < mm; ++k) loc[S.front_dofs[F.idx_off + k]] = k;
+    for (int64_t at = cnt[t]; at < cnt[t + 1]; ++at) {
+      int64_t q = bucket[at];
+      int32_t r = (int32_t)rowof[at], c = m.col_idx[q];
+      int32_t lr = loc[r], lc = loc[c];
+      if (lr < 0 || lc < 0) { set_error("entry outside its owner front"); return ELP_ERR_ARG; }
+      S.entry_off[q] = F.off + (int64_t)lc * mm + lr;
+    }
+    for (int k = 0; k < mm; ++k) loc[S.front_dofs[F.idx_off + k]] = -1;
+  }
+
+  // ---- levels
+  int L = 0;
+  for (int t = 0; t < T; ++t) L = std::max(L, level[t] + 1);
+  S.n_levels = L;
+  S.level_fronts.assign(L, {});
+  for (int t = 0; t < T; ++t) S.level_fronts[level[t]].push_back(t);
+  return ELP_OK;
+}
+
+}  // namespace elp

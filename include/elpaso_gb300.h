@@ -1,0 +1,243 @@
+/*
+ * elpaso_gb300.h -- C ABI of the GB300 frequency-response path.
+ *
+ * Drop-in for the PETSc Mat-assembly + KSP section of elpasoC's
+ * `frequency-basic` analysis:
+ *
+ *   reference seam (paths inside elpasoCore/source/)
+ *   ------------------------------------------------------------------
+ *   analysis/frequency/analysisfrequencybasic.cpp:74-279  FullRun
+ *     :75  activateDofsAtNodes          -> numbering in elp_model_create
+ *     :76  optimizeMatrixPattern        -> pattern in elp_model_create
+ *     :81  initializeSolverObjects      -> symbolic phase, elp_model_analyse
+ *     :128 assembleGlobalTensors        -> elp_model_assemble (once, not per w)
+ *     :137 interface contributions      -> elp_model_assemble
+ *     :143 applyNodalLoads              -> right-hand side in elp_model_create
+ *     :156 getGlobalBCs/insertBoundaryConditions -> per-w combine in elp_solve
+ *     :181 solveEquationSystem (MUMPS)  -> elp_solve
+ *
+ * Conventions (mirroring PetscErrorCode / INFAMCHKERRQ in
+ * math/mathlibrary.h:101-109, but never aborting the process):
+ *   - every call returns int status, 0 = success; elp_last_error() gives text;
+ *   - caller-owned inputs are copied; outputs go to caller buffers;
+ *   - complex numbers are interleaved (re, im) doubles, like the HDF5 compound
+ *     {real, imag} the reference writes (misc/hdf5/outputh5.h:231);
+ *   - row/column indices are 0-based (the reference's HDF5 export is 1-based,
+ *     math/mathlibrary.cpp:62).
+ *   - a model handle may be used by one host thread at a time; distinct
+ *     handles are independent. The server API is thread-safe.
+ */
+#ifndef ELPASO_GB300_H
+#define ELPASO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define ELP_OK 0
+#define ELP_ERR_ARG 1          /* invalid argument / malformed model        */
+#define ELP_ERR_CUDA 2         /* CUDA runtime error                        */
+#define ELP_ERR_NOMEM 3        /* allocation failed / HBM budget exceeded   */
+#define ELP_ERR_GEOMETRY 4     /* non-positive Jacobian (elementfem.cpp:97) */
+#define ELP_ERR_SINGULAR 5     /* zero pivot that static pivoting can't fix */
+#define ELP_ERR_NOCONV 6       /* refinement did not reach the tolerance    */
+#define ELP_ERR_STATE 7        /* call out of order (e.g. solve before assemble) */
+#define ELP_ERR_TIMEOUT 8      /* server wait ran out                        */
+
+/* ---- element and material vocabulary (reference names) ----------------- */
+/* element/elementfactory.cpp:34-109 string tags */
+#define ELP_BRICK8 1   /* "Brick8": 8-node linear solid hexahedron, x1 x2 x3      */
+#define ELP_DSG4 2     /* "DSG4":   4-node Reissner-Mindlin plate, x3 w1 w2       */
+#define ELP_FLUID8 3   /* "Fluid8": 8-node acoustic hexahedron, fluid pressure    */
+
+/* material/materialfactory.cpp:34-113 tags */
+#define ELP_STR_LIN_ELA_ISO_DIR 1 /* isotropic elastic, real E               */
+#define ELP_STR_LIN_VIS_ISO_DIR 2 /* isotropic visco, E(1+i eta) / E(1+i w eta) */
+#define ELP_AF_LIN_UAF_ISO_DIR 3  /* ideal acoustic fluid: c, rho            */
+
+/* degrees of freedom: fedata/basics_dof.h:24-60 (subset used on this path) */
+#define ELP_DOF_X1 0
+#define ELP_DOF_X2 1
+#define ELP_DOF_X3 2
+#define ELP_DOF_W1 3
+#define ELP_DOF_W2 4
+#define ELP_DOF_FLUID 16
+#define ELP_NUM_KNOWN_DOFS 21
+
+typedef struct {
+  int kind;        /* ELP_STR_LIN_ELA_ISO_DIR / ELP_STR_LIN_VIS_ISO_DIR / ELP_AF_LIN_UAF_ISO_DIR */
+  double E;        /* Young's modulus (structure)                             */
+  double nu;       /* Poisson's ratio                                         */
+  double rho;      /* density (structure or fluid)                            */
+  double t;        /* plate thickness (DSG4)                                  */
+  double eta;      /* loss factor (visco)                                     */
+  int visco_type;  /* 1: E(1+i eta), 2: E(1+i w eta) (materialstructurevisco.cpp:284-285) */
+  double c;        /* speed of sound (fluid)                                  */
+} elp_material;
+
+typedef struct {
+  int type;               /* ELP_BRICK8 / ELP_DSG4 / ELP_FLUID8                 */
+  int material;           /* index into elp_model_desc.materials                */
+  int64_t n_elements;
+  const int32_t* connectivity; /* n_elements x nodes-per-element node INDICES    */
+} elp_element_block;
+
+typedef struct {
+  double ori;             /* orientation (+1/-1); C and C^T scaled by -ori       */
+  int32_t structure_nodes[4]; /* node indices (DSG4 plate nodes)                 */
+  int32_t fluid_nodes[4];     /* node indices (Fluid8 nodes; geometry taken here) */
+  int fluid_material;     /* index into materials (kept for the interface)       */
+} elp_interface_quad;      /* InterfaceMindlin: elementinterfacefactory.cpp:62-98 */
+
+typedef struct {
+  int32_t node;           /* node index                                          */
+  int32_t dof;            /* ELP_DOF_*                                           */
+  double value_re, value_im; /* prescribed value (F[row] = value)                */
+} elp_fixed_dof;
+
+typedef struct {
+  int32_t node;           /* node index                                          */
+  double f[3];            /* Fx Fy Fz on x1 x2 x3 (nodalforcestructure.cpp:46-73) */
+} elp_nodal_force;
+
+typedef struct {
+  int64_t n_nodes;
+  const int64_t* node_ids;  /* reference node ids; numbering follows ascending id */
+  const double* coords;     /* 3 x n_nodes                                        */
+  int n_materials;
+  const elp_material* materials;
+  int n_blocks;
+  const elp_element_block* blocks;
+  int64_t n_interfaces;
+  const elp_interface_quad* interfaces;
+  int64_t n_fixed;
+  const elp_fixed_dof* fixed;
+  int64_t n_forces;
+  const elp_nodal_force* forces;
+} elp_model_desc;
+
+typedef struct elp_model elp_model;
+
+typedef struct {
+  int64_t n_dofs;
+  int64_t nnz;
+  int64_t n_elements;
+  int64_t n_fronts;
+  int64_t factor_entries;   /* sum over fronts of m^2                         */
+  double factor_flops;      /* real flops of one complex numeric factorisation */
+  int n_levels;
+  int max_front;
+  int n_struct_groups;      /* distinct loss-factor groups of structure K     */
+} elp_model_info;
+
+/* precision of the numeric factorisation */
+#define ELP_FP64_PLAIN 0   /* FP64 fronts, FP64 refinement (the drop-in)       */
+#define ELP_MIXED 1        /* FP32 fronts (tensor-core Schur updates) + FP64 refinement */
+
+typedef struct {
+  double rel_residual;     /* ||f - A u||_2 / ||f||_2, computed in FP64          */
+  double growth;           /* max |U| / max |A| over fronts (pivot growth)       */
+  int iterations;          /* refinement iterations taken                        */
+  int static_pivots;       /* pivots replaced by the static-pivot floor          */
+  int converged;           /* rel_residual <= tolerance                          */
+  double ms_combine, ms_factor, ms_solve, ms_refine; /* device time per phase    */
+} elp_solve_info;
+
+/* ---- model lifetime ---------------------------------------------------- */
+
+/* Copies the description, numbers DOFs (analysis.cpp:475-520), builds the
+ * CSR pattern (analysis.cpp:806-867 + 1238-1246, interface blocks
+ * elementinterfacestructural.cpp:152-179; negative rows dropped, explicit
+ * zeros kept, diagonal always present), BC rows (analysis.cpp:366-454) and
+ * the nodal-force right-hand side (analysis.cpp:171-279). Host only. */
+int elp_model_create(const elp_model_desc* desc, elp_model** out);
+
+/* Integrates every element once on the GPU (one persistent launch over all
+ * element types) and scatters K, M, fluid K/M and the coupling C into
+ * w-independent CSR value arrays resident in HBM. Replaces the per-w
+ * element loop analysisfrequencybasic.cpp:281-304. */
+int elp_model_assemble(elp_model* m);
+
+/* Symbolic phase: nested-dissection ordering, assembly tree, front index
+ * maps (once per model; the reference leaves this to MUMPS's analysis). */
+int elp_model_analyse(elp_model* m);
+
+int elp_model_get_info(const elp_model* m, elp_model_info* info);
+
+/* CSR pattern, 0-based. row_ptr has n+1 entries, col_idx nnz. */
+int elp_model_pattern(const elp_model* m, int32_t* row_ptr, int32_t* col_idx, int64_t* nnz);
+
+/* Global row of (node index, dof) or -1 if inactive (cDegreesOfFreedom::getGlobalRow). */
+int elp_model_global_rows(const elp_model* m, int32_t* rows_out /* n_nodes x 21 */);
+
+/* Values of A(w) on the pattern after BC rows (what the reference holds in
+ * m_K right before KSPSolve), complex interleaved, nnz entries. Device
+ * combine, copied to the host. */
+int elp_model_system_values(elp_model* m, double omega, double* values_out);
+
+/* Right-hand side F after nodal loads and BC values, complex interleaved. */
+int elp_model_rhs(const elp_model* m, double* f_out);
+
+/* Solve A(w_k) u_k = f for n_omega angular frequencies. f == NULL uses the
+ * model's own right-hand side. x_out: n_omega x n complex interleaved.
+ * info: n_omega entries (may be NULL). tol: target relative residual
+ * (<= 0 selects 1e-10). */
+int elp_solve(elp_model* m, const double* omegas, int n_omega, int precision,
+              const double* f_or_null, double* x_out, elp_solve_info* info, double tol);
+
+int elp_model_destroy(elp_model* m);
+
+/* Text of the last error on the calling thread. */
+const char* elp_last_error(void);
+
+/* ---- device-resident variants (inputs/outputs already in HBM) ----------- */
+
+/* Same as elp_solve but f_dev / x_dev are device pointers (complex
+ * interleaved doubles, n_omega x n for x). stream may be 0. */
+int elp_solve_device(elp_model* m, const double* omegas, int n_omega, int precision,
+                     const double* f_dev, double* x_dev, elp_solve_info* info, double tol,
+                     void* stream);
+
+/* Re-runs the element integration on the device without host work, for
+ * timing: returns the device time of the assembly kernel(s) in ms. */
+int elp_model_time_assembly(elp_model* m, int repeats, double* ms_per_assembly,
+                            double* ms_kernel_only);
+
+/* ---- serving loop (continuous batching over resident models) ------------ */
+
+typedef struct elp_server elp_server;
+
+typedef struct {
+  int64_t hbm_budget_bytes;  /* admission limit for resident models + work    */
+  int max_inflight;          /* slots: frequency work items on the device     */
+  int precision;             /* ELP_FP64_PLAIN / ELP_MIXED                    */
+  double tol;                /* relative residual target                      */
+  int omega_batch;           /* frequencies factorised together per launch    */
+} elp_server_config;
+
+typedef struct {
+  int64_t request_id;
+  int status;                /* ELP_OK or error code                          */
+  int n_omega;
+  double latency_ms;         /* arrival -> last frequency done                */
+  double max_rel_residual;
+} elp_request_result;
+
+int elp_server_create(const elp_server_config* cfg, elp_server** out);
+/* Registers a model (assembled + analysed on first use); returns its slot id. */
+int elp_server_add_model(elp_server* s, elp_model* m, int* model_id);
+/* Queues a sweep request. x_out (n_omega x n complex) must stay valid until
+ * the result is returned by elp_server_wait. */
+int elp_server_submit(elp_server* s, int model_id, const double* omegas, int n_omega,
+                      double* x_out, int64_t* request_id);
+/* Waits for the next completed request (timeout_ms < 0: wait forever). */
+int elp_server_wait(elp_server* s, elp_request_result* result, double timeout_ms);
+int elp_server_destroy(elp_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ELPASO_GB300_H */

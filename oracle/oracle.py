@@ -1,0 +1,255 @@
+"""Test infrastructure (CPU oracle), not product code.
+
+Only tests/, `__graft_entry__.smoke()` and bench.py's CPU baseline use this
+module, and only as the checker. It restates, independently of the product
+code, the reference's host-side flow for one frequency (paths inside
+elpasoCore/source/ of the reference):
+
+  numbering      analysis/analysis.cpp:475-520 (nodes by id, DOF enum order)
+  pattern        analysis/analysis.cpp:806-867 + 1238-1246, interface blocks
+                 element/interface/elementinterfacestructural.cpp:152-179;
+                 negative rows dropped by PETSc, explicit zeros kept,
+                 diagonal inserted by preallocateMatrix (analysis.cpp:791)
+  BC rows        analysis/analysis.cpp:366-454 (MatZeroRows diag = 1, F[row] = value)
+  RHS            analysis/analysis.cpp:171-279 (nodal forces, ADD)
+  values         element matrices EM(w) of oracle/elp_oracle.c, inserted per
+                 element, interfaces with -ori (analysisfrequencybasic.cpp:101-157)
+  solve          SciPy SuperLU, complex128 (stand-in for MUMPS, which is not
+                 available here) -- the FP64 direct-solve oracle
+
+The element restatement itself is pinned against the reference's own
+element code compiled from its sources (oracle/_ref, tests/golden/).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libelpref.so")
+
+BRICK8, DSG4, FLUID8 = 1, 2, 3
+ELA, VIS, FLU = 1, 2, 3
+ELEM_DOFS = {BRICK8: (0, 1, 2), DSG4: (2, 3, 4), FLUID8: (16,)}
+NPE = {BRICK8: 8, DSG4: 4, FLUID8: 8}
+
+_lib = None
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "elp_oracle.c")):
+            build_oracle()
+        _lib = C.CDLL(LIB)
+        for f in ("orc_brick8", "orc_dsg4", "orc_fluid8", "orc_interface_mindlin", "orc_assemble"):
+            getattr(_lib, f).restype = C.c_int
+    return _lib
+
+
+def ref_lib():
+    """The reference's own element code (oracle/_ref), or None when absent."""
+    if not os.path.exists(REF_LIB):
+        return None
+    return C.CDLL(REF_LIB)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _d(x):
+    return C.c_double(float(x))
+
+
+# ------------------------------------------------------------------ elements
+def brick8(xyz, E, nu, rho, omega):
+    K = np.zeros(2 * 576); M = np.zeros(2 * 576); EM = np.zeros(2 * 576)
+    x = np.ascontiguousarray(xyz, np.float64)
+    lib().orc_brick8(_p(x), _d(complex(E).real), _d(complex(E).imag), _d(nu), _d(rho), _d(omega), _p(K), _p(M), _p(EM))
+    f = lambda a: a.view(np.complex128).reshape(24, 24)
+    return f(K), f(M), f(EM)
+
+
+def dsg4(xyz, E, nu, rho, t, omega):
+    K = np.zeros(2 * 144); M = np.zeros(2 * 144); EM = np.zeros(2 * 144)
+    x = np.ascontiguousarray(xyz, np.float64)
+    rc = lib().orc_dsg4(_p(x), _d(complex(E).real), _d(complex(E).imag), _d(nu), _d(rho), _d(t), _d(omega),
+                        _p(K), _p(M), _p(EM))
+    f = lambda a: a.view(np.complex128).reshape(12, 12)
+    return f(K), f(M), f(EM), rc
+
+
+def fluid8(xyz, c, rho, omega):
+    K = np.zeros(128); M = np.zeros(128); EM = np.zeros(128)
+    x = np.ascontiguousarray(xyz, np.float64)
+    lib().orc_fluid8(_p(x), _d(c), _d(rho), _d(omega), _p(K), _p(M), _p(EM))
+    f = lambda a: a.view(np.complex128).reshape(8, 8)
+    return f(K), f(M), f(EM)
+
+
+def interface_mindlin(xyz_fluid, transform=False):
+    Cm = np.zeros(96)
+    x = np.ascontiguousarray(xyz_fluid, np.float64)
+    lib().orc_interface_mindlin(_p(x), int(bool(transform)), _p(Cm))
+    return Cm.view(np.complex128).reshape(12, 4)
+
+
+def e_vis(mat, omega):
+    """E_vis of materialstructurevisco.cpp:284-285, real E for the elastic kind."""
+    if mat["kind"] == VIS:
+        if int(mat.get("visco_type", 1)) == 2:
+            return mat["E"] * (1.0 + 1j * omega * mat["eta"])
+        return mat["E"] * (1.0 + 1j * mat["eta"])
+    return complex(mat["E"])
+
+
+# ------------------------------------------------------------------ host flow
+class System:
+    """Numbering, pattern, BC rows and RHS of a model description."""
+
+    def __init__(self, d):
+        self.d = d
+        N = len(d.node_ids)
+        order = np.argsort(np.asarray(d.node_ids), kind="stable")
+        active = [set() for _ in range(N)]
+        for typ, _, conn in d.blocks:
+            for e in np.asarray(conn):
+                for v in e:
+                    active[v].update(ELEM_DOFS[typ])
+        rows = -np.ones((N, 21), np.int64)
+        r = 0
+        for v in order:
+            for k in range(21):
+                if k in active[v]:
+                    rows[v, k] = r
+                    r += 1
+        self.rows = rows
+        self.n = r
+        pattern = [set([i]) for i in range(r)]
+        for typ, _, conn in d.blocks:
+            for e in np.asarray(conn):
+                g = [rows[v, k] for v in e for k in ELEM_DOFS[typ]]
+                g = [x for x in g if x >= 0]
+                for i in g:
+                    pattern[i].update(g)
+        self.iface_rows = []
+        if d.interfaces is not None:
+            for q in range(len(d.interfaces["ori"])):
+                sr = [rows[d.interfaces["snodes"][q][k], dd] for k in range(4) for dd in (0, 1, 2)]
+                fr = [rows[d.interfaces["fnodes"][q][k], 16] for k in range(4)]
+                self.iface_rows.append(sr + fr)
+                for z in sr:
+                    if z < 0:
+                        continue
+                    for s in fr:
+                        if s >= 0:
+                            pattern[z].add(s)
+                            pattern[s].add(z)
+        self.row_ptr = np.zeros(r + 1, np.int32)
+        cols = []
+        for i in range(r):
+            c = sorted(pattern[i])
+            cols.extend(c)
+            self.row_ptr[i + 1] = self.row_ptr[i] + len(c)
+        self.col_idx = np.asarray(cols, np.int32)
+        # BC rows in reference order
+        self.bc_rows, self.bc_vals = [], []
+        if d.fixed is not None:
+            by_node = {}
+            for k in range(len(d.fixed["node"])):
+                by_node.setdefault(int(d.fixed["node"][k]), []).append(k)
+            for v in order:
+                for k in by_node.get(int(v), []):
+                    dof = int(d.fixed["dof"][k])
+                    if rows[v, dof] >= 0:
+                        self.bc_rows.append(int(rows[v, dof]))
+                        self.bc_vals.append(complex(d.fixed["value"][k]) if "value" in d.fixed else 0j)
+        f = np.zeros(r, np.complex128)
+        if d.forces is not None:
+            for k in range(len(d.forces["node"])):
+                v = int(d.forces["node"][k])
+                for dd in range(3):
+                    if rows[v, dd] >= 0:
+                        f[rows[v, dd]] += d.forces["f"][k][dd]
+        for rr, val in zip(self.bc_rows, self.bc_vals):
+            f[rr] = val
+        self.f = f
+
+    def values(self, omega):
+        """A(w) on the pattern after BC rows (complex128, nnz)."""
+        d = self.d
+        rows = self.rows
+        buf = {}
+
+        def pack(typ):
+            xyz, mat, rr = [], [], []
+            for btyp, mi, conn in d.blocks:
+                if btyp != typ:
+                    continue
+                m = d.materials[mi]
+                for e in np.asarray(conn):
+                    xyz.append(d.coords[e].reshape(-1))
+                    if typ == FLUID8:
+                        mat.append([m["c"], m["rho"]])
+                    else:
+                        E = e_vis(m, omega)
+                        mm = [E.real, E.imag, m["nu"], m["rho"]]
+                        if typ == DSG4:
+                            mm.append(m["t"])
+                        mat.append(mm)
+                    rr.append([rows[v, k] for v in e for k in ELEM_DOFS[typ]])
+            w = {BRICK8: 4, DSG4: 5, FLUID8: 2}[typ]
+            a = (np.ascontiguousarray(np.asarray(xyz, np.float64).reshape(-1)),
+                 np.ascontiguousarray(np.asarray(mat, np.float64).reshape(-1, w).reshape(-1)),
+                 np.ascontiguousarray(np.asarray(rr, np.int32).reshape(-1)), len(xyz))
+            buf[typ] = a
+            return a
+        b, p, fl = pack(BRICK8), pack(DSG4), pack(FLUID8)
+        nq = len(self.iface_rows)
+        if nq:
+            ixyz = np.ascontiguousarray(np.concatenate(
+                [d.coords[np.asarray(d.interfaces["fnodes"][q])].reshape(-1) for q in range(nq)]))
+            iori = np.ascontiguousarray(np.asarray(d.interfaces["ori"], np.float64))
+            irows = np.ascontiguousarray(np.asarray(self.iface_rows, np.int32).reshape(-1))
+            itr = np.ascontiguousarray(np.asarray(
+                [1 if rows[d.interfaces["snodes"][q][0], 0] >= 0 else 0 for q in range(nq)], np.int32))
+        else:
+            ixyz = np.zeros(1); iori = np.zeros(1); irows = np.zeros(16, np.int32); itr = np.zeros(1, np.int32)
+        bc = np.ascontiguousarray(np.asarray(self.bc_rows, np.int32)) if self.bc_rows else np.zeros(1, np.int32)
+
+        class S(C.Structure):
+            _fields_ = [("n", C.c_int64), ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p),
+                        ("n_brick", C.c_int64), ("n_plate", C.c_int64), ("n_fluid", C.c_int64), ("n_iface", C.c_int64),
+                        ("brick_xyz", C.c_void_p), ("brick_mat", C.c_void_p), ("brick_rows", C.c_void_p),
+                        ("plate_xyz", C.c_void_p), ("plate_mat", C.c_void_p), ("plate_rows", C.c_void_p),
+                        ("fluid_xyz", C.c_void_p), ("fluid_mat", C.c_void_p), ("fluid_rows", C.c_void_p),
+                        ("iface_xyz", C.c_void_p), ("iface_ori", C.c_void_p), ("iface_rows", C.c_void_p),
+                        ("iface_transform", C.c_void_p), ("n_bc", C.c_int64), ("bc_rows", C.c_void_p)]
+        s = S(self.n, _p(self.row_ptr), _p(self.col_idx), b[3], p[3], fl[3], nq,
+              _p(b[0]), _p(b[1]), _p(b[2]), _p(p[0]), _p(p[1]), _p(p[2]), _p(fl[0]), _p(fl[1]), _p(fl[2]),
+              _p(ixyz), _p(iori), _p(irows), _p(itr), len(self.bc_rows), _p(bc))
+        out = np.zeros(2 * len(self.col_idx))
+        rc = lib().orc_assemble(C.byref(s), _d(omega), _p(out))
+        if rc:
+            raise RuntimeError(f"oracle assembly failed ({rc})")
+        return out.view(np.complex128)
+
+    def matrix(self, omega):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.values(omega), self.col_idx, self.row_ptr), shape=(self.n, self.n))
+
+    def solve(self, omega, f=None):
+        import scipy.sparse.linalg as sla
+        A = self.matrix(omega).tocsc()
+        rhs = self.f if f is None else f
+        x = sla.splu(A).solve(rhs)
+        return x

@@ -1,0 +1,2 @@
+/* forwards to the PETSc type stand-in (oracle only) */
+#include "petsc.h"
