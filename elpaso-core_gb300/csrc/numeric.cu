@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
   for (int j = k0; j < k0 + w; ++j) {
     // ---- pivot search over the fully summed rows j..p-1
     R best = -1;
-    int bi = 0x7fffffff;
+    int bi = j;  // stays in range even when the whole column is NaN
     for (int r = j + tid; r < p; r += blockDim.x) {
       R a = cabs2(F[(int64_t)j * m + r]);
       if (a > best) { best = a; bi = r; }
@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
       int i0 = red_i[0];
       for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
         if (red_v[q] > b0 || (red_v[q] == b0 && red_i[q] < i0)) { b0 = red_v[q]; i0 = red_i[q]; }
+      if (i0 < j || i0 >= p) i0 = j;
       s_piv = i0;
       pv[j] = i0;
     }
