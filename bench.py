@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Frequency-point solves/s at 1e-10 relative residual on one GB300.
+
+Workload: the coupled vibroacoustic sweep -- a 60 x 40 DSG4 aluminium plate
+(0.6 x 0.4 m, t = 2 mm, eta = 0.02, simply supported) on a 60 x 40 x 30 Fluid8
+air cavity (depth 0.3 m), 2,400 InterfaceMindlin quads, unit force at a
+seeded plate node, f = 1..500 Hz (n = 85,034 DOFs). Synthetic, seeded
+(no public dataset exists for this path).
+
+A step solves one batch of `--batch` frequencies of the sweep through the
+mixed path (FP32 fronts + FP64 refinement to ||f - A u|| / ||f|| <= 1e-10);
+the plain FP64 path is timed beside it. `value` is whole-job solves/s with
+inputs resident in HBM; `e2e` is the same metric through elp_solve with host
+buffers (the right-hand side copied in and every solution copied out each step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "freq-point solves/s at 1e-10 rel residual (mixed FP32-front LU + FP64 refinement)"
+UNIT = "solves/s"
+TOL = 1e-10
+
+
+def load_pkg():
+    name = "elpaso_core_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    path = os.path.join(ROOT, "elpaso-core_gb300", "__init__.py")
+    spec = importlib.util.spec_from_file_location(name, path, submodule_search_locations=[os.path.dirname(path)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload(meshes, args):
+    if args.workload == "plate_cavity":
+        return meshes.plate_cavity()
+    if args.workload == "plate_cavity_small":
+        return meshes.plate_cavity(20, 14, 10, 0.6, 0.4, 0.3)
+    raise SystemExit(f"unknown workload {args.workload}")
+
+
+def sweep(rank, world, step, batch):
+    """Frequencies (Hz) of one step on one rank: consecutive blocks of the 1..500 Hz sweep."""
+    base = (step * world + rank) * batch
+    return 1.0 + (np.arange(base, base + batch) % 500)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self, device=0):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9 or f[0] != str(device):
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def cpu_baseline(meshes, args, n_freq=1):
+    """The oracle (CPU restatement of the reference path) timed on this host:
+    per frequency, the reference's per-w element loop (C) + an FP64 sparse LU
+    solve (SciPy SuperLU, standing in for MUMPS which is not available)."""
+    from oracle import oracle as orc
+    d = workload(meshes, args)
+    s = orc.System(d)
+    import scipy.sparse.linalg as sla
+    t0 = time.perf_counter()
+    done = 0
+    for k in range(n_freq):
+        om = 2 * np.pi * (1.0 + 37.0 * k)
+        A = s.matrix(om).tocsc()
+        lu = sla.splu(A)
+        x = lu.solve(s.f)
+        done += 1
+        if time.perf_counter() - t0 > args.cpu_budget_s:
+            break
+    dt = time.perf_counter() - t0
+    res = float(np.linalg.norm(s.f - A @ x) / np.linalg.norm(s.f))
+    return {"value": done / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{done} frequency of the {d.name} sweep: C element loop + SciPy SuperLU FP64 "
+                      f"(MUMPS stand-in), {dt:.1f} s, rel residual {res:.1e}"}
+
+
+def run_ours(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    elp = load_pkg()
+    meshes = importlib.import_module("elpaso_core_gb300.meshes")
+    d = workload(meshes, args)
+    t0 = time.perf_counter()
+    m = elp.Model(d)
+    t_create = time.perf_counter() - t0
+    m.assemble()
+    asm_ms, asm_best = m.time_assembly(3)
+    t0 = time.perf_counter()
+    m.analyse()
+    t_sym = time.perf_counter() - t0
+    info = m.info()
+    n = info["n_dofs"]
+    S = args.batch
+    stream = torch.cuda.current_stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    lib = elp.load_library()
+    rhs = torch.from_numpy(m.rhs().view(np.float64).copy()).cuda()
+    f_dev = rhs.view(1, n * 2).repeat(S, 1).contiguous()
+    x_dev = torch.zeros((S, n * 2), dtype=torch.float64, device="cuda")
+    infos = (elp.SolveInfo * S)()
+
+    def solve_step(step, prec, stats=None):
+        oms = np.ascontiguousarray(2 * np.pi * sweep(rank, world, step, S))
+        rc = lib.elp_solve_device(m.handle, oms.ctypes.data_as(C.c_void_p), S, prec, C.c_void_p(f_dev.data_ptr()),
+                                  C.c_void_p(x_dev.data_ptr()), C.cast(infos, C.c_void_p), TOL, sh)
+        if rc != 0:
+            raise RuntimeError(lib.elp_last_error().decode())
+        if stats is not None:
+            for i in range(S):
+                stats.append(infos[i].rel_residual)
+                stats_it.append(infos[i].iterations)
+
+    def timed(prec, steps, warmup):
+        for w in range(warmup):
+            solve_step(10_000 + w, prec)
+        res = []
+        global stats_it
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(steps):
+            solve_step(k, prec, res)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, res
+
+    global stats_it
+    stats_it = []
+    clocks = Clocks()
+    elp.profile(False)
+    clocks.start()
+    ms_mixed, res_mixed = timed(elp.MIXED, args.steps, args.warmup)
+    clk = clocks.stop(local)
+    launches = elp.profile_read()
+    it_mixed = list(stats_it)
+    stats_it = []
+    plain_steps = max(1, args.plain_steps)
+    ms_plain, res_plain = timed(elp.FP64_PLAIN, plain_steps, 1)
+    it_plain = list(stats_it)
+    value = args.steps * S * world / (ms_mixed / 1e3)
+    plain = plain_steps * S * world / (ms_plain / 1e3)
+
+    # end to end through elp_solve with host buffers
+    f_host = np.ascontiguousarray(np.broadcast_to(m.rhs(), (S, n)))
+    e2e_steps = max(1, args.steps // 2)
+    m.solve(2 * np.pi * sweep(rank, world, 20_000, S), precision=elp.MIXED, f=f_host)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        xh, _ = m.solve(2 * np.pi * sweep(rank, world, k, S), precision=elp.MIXED, f=f_host)
+    e2e_s = time.perf_counter() - t0
+    e2e = e2e_steps * S * world / e2e_s
+
+    # live per-kernel-class timing for the roofline (one profiled step)
+    elp.profile(True)
+    solve_step(0, elp.MIXED)
+    torch.cuda.synchronize()
+    prof = elp.profile_read()
+    elp.profile(False)
+    top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    hbm, bf16, src = peaks()
+    launches_per_step = sum(v["launches"] for v in prof.values())
+    roof = None
+    if top[0] == "gemm" or top[0] == "gemm_tc":
+        flops = info["gemm_flops"] * S
+        ach = flops / (top[1]["ms"] / 1e3) / 1e12
+        roof = {"kernel": top[0], "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                "frac": ach / bf16, "traffic": None,
+                "note": f"algorithmic = Schur-update flops of one factorisation x {S} frequencies; "
+                        f"peak = dense bf16 ({src})"}
+    else:
+        if top[0] in ("forward", "backward"):
+            byts = info["factor_bytes"] * S / 2 * prof[top[0]]["launches"] / max(1, info["n_levels"])
+        else:
+            byts = None
+        ach = byts / (top[1]["ms"] / 1e3) / 1e9 if byts else None
+        roof = {"kernel": top[0], "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": (ach / hbm) if ach else None, "traffic": None, "note": f"peak = copy bandwidth ({src})"}
+    roof["breakdown_ms_per_step"] = {k: round(v["ms"], 3) for k, v in prof.items() if v["launches"]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(importlib.import_module("elpaso_core_gb300.meshes"), args)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 fronts + f64 refinement", "data": "synthetic",
+            "config": {"workload": f"{d.name}: DSG4 60x40 plate + Fluid8 60x40x30 cavity, 1-500 Hz sweep",
+                       "n_dofs": n, "nnz": info["nnz"], "frequencies_per_step": S, "parallelism": f"freq-shard x{world}",
+                       "l2": "inputs larger than L2 (front arena "
+                             f"{info['factor_entries'] * 8 * S / 1e9:.1f} GB per step)",
+                       "fronts": info["n_fronts"], "max_front": info["max_front"], "levels": info["n_levels"],
+                       "factor_gflop": info["factor_flops"] / 1e9},
+            "plain_fp64": {"value": plain, "unit": UNIT, "ms_per_step": ms_plain / plain_steps,
+                           "max_rel_residual": max(res_plain), "iterations": [min(it_plain), max(it_plain)]},
+            "speedup_mixed_vs_plain": value / plain,
+            "max_rel_residual": max(res_mixed), "refine_iterations": [min(it_mixed), max(it_mixed)],
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": S * n * 16, "d2h_bytes_per_step": S * n * 16},
+            "gpu_launches": int(launches_per_step * args.steps),
+            "roofline": roof,
+            "assembly": {"kernel_ms": asm_best, "elements": info["n_elements"], "host_create_s": t_create,
+                         "symbolic_s": t_sym},
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    meshes_mod = None
+    elp = load_pkg()
+    meshes_mod = importlib.import_module("elpaso_core_gb300.meshes")
+    b = cpu_baseline(meshes_mod, args, n_freq=max(1, args.steps))
+    line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "impl": "reference", "data": "synthetic",
+            "config": {"workload": "plate_cavity_60x40x30 sweep (CPU restatement of the reference path)"},
+            "cpu_baseline": b,
+            "e2e": {"value": b["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plate_cavity")
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget-s", type=float, default=30.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -88,7 +88,8 @@ class _Desc(C.Structure):
 class _Info(C.Structure):
     _fields_ = [("n_dofs", C.c_int64), ("nnz", C.c_int64), ("n_elements", C.c_int64), ("n_fronts", C.c_int64),
                 ("factor_entries", C.c_int64), ("factor_flops", C.c_double), ("n_levels", C.c_int),
-                ("max_front", C.c_int), ("n_struct_groups", C.c_int)]
+                ("max_front", C.c_int), ("n_struct_groups", C.c_int), ("gemm_flops", C.c_double),
+                ("factor_bytes", C.c_double)]
 
 
 class SolveInfo(C.Structure):
@@ -116,8 +117,10 @@ EXPORTS = [
     "elp_model_pattern", "elp_model_global_rows", "elp_model_system_values", "elp_model_rhs",
     "elp_solve", "elp_model_destroy", "elp_last_error", "elp_solve_device", "elp_model_time_assembly",
     "elp_server_create", "elp_server_add_model", "elp_server_submit", "elp_server_wait",
-    "elp_server_destroy",
+    "elp_server_destroy", "elp_profile", "elp_profile_read",
 ]
+KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
+                  "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc"]
 
 _lib = None
 
@@ -150,6 +153,8 @@ def load_library(path: str | None = None):
     lib.elp_server_submit.argtypes = [P, C.c_int, P, C.c_int, P, C.POINTER(C.c_int64)]
     lib.elp_server_wait.argtypes = [P, C.POINTER(RequestResult), C.c_double]
     lib.elp_server_destroy.argtypes = [P]
+    lib.elp_profile.argtypes = [C.c_int]
+    lib.elp_profile_read.argtypes = [P, P, P, C.POINTER(C.c_int)]
     if path is None:
         _lib = lib
     return lib
@@ -321,6 +326,21 @@ class Model:
         if rc != 0 and (rc != 6 or raise_on_noconv):
             _check(rc)
         return x, [infos[i].as_dict() for i in range(len(om))]
+
+
+def profile(enable: bool = True):
+    """Resets the launch counters; with enable, times every launch by class."""
+    _check(load_library().elp_profile(int(bool(enable))))
+
+
+def profile_read() -> dict:
+    ms = np.zeros(16)
+    launches = np.zeros(16, np.int64)
+    timed = np.zeros(16, np.int64)
+    nc = C.c_int()
+    _check(load_library().elp_profile_read(_ptr(ms), _ptr(launches), _ptr(timed), C.byref(nc)))
+    return {KERNEL_CLASSES[i]: {"ms": float(ms[i]), "launches": int(launches[i]), "timed": int(timed[i])}
+            for i in range(nc.value)}
 
 
 class Server:

@@ -30,6 +30,7 @@
 #include <cstring>
 
 #include "device.cuh"
+#include "prof.cuh"
 
 namespace elp {
 
@@ -664,10 +665,11 @@ int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms) {
   ELP_CUDA(cudaEventCreate(&e0));
   ELP_CUDA(cudaEventCreate(&e1));
   ELP_CUDA(cudaEventRecord(e0, stream));
-  if (grid > 0) assemble_kernel<<<(unsigned)grid, kThreads, 0, stream>>>(A);
+  if (grid > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, assemble_kernel<<<(unsigned)grid, kThreads, 0, stream>>>(A));
   ELP_CUDA(cudaGetLastError());
   ELP_CUDA(cudaEventRecord(e1, stream));
   ELP_CUDA(cudaEventSynchronize(e1));
+  prof_resolve();
   float ms = 0.f;
   ELP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
   cudaEventDestroy(e0);

@@ -14,9 +14,6 @@
 
 using namespace elp;
 
-struct elp_model {
-  Model m;
-};
 
 namespace elp {
 Model::Model() = default;
@@ -113,12 +110,16 @@ int elp_model_time_assembly(elp_model* h, int repeats, double* ms_per_assembly, 
 int elp_model_analyse(elp_model* h) {
   GUARD_BEGIN
   if (!h) { set_error("null model"); return ELP_ERR_ARG; }
-  int rc = check_cuda_device();
-  if (rc) return rc;
   Model& m = h->m;
   if (m.analysed) return ELP_OK;
-  m.sym.reset(new Symbolic());
-  rc = symbolic_analyse(m, *m.sym, 128);
+  int rc;
+  if (!m.sym) {  // host phase; kept when the device step below fails
+    std::unique_ptr<Symbolic> s(new Symbolic());
+    rc = symbolic_analyse(m, *s, 128);
+    if (rc) return rc;
+    m.sym = std::move(s);
+  }
+  rc = check_cuda_device();
   if (rc) return rc;
   rc = device_upload_symbolic(m);
   if (rc) return rc;
@@ -140,6 +141,8 @@ int elp_model_get_info(const elp_model* h, elp_model_info* info) {
     info->n_fronts = (int64_t)m.sym->fronts.size();
     info->factor_entries = m.sym->arena;
     info->factor_flops = m.sym->flops;
+    info->gemm_flops = m.sym->gemm_flops;
+    info->factor_bytes = m.sym->factor_bytes;
     info->n_levels = m.sym->n_levels;
     info->max_front = m.sym->max_front;
   }

@@ -109,3 +109,8 @@ void set_error(const std::string& s);
 const std::string& get_error();
 
 }  // namespace elp
+
+// the opaque handle of the C ABI
+struct elp_model {
+  elp::Model m;
+};

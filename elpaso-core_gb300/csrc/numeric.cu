@@ -25,6 +25,7 @@
 #include <cstring>
 
 #include "numeric.cuh"
+#include "prof.cuh"
 
 namespace elp {
 
@@ -774,7 +775,7 @@ int numeric_system_values(Model& m, double omega, double2* out_dev) {
   make_coef(m, omega, h);
   ELP_CUDA(c.upload(&h, 1));
   CombineArgs A = combine_args(m);
-  k_values<<<1024, 256>>>(A, c.p, out_dev);
+  PROF_LAUNCH(KC_VALUES, 0, k_values<<<1024, 256>>>(A, c.p, out_dev));
   ELP_CUDA(cudaGetLastError());
   ELP_CUDA(cudaDeviceSynchronize());
   return ELP_OK;
@@ -792,13 +793,13 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   ELP_CUDA(cudaMemsetAsync(w.stats.p, 0, sizeof(unsigned long long) * 4 * S_used, st));
   {
     dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 4096), S_used);
-    k_dscale<<<g, 256, 0, st>>>(A, w.coef.p, G.diag_idx.p, n, w.dscale.p);
+    PROF_LAUNCH(KC_DSCALE, st, k_dscale<<<g, 256, 0, st>>>(A, w.coef.p, G.diag_idx.p, n, w.dscale.p));
   }
   ELP_CUDA(cudaMemsetAsync(w.arena.p, 0, (size_t)S_used * D.arena * sizeof(V), st));
   {
     dim3 g((unsigned)std::min<int64_t>((n + 7) / 8, 8192), S_used);
-    k_scatter<V><<<g, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, D.entry_off.p, w.dscale.p, n, arena,
-                                    D.arena, w.stats.p);
+    PROF_LAUNCH(KC_SCATTER, st, k_scatter<V><<<g, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, D.entry_off.p, w.dscale.p, n, arena,
+                                    D.arena, w.stats.p));
   }
   ELP_CUDA(cudaGetLastError());
   LevelArgs L;
@@ -816,25 +817,25 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     const int steps = (LV.max_p + NB - 1) / NB;
     for (int k = 0; k < steps; ++k) {
       dim3 g1(LV.count, S_used);
-      k_panel<R, NB><<<g1, 256, 0, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p);
+      PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB><<<g1, 256, 0, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p));
       if (LV.max_b > 0) {
         dim3 g2(LV.count, S_used, (unsigned)std::min(65535, (LV.max_b + 127) / 128));
-        k_border<R, NB><<<g2, 128, 0, st>>>(L, arena, k);
+        PROF_LAUNCH(KC_BORDER, st, k_border<R, NB><<<g2, 128, 0, st>>>(L, arena, k));
       }
       const int rest = LV.max_m - k * NB - 1;
       if (rest > 0) {
         dim3 g3(LV.count, S_used, (unsigned)std::min(65535, (rest + 127) / 128));
-        k_urow<R, NB><<<g3, 128, 0, st>>>(L, arena, k);
+        PROF_LAUNCH(KC_UROW, st, k_urow<R, NB><<<g3, 128, 0, st>>>(L, arena, k));
         const int tr = (rest + 63) / 64;
         dim3 g4(LV.count, S_used, (unsigned)std::min(65535, tr * tr));
-        k_gemm<R, NB><<<g4, 256, 0, st>>>(L, arena, k);
+        PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB><<<g4, 256, 0, st>>>(L, arena, k));
       }
     }
     for (size_t k = 0; k < LV.ea_count.size(); ++k) {
       if (!LV.ea_count[k]) continue;
       dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, LV.ea_max_b));
-      k_extend_add<R><<<g5, 256, 0, st>>>(D.ea_list.p + LV.ea_start[k], D.f_p.p, D.f_b.p, D.f_parent.p, D.f_map_off.p,
-                                          D.f_off.p, D.parent_map.p, arena, D.arena);
+      PROF_LAUNCH(KC_EXTEND_ADD, st, k_extend_add<R><<<g5, 256, 0, st>>>(D.ea_list.p + LV.ea_start[k], D.f_p.p, D.f_b.p, D.f_parent.p, D.f_map_off.p,
+                                          D.f_off.p, D.parent_map.p, arena, D.arena));
     }
   }
   ELP_CUDA(cudaGetLastError());
@@ -869,14 +870,14 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st) {
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
     size_t sm = (size_t)LV.max_m * sizeof(V);
-    k_forward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, w.perm.p, z, cb);
+    PROF_LAUNCH(KC_FORWARD, st, k_forward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, w.perm.p, z, cb));
   }
   for (int l = (int)D.levels.size() - 1; l >= 0; --l) {
     const auto& LV = D.levels[l];
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
     size_t sm = (size_t)LV.max_m * sizeof(V);
-    k_backward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, z);
+    PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, z));
   }
   ELP_CUDA(cudaGetLastError());
   return ELP_OK;
@@ -910,18 +911,18 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
   int it = 0;
   float solve_ms = 0.f, refine_ms = 0.f;
   // initial residual r = f (x = 0)
-  k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p, w.r.p, w.partial.p,
-                                 w.nparts, w.active.p);
+  PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p, w.r.p, w.partial.p,
+                                 w.nparts, w.active.p));
   for (it = 0; it < max_iter; ++it) {
     ELP_CUDA(cudaEventRecord(w.ev[2], st));
-    k_rhs<V><<<gv, 256, 0, st>>>(w.r.p, w.dscale.p, n, reinterpret_cast<V*>(w.z.p), w.active.p);
+    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(w.r.p, w.dscale.p, n, reinterpret_cast<V*>(w.z.p), w.active.p));
     rc = solve_sweep<R>(m, w, S_used, st);
     if (rc) return rc;
-    k_update<V><<<gv, 256, 0, st>>>(w.x.p, w.dscale.p, n, reinterpret_cast<const V*>(w.z.p), w.active.p);
+    PROF_LAUNCH(KC_UPDATE, st, k_update<V><<<gv, 256, 0, st>>>(w.x.p, w.dscale.p, n, reinterpret_cast<const V*>(w.z.p), w.active.p));
     ELP_CUDA(cudaEventRecord(w.ev[3], st));
-    k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p, w.r.p, w.partial.p,
-                                   w.nparts, w.active.p);
-    k_norms<<<S_used, 256, 0, st>>>(w.partial.p, w.nparts, w.norms.p, w.active.p);
+    PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p, w.r.p, w.partial.p,
+                                   w.nparts, w.active.p));
+    PROF_LAUNCH(KC_NORMS, st, k_norms<<<S_used, 256, 0, st>>>(w.partial.p, w.nparts, w.norms.p, w.active.p));
     ELP_CUDA(cudaMemcpyAsync(w.h_norms, w.norms.p, sizeof(double) * 2 * S_used, cudaMemcpyDeviceToHost, st));
     ELP_CUDA(cudaEventRecord(w.ev[4], st));
     ELP_CUDA(cudaEventSynchronize(w.ev[4]));
@@ -976,6 +977,7 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
   ELP_CUDA(cudaMemcpyAsync(x_dev, w.x.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToDevice, st));
   ELP_CUDA(cudaMemcpyAsync(w.h_stats, w.stats.p, sizeof(unsigned long long) * 4 * n_omega, cudaMemcpyDeviceToHost, st));
   ELP_CUDA(cudaStreamSynchronize(st));
+  prof_resolve();
   bool ok = true;
   for (int s = 0; s < n_omega; ++s) {
     double fn = w.h_norms[2 * s + 1];

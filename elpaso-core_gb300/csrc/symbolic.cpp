@@ -250,6 +250,14 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
       double r = (double)(mm - k - 1);
       flops += 8.0 * r * r + 8.0 * r;
     }
+    // trailing updates of the blocked LU (panel width 32): rows/cols t0..m-1, depth w
+    for (int k0 = 0; k0 < p; k0 += 32) {
+      const int w = std::min(32, p - k0);
+      const double t = (double)(mm - k0 - w);
+      S.gemm_flops += 8.0 * t * t * w;
+    }
+    // factors read by one forward + backward sweep: L (m x p) and U12 (p x b), complex FP32
+    S.factor_bytes += 8.0 * ((double)mm * p + (double)p * b);
     if (S.front_dofs.size() > (size_t)INT32_MAX) { set_error("front index lists too large"); return ELP_ERR_NOMEM; }
   }
   S.arena = arena;

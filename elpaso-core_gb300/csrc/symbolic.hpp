@@ -34,6 +34,8 @@ struct Symbolic {
   int64_t arena = 0;                   // sum of m^2
   int64_t cb_total = 0;                // sum of b
   double flops = 0.0;                  // real flops of one complex factorisation
+  double gemm_flops = 0.0;             // of which trailing (Schur) updates
+  double factor_bytes = 0.0;           // factor bytes read per forward + backward sweep (FP32)
 };
 
 // Geometric nested dissection on the node graph; leaf_dofs bounds leaf size.

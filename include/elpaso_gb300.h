@@ -131,6 +131,8 @@ typedef struct {
   int n_levels;
   int max_front;
   int n_struct_groups;      /* distinct loss-factor groups of structure K     */
+  double gemm_flops;        /* real flops of the Schur (trailing) updates of one factorisation */
+  double factor_bytes;      /* bytes of the factors read by one forward+backward sweep, FP32 fronts */
 } elp_model_info;
 
 /* precision of the numeric factorisation */
@@ -205,6 +207,20 @@ int elp_solve_device(elp_model* m, const double* omegas, int n_omega, int precis
  * timing: returns the device time of the assembly kernel(s) in ms. */
 int elp_model_time_assembly(elp_model* m, int repeats, double* ms_per_assembly,
                             double* ms_kernel_only);
+
+/* ---- launch counting and per-kernel device timing ---------------------- */
+
+/* Kernel classes, in the order of the arrays below:
+ *  0 assemble, 1 dscale, 2 scatter, 3 panel, 4 border, 5 urow, 6 gemm,
+ *  7 extend_add, 8 forward, 9 backward, 10 residual, 11 norms, 12 rhs,
+ *  13 update, 14 values, 15 gemm_tc.
+ * No reference counterpart (the reference times whole phases with
+ * cStopwatch, basics/watch/stopwatch.cpp:35-64). elp_profile(1) resets the
+ * counters and records a CUDA event pair around every launch on its stream;
+ * elp_profile(0) resets and counts launches only. */
+int elp_profile(int enable);
+int elp_profile_read(double* ms /* [16] */, int64_t* launches /* [16] */, int64_t* timed /* [16] */,
+                     int* n_classes);
 
 /* ---- serving loop (continuous batching over resident models) ------------ */
 

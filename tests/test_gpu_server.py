@@ -1,0 +1,89 @@
+"""Serving loop on the GPU: continuous batching over resident models.
+
+- a request's result is the same alone and in a mix of concurrent requests
+  on several models (tolerance: relative difference <= 1e-12; the kernels
+  compute each frequency slot independently, so equality is expected);
+- every result meets the 1e-10 relative residual (checked by the oracle);
+- a model that does not fit the HBM budget fails its requests with
+  ELP_ERR_NOMEM (status 3) while the others complete.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+SAME_TOL = 1e-12
+
+
+def _models(elp, meshes):
+    ds = [meshes.plate(16, 12, 0.6, 0.4, 0.002), meshes.plate_cavity(8, 6, 4, 0.6, 0.4, 0.3), meshes.cube(5)]
+    return ds, [elp.Model(d) for d in ds]
+
+
+def _run(srv, reqs, n_of):
+    outs = {}
+    ids = {}
+    for key, (mid, oms) in reqs.items():
+        x = np.zeros((len(oms), n_of[mid]), np.complex128)
+        rid = srv.submit(mid, oms, x)
+        ids[rid] = key
+        outs[key] = x
+    res = {}
+    for _ in range(len(reqs)):
+        r = srv.wait(60000.0)
+        res[ids[r["request_id"]]] = r
+    return outs, res
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_alone_equals_in_mix(elp, meshes, oracle, prec):
+    ds, ms = _models(elp, meshes)
+    srv = elp.Server(hbm_budget_bytes=8 << 30, max_inflight=3, precision=prec, tol=1e-10, omega_batch=4)
+    mids = [srv.add_model(m) for m in ms]
+    n_of = {mid: ms[i].n for i, mid in enumerate(mids)}
+    probe = (mids[1], 2 * np.pi * np.array([17.0, 140.0, 333.0]))
+    alone, res = _run(srv, {"probe": probe}, n_of)
+    assert res["probe"]["status"] == 0
+    rng = np.random.default_rng(7)
+    mix = {"probe": probe}
+    for k in range(9):
+        mid = mids[k % 3]
+        mix[f"r{k}"] = (mid, 2 * np.pi * rng.uniform(1.0, 500.0, size=int(rng.integers(1, 7))))
+    outs, res = _run(srv, mix, n_of)
+    for key, r in res.items():
+        assert r["status"] == 0, (key, r)
+        assert r["max_rel_residual"] <= 1e-10
+        assert r["latency_ms"] > 0
+    diff = np.max(np.abs(outs["probe"] - alone["probe"])) / np.max(np.abs(alone["probe"]))
+    assert diff <= SAME_TOL
+    # the oracle confirms the residual of a mixed-in result
+    s = oracle.System(ds[1])
+    A = s.matrix(probe[1][1])
+    assert np.linalg.norm(s.f - A @ outs["probe"][1]) / np.linalg.norm(s.f) <= 1e-10
+    srv.close()
+
+
+def test_budget_admission(elp, meshes):
+    small = elp.Model(meshes.plate(8, 8, 0.3, 0.3, 0.002))
+    big = elp.Model(meshes.cube(10))
+    srv = elp.Server(hbm_budget_bytes=24 << 20, max_inflight=2, precision=1, tol=1e-10, omega_batch=4)
+    a = srv.add_model(small)
+    b = srv.add_model(big)
+    xa = np.zeros((2, small.n), np.complex128)
+    xb = np.zeros((2, big.n), np.complex128)
+    ra = srv.submit(a, 2 * np.pi * np.array([10.0, 20.0]), xa)
+    rb = srv.submit(b, 2 * np.pi * np.array([10.0, 20.0]), xb)
+    got = {}
+    for _ in range(2):
+        r = srv.wait(60000.0)
+        got[r["request_id"]] = r
+    assert got[ra]["status"] == 0
+    assert got[rb]["status"] == 3
+    srv.close()
+
+
+def test_wait_times_out_without_work(elp):
+    srv = elp.Server(hbm_budget_bytes=1 << 30, max_inflight=1, precision=1)
+    with pytest.raises(elp.ElpasoError) as e:
+        srv.wait(50.0)
+    assert e.value.code == 8
+    srv.close()

@@ -1,14 +1,27 @@
 """Per-frequency solve on the GPU (plain FP64 and mixed FP32 fronts + FP64
 refinement) against the FP64 direct-solve oracle (SciPy SuperLU on the
-oracle's own CSR). Bar: relative residual <= 1e-10 measured by the oracle's
-matrix, and relative error vs the oracle <= 1e-7 (both paths)."""
+oracle's own CSR).
+
+Bars: relative residual ||f - A x||_2 / ||f||_2 <= 1e-10, measured with the
+ORACLE's matrix; relative error vs the oracle's solution within what the
+residual allows, ||x - x_ref|| / ||x_ref|| <= 4 * kappa_1(A) * 1e-10 (kappa_1
+estimated with onenormest; thin-hex and near-resonance systems reach 1e7+)."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+RES_TOL = 1e-10
 
 
-def check(elp, oracle, d, f_list, prec, err_tol=1e-7):
+def cond1(A):
+    import scipy.sparse.linalg as sla
+    lu = sla.splu(A.tocsc())
+    n = A.shape[0]
+    inv = sla.LinearOperator((n, n), matvec=lu.solve, rmatvec=lambda b: lu.solve(b, trans="H"), dtype=complex)
+    return sla.onenormest(A) * sla.onenormest(inv)
+
+
+def check(elp, oracle, d, f_list, prec):
     m = elp.Model(d).assemble().analyse()
     s = oracle.System(d)
     oms = 2 * np.pi * np.asarray(f_list, float)
@@ -18,8 +31,8 @@ def check(elp, oracle, d, f_list, prec, err_tol=1e-7):
         res = np.linalg.norm(s.f - A @ x[k]) / np.linalg.norm(s.f)
         xr = s.solve(om)
         err = np.linalg.norm(x[k] - xr) / np.linalg.norm(xr)
-        assert res <= 1e-10, (k, res)
-        assert err <= err_tol, (k, err)
+        assert res <= RES_TOL, (k, res)
+        assert err <= max(1e-12, 4.0 * cond1(A) * RES_TOL), (k, err)
         assert infos[k]["converged"] == 1
         assert abs(infos[k]["rel_residual"] - res) <= 1e-10
     return m, infos
