@@ -596,15 +596,15 @@ __global__ void k_norms(const double* __restrict__ partial, int nparts, double* 
   if (threadIdx.x == 0) { norms[2 * s] = a[0]; norms[2 * s + 1] = b[0]; }
 }
 
-// z = D r in front precision
+// z = D r in front precision (r of slot s at r + s * sstride)
 template <class V>
-__global__ void k_rhs(const double2* __restrict__ r, const double* __restrict__ dscale, int64_t n, V* __restrict__ z,
-                      const int* __restrict__ active) {
+__global__ void k_rhs(const double2* __restrict__ r, int64_t sstride, const double* __restrict__ dscale, int64_t n,
+                      V* __restrict__ z, const int* __restrict__ active) {
   const int s = blockIdx.y;
   if (!active[s]) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double d = dscale[s * n + i];
-    double2 v = r[s * n + i];
+    double2 v = r[s * sstride + i];
     z[s * n + i] = cmk<V>(v.x * d, v.y * d);
   }
 }
@@ -625,12 +625,161 @@ __global__ void k_update(double2* __restrict__ x, const double* __restrict__ dsc
   }
 }
 
+// ------------------------------------------------------------- GMRES (FP64)
+// Right-preconditioned restarted GMRES on A(w) x = f, preconditioner
+// M^-1 = D (LU)^-1 D with the front-precision factors. The Arnoldi vectors,
+// the SpMV and the orthogonalisation (classical Gram-Schmidt, twice) are
+// FP64; only the preconditioner solve runs in the front precision.
+constexpr int kMaxBasis = 32;
+
+// w = A u (FP64, unscaled A)
+__global__ void k_spmv(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ row_ptr,
+                       const int32_t* __restrict__ col_idx, int64_t n, const double2* __restrict__ u,
+                       double2* __restrict__ w, const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  const Coef c = coef[s];
+  const int lane = threadIdx.x & 31;
+  const double2* us = u + s * n;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    double sx = 0.0, sy = 0.0;
+    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
+      double2 a = combine(A, c, q);
+      double2 v = us[col_idx[q]];
+      sx += a.x * v.x - a.y * v.y;
+      sy += a.x * v.y + a.y * v.x;
+    }
+    for (int o = 16; o; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    }
+    if (lane == 0) w[s * n + i] = make_double2(sx, sy);
+  }
+}
+
+// partial[s][block][i] = sum_r conj(V_i[r]) w[r], V_i = basis + s*sstride + i*vstride
+__global__ void k_dots(const double2* __restrict__ basis, int64_t sstride, int64_t vstride, int nv,
+                       const double2* __restrict__ w, int64_t n, double2* __restrict__ partial, int nparts,
+                       const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  __shared__ double red[2][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const double2* ws = w + s * n;
+  for (int i = 0; i < nv; ++i) {
+    const double2* v = basis + s * sstride + (int64_t)i * vstride;
+    double ax = 0.0, ay = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+      double2 a = v[r], b = ws[r];
+      ax += a.x * b.x + a.y * b.y;
+      ay += a.x * b.y - a.y * b.x;
+    }
+    for (int o = 16; o; o >>= 1) {
+      ax += __shfl_xor_sync(0xffffffffu, ax, o);
+      ay += __shfl_xor_sync(0xffffffffu, ay, o);
+    }
+    if (lane == 0) { red[0][wid] = ax; red[1][wid] = ay; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tx = 0, ty = 0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { tx += red[0][q]; ty += red[1][q]; }
+      partial[((int64_t)s * nparts + blockIdx.x) * kMaxBasis + i] = make_double2(tx, ty);
+    }
+    __syncthreads();
+  }
+}
+
+// h[s][i] = sum over blocks (fixed order)
+__global__ void k_dots_reduce(const double2* __restrict__ partial, int nparts, int nv, double2* __restrict__ h,
+                              const int* __restrict__ active) {
+  const int s = blockIdx.x;
+  if (!active[s]) return;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    double tx = 0, ty = 0;
+    for (int b = 0; b < nparts; ++b) {
+      double2 v = partial[((int64_t)s * nparts + b) * kMaxBasis + i];
+      tx += v.x;
+      ty += v.y;
+    }
+    h[s * kMaxBasis + i] = make_double2(tx, ty);
+  }
+}
+
+// w -= sum_i h_i V_i ; accumulates h into hsum
+__global__ void k_gs(const double2* __restrict__ basis, int64_t sstride, int64_t vstride, int nv,
+                     const double2* __restrict__ h, double2* __restrict__ w, int64_t n, const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  __shared__ double2 hs[kMaxBasis];
+  if (threadIdx.x < nv) hs[threadIdx.x] = h[s * kMaxBasis + threadIdx.x];
+  __syncthreads();
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 t = w[s * n + r];
+    for (int i = 0; i < nv; ++i) {
+      double2 v = basis[s * sstride + (int64_t)i * vstride + r];
+      t.x -= hs[i].x * v.x - hs[i].y * v.y;
+      t.y -= hs[i].x * v.y + hs[i].y * v.x;
+    }
+    w[s * n + r] = t;
+  }
+}
+
+// dst = src * scale[s] (real scale from the host)
+__global__ void k_vscale(const double2* __restrict__ src, double2* __restrict__ dst, int64_t sstride_dst,
+                         const double* __restrict__ scale, int64_t n, const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  const double a = scale[s];
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 v = src[s * n + r];
+    dst[s * sstride_dst + r] = make_double2(v.x * a, v.y * a);
+  }
+}
+
+// t = sum_i y_i V_i
+__global__ void k_combo(const double2* __restrict__ basis, int64_t sstride, int64_t vstride, int nv,
+                        const double2* __restrict__ y, double2* __restrict__ t, int64_t n, const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  __shared__ double2 ys[kMaxBasis];
+  if (threadIdx.x < nv) ys[threadIdx.x] = y[s * kMaxBasis + threadIdx.x];
+  __syncthreads();
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double ax = 0, ay = 0;
+    for (int i = 0; i < nv; ++i) {
+      double2 v = basis[s * sstride + (int64_t)i * vstride + r];
+      ax += ys[i].x * v.x - ys[i].y * v.y;
+      ay += ys[i].x * v.y + ys[i].y * v.x;
+    }
+    t[s * n + r] = make_double2(ax, ay);
+  }
+}
+
+// u = D z (front precision -> FP64)
+template <class V>
+__global__ void k_unscale(const V* __restrict__ z, const double* __restrict__ dscale, int64_t n, double2* __restrict__ u,
+                          const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double d = dscale[s * n + i];
+    V v = z[s * n + i];
+    u[s * n + i] = make_double2(d * (double)v.x, d * (double)v.y);
+  }
+}
+
 // ------------------------------------------------------------- host side
 Workspace::~Workspace() {
   if (h_coef) cudaFreeHost(h_coef);
   if (h_norms) cudaFreeHost(h_norms);
   if (h_active) cudaFreeHost(h_active);
   if (h_stats) cudaFreeHost(h_stats);
+  if (h_h) cudaFreeHost(h_h);
+  if (h_y) cudaFreeHost(h_y);
+  if (h_scal) cudaFreeHost(h_scal);
+  if (h_inner) cudaFreeHost(h_inner);
   if (stream) {
     for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
     cudaStreamDestroy(stream);
@@ -843,7 +992,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
 }
 
 template <class R>
-static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st) {
+static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, const int* mask) {
   using V = typename Vec2<R>::T;
   DeviceSymbolic& D = *m.dsym;
   SolveArgs S;
@@ -861,7 +1010,7 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st) {
   S.arena_size = D.arena;
   S.n = m.n;
   S.cb_total = std::max<int64_t>(1, D.cb_total);
-  S.active = w.active.p;
+  S.active = mask;
   const V* arena = reinterpret_cast<const V*>(w.arena.p);
   V* z = reinterpret_cast<V*>(w.z.p);
   V* cb = reinterpret_cast<V*>(w.cb.p);
@@ -899,7 +1048,7 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
     set_error("front larger than the shared-memory solve buffer (max 227 KB)");
     return ELP_ERR_NOMEM;
   }
-  for (int s = 0; s < S_used; ++s) w.h_active[s] = 1;
+  for (int s = 0; s < S_used; ++s) { w.h_active[s] = 1; w.iters[s] = 0; }
   ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
   ELP_CUDA(cudaEventRecord(w.ev[0], st));
   int rc = factor_and_setup<R>(m, w, S_used, st);
@@ -915,8 +1064,8 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
                                  w.nparts, w.active.p));
   for (it = 0; it < max_iter; ++it) {
     ELP_CUDA(cudaEventRecord(w.ev[2], st));
-    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(w.r.p, w.dscale.p, n, reinterpret_cast<V*>(w.z.p), w.active.p));
-    rc = solve_sweep<R>(m, w, S_used, st);
+    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(w.r.p, n, w.dscale.p, n, reinterpret_cast<V*>(w.z.p), w.active.p));
+    rc = solve_sweep<R>(m, w, S_used, st, w.active.p);
     if (rc) return rc;
     PROF_LAUNCH(KC_UPDATE, st, k_update<V><<<gv, 256, 0, st>>>(w.x.p, w.dscale.p, n, reinterpret_cast<const V*>(w.z.p), w.active.p));
     ELP_CUDA(cudaEventRecord(w.ev[3], st));
@@ -932,10 +1081,13 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
     solve_ms += a;
     refine_ms += b;
     bool all = true, changed = false;
+    static const bool trace = getenv("ELP_TRACE") != nullptr;
     for (int s = 0; s < S_used; ++s) {
       if (!w.h_active[s]) continue;
+      w.iters[s]++;
       double fn = w.h_norms[2 * s + 1];
       double rel = fn > 0 ? std::sqrt(w.h_norms[2 * s] / fn) : std::sqrt(w.h_norms[2 * s]);
+      if (trace) fprintf(stderr, "[elp] it %d slot %d rel_residual %.3e\n", it, s, rel);
       if (rel <= tol || !std::isfinite(rel)) { w.h_active[s] = 0; changed = true; }
       else all = false;
     }
@@ -948,6 +1100,205 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
   ms[1] = solve_ms;
   ms[2] = refine_ms;
   *iters = it;
+  return ELP_OK;
+}
+
+static int gmres_alloc(Workspace& w, int64_t n, int S, int rst) {
+  if (w.rst == rst && w.Vb.p) return ELP_OK;
+  w.rst = rst;
+  ELP_CUDA(w.Vb.alloc((size_t)S * (rst + 1) * n));
+  ELP_CUDA(w.wv.alloc((size_t)S * n));
+  ELP_CUDA(w.uv.alloc((size_t)S * n));
+  ELP_CUDA(w.tv.alloc((size_t)S * n));
+  ELP_CUDA(w.hd1.alloc((size_t)S * kMaxBasis));
+  ELP_CUDA(w.hd2.alloc((size_t)S * kMaxBasis));
+  ELP_CUDA(w.hnd.alloc((size_t)S * kMaxBasis));
+  ELP_CUDA(w.ydev.alloc((size_t)S * kMaxBasis));
+  ELP_CUDA(w.dpart.alloc((size_t)S * w.nparts * kMaxBasis));
+  ELP_CUDA(w.scal.alloc(S));
+  ELP_CUDA(w.inner.alloc(S));
+  if (!w.h_h) ELP_CUDA(cudaMallocHost((void**)&w.h_h, sizeof(double2) * 3 * S * kMaxBasis));
+  if (!w.h_y) ELP_CUDA(cudaMallocHost((void**)&w.h_y, sizeof(double2) * S * kMaxBasis));
+  if (!w.h_scal) ELP_CUDA(cudaMallocHost((void**)&w.h_scal, sizeof(double) * S));
+  if (!w.h_inner) ELP_CUDA(cudaMallocHost((void**)&w.h_inner, sizeof(int) * S));
+  return ELP_OK;
+}
+
+// GMRES-IR: restarted right-preconditioned GMRES in FP64 with the
+// front-precision factors as preconditioner (used for the mixed path, where
+// plain refinement stalls once kappa(A) * eps_fp32 approaches 1).
+template <class R>
+static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cycles, cudaStream_t st, float* ms) {
+  using V = typename Vec2<R>::T;
+  typedef std::complex<double> cd;
+  const int64_t n = m.n;
+  DeviceModel& G = *m.dev;
+  CombineArgs A = combine_args(m);
+  const size_t smem_need = (size_t)m.dsym->max_front * sizeof(V);
+  if (smem_need > 227 * 1024) {
+    set_error("front larger than the shared-memory solve buffer (max 227 KB)");
+    return ELP_ERR_NOMEM;
+  }
+  if (smem_need > 48 * 1024) {
+    ELP_CUDA(cudaFuncSetAttribute(k_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+    ELP_CUDA(cudaFuncSetAttribute(k_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+  }
+  const int RST = 24;
+  int rc = gmres_alloc(w, n, w.slots, RST);
+  if (rc) return rc;
+  const int64_t vst = (int64_t)(RST + 1) * n;  // slot stride of the basis
+  for (int s = 0; s < S_used; ++s) { w.h_active[s] = 1; w.iters[s] = 0; }
+  ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+  ELP_CUDA(cudaEventRecord(w.ev[0], st));
+  rc = factor_and_setup<R>(m, w, S_used, st);
+  if (rc) return rc;
+  ELP_CUDA(cudaEventRecord(w.ev[1], st));
+  ELP_CUDA(cudaMemsetAsync(w.x.p, 0, sizeof(double2) * S_used * n, st));
+  const dim3 gv((unsigned)std::min<int64_t>((n + 255) / 256, 4096), S_used);
+  const dim3 gr((unsigned)w.nparts, S_used);
+  V* z = reinterpret_cast<V*>(w.z.p);
+  static const bool trace = getenv("ELP_TRACE") != nullptr;
+  std::vector<double> fn(S_used), rel(S_used);
+  auto residual = [&]() -> int {
+    PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p,
+                                                                   w.r.p, w.partial.p, w.nparts, w.active.p));
+    PROF_LAUNCH(KC_NORMS, st, k_norms<<<S_used, 256, 0, st>>>(w.partial.p, w.nparts, w.norms.p, w.active.p));
+    ELP_CUDA(cudaMemcpyAsync(w.h_norms, w.norms.p, sizeof(double) * 2 * S_used, cudaMemcpyDeviceToHost, st));
+    ELP_CUDA(cudaStreamSynchronize(st));
+    for (int s = 0; s < S_used; ++s) {
+      if (!w.h_active[s]) continue;
+      fn[s] = std::sqrt(w.h_norms[2 * s + 1]);
+      rel[s] = fn[s] > 0 ? std::sqrt(w.h_norms[2 * s]) / fn[s] : std::sqrt(w.h_norms[2 * s]);
+    }
+    return ELP_OK;
+  };
+  auto precond = [&](const double2* src, int64_t sstride, const int* mask) -> int {
+    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(src, sstride, w.dscale.p, n, z, mask));
+    return solve_sweep<R>(m, w, S_used, st, mask);
+  };
+  rc = residual();
+  if (rc) return rc;
+  std::vector<std::vector<cd>> H(S_used, std::vector<cd>((RST + 1) * RST));
+  std::vector<std::vector<cd>> g(S_used, std::vector<cd>(RST + 1)), sn(S_used, std::vector<cd>(RST));
+  std::vector<std::vector<double>> cs(S_used, std::vector<double>(RST));
+  std::vector<int> ncol(S_used);
+  float solve_ms = 0.f;
+  for (int cycle = 0; cycle < max_cycles; ++cycle) {
+    bool any = false;
+    for (int s = 0; s < S_used; ++s) {
+      if (w.h_active[s] && (rel[s] <= tol || !std::isfinite(rel[s]))) w.h_active[s] = 0;
+      any |= w.h_active[s] != 0;
+      w.h_inner[s] = w.h_active[s];
+      w.h_scal[s] = w.h_active[s] ? 1.0 / (rel[s] * fn[s]) : 0.0;
+      ncol[s] = 0;
+      if (w.h_active[s]) {
+        std::fill(g[s].begin(), g[s].end(), cd(0));
+        g[s][0] = rel[s] * fn[s];
+      }
+      if (trace && w.h_active[s]) fprintf(stderr, "[elp] gmres cycle %d slot %d rel_residual %.3e\n", cycle, s, rel[s]);
+    }
+    if (!any) break;
+    ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+    ELP_CUDA(cudaMemcpyAsync(w.inner.p, w.h_inner, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+    ELP_CUDA(cudaMemcpyAsync(w.scal.p, w.h_scal, sizeof(double) * S_used, cudaMemcpyHostToDevice, st));
+    k_vscale<<<gv, 256, 0, st>>>(w.r.p, w.Vb.p, vst, w.scal.p, n, w.inner.p);
+    for (int j = 0; j < RST; ++j) {
+      ELP_CUDA(cudaEventRecord(w.ev[2], st));
+      rc = precond(w.Vb.p + (int64_t)j * n, vst, w.inner.p);
+      if (rc) return rc;
+      ELP_CUDA(cudaEventRecord(w.ev[3], st));
+      k_unscale<V><<<gv, 256, 0, st>>>(z, w.dscale.p, n, w.uv.p, w.inner.p);
+      PROF_LAUNCH(KC_RESIDUAL, st, k_spmv<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.uv.p, w.wv.p,
+                                                                 w.inner.p));
+      const int nv = j + 1;
+      k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p);
+      k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd1.p, w.inner.p);
+      k_gs<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.hd1.p, w.wv.p, n, w.inner.p);
+      k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p);
+      k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd2.p, w.inner.p);
+      k_gs<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.hd2.p, w.wv.p, n, w.inner.p);
+      k_dots<<<gr, 256, 0, st>>>(w.wv.p, n, 0, 1, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p);
+      k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, 1, w.hnd.p, w.inner.p);
+      ELP_CUDA(cudaMemcpyAsync(w.h_h, w.hd1.p, sizeof(double2) * S_used * kMaxBasis, cudaMemcpyDeviceToHost, st));
+      ELP_CUDA(cudaMemcpyAsync(w.h_h + S_used * kMaxBasis, w.hd2.p, sizeof(double2) * S_used * kMaxBasis,
+                               cudaMemcpyDeviceToHost, st));
+      ELP_CUDA(cudaMemcpyAsync(w.h_h + 2 * S_used * kMaxBasis, w.hnd.p, sizeof(double2) * S_used * kMaxBasis,
+                               cudaMemcpyDeviceToHost, st));
+      ELP_CUDA(cudaStreamSynchronize(st));
+      float a = 0.f;
+      cudaEventElapsedTime(&a, w.ev[2], w.ev[3]);
+      solve_ms += a;
+      bool more = false;
+      for (int s = 0; s < S_used; ++s) {
+        if (!w.h_inner[s]) continue;
+        w.iters[s]++;
+        cd* Hs = H[s].data();  // column-major (RST + 1) x RST
+        for (int i = 0; i <= j; ++i) {
+          double2 h1 = w.h_h[s * kMaxBasis + i], h2 = w.h_h[(S_used + s) * kMaxBasis + i];
+          Hs[j * (RST + 1) + i] = cd(h1.x + h2.x, h1.y + h2.y);
+        }
+        const double hn = std::sqrt(std::max(0.0, w.h_h[(2 * S_used + s) * kMaxBasis].x));
+        Hs[j * (RST + 1) + j + 1] = cd(hn, 0.0);
+        for (int i = 0; i < j; ++i) {  // previous rotations
+          cd a0 = Hs[j * (RST + 1) + i], b0 = Hs[j * (RST + 1) + i + 1];
+          Hs[j * (RST + 1) + i] = cs[s][i] * a0 + sn[s][i] * b0;
+          Hs[j * (RST + 1) + i + 1] = -std::conj(sn[s][i]) * a0 + cs[s][i] * b0;
+        }
+        cd a0 = Hs[j * (RST + 1) + j], b0 = Hs[j * (RST + 1) + j + 1];
+        double rho = std::sqrt(std::norm(a0) + std::norm(b0));
+        if (std::abs(a0) == 0.0) { cs[s][j] = 0.0; sn[s][j] = cd(1.0, 0.0); }
+        else {
+          cs[s][j] = std::abs(a0) / rho;
+          sn[s][j] = (a0 / std::abs(a0)) * std::conj(b0) / rho;
+        }
+        Hs[j * (RST + 1) + j] = cs[s][j] * a0 + sn[s][j] * b0;
+        Hs[j * (RST + 1) + j + 1] = 0.0;
+        g[s][j + 1] = -std::conj(sn[s][j]) * g[s][j];
+        g[s][j] = cs[s][j] * g[s][j];
+        ncol[s] = j + 1;
+        const double est = std::abs(g[s][j + 1]) / fn[s];
+        if (trace) fprintf(stderr, "[elp]   arnoldi %d slot %d estimate %.3e\n", j, s, est);
+        if (est <= 0.25 * tol || hn <= 1e-300 || j == RST - 1 || !std::isfinite(est)) w.h_inner[s] = 0;
+        else more = true;
+        w.h_scal[s] = hn > 0 ? 1.0 / hn : 0.0;
+      }
+      ELP_CUDA(cudaMemcpyAsync(w.scal.p, w.h_scal, sizeof(double) * S_used, cudaMemcpyHostToDevice, st));
+      k_vscale<<<gv, 256, 0, st>>>(w.wv.p, w.Vb.p + (int64_t)(j + 1) * n, vst, w.scal.p, n, w.inner.p);
+      ELP_CUDA(cudaMemcpyAsync(w.inner.p, w.h_inner, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+      if (!more) break;
+    }
+    // x += M^-1 V y
+    int nvmax = 0;
+    for (int s = 0; s < S_used; ++s) {
+      for (int i = 0; i < kMaxBasis; ++i) w.h_y[s * kMaxBasis + i] = make_double2(0, 0);
+      if (!w.h_active[s]) continue;
+      const int k = ncol[s];
+      nvmax = std::max(nvmax, k);
+      std::vector<cd> y(k);
+      const cd* Hs = H[s].data();
+      for (int i = k - 1; i >= 0; --i) {
+        cd t = g[s][i];
+        for (int c = i + 1; c < k; ++c) t -= Hs[c * (RST + 1) + i] * y[c];
+        y[i] = t / Hs[i * (RST + 1) + i];
+      }
+      for (int i = 0; i < k; ++i) w.h_y[s * kMaxBasis + i] = make_double2(y[i].real(), y[i].imag());
+    }
+    ELP_CUDA(cudaMemcpyAsync(w.ydev.p, w.h_y, sizeof(double2) * S_used * kMaxBasis, cudaMemcpyHostToDevice, st));
+    k_combo<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nvmax, w.ydev.p, w.tv.p, n, w.active.p);
+    rc = precond(w.tv.p, n, w.active.p);
+    if (rc) return rc;
+    PROF_LAUNCH(KC_UPDATE, st, k_update<V><<<gv, 256, 0, st>>>(w.x.p, w.dscale.p, n, z, w.active.p));
+    for (int s = 0; s < S_used; ++s)
+      if (w.h_active[s]) w.iters[s]++;
+    rc = residual();
+    if (rc) return rc;
+  }
+  ELP_CUDA(cudaGetLastError());
+  float fms = 0.f;
+  cudaEventElapsedTime(&fms, w.ev[0], w.ev[1]);
+  ms[0] = fms;
+  ms[1] = solve_ms;
+  ms[2] = 0.f;
   return ELP_OK;
 }
 
@@ -970,9 +1321,8 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
   }
   int iters = 0;
   float ms[3] = {0, 0, 0};
-  const int max_iter = precision == ELP_MIXED ? 40 : 8;
-  if (precision == ELP_MIXED) rc = run_batch<float>(m, w, n_omega, tol, max_iter, st, &iters, ms);
-  else rc = run_batch<double>(m, w, n_omega, tol, max_iter, st, &iters, ms);
+  if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 8, st, ms);
+  else rc = run_batch<double>(m, w, n_omega, tol, 8, st, &iters, ms);
   if (rc) return rc;
   ELP_CUDA(cudaMemcpyAsync(x_dev, w.x.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToDevice, st));
   ELP_CUDA(cudaMemcpyAsync(w.h_stats, w.stats.p, sizeof(unsigned long long) * 4 * n_omega, cudaMemcpyDeviceToHost, st));
@@ -991,7 +1341,7 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
       memcpy(&umax, &b1, 8);
       memcpy(&amax, &b3, 8);
       I.growth = amax > 0 ? umax / amax : 0.0;
-      I.iterations = iters;
+      I.iterations = w.iters[s];
       I.static_pivots = (int)w.h_stats[4 * s + 0];
       I.converged = rel <= tol ? 1 : 0;
       I.ms_factor = ms[0] / n_omega;

@@ -60,6 +60,16 @@ struct Workspace {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8];
   int nparts = 0;
+  // GMRES: basis (slots x (rst + 1) x n), work vectors, Hessenberg columns
+  int rst = 0;
+  DevBuf<double2> Vb, wv, uv, tv, hd1, hd2, hnd, ydev, dpart;
+  DevBuf<double> scal;
+  DevBuf<int> inner;
+  double2* h_h = nullptr;         // pinned: 3 x slots x 32 (h1, h2, |w|^2)
+  double2* h_y = nullptr;         // pinned: slots x 32
+  double* h_scal = nullptr;       // pinned: slots
+  int* h_inner = nullptr;         // pinned: slots
+  int iters[kMaxSlots];           // preconditioner applications per slot
   ~Workspace();
 };
 
