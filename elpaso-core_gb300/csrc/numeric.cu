@@ -634,13 +634,13 @@ constexpr int kMaxBasis = 32;
 
 // w = A u (FP64, unscaled A)
 __global__ void k_spmv(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ row_ptr,
-                       const int32_t* __restrict__ col_idx, int64_t n, const double2* __restrict__ u,
+                       const int32_t* __restrict__ col_idx, int64_t n, const double2* __restrict__ u, int64_t ustride,
                        double2* __restrict__ w, const int* __restrict__ active) {
   const int s = blockIdx.y;
   if (!active[s]) return;
   const Coef c = coef[s];
   const int lane = threadIdx.x & 31;
-  const double2* us = u + s * n;
+  const double2* us = u + s * ustride;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = warp; i < n; i += nwarps) {
@@ -738,7 +738,7 @@ __global__ void k_vscale(const double2* __restrict__ src, double2* __restrict__ 
   }
 }
 
-// t = sum_i y_i V_i
+// t += sum_i y_i Z_i
 __global__ void k_combo(const double2* __restrict__ basis, int64_t sstride, int64_t vstride, int nv,
                         const double2* __restrict__ y, double2* __restrict__ t, int64_t n, const int* __restrict__ active) {
   const int s = blockIdx.y;
@@ -747,7 +747,7 @@ __global__ void k_combo(const double2* __restrict__ basis, int64_t sstride, int6
   if (threadIdx.x < nv) ys[threadIdx.x] = y[s * kMaxBasis + threadIdx.x];
   __syncthreads();
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-    double ax = 0, ay = 0;
+    double ax = t[s * n + r].x, ay = t[s * n + r].y;
     for (int i = 0; i < nv; ++i) {
       double2 v = basis[s * sstride + (int64_t)i * vstride + r];
       ax += ys[i].x * v.x - ys[i].y * v.y;
@@ -757,16 +757,16 @@ __global__ void k_combo(const double2* __restrict__ basis, int64_t sstride, int6
   }
 }
 
-// u = D z (front precision -> FP64)
+// u = D z (front precision -> FP64), u of slot s at u + s * sstride
 template <class V>
 __global__ void k_unscale(const V* __restrict__ z, const double* __restrict__ dscale, int64_t n, double2* __restrict__ u,
-                          const int* __restrict__ active) {
+                          int64_t sstride, const int* __restrict__ active) {
   const int s = blockIdx.y;
   if (!active[s]) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double d = dscale[s * n + i];
     V v = z[s * n + i];
-    u[s * n + i] = make_double2(d * (double)v.x, d * (double)v.y);
+    u[s * sstride + i] = make_double2(d * (double)v.x, d * (double)v.y);
   }
 }
 
@@ -1107,9 +1107,8 @@ static int gmres_alloc(Workspace& w, int64_t n, int S, int rst) {
   if (w.rst == rst && w.Vb.p) return ELP_OK;
   w.rst = rst;
   ELP_CUDA(w.Vb.alloc((size_t)S * (rst + 1) * n));
+  ELP_CUDA(w.Zb.alloc((size_t)S * rst * n));
   ELP_CUDA(w.wv.alloc((size_t)S * n));
-  ELP_CUDA(w.uv.alloc((size_t)S * n));
-  ELP_CUDA(w.tv.alloc((size_t)S * n));
   ELP_CUDA(w.hd1.alloc((size_t)S * kMaxBasis));
   ELP_CUDA(w.hd2.alloc((size_t)S * kMaxBasis));
   ELP_CUDA(w.hnd.alloc((size_t)S * kMaxBasis));
@@ -1146,7 +1145,8 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
   const int RST = 24;
   int rc = gmres_alloc(w, n, w.slots, RST);
   if (rc) return rc;
-  const int64_t vst = (int64_t)(RST + 1) * n;  // slot stride of the basis
+  const int64_t vst = (int64_t)(RST + 1) * n;  // slot stride of the Arnoldi basis V
+  const int64_t zst = (int64_t)RST * n;        // slot stride of Z = M^-1 V
   for (int s = 0; s < S_used; ++s) { w.h_active[s] = 1; w.iters[s] = 0; }
   ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
   ELP_CUDA(cudaEventRecord(w.ev[0], st));
@@ -1207,9 +1207,11 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
       rc = precond(w.Vb.p + (int64_t)j * n, vst, w.inner.p);
       if (rc) return rc;
       ELP_CUDA(cudaEventRecord(w.ev[3], st));
-      k_unscale<V><<<gv, 256, 0, st>>>(z, w.dscale.p, n, w.uv.p, w.inner.p);
-      PROF_LAUNCH(KC_RESIDUAL, st, k_spmv<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.uv.p, w.wv.p,
-                                                                 w.inner.p));
+      // Z_j = M^-1 V_j kept in FP64 (flexible GMRES: the update uses Z y, so
+      // rounding of the front-precision solve never enters the Arnoldi relation)
+      k_unscale<V><<<gv, 256, 0, st>>>(z, w.dscale.p, n, w.Zb.p + (int64_t)j * n, zst, w.inner.p);
+      PROF_LAUNCH(KC_RESIDUAL, st, k_spmv<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n,
+                                                                 w.Zb.p + (int64_t)j * n, zst, w.wv.p, w.inner.p));
       const int nv = j + 1;
       k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p);
       k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd1.p, w.inner.p);
@@ -1258,7 +1260,7 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
         ncol[s] = j + 1;
         const double est = std::abs(g[s][j + 1]) / fn[s];
         if (trace) fprintf(stderr, "[elp]   arnoldi %d slot %d estimate %.3e\n", j, s, est);
-        if (est <= 0.25 * tol || hn <= 1e-300 || j == RST - 1 || !std::isfinite(est)) w.h_inner[s] = 0;
+        if (est <= 0.5 * tol || hn <= 1e-300 || j == RST - 1 || !std::isfinite(est)) w.h_inner[s] = 0;
         else more = true;
         w.h_scal[s] = hn > 0 ? 1.0 / hn : 0.0;
       }
@@ -1284,12 +1286,7 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
       for (int i = 0; i < k; ++i) w.h_y[s * kMaxBasis + i] = make_double2(y[i].real(), y[i].imag());
     }
     ELP_CUDA(cudaMemcpyAsync(w.ydev.p, w.h_y, sizeof(double2) * S_used * kMaxBasis, cudaMemcpyHostToDevice, st));
-    k_combo<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nvmax, w.ydev.p, w.tv.p, n, w.active.p);
-    rc = precond(w.tv.p, n, w.active.p);
-    if (rc) return rc;
-    PROF_LAUNCH(KC_UPDATE, st, k_update<V><<<gv, 256, 0, st>>>(w.x.p, w.dscale.p, n, z, w.active.p));
-    for (int s = 0; s < S_used; ++s)
-      if (w.h_active[s]) w.iters[s]++;
+    PROF_LAUNCH(KC_UPDATE, st, k_combo<<<gv, 256, 0, st>>>(w.Zb.p, zst, n, nvmax, w.ydev.p, w.x.p, n, w.active.p));
     rc = residual();
     if (rc) return rc;
   }

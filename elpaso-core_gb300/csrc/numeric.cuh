@@ -62,7 +62,7 @@ struct Workspace {
   int nparts = 0;
   // GMRES: basis (slots x (rst + 1) x n), work vectors, Hessenberg columns
   int rst = 0;
-  DevBuf<double2> Vb, wv, uv, tv, hd1, hd2, hnd, ydev, dpart;
+  DevBuf<double2> Vb, Zb, wv, hd1, hd2, hnd, ydev, dpart;
   DevBuf<double> scal;
   DevBuf<int> inner;
   double2* h_h = nullptr;         // pinned: 3 x slots x 32 (h1, h2, |w|^2)
