@@ -59,10 +59,15 @@ def workload(meshes, args):
     raise SystemExit(f"unknown workload {args.workload}")
 
 
+SWEEP = 1.0 + np.random.default_rng(20260101).permutation(500)
+
+
 def sweep(rank, world, step, batch):
-    """Frequencies (Hz) of one step on one rank: consecutive blocks of the 1..500 Hz sweep."""
+    """Frequencies (Hz) of one step on one rank: consecutive blocks of a seeded
+    permutation of the 1..500 Hz (1 Hz step) sweep, so every step mixes the
+    ill-conditioned low end with the rest of the band."""
     base = (step * world + rank) * batch
-    return 1.0 + (np.arange(base, base + batch) % 500)
+    return SWEEP[np.arange(base, base + batch) % 500]
 
 
 class Clocks:

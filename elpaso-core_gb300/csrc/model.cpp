@@ -325,6 +325,7 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
       else if (m.dof_kind[r] == 0 && m.dof_kind[c] == 0) k = CLS_STRUCT;
       else if (m.dof_kind[r] == 1 && m.dof_kind[c] == 1) k = CLS_FLUID;
       else k = CLS_COUPLE;
+      if (!m.is_bc_row[r] && m.is_bc_row[c]) k |= CLS_BC_COLUMN;
       m.cls[p] = k;
     }
   }

@@ -26,6 +26,12 @@ enum EntryClass : uint8_t {
   CLS_BC_OFF = 3,   // off-diagonal of a Dirichlet row: 0
   CLS_BC_DIAG = 4,  // diagonal of a Dirichlet row: 1 (MatZeroRows diag = 1)
 };
+// Flag bit on entries of non-Dirichlet rows whose COLUMN is a Dirichlet dof.
+// A(w) keeps them (the reference zeroes rows only); the factorisation drops
+// them and the solve lifts them to the right-hand side instead
+// (x_bc = f_bc, f_r -= a_r,bc x_bc), which is exact block elimination.
+constexpr uint8_t CLS_BC_COLUMN = 0x80;
+constexpr uint8_t CLS_MASK = 0x7f;
 
 // Loss-factor group of the structure stiffness: coefficient c_g(w).
 struct StructGroup {

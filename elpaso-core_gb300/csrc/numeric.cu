@@ -74,7 +74,7 @@ struct CombineArgs {
 };
 
 __device__ __forceinline__ double2 combine(const CombineArgs& A, const Coef& c, int64_t q) {
-  const uint8_t k = A.cls[q];
+  const uint8_t k = A.cls[q] & CLS_MASK;
   if (k == CLS_BC_DIAG) return make_double2(1.0, 0.0);
   if (k == CLS_BC_OFF) return make_double2(0.0, 0.0);
   const double vk = A.VK[q], vm = A.VM[q];
@@ -124,6 +124,7 @@ __global__ void k_scatter(CombineArgs A, const Coef* __restrict__ coef, const in
   for (int64_t i = warp; i < n; i += nwarps) {
     const double di = d[i];
     for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
+      if (A.cls[q] & CLS_BC_COLUMN) continue;  // lifted to the right-hand side by the solve
       double2 v = combine(A, c, q);
       double sc = di * d[col_idx[q]];
       v.x *= sc;
@@ -596,16 +597,39 @@ __global__ void k_norms(const double* __restrict__ partial, int nparts, double* 
   if (threadIdx.x == 0) { norms[2 * s] = a[0]; norms[2 * s + 1] = b[0]; }
 }
 
-// z = D r in front precision (r of slot s at r + s * sstride)
+// z = D (r - A(:, bc) r_bc) in front precision (r of slot s at r + s * sstride):
+// Dirichlet columns are lifted to the right-hand side (the factorisation
+// holds A with those columns removed, and r_bc passes through the identity
+// rows), so the preconditioner is the exact inverse of A up to the front
+// precision.
 template <class V>
-__global__ void k_rhs(const double2* __restrict__ r, int64_t sstride, const double* __restrict__ dscale, int64_t n,
-                      V* __restrict__ z, const int* __restrict__ active) {
+__global__ void k_rhs(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ row_ptr,
+                      const int32_t* __restrict__ col_idx, const double2* __restrict__ r, int64_t sstride,
+                      const double* __restrict__ dscale, int64_t n, V* __restrict__ z, const int* __restrict__ active) {
   const int s = blockIdx.y;
   if (!active[s]) return;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double d = dscale[s * n + i];
-    double2 v = r[s * sstride + i];
-    z[s * n + i] = cmk<V>(v.x * d, v.y * d);
+  const int lane = threadIdx.x & 31;
+  const double2* rs = r + s * sstride;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    double sx = 0.0, sy = 0.0;
+    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
+      if (!(A.cls[q] & CLS_BC_COLUMN)) continue;
+      double2 a = combine(A, coef[s], q);
+      double2 v = rs[col_idx[q]];
+      sx += a.x * v.x - a.y * v.y;
+      sy += a.x * v.y + a.y * v.x;
+    }
+    for (int o = 16; o; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    }
+    if (lane == 0) {
+      const double d = dscale[s * n + i];
+      const double2 v = rs[i];
+      z[s * n + i] = cmk<V>((v.x - sx) * d, (v.y - sy) * d);
+    }
   }
 }
 
@@ -1064,7 +1088,7 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
                                  w.nparts, w.active.p));
   for (it = 0; it < max_iter; ++it) {
     ELP_CUDA(cudaEventRecord(w.ev[2], st));
-    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(w.r.p, n, w.dscale.p, n, reinterpret_cast<V*>(w.z.p), w.active.p));
+    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, w.r.p, n, w.dscale.p, n, reinterpret_cast<V*>(w.z.p), w.active.p));
     rc = solve_sweep<R>(m, w, S_used, st, w.active.p);
     if (rc) return rc;
     PROF_LAUNCH(KC_UPDATE, st, k_update<V><<<gv, 256, 0, st>>>(w.x.p, w.dscale.p, n, reinterpret_cast<const V*>(w.z.p), w.active.p));
@@ -1173,7 +1197,7 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
     return ELP_OK;
   };
   auto precond = [&](const double2* src, int64_t sstride, const int* mask) -> int {
-    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(src, sstride, w.dscale.p, n, z, mask));
+    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, src, sstride, w.dscale.p, n, z, mask));
     return solve_sweep<R>(m, w, S_used, st, mask);
   };
   rc = residual();
@@ -1318,7 +1342,7 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
   }
   int iters = 0;
   float ms[3] = {0, 0, 0};
-  if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 8, st, ms);
+  if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 12, st, ms);
   else rc = run_batch<double>(m, w, n_omega, tol, 8, st, &iters, ms);
   if (rc) return rc;
   ELP_CUDA(cudaMemcpyAsync(x_dev, w.x.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToDevice, st));
