@@ -64,31 +64,6 @@ template <class V> __device__ __forceinline__ V cinv(V a) {
 }
 
 // ------------------------------------------------------------- combine
-struct CombineArgs {
-  const double* VK;
-  const double* VM;
-  const double* VKg;
-  const uint8_t* cls;
-  int64_t nnz;
-  int ngroups;
-};
-
-__device__ __forceinline__ double2 combine(const CombineArgs& A, const Coef& c, int64_t q) {
-  const uint8_t k = A.cls[q] & CLS_MASK;
-  if (k == CLS_BC_DIAG) return make_double2(1.0, 0.0);
-  if (k == CLS_BC_OFF) return make_double2(0.0, 0.0);
-  const double vk = A.VK[q], vm = A.VM[q];
-  double2 v;
-  v.x = c.a[k].x * vk + c.b[k] * vm;
-  v.y = c.a[k].y * vk;
-  if (k == CLS_STRUCT)
-    for (int g = 1; g < A.ngroups; ++g) {
-      double e = A.VKg[(int64_t)(g - 1) * A.nnz + q];
-      v.x += c.g[g].x * e;
-      v.y += c.g[g].y * e;
-    }
-  return v;
-}
 
 __global__ void k_dscale(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ diag,
                          int64_t n, double* __restrict__ dscale) {
@@ -931,7 +906,7 @@ int workspace_ensure(Model& m, int precision, int slots) {
   return ELP_OK;
 }
 
-static CombineArgs combine_args(const Model& m) {
+CombineArgs combine_args(const Model& m) {
   CombineArgs A;
   A.VK = m.dev->VK.p;
   A.VM = m.dev->VM.p;

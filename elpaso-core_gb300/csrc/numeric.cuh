@@ -19,6 +19,36 @@ struct Coef {
   double2 g[kMaxGroups];         // coefficient of VKg[g - 1] (g >= 1) on structure entries
 };
 
+// the w-independent value arrays of a model and the per-w combine
+struct CombineArgs {
+  const double* VK;
+  const double* VM;
+  const double* VKg;
+  const uint8_t* cls;
+  int64_t nnz;
+  int ngroups;
+};
+
+// A(w) at CSR entry q, Dirichlet rows included (MatZeroRows, diag = 1)
+__device__ __forceinline__ double2 combine(const CombineArgs& A, const Coef& c, int64_t q) {
+  const uint8_t k = A.cls[q] & CLS_MASK;
+  if (k == CLS_BC_DIAG) return make_double2(1.0, 0.0);
+  if (k == CLS_BC_OFF) return make_double2(0.0, 0.0);
+  const double vk = A.VK[q], vm = A.VM[q];
+  double2 v;
+  v.x = c.a[k].x * vk + c.b[k] * vm;
+  v.y = c.a[k].y * vk;
+  if (k == CLS_STRUCT)
+    for (int g = 1; g < A.ngroups; ++g) {
+      double e = A.VKg[(int64_t)(g - 1) * A.nnz + q];
+      v.x += c.g[g].x * e;
+      v.y += c.g[g].y * e;
+    }
+  return v;
+}
+
+CombineArgs combine_args(const Model& m);
+
 struct DeviceSymbolic {
   DevBuf<int32_t> f_p, f_b, f_parent, f_idx_off, f_map_off, f_cb_off, f_piv_off;
   DevBuf<int64_t> f_off;
