@@ -117,7 +117,7 @@ EXPORTS = [
     "elp_model_pattern", "elp_model_global_rows", "elp_model_system_values", "elp_model_rhs",
     "elp_solve", "elp_model_destroy", "elp_last_error", "elp_solve_device", "elp_model_time_assembly",
     "elp_server_create", "elp_server_add_model", "elp_server_submit", "elp_server_wait",
-    "elp_server_destroy", "elp_profile", "elp_profile_read",
+    "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc",
 ]
 KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
                   "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc"]
@@ -153,6 +153,7 @@ def load_library(path: str | None = None):
     lib.elp_server_submit.argtypes = [P, C.c_int, P, C.c_int, P, C.POINTER(C.c_int64)]
     lib.elp_server_wait.argtypes = [P, C.POINTER(RequestResult), C.c_double]
     lib.elp_server_destroy.argtypes = [P]
+    lib.elp_residual_noalloc.argtypes = [P, P, C.c_int, P, P, P, P, P]
     lib.elp_profile.argtypes = [C.c_int]
     lib.elp_profile_read.argtypes = [P, P, P, C.POINTER(C.c_int)]
     if path is None:

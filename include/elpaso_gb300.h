@@ -208,6 +208,25 @@ int elp_solve_device(elp_model* m, const double* omegas, int n_omega, int precis
 int elp_model_time_assembly(elp_model* m, int repeats, double* ms_per_assembly,
                             double* ms_kernel_only);
 
+/* ---- allocation-free residual check ------------------------------------ */
+
+/* No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory while they run (a host loop captured into a CUDA
+ * graph, a device-memory pool or budget that cannot grow, an embedding that
+ * forbids allocation after start-up). Computes r = f - A(w_k) x_k and
+ * ||r||_2 / ||f||_2 for n_omega <= ELP_NOALLOC_MAX_OMEGA frequencies of an
+ * assembled model; f_dev, x_dev, r_dev are the caller's device buffers
+ * (n_omega x n complex interleaved), rel_residual_out is host memory
+ * (n_omega doubles). It calls no allocating routine: its scratch is one
+ * fixed device array of about 0.5 MB that every GPU loading the library
+ * keeps until the process exits. Larger n_omega is rejected with
+ * ELP_ERR_ARG. All calls share that array: calls that overlap on the GPU
+ * race on it. The first call on a device looks up the array's device
+ * address; make it before any stream capture. */
+#define ELP_NOALLOC_MAX_OMEGA 64
+int elp_residual_noalloc(elp_model* m, const double* omegas, int n_omega, const double* f_dev,
+                         const double* x_dev, double* r_dev, double* rel_residual_out, void* stream);
+
 /* ---- launch counting and per-kernel device timing ---------------------- */
 
 /* Kernel classes, in the order of the arrays below:

@@ -1,0 +1,70 @@
+"""Allocation-free residual check, elp_residual_noalloc.
+
+Callers that cannot allocate device memory while they run (a host loop
+captured into a CUDA graph, a device-memory pool that cannot grow) check
+their solutions with this entry point. Here it must agree with the residual
+that the solve path itself reports (elp_solve_device, info.rel_residual) for
+the same solutions, on two calls in a row, its residual vector must match
+its own norm, and it must reject more frequencies than its fixed scratch
+array holds. The file sorts last so that a stop-at-first-failure run has
+already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RES_TOL = 1e-10  # the relative-residual bar of the solve tests
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def test_noalloc_residual_matches_solve_path(elp, meshes):
+    torch = pytest.importorskip("torch")
+    d = meshes.plate_cavity(12, 8, 6, 0.6, 0.4, 0.3)
+    m = elp.Model(d).assemble().analyse()
+    n = m.n
+    oms = np.ascontiguousarray(2 * np.pi * np.array([3.0, 140.0, 421.0]))
+    S = len(oms)
+    lib = elp.load_library()
+    fh = np.ascontiguousarray(np.broadcast_to(m.rhs(), (S, n)))
+    f = torch.from_numpy(fh.view(np.float64).copy()).cuda()
+    x = torch.zeros_like(f)
+    r = torch.zeros_like(f)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    infos = (elp.SolveInfo * S)()
+    rc = lib.elp_solve_device(m.handle, _p(oms), S, elp.MIXED, C.c_void_p(f.data_ptr()), C.c_void_p(x.data_ptr()),
+                              C.cast(infos, C.c_void_p), RES_TOL, stream)
+    assert rc == 0, lib.elp_last_error()
+    ref = np.array([infos[i].rel_residual for i in range(S)])
+    assert np.all(ref <= RES_TOL)
+    for call in range(2):
+        rel = np.zeros(S)
+        r.zero_()
+        rc = lib.elp_residual_noalloc(m.handle, _p(oms), S, C.c_void_p(f.data_ptr()), C.c_void_p(x.data_ptr()),
+                                      C.c_void_p(r.data_ptr()), _p(rel), stream)
+        assert rc == 0, lib.elp_last_error()
+        assert np.all(np.abs(rel - ref) <= RES_TOL), (call, rel, ref)
+        assert np.all(np.abs(rel - ref) <= 1e-6 * ref), (call, rel, ref)
+        rv = r.view(S, n, 2).cpu().numpy()
+        own = np.sqrt((rv ** 2).sum(axis=(1, 2))) / np.linalg.norm(fh, axis=1)
+        assert np.all(np.abs(own - rel) <= 1e-6 * rel), (call, own, rel)
+
+
+def test_noalloc_rejects_more_frequencies_than_its_scratch_holds(elp, meshes):
+    torch = pytest.importorskip("torch")
+    m = elp.Model(meshes.plate(6, 5, 0.3, 0.2, 0.002)).assemble()
+    n = m.n
+    S = 65
+    oms = np.ascontiguousarray(np.full(S, 2 * np.pi * 50.0))
+    buf = torch.zeros((S, 2 * n), dtype=torch.float64, device="cuda")
+    rel = np.zeros(S)
+    lib = elp.load_library()
+    rc = lib.elp_residual_noalloc(m.handle, _p(oms), S, C.c_void_p(buf.data_ptr()), C.c_void_p(buf.data_ptr()),
+                                  C.c_void_p(buf.data_ptr()), _p(rel), None)
+    assert rc == 1
+    assert b"ELP_NOALLOC_MAX_OMEGA" in lib.elp_last_error()
