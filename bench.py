@@ -59,6 +59,11 @@ def workload(meshes, args):
     raise SystemExit(f"unknown workload {args.workload}")
 
 
+def workload_label(d):
+    return (f"{d.name}: DSG4 plate + Fluid8 cavity coupled by InterfaceMindlin quads, "
+            "1-500 Hz sweep (1 Hz step, seeded order), unit force")
+
+
 SWEEP = 1.0 + np.random.default_rng(20260101).permutation(500)
 
 
@@ -123,28 +128,31 @@ def peaks():
 
 
 def cpu_baseline(meshes, args, n_freq=1):
-    """The oracle (CPU restatement of the reference path) timed on this host:
-    per frequency, the reference's per-w element loop (C) + an FP64 sparse LU
-    solve (SciPy SuperLU, standing in for MUMPS which is not available)."""
+    """The oracle (CPU restatement of the reference path) timed on this host.
+    Per frequency: the reference's per-w element loop (C, one thread) and an
+    FP64 multifrontal LU with nested dissection (oracle/mf.py, the MUMPS
+    algorithm restated; dense fronts in LAPACK/BLAS on every host core).
+    The symbolic analysis is done once, outside the timed sample, as MUMPS
+    reuses it across frequencies."""
     from oracle import oracle as orc
     d = workload(meshes, args)
     s = orc.System(d)
-    import scipy.sparse.linalg as sla
+    mf = orc.multifrontal(s)
     t0 = time.perf_counter()
-    done = 0
+    done, worst = 0, 0.0
     for k in range(n_freq):
-        om = 2 * np.pi * (1.0 + 37.0 * k)
-        A = s.matrix(om).tocsc()
-        lu = sla.splu(A)
-        x = lu.solve(s.f)
+        om = 2 * np.pi * SWEEP[k % 500]
+        A = s.matrix(om)
+        mf.factor(A)
+        x = mf.solve(s.f)
+        worst = max(worst, float(np.linalg.norm(s.f - A @ x) / np.linalg.norm(s.f)))
         done += 1
         if time.perf_counter() - t0 > args.cpu_budget_s:
             break
     dt = time.perf_counter() - t0
-    res = float(np.linalg.norm(s.f - A @ x) / np.linalg.norm(s.f))
-    return {"value": done / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{done} frequency of the {d.name} sweep: C element loop + SciPy SuperLU FP64 "
-                      f"(MUMPS stand-in), {dt:.1f} s, rel residual {res:.1e}"}
+    return {"value": done / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{done} frequency(ies) of the {d.name} sweep: C element loop + FP64 multifrontal LU "
+                      f"(LAPACK/BLAS on {os.cpu_count()} threads), {dt:.1f} s, max rel residual {worst:.1e}"}
 
 
 def run_ours(args):
@@ -275,7 +283,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 fronts + f64 refinement", "data": "synthetic",
-            "config": {"workload": f"{d.name}: DSG4 60x40 plate + Fluid8 60x40x30 cavity, 1-500 Hz sweep",
+            "config": {"workload": workload_label(d),
                        "n_dofs": n, "nnz": info["nnz"], "frequencies_per_step": S, "parallelism": f"freq-shard x{world}",
                        "l2": "inputs larger than L2 (front arena "
                              f"{info['factor_entries'] * 8 * S / 1e9:.1f} GB per step)",
@@ -302,13 +310,16 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    meshes_mod = None
-    elp = load_pkg()
+    load_pkg()
     meshes_mod = importlib.import_module("elpaso_core_gb300.meshes")
     b = cpu_baseline(meshes_mod, args, n_freq=max(1, args.steps))
+    d = workload(meshes_mod, args)
     line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "impl": "reference", "data": "synthetic",
-            "config": {"workload": "plate_cavity_60x40x30 sweep (CPU restatement of the reference path)"},
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "impl": "reference", "data": "synthetic",
+            "config": {"workload": workload_label(d),
+                       "note": "the reference (PETSc/MUMPS) cannot be built here; its CPU path is timed "
+                               "as the oracle restatement (element loop + multifrontal LU)"},
             "cpu_baseline": b,
             "e2e": {"value": b["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

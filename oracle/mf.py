@@ -1,0 +1,192 @@
+"""Test infrastructure (CPU oracle), not product code.
+
+A CPU multifrontal LU for the FP64 direct-solve oracle and the CPU baseline,
+restating the published algorithm of the reference's solver, MUMPS
+(KSPPREONLY + PCLU + MUMPS, elpasoCore/source/analysis/analysis.cpp:1159-1169,
+1293-1332; PETSc 3.19.1's MUMPS, version not pinned in the reference tree):
+a fill-reducing nested-dissection order, an assembly tree of dense fronts,
+partial pivoting within each front's fully summed block, and Schur
+complements extend-added into the parent. Dense work goes to LAPACK/BLAS
+(SciPy), which uses every host thread.
+
+It is written independently of the product's symbolic phase. The ordering
+is a geometric nested dissection on node coordinates (median cut along the
+longest box axis, separator = the side boundary of the smaller cost).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg as sla
+import scipy.sparse as sp
+
+
+def _node_graph(indptr, indices, dof_node, n_nodes):
+    rows = np.repeat(np.arange(len(indptr) - 1), np.diff(indptr))
+    a = dof_node[rows]
+    b = dof_node[indices]
+    keep = a != b
+    G = sp.coo_matrix((np.ones(int(keep.sum()), np.int8), (a[keep], b[keep])), shape=(n_nodes, n_nodes)).tocsr()
+    G.sum_duplicates()
+    return G.indptr, G.indices
+
+
+def _dissect(nodes, coords, gptr, gidx, ndof, leaf, mark, stamp, out):
+    """Appends (pivot_nodes, children) tuples in postorder; returns root ids."""
+    if ndof[nodes].sum() <= leaf or len(nodes) <= 2:
+        out.append((nodes, []))
+        return [len(out) - 1]
+    xyz = coords[nodes]
+    ext = xyz.max(0) - xyz.min(0)
+    ax = int(np.argmax(ext))
+    if ext[ax] <= 0:
+        left, right = nodes[: len(nodes) // 2], nodes[len(nodes) // 2:]
+    else:
+        med = np.median(xyz[:, ax])
+        lm = xyz[:, ax] < med
+        if lm.all() or not lm.any():
+            lm = xyz[:, ax] <= med
+        if lm.all() or not lm.any():
+            lm = np.zeros(len(nodes), bool)
+            lm[: len(nodes) // 2] = True
+        left, right = nodes[lm], nodes[~lm]
+    stamp[0] += 1
+    s = stamp[0]
+    mark[left] = 2 * s
+    mark[right] = 2 * s + 1
+
+    def boundary(side, other):
+        sep = []
+        for v in side:
+            nb = gidx[gptr[v]:gptr[v + 1]]
+            if np.any(mark[nb] == other):
+                sep.append(v)
+        return np.asarray(sep, np.int64)
+    sl, sr = boundary(left, 2 * s + 1), boundary(right, 2 * s)
+    if ndof[sl].sum() < ndof[sr].sum():
+        sep, left = sl, np.setdiff1d(left, sl, assume_unique=True)
+    else:
+        sep, right = sr, np.setdiff1d(right, sr, assume_unique=True)
+    kids = []
+    if len(left):
+        kids += _dissect(left, coords, gptr, gidx, ndof, leaf, mark, stamp, out)
+    if len(right):
+        kids += _dissect(right, coords, gptr, gidx, ndof, leaf, mark, stamp, out)
+    if len(sep) == 0:
+        return kids
+    out.append((sep, kids))
+    return [len(out) - 1]
+
+
+class Multifrontal:
+    """Symbolic analysis once per pattern; factor + solve per matrix."""
+
+    def __init__(self, indptr, indices, dof_node, coords, leaf=96):
+        n = len(indptr) - 1
+        n_nodes = len(coords)
+        dof_node = np.asarray(dof_node)
+        ndof = np.bincount(dof_node, minlength=n_nodes)
+        node_dofs = [[] for _ in range(n_nodes)]
+        for d, v in enumerate(dof_node):
+            node_dofs[v].append(d)
+        gptr, gidx = _node_graph(indptr, indices, dof_node, n_nodes)
+        import sys
+        sys.setrecursionlimit(10000)
+        out = []
+        mark = np.zeros(n_nodes, np.int64)
+        active = np.nonzero(ndof)[0]
+        _dissect(active, np.asarray(coords, float), gptr, gidx, ndof, leaf, mark, [0], out)
+        T = len(out)
+        snode = np.full(n_nodes, -1, np.int64)
+        for t, (nodes, _) in enumerate(out):
+            snode[nodes] = t
+        rank = np.empty(n_nodes, np.int64)
+        r = 0
+        for nodes, _ in out:
+            rank[nodes] = np.arange(r, r + len(nodes))
+            r += len(nodes)
+        parent = np.full(T, -1, np.int64)
+        for t, (_, kids) in enumerate(out):
+            for c in kids:
+                parent[c] = t
+        borders = []
+        for t, (nodes, kids) in enumerate(out):
+            cand = set()
+            for v in nodes:
+                for u in gidx[gptr[v]:gptr[v + 1]]:
+                    if snode[u] > t:
+                        cand.add(int(u))
+            for c in kids:
+                cand.update(x for x in borders[c] if snode[x] > t)
+            borders.append(sorted(cand, key=lambda u: rank[u]))
+        self.fronts = []
+        pos = np.empty(n, np.int64)   # elimination position of every dof
+        owner_of_pos = np.empty(n, np.int64)
+        e = 0
+        for t, (nodes, kids) in enumerate(out):
+            piv = np.asarray([d for v in nodes for d in node_dofs[v]], np.int64)
+            bor = np.asarray([d for v in borders[t] for d in node_dofs[v]], np.int64)
+            self.fronts.append((piv, bor, list(kids)))
+            pos[piv] = np.arange(e, e + len(piv))
+            owner_of_pos[e:e + len(piv)] = t
+            e += len(piv)
+        # every CSR entry goes to the front of whichever of row/column is eliminated first
+        rows = np.repeat(np.arange(n), np.diff(indptr))
+        owner = owner_of_pos[np.minimum(pos[rows], pos[indices])]
+        order = np.argsort(owner, kind="stable")
+        bounds = np.searchsorted(owner[order], np.arange(T + 1))
+        local = np.full(n, -1, np.int64)
+        self.assembly = []
+        for t, (piv, bor, kids) in enumerate(self.fronts):
+            idx = np.concatenate([piv, bor])
+            local[idx] = np.arange(len(idx))
+            q = order[bounds[t]:bounds[t + 1]]
+            kid_maps = [local[np.concatenate([self.fronts[c][1]])] for c in kids]
+            self.assembly.append((q, local[rows[q]], local[indices[q]], kid_maps))
+            local[idx] = -1
+        self.n = n
+        self.indptr, self.indices = indptr, indices
+
+    def factor(self, A):
+        """A: scipy CSR (complex128) on the analysed pattern."""
+        A = A.tocsr()
+        assert np.array_equal(A.indptr, self.indptr) and np.array_equal(A.indices, self.indices)
+        data = A.data
+        F_all = []
+        cb = {}
+        for t, (piv, bor, kids) in enumerate(self.fronts):
+            p, m = len(piv), len(piv) + len(bor)
+            q, lr, lc, kid_maps = self.assembly[t]
+            F = np.zeros((m, m), np.complex128)
+            F[lr, lc] = data[q]
+            for c, loc in zip(kids, kid_maps):
+                S = cb.pop(c)
+                F[np.ix_(loc, loc)] += S
+            lu, perm = sla.lu_factor(F[:p, :p], check_finite=False)
+            F12 = F[:p, p:]
+            for k, pk in enumerate(perm):  # LAPACK row interchanges on F12
+                if pk != k:
+                    F12[[k, pk]] = F12[[pk, k]]
+            U12 = sla.solve_triangular(lu, F12, lower=True, unit_diagonal=True, check_finite=False)
+            L21 = sla.solve_triangular(lu, F[p:, :p].T, trans="T", lower=False, check_finite=False).T
+            if m > p:
+                cb[t] = F[p:, p:] - L21 @ U12
+            F_all.append((lu, perm, L21, U12))
+        self.F = F_all
+
+    def solve(self, b):
+        y = np.array(b, np.complex128, copy=True)
+        for (piv, bor, _), (lu, perm, L21, U12) in zip(self.fronts, self.F):
+            yp = y[piv]
+            for k, pk in enumerate(perm):
+                if pk != k:
+                    yp[[k, pk]] = yp[[pk, k]]
+            yp = sla.solve_triangular(lu, yp, lower=True, unit_diagonal=True, check_finite=False)
+            y[piv] = yp
+            if len(bor):
+                y[bor] -= L21 @ yp
+        for (piv, bor, _), (lu, perm, L21, U12) in zip(reversed(self.fronts), reversed(self.F)):
+            t = y[piv]
+            if len(bor):
+                t = t - U12 @ y[bor]
+            y[piv] = sla.solve_triangular(lu, t, lower=False, check_finite=False)
+        return y

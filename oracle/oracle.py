@@ -253,3 +253,17 @@ class System:
         rhs = self.f if f is None else f
         x = sla.splu(A).solve(rhs)
         return x
+
+
+def dof_nodes(system):
+    """Node index of every dof (global row) of an oracle System."""
+    out = np.empty(system.n, np.int64)
+    r, k = np.nonzero(system.rows >= 0)
+    out[system.rows[r, k]] = r
+    return out
+
+
+def multifrontal(system, leaf=96):
+    """CPU multifrontal LU (oracle/mf.py) analysed on the system's pattern."""
+    from oracle.mf import Multifrontal
+    return Multifrontal(system.row_ptr, system.col_idx, dof_nodes(system), system.d.coords, leaf=leaf)
