@@ -74,20 +74,20 @@ __global__ void k_noalloc_residual(CombineArgs A, NoAllocScratch* sc, const int3
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = warp; i < n; i += nwarps) {
-    double sx = 0.0, sy = 0.0;
+    DD sx{0.0, 0.0}, sy{0.0, 0.0};
     for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
       double2 a = combine(A, c, q);
       double2 v = xs[col_idx[q]];
-      sx += a.x * v.x - a.y * v.y;
-      sy += a.x * v.y + a.y * v.x;
+      dd_fma(sx, a.x, v.x);
+      dd_fma(sx, -a.y, v.y);
+      dd_fma(sy, a.x, v.y);
+      dd_fma(sy, a.y, v.x);
     }
-    for (int o = 16; o; o >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, o);
-      sy += __shfl_xor_sync(0xffffffffu, sy, o);
-    }
+    sx = dd_warp_sum(sx);
+    sy = dd_warp_sum(sy);
     if (lane == 0) {
       double2 fi = f[s * n + i];
-      double2 ri = make_double2(fi.x - sx, fi.y - sy);
+      double2 ri = make_double2(dd_residual(fi.x, sx), dd_residual(fi.y, sy));
       r[s * n + i] = ri;
       rr += ri.x * ri.x + ri.y * ri.y;
       ff += fi.x * fi.x + fi.y * fi.y;

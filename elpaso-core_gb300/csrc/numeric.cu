@@ -284,55 +284,75 @@ __global__ void __launch_bounds__(128) k_urow(LevelArgs L, typename Vec2<R>::T* 
   }
 }
 
-// trailing update F22 -= L(:, panel) U(panel, :) on rows/cols k0+w..m-1
-template <class R, int NB>
-__global__ void __launch_bounds__(256) k_gemm(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
+// Left-looking (Crout) updates of a front, complex GEMM C -= A B on
+// sub-blocks of the same column-major front F (ld = m):
+//   GM_COL   before panel k: F[k0:m, k0:k0+w]   -= F[k0:m, 0:k0]  F[0:k0, k0:k0+w]
+//   GM_ROW   after panel k:  F[k0:k0+w, k0+w:m] -= F[k0:k0+w, 0:k0] F[0:k0, k0+w:m]
+//   GM_SCHUR after the last: F[p:m, p:m]        -= F[p:m, 0:p]   F[0:p, p:m]
+// Every output is read and written once per call, and the depth K grows to
+// the number of eliminated pivots, instead of a rank-32 read-modify-write of
+// the whole trailing matrix per panel.
+enum GemmMode { GM_COL = 0, GM_ROW = 1, GM_SCHUR = 2 };
+
+__device__ __forceinline__ bool gemm_block(int mode, int p, int m, int k0, int w, int& ra, int& M, int& ca, int& N,
+                                           int& K) {
+  if (mode == GM_COL) { ra = k0; M = m - k0; ca = k0; N = w; K = k0; }
+  else if (mode == GM_ROW) { ra = k0; M = w; ca = k0 + w; N = m - k0 - w; K = k0; }
+  else { ra = p; M = m - p; ca = p; N = m - p; K = p; }
+  return M > 0 && N > 0 && K > 0;
+}
+
+template <class R, int NB, int TM, int TN>
+__global__ void __launch_bounds__(256) k_gemm(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step, int mode) {
   using V = typename Vec2<R>::T;
-  constexpr int TM = 64, TN = 64;
+  constexpr int TX = TN / 4, TY = TM / 4;  // 256 threads, 4 x 4 outputs each
+  static_assert(TX * TY == 256, "tile");
   const int f = L.list[blockIdx.x];
   const int s = blockIdx.y;
   const int p = L.fp[f], m = p + L.fb[f];
   const int k0 = step * NB;
-  if (k0 >= p) return;
+  if (mode != GM_SCHUR && k0 >= p) return;
   const int w = min(NB, p - k0);
-  const int t0 = k0 + w;
-  const int mt = m - t0;
-  if (mt <= 0) return;
-  const int tiles_r = (mt + TM - 1) / TM;
-  const int ntiles = tiles_r * tiles_r;
+  int ra, M, ca, N, K;
+  if (!gemm_block(mode, p, m, k0, w, ra, M, ca, N, K)) return;
+  const int tiles_r = (M + TM - 1) / TM, tiles_c = (N + TN - 1) / TN;
+  const int ntiles = tiles_r * tiles_c;
   V* F = arena + s * L.arena_size + L.foff[f];
   constexpr int KC = 16;  // k chunk staged in shared memory
   __shared__ R As_re[KC][TM], As_im[KC][TM];
   __shared__ R Bs_re[KC][TN], Bs_im[KC][TN];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // 16 x 16 threads, 4 x 4 outputs each
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   for (int tile = blockIdx.z; tile < ntiles; tile += gridDim.z) {
-    const int r0 = t0 + (tile % tiles_r) * TM;
-    const int c0 = t0 + (tile / tiles_r) * TN;
+    const int r0 = ra + (tile % tiles_r) * TM;
+    const int c0 = ca + (tile / tiles_r) * TN;
+    const int rend = ra + M, cend = ca + N;
     R acc_re[4][4], acc_im[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
       for (int b2 = 0; b2 < 4; ++b2) { acc_re[a][b2] = 0; acc_im[a][b2] = 0; }
-    for (int kc = 0; kc < w; kc += KC) {
+    for (int kc = 0; kc < K; kc += KC) {
       __syncthreads();
       for (int t = threadIdx.x; t < KC * TM; t += blockDim.x) {
         int k = t / TM, i = t % TM;
-        V a = (kc + k < w && r0 + i < m) ? F[(int64_t)(k0 + kc + k) * m + r0 + i] : cmk<V>(0.0, 0.0);
+        V a = (kc + k < K && r0 + i < rend) ? F[(int64_t)(kc + k) * m + r0 + i] : cmk<V>(0.0, 0.0);
         As_re[k][i] = a.x;
         As_im[k][i] = a.y;
+      }
+      for (int t = threadIdx.x; t < KC * TN; t += blockDim.x) {
         int j = t / KC, kk = t % KC;
-        V bv = (kc + kk < w && c0 + j < m) ? F[(int64_t)(c0 + j) * m + k0 + kc + kk] : cmk<V>(0.0, 0.0);
+        V bv = (kc + kk < K && c0 + j < cend) ? F[(int64_t)(c0 + j) * m + kc + kk] : cmk<V>(0.0, 0.0);
         Bs_re[kk][j] = bv.x;
         Bs_im[kk][j] = bv.y;
       }
       __syncthreads();
-      const int kend = min(KC, w - kc);
+      const int kend = min(KC, K - kc);
       for (int k = 0; k < kend; ++k) {
         R ar[4], ai[4], br[4], bi[4];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) { ar[a] = As_re[k][ty + 16 * a]; ai[a] = As_im[k][ty + 16 * a]; }
+        for (int a = 0; a < 4; ++a) { ar[a] = As_re[k][ty + TY * a]; ai[a] = As_im[k][ty + TY * a]; }
 #pragma unroll
-        for (int b2 = 0; b2 < 4; ++b2) { br[b2] = Bs_re[k][tx + 16 * b2]; bi[b2] = Bs_im[k][tx + 16 * b2]; }
+        for (int b2 = 0; b2 < 4; ++b2) { br[b2] = Bs_re[k][tx + TX * b2]; bi[b2] = Bs_im[k][tx + TX * b2]; }
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -346,8 +366,8 @@ __global__ void __launch_bounds__(256) k_gemm(LevelArgs L, typename Vec2<R>::T* 
     for (int a = 0; a < 4; ++a)
 #pragma unroll
       for (int b2 = 0; b2 < 4; ++b2) {
-        int r = r0 + ty + 16 * a, c = c0 + tx + 16 * b2;
-        if (r < m && c < m) {
+        int r = r0 + ty + TY * a, c = c0 + tx + TX * b2;
+        if (r < rend && c < cend) {
           V* dst = F + (int64_t)c * m + r;
           V v = *dst;
           v.x -= acc_re[a][b2];
@@ -431,6 +451,8 @@ __global__ void __launch_bounds__(256) k_forward(SolveArgs S, const typename Vec
   }
   __syncthreads();
   const int lane = tid & 31, wid = tid >> 5;
+  // L11 solve on the pivot block only; the border rows (L21) are updated by
+  // k_fwd_border across many CTAs
   for (int j0 = 0; j0 < p; j0 += 32) {
     const int jw = min(32, p - j0);
     if (wid == 0) {
@@ -444,7 +466,7 @@ __global__ void __launch_bounds__(256) k_forward(SolveArgs S, const typename Vec
       if (lane < jw) w[j0 + lane] = val;
     }
     __syncthreads();
-    for (int r = j0 + jw + tid; r < m; r += blockDim.x) {
+    for (int r = j0 + jw + tid; r < p; r += blockDim.x) {
       V t = w[r];
       for (int jj = 0; jj < jw; ++jj) t = cfms(t, F[(int64_t)(j0 + jj) * m + r], w[j0 + jj]);
       w[r] = t;
@@ -457,28 +479,93 @@ __global__ void __launch_bounds__(256) k_forward(SolveArgs S, const typename Vec
   }
 }
 
+// border rows of the forward step: cb -= L21 y_p, rows split across CTAs
+template <class R>
+__global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
+                                                    const typename Vec2<R>::T* __restrict__ z,
+                                                    typename Vec2<R>::T* __restrict__ cb) {
+  using V = typename Vec2<R>::T;
+  extern __shared__ unsigned char smraw[];
+  V* y = reinterpret_cast<V*>(smraw);
+  const int f = S.list[blockIdx.x];
+  const int s = blockIdx.y;
+  if (!S.active[s]) return;
+  const int p = S.fp[f], b = S.fb[f], m = p + b;
+  if (blockIdx.z * blockDim.x >= (unsigned)b) return;
+  const V* F = arena + s * S.arena_size + S.foff[f];
+  const int32_t* I = S.dofs + S.idx_off[f];
+  const V* zs = z + s * S.n;
+  for (int k = threadIdx.x; k < p; k += blockDim.x) y[k] = zs[I[k]];
+  __syncthreads();
+  const int i = blockIdx.z * blockDim.x + threadIdx.x;
+  if (i >= b) return;
+  V* dst = cb + s * S.cb_total + S.cb_off[f] + i;
+  V t = *dst;
+  const V* col = F + p + i;
+  int j = 0;
+  for (; j + 4 <= p; j += 4) {
+    V a0 = col[(int64_t)(j + 0) * m], a1 = col[(int64_t)(j + 1) * m];
+    V a2 = col[(int64_t)(j + 2) * m], a3 = col[(int64_t)(j + 3) * m];
+    t = cfms(t, a0, y[j + 0]);
+    t = cfms(t, a1, y[j + 1]);
+    t = cfms(t, a2, y[j + 2]);
+    t = cfms(t, a3, y[j + 3]);
+  }
+  for (; j < p; ++j) t = cfms(t, col[(int64_t)j * m], y[j]);
+  *dst = t;
+}
+
+// pivot rows of the backward step: t = y_p - U12 x_b, rows split across CTAs
+template <class R>
+__global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
+                                                 const typename Vec2<R>::T* __restrict__ z,
+                                                 typename Vec2<R>::T* __restrict__ tb) {
+  using V = typename Vec2<R>::T;
+  extern __shared__ unsigned char smraw[];
+  V* xb = reinterpret_cast<V*>(smraw);
+  const int f = S.list[blockIdx.x];
+  const int s = blockIdx.y;
+  if (!S.active[s]) return;
+  const int p = S.fp[f], b = S.fb[f], m = p + b;
+  if (blockIdx.z * blockDim.x >= (unsigned)p) return;
+  const V* F = arena + s * S.arena_size + S.foff[f];
+  const int32_t* I = S.dofs + S.idx_off[f];
+  const V* zs = z + s * S.n;
+  for (int k = threadIdx.x; k < b; k += blockDim.x) xb[k] = zs[I[p + k]];
+  __syncthreads();
+  const int r = blockIdx.z * blockDim.x + threadIdx.x;
+  if (r >= p) return;
+  V t = zs[I[r]];
+  const V* row = F + (int64_t)p * m + r;
+  int i = 0;
+  for (; i + 4 <= b; i += 4) {
+    V a0 = row[(int64_t)(i + 0) * m], a1 = row[(int64_t)(i + 1) * m];
+    V a2 = row[(int64_t)(i + 2) * m], a3 = row[(int64_t)(i + 3) * m];
+    t = cfms(t, a0, xb[i + 0]);
+    t = cfms(t, a1, xb[i + 1]);
+    t = cfms(t, a2, xb[i + 2]);
+    t = cfms(t, a3, xb[i + 3]);
+  }
+  for (; i < b; ++i) t = cfms(t, row[(int64_t)i * m], xb[i]);
+  tb[s * S.n + S.piv_off[f] + r] = t;
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) k_backward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
-                                                  typename Vec2<R>::T* __restrict__ z) {
+                                                  typename Vec2<R>::T* __restrict__ z,
+                                                  const typename Vec2<R>::T* __restrict__ tb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
   V* w = reinterpret_cast<V*>(smraw);
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
   if (!S.active[s]) return;
-  const int p = S.fp[f], b = S.fb[f], m = p + b;
+  const int p = S.fp[f], m = p + S.fb[f];
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   V* zs = z + s * S.n;
   const int tid = threadIdx.x;
-  for (int k = tid; k < m; k += blockDim.x) w[k] = zs[I[k]];
-  __syncthreads();
-  // t = y - U12 x_border
-  for (int r = tid; r < p; r += blockDim.x) {
-    V t = w[r];
-    for (int i = 0; i < b; ++i) t = cfms(t, F[(int64_t)(p + i) * m + r], w[p + i]);
-    w[r] = t;
-  }
+  for (int k = tid; k < p; k += blockDim.x) w[k] = tb[s * S.n + S.piv_off[f] + k];
   __syncthreads();
   const int lane = tid & 31, wid = tid >> 5;
   for (int jend = p; jend > 0; jend -= 32) {
@@ -521,20 +608,20 @@ __global__ void k_residual(CombineArgs A, const Coef* __restrict__ coef, const i
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = warp; i < n; i += nwarps) {
-    double sx = 0.0, sy = 0.0;
+    DD sx{0.0, 0.0}, sy{0.0, 0.0};
     for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
       double2 a = combine(A, c, q);
       double2 v = xs[col_idx[q]];
-      sx += a.x * v.x - a.y * v.y;
-      sy += a.x * v.y + a.y * v.x;
+      dd_fma(sx, a.x, v.x);
+      dd_fma(sx, -a.y, v.y);
+      dd_fma(sy, a.x, v.y);
+      dd_fma(sy, a.y, v.x);
     }
-    for (int o = 16; o; o >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, o);
-      sy += __shfl_xor_sync(0xffffffffu, sy, o);
-    }
+    sx = dd_warp_sum(sx);
+    sy = dd_warp_sum(sy);
     if (lane == 0) {
       double2 fi = f[s * n + i];
-      double2 ri = make_double2(fi.x - sx, fi.y - sy);
+      double2 ri = make_double2(dd_residual(fi.x, sx), dd_residual(fi.y, sy));
       r[s * n + i] = ri;
       rr += ri.x * ri.x + ri.y * ri.y;
       ff += fi.x * fi.x + fi.y * fi.y;
@@ -886,6 +973,7 @@ int workspace_ensure(Model& m, int precision, int slots) {
   }
   ELP_CUDA(w.cb.alloc((size_t)slots * std::max<int64_t>(1, D.cb_total) * w.elem));
   ELP_CUDA(w.z.alloc((size_t)slots * n * w.elem));
+  ELP_CUDA(w.tb.alloc((size_t)slots * n * w.elem));
   ELP_CUDA(w.perm.alloc((size_t)slots * n));
   ELP_CUDA(w.dscale.alloc((size_t)slots * n));
   ELP_CUDA(w.x.alloc((size_t)slots * n));
@@ -964,20 +1052,31 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     L.count = LV.count;
     const int steps = (LV.max_p + NB - 1) / NB;
     for (int k = 0; k < steps; ++k) {
+      const int rows = LV.max_m - k * NB;       // rows k0..m-1 of the panel columns
+      const int rest = LV.max_m - k * NB - 1;   // columns right of the panel (upper bound)
+      if (k > 0) {                              // panel columns from all previous panels
+        dim3 gc(LV.count, S_used, (unsigned)std::min(65535, (rows + 127) / 128));
+        PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 128, 32><<<gc, 256, 0, st>>>(L, arena, k, GM_COL));
+      }
       dim3 g1(LV.count, S_used);
       PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB><<<g1, 256, 0, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p));
       if (LV.max_b > 0) {
         dim3 g2(LV.count, S_used, (unsigned)std::min(65535, (LV.max_b + 127) / 128));
         PROF_LAUNCH(KC_BORDER, st, k_border<R, NB><<<g2, 128, 0, st>>>(L, arena, k));
       }
-      const int rest = LV.max_m - k * NB - 1;
       if (rest > 0) {
+        if (k > 0) {                            // pivot rows right of the panel from all previous panels
+          dim3 gr(LV.count, S_used, (unsigned)std::min(65535, (rest + 127) / 128));
+          PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 32, 128><<<gr, 256, 0, st>>>(L, arena, k, GM_ROW));
+        }
         dim3 g3(LV.count, S_used, (unsigned)std::min(65535, (rest + 127) / 128));
         PROF_LAUNCH(KC_UROW, st, k_urow<R, NB><<<g3, 128, 0, st>>>(L, arena, k));
-        const int tr = (rest + 63) / 64;
-        dim3 g4(LV.count, S_used, (unsigned)std::min(65535, tr * tr));
-        PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB><<<g4, 256, 0, st>>>(L, arena, k));
       }
+    }
+    if (LV.max_b > 0) {                         // Schur complement, depth p
+      const int tb = (LV.max_b + 63) / 64;
+      dim3 gs(LV.count, S_used, (unsigned)std::min(65535, tb * tb));
+      PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 64, 64><<<gs, 256, 0, st>>>(L, arena, 0, GM_SCHUR));
     }
     for (size_t k = 0; k < LV.ea_count.size(); ++k) {
       if (!LV.ea_count[k]) continue;
@@ -1019,15 +1118,41 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     S.count = LV.count;
     size_t sm = (size_t)LV.max_m * sizeof(V);
     PROF_LAUNCH(KC_FORWARD, st, k_forward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, w.perm.p, z, cb));
+    if (LV.max_b > 0) {
+      const unsigned chunks = (unsigned)((LV.max_b + 255) / 256);
+      PROF_LAUNCH(KC_FORWARD, st, k_fwd_border<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)LV.max_p * sizeof(V), st>>>(
+                                      S, arena, z, cb));
+    }
   }
+  V* tb = reinterpret_cast<V*>(w.tb.p);
   for (int l = (int)D.levels.size() - 1; l >= 0; --l) {
     const auto& LV = D.levels[l];
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
-    size_t sm = (size_t)LV.max_m * sizeof(V);
-    PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, z));
+    const unsigned chunks = (unsigned)((LV.max_p + 255) / 256);
+    PROF_LAUNCH(KC_BACKWARD, st, k_bwd_u12<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)std::max(1, LV.max_b) * sizeof(V), st>>>(
+                                     S, arena, z, tb));
+    size_t sm = (size_t)LV.max_p * sizeof(V);
+    PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, z, tb));
   }
   ELP_CUDA(cudaGetLastError());
+  return ELP_OK;
+}
+
+template <class R>
+static int solve_smem(const Model& m) {
+  using V = typename Vec2<R>::T;
+  const size_t smem_need = (size_t)m.dsym->max_front * sizeof(V);
+  if (smem_need > 227 * 1024) {
+    set_error("front larger than the shared-memory solve buffer (max 227 KB)");
+    return ELP_ERR_NOMEM;
+  }
+  if (smem_need > 48 * 1024) {
+    ELP_CUDA(cudaFuncSetAttribute(k_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+    ELP_CUDA(cudaFuncSetAttribute(k_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+    ELP_CUDA(cudaFuncSetAttribute(k_fwd_border<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+    ELP_CUDA(cudaFuncSetAttribute(k_bwd_u12<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+  }
   return ELP_OK;
 }
 
@@ -1038,15 +1163,8 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
   const int64_t n = m.n;
   DeviceModel& G = *m.dev;
   CombineArgs A = combine_args(m);
-  const size_t smem_need = (size_t)m.dsym->max_front * sizeof(V);
-  if (smem_need > 48 * 1024) {
-    ELP_CUDA(cudaFuncSetAttribute(k_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-    ELP_CUDA(cudaFuncSetAttribute(k_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-  }
-  if (smem_need > 227 * 1024) {
-    set_error("front larger than the shared-memory solve buffer (max 227 KB)");
-    return ELP_ERR_NOMEM;
-  }
+  int rc0 = solve_smem<R>(m);
+  if (rc0) return rc0;
   for (int s = 0; s < S_used; ++s) { w.h_active[s] = 1; w.iters[s] = 0; }
   ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
   ELP_CUDA(cudaEventRecord(w.ev[0], st));
@@ -1132,15 +1250,8 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
   const int64_t n = m.n;
   DeviceModel& G = *m.dev;
   CombineArgs A = combine_args(m);
-  const size_t smem_need = (size_t)m.dsym->max_front * sizeof(V);
-  if (smem_need > 227 * 1024) {
-    set_error("front larger than the shared-memory solve buffer (max 227 KB)");
-    return ELP_ERR_NOMEM;
-  }
-  if (smem_need > 48 * 1024) {
-    ELP_CUDA(cudaFuncSetAttribute(k_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-    ELP_CUDA(cudaFuncSetAttribute(k_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-  }
+  int rc0 = solve_smem<R>(m);
+  if (rc0) return rc0;
   const int RST = 24;
   int rc = gmres_alloc(w, n, w.slots, RST);
   if (rc) return rc;

@@ -29,6 +29,9 @@ struct CombineArgs {
   int ngroups;
 };
 
+CombineArgs combine_args(const Model& m);
+
+#ifdef __CUDACC__
 // A(w) at CSR entry q, Dirichlet rows included (MatZeroRows, diag = 1)
 __device__ __forceinline__ double2 combine(const CombineArgs& A, const Coef& c, int64_t q) {
   const uint8_t k = A.cls[q] & CLS_MASK;
@@ -47,7 +50,49 @@ __device__ __forceinline__ double2 combine(const CombineArgs& A, const Coef& c, 
   return v;
 }
 
-CombineArgs combine_args(const Model& m);
+// Double-double accumulation for the FP64 residual r = f - A x. Near a
+// resonance |A| |x| >> |f|, and a plain FP64 sum leaves ||f - A x|| / ||f||
+// at a rounding floor near 1e-10; error-free transformations (products by
+// FMA, sums by TwoSum) make the computed residual accurate to the last bits
+// of the stored A and x instead.
+struct DD {
+  double hi, lo;
+};
+__device__ __forceinline__ void dd_add(DD& s, double b) {
+  double t = s.hi + b;
+  double bb = t - s.hi;
+  double e = (s.hi - (t - bb)) + (b - bb);
+  s.hi = t;
+  s.lo += e;
+}
+__device__ __forceinline__ void dd_fma(DD& s, double a, double b) {  // s += a * b exactly (to dd)
+  double p = a * b;
+  double e = fma(a, b, -p);
+  dd_add(s, p);
+  s.lo += e;
+}
+__device__ __forceinline__ void dd_merge(DD& s, const DD& o) {
+  dd_add(s, o.hi);
+  s.lo += o.lo;
+}
+// warp-wide sum of a DD held per lane
+__device__ __forceinline__ DD dd_warp_sum(DD v) {
+  for (int o = 16; o; o >>= 1) {
+    DD w;
+    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    dd_merge(v, w);
+  }
+  return v;
+}
+// f - (a.hi + a.lo), rounded once
+__device__ __forceinline__ double dd_residual(double f, const DD& a) {
+  DD s{f, 0.0};
+  dd_add(s, -a.hi);
+  s.lo -= a.lo;
+  return s.hi + s.lo;
+}
+#endif  // __CUDACC__
 
 struct DeviceSymbolic {
   DevBuf<int32_t> f_p, f_b, f_parent, f_idx_off, f_map_off, f_cb_off, f_piv_off;
@@ -75,6 +120,7 @@ struct Workspace {
   DevBuf<char> arena;             // slots x arena complex entries
   DevBuf<char> cb;                // slots x cb_total complex (solve contributions)
   DevBuf<char> z;                 // slots x n complex (solve vector, front precision)
+  DevBuf<char> tb;                // slots x n complex (backward pivot-row buffer)
   DevBuf<int32_t> perm;           // slots x n local pivot rows
   DevBuf<double> dscale;          // slots x n symmetric diagonal scaling
   DevBuf<double2> x, r, f;        // slots x n FP64 solution, residual, rhs
