@@ -21,6 +21,7 @@
 //    the correction is solved with the front-precision factors, and x is
 //    updated in FP64 until ||r||/||f|| <= tol.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 
@@ -377,6 +378,10 @@ __global__ void __launch_bounds__(256) k_gemm(LevelArgs L, typename Vec2<R>::T* 
       }
   }
 }
+
+}  // namespace elp
+#include "gemm_tc.cuh"
+namespace elp {
 
 // extend-add of children's Schur complements into their parents
 template <class R>
@@ -985,6 +990,8 @@ int workspace_ensure(Model& m, int precision, int slots) {
   ELP_CUDA(w.partial.alloc((size_t)slots * w.nparts * 2));
   ELP_CUDA(w.active.alloc(slots));
   ELP_CUDA(w.stats.alloc(4 * (size_t)slots));
+  ELP_CUDA(w.tc_err.alloc(1));
+  ELP_CUDA(cudaMemset(w.tc_err.p, 0, sizeof(int)));
   ELP_CUDA(cudaMallocHost((void**)&w.h_coef, sizeof(Coef) * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_norms, sizeof(double) * 2 * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_active, sizeof(int) * slots));
@@ -1046,6 +1053,50 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   L.arena_size = D.arena;
   L.n = n;
   const R tiny = sizeof(R) == 8 ? (R)1e-10 : (R)1e-6;
+  // FP32 fronts: Schur updates on the tensor cores (tcgen05, 3xTF32) unless ELP_TC=0
+  static const bool use_tc = !(getenv("ELP_TC") && getenv("ELP_TC")[0] == '0');
+  const bool tc = std::is_same<R, float>::value && use_tc;
+  if (tc) {
+    static bool attr = false;
+    if (!attr) {
+      ELP_CUDA(cudaFuncSetAttribute(k_gemm_tc<NB, 32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(TcSmem<32>)));
+      ELP_CUDA(cudaFuncSetAttribute(k_gemm_tc<NB, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(TcSmem<32>)));
+      ELP_CUDA(cudaFuncSetAttribute(k_gemm_tc<NB, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(TcSmem<64>)));
+      attr = true;
+    }
+  }
+  // mode: GM_COL / GM_ROW / GM_SCHUR; rows_c, cols_c: upper bounds of the C block over the level
+  auto gemm = [&](int mode, int k, int rows_c, int cols_c) {
+    if (tc) {
+      float2* fa = reinterpret_cast<float2*>(arena);
+      if (mode == GM_SCHUR) {
+        const int t = ((rows_c + 127) / 128) * ((cols_c + 63) / 64);
+        dim3 g(L.count, S_used, (unsigned)std::min(65535, t));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 64, false><<<g, 256, sizeof(TcSmem<64>), st>>>(L, fa, k, mode, w.tc_err.p));
+      } else if (mode == GM_COL) {
+        dim3 g(L.count, S_used, (unsigned)std::min(65535, (rows_c + 127) / 128));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, false><<<g, 256, sizeof(TcSmem<32>), st>>>(L, fa, k, mode, w.tc_err.p));
+      } else {
+        dim3 g(L.count, S_used, (unsigned)std::min(65535, (cols_c + 127) / 128));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, true><<<g, 256, sizeof(TcSmem<32>), st>>>(L, fa, k, mode, w.tc_err.p));
+      }
+      return;
+    }
+    if (mode == GM_SCHUR) {
+      const int t = ((rows_c + 63) / 64) * ((cols_c + 63) / 64);
+      dim3 g(L.count, S_used, (unsigned)std::min(65535, t));
+      PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 64, 64><<<g, 256, 0, st>>>(L, arena, k, mode));
+    } else if (mode == GM_COL) {
+      dim3 g(L.count, S_used, (unsigned)std::min(65535, (rows_c + 127) / 128));
+      PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 128, 32><<<g, 256, 0, st>>>(L, arena, k, mode));
+    } else {
+      dim3 g(L.count, S_used, (unsigned)std::min(65535, (cols_c + 127) / 128));
+      PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 32, 128><<<g, 256, 0, st>>>(L, arena, k, mode));
+    }
+  };
   for (size_t l = 0; l < D.levels.size(); ++l) {
     const auto& LV = D.levels[l];
     L.list = D.level_list.p + LV.start;
@@ -1054,10 +1105,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     for (int k = 0; k < steps; ++k) {
       const int rows = LV.max_m - k * NB;       // rows k0..m-1 of the panel columns
       const int rest = LV.max_m - k * NB - 1;   // columns right of the panel (upper bound)
-      if (k > 0) {                              // panel columns from all previous panels
-        dim3 gc(LV.count, S_used, (unsigned)std::min(65535, (rows + 127) / 128));
-        PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 128, 32><<<gc, 256, 0, st>>>(L, arena, k, GM_COL));
-      }
+      if (k > 0) gemm(GM_COL, k, rows, NB);     // panel columns from all previous panels
       dim3 g1(LV.count, S_used);
       PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB><<<g1, 256, 0, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p));
       if (LV.max_b > 0) {
@@ -1065,19 +1113,12 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
         PROF_LAUNCH(KC_BORDER, st, k_border<R, NB><<<g2, 128, 0, st>>>(L, arena, k));
       }
       if (rest > 0) {
-        if (k > 0) {                            // pivot rows right of the panel from all previous panels
-          dim3 gr(LV.count, S_used, (unsigned)std::min(65535, (rest + 127) / 128));
-          PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 32, 128><<<gr, 256, 0, st>>>(L, arena, k, GM_ROW));
-        }
+        if (k > 0) gemm(GM_ROW, k, NB, rest);  // pivot rows right of the panel from all previous panels
         dim3 g3(LV.count, S_used, (unsigned)std::min(65535, (rest + 127) / 128));
         PROF_LAUNCH(KC_UROW, st, k_urow<R, NB><<<g3, 128, 0, st>>>(L, arena, k));
       }
     }
-    if (LV.max_b > 0) {                         // Schur complement, depth p
-      const int tb = (LV.max_b + 63) / 64;
-      dim3 gs(LV.count, S_used, (unsigned)std::min(65535, tb * tb));
-      PROF_LAUNCH(KC_GEMM, st, k_gemm<R, NB, 64, 64><<<gs, 256, 0, st>>>(L, arena, 0, GM_SCHUR));
-    }
+    if (LV.max_b > 0) gemm(GM_SCHUR, 0, LV.max_b, LV.max_b);  // Schur complement, depth p
     for (size_t k = 0; k < LV.ea_count.size(); ++k) {
       if (!LV.ea_count[k]) continue;
       dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, LV.ea_max_b));
@@ -1433,8 +1474,14 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
   if (rc) return rc;
   ELP_CUDA(cudaMemcpyAsync(x_dev, w.x.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToDevice, st));
   ELP_CUDA(cudaMemcpyAsync(w.h_stats, w.stats.p, sizeof(unsigned long long) * 4 * n_omega, cudaMemcpyDeviceToHost, st));
+  int tcerr = 0;
+  ELP_CUDA(cudaMemcpyAsync(&tcerr, w.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   ELP_CUDA(cudaStreamSynchronize(st));
   prof_resolve();
+  if (tcerr) {
+    set_error("a tensor-core Schur update gave up waiting for its MMAs");
+    return ELP_ERR_CUDA;
+  }
   bool ok = true;
   for (int s = 0; s < n_omega; ++s) {
     double fn = w.h_norms[2 * s + 1];

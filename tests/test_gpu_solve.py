@@ -33,6 +33,8 @@ def check(elp, oracle, d, f_list, prec):
         err = np.linalg.norm(x[k] - xr) / np.linalg.norm(xr)
         assert res <= RES_TOL, (k, res)
         assert err <= max(1e-12, 4.0 * cond1(A) * RES_TOL), (k, err)
+        if prec == 1:  # FP32 fronts are a good preconditioner: few GMRES steps
+            assert infos[k]["iterations"] <= 24, (k, infos[k]["iterations"])
         assert infos[k]["converged"] == 1
         assert abs(infos[k]["rel_residual"] - res) <= 1e-10
     return m, infos

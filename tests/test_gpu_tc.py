@@ -1,0 +1,48 @@
+"""Tensor-core (tcgen05, 3xTF32) Schur updates against the SIMT FP32 ones.
+
+The mixed path runs its FP32 front updates on the tensor cores; ELP_TC=0
+selects the SIMT kernels instead. Both factorisations are preconditioners
+for the same FP64 GMRES, so with the 3xTF32 split (FP32-level products) the
+two must converge to the 1e-10 relative residual in nearly the same number
+of steps (difference <= 2) at every frequency. Each variant runs in its own
+process because the switch is read once per process.
+"""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+PROBE = r"""
+import importlib, json, sys
+import numpy as np
+sys.path.insert(0, ROOT)
+from tests.conftest import load_package
+elp = load_package()
+meshes = importlib.import_module("elpaso_core_gb300.meshes")
+out = {}
+for name, d in (("pc", meshes.plate_cavity(16, 12, 8, 0.6, 0.4, 0.3)), ("cube", meshes.cube(7))):
+    m = elp.Model(d).assemble().analyse()
+    x, info = m.solve(2 * np.pi * np.array([2.0, 37.0, 111.0, 260.0, 499.0]), precision=1)
+    out[name] = [(i["iterations"], i["rel_residual"]) for i in info]
+print(json.dumps(out))
+""".replace("ROOT", repr(ROOT))
+
+
+def _run(tc):
+    env = dict(os.environ, ELP_TC=tc)
+    p = subprocess.run([sys.executable, "-c", PROBE], env=env, capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    return json.loads(p.stdout.strip().splitlines()[-1])
+
+
+def test_tensor_core_updates_match_simt_convergence():
+    tc, simt = _run("1"), _run("0")
+    for name in tc:
+        for (it_a, res_a), (it_b, res_b) in zip(tc[name], simt[name]):
+            assert res_a <= 1e-10 and res_b <= 1e-10
+            assert abs(it_a - it_b) <= 2, (name, tc[name], simt[name])
