@@ -120,7 +120,8 @@ EXPORTS = [
     "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc",
 ]
 KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
-                  "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc"]
+                  "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc", "spmv", "fwd_border",
+                  "bwd_u12", "krylov"]
 
 _lib = None
 
@@ -335,9 +336,9 @@ def profile(enable: bool = True):
 
 
 def profile_read() -> dict:
-    ms = np.zeros(16)
-    launches = np.zeros(16, np.int64)
-    timed = np.zeros(16, np.int64)
+    ms = np.zeros(len(KERNEL_CLASSES))
+    launches = np.zeros(len(KERNEL_CLASSES), np.int64)
+    timed = np.zeros(len(KERNEL_CLASSES), np.int64)
     nc = C.c_int()
     _check(load_library().elp_profile_read(_ptr(ms), _ptr(launches), _ptr(timed), C.byref(nc)))
     return {KERNEL_CLASSES[i]: {"ms": float(ms[i]), "launches": int(launches[i]), "timed": int(timed[i])}

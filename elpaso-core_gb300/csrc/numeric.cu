@@ -458,15 +458,21 @@ __global__ void __launch_bounds__(256) k_forward(SolveArgs S, const typename Vec
   const int lane = tid & 31, wid = tid >> 5;
   // L11 solve on the pivot block only; the border rows (L21) are updated by
   // k_fwd_border across many CTAs
+  __shared__ V dblk[32][33];  // diagonal 32 x 32 block, staged so the warp solve never waits on DRAM
   for (int j0 = 0; j0 < p; j0 += 32) {
     const int jw = min(32, p - j0);
+    for (int t = tid; t < 32 * 32; t += blockDim.x) {
+      const int jj = t >> 5, ii = t & 31;
+      if (jj < jw && ii < jw) dblk[ii][jj] = F[(int64_t)(j0 + jj) * m + j0 + ii];
+    }
+    __syncthreads();
     if (wid == 0) {
       V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
       for (int jj = 0; jj < jw; ++jj) {
         V x;
         x.x = __shfl_sync(0xffffffffu, val.x, jj);
         x.y = __shfl_sync(0xffffffffu, val.y, jj);
-        if (lane > jj && lane < jw) val = cfms(val, F[(int64_t)(j0 + jj) * m + j0 + lane], x);
+        if (lane > jj && lane < jw) val = cfms(val, dblk[lane][jj], x);
       }
       if (lane < jw) w[j0 + lane] = val;
     }
@@ -573,17 +579,23 @@ __global__ void __launch_bounds__(256) k_backward(SolveArgs S, const typename Ve
   for (int k = tid; k < p; k += blockDim.x) w[k] = tb[s * S.n + S.piv_off[f] + k];
   __syncthreads();
   const int lane = tid & 31, wid = tid >> 5;
+  __shared__ V dblk[32][33];  // diagonal 32 x 32 block, staged so the warp solve never waits on DRAM
   for (int jend = p; jend > 0; jend -= 32) {
     const int j0 = max(0, jend - 32);
     const int jw = jend - j0;
+    for (int t = tid; t < 32 * 32; t += blockDim.x) {
+      const int jj = t >> 5, ii = t & 31;
+      if (jj < jw && ii < jw) dblk[ii][jj] = F[(int64_t)(j0 + jj) * m + j0 + ii];
+    }
+    __syncthreads();
     if (wid == 0) {
       V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
       for (int jj = jw - 1; jj >= 0; --jj) {
-        if (lane == jj) val = cmul(val, cinv(F[(int64_t)(j0 + jj) * m + j0 + jj]));
+        if (lane == jj) val = cmul(val, cinv(dblk[jj][jj]));
         V x;
         x.x = __shfl_sync(0xffffffffu, val.x, jj);
         x.y = __shfl_sync(0xffffffffu, val.y, jj);
-        if (lane < jj) val = cfms(val, F[(int64_t)(j0 + jj) * m + j0 + lane], x);
+        if (lane < jj) val = cfms(val, dblk[lane][jj], x);
       }
       if (lane < jw) w[j0 + lane] = val;
     }
@@ -1161,7 +1173,7 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     PROF_LAUNCH(KC_FORWARD, st, k_forward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, w.perm.p, z, cb));
     if (LV.max_b > 0) {
       const unsigned chunks = (unsigned)((LV.max_b + 255) / 256);
-      PROF_LAUNCH(KC_FORWARD, st, k_fwd_border<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)LV.max_p * sizeof(V), st>>>(
+      PROF_LAUNCH(KC_FWD_BORDER, st, k_fwd_border<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)LV.max_p * sizeof(V), st>>>(
                                       S, arena, z, cb));
     }
   }
@@ -1171,7 +1183,7 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
     const unsigned chunks = (unsigned)((LV.max_p + 255) / 256);
-    PROF_LAUNCH(KC_BACKWARD, st, k_bwd_u12<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)std::max(1, LV.max_b) * sizeof(V), st>>>(
+    PROF_LAUNCH(KC_BWD_U12, st, k_bwd_u12<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)std::max(1, LV.max_b) * sizeof(V), st>>>(
                                      S, arena, z, tb));
     size_t sm = (size_t)LV.max_p * sizeof(V);
     PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, z, tb));
@@ -1188,12 +1200,12 @@ static int solve_smem(const Model& m) {
     set_error("front larger than the shared-memory solve buffer (max 227 KB)");
     return ELP_ERR_NOMEM;
   }
-  if (smem_need > 48 * 1024) {
-    ELP_CUDA(cudaFuncSetAttribute(k_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-    ELP_CUDA(cudaFuncSetAttribute(k_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-    ELP_CUDA(cudaFuncSetAttribute(k_fwd_border<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-    ELP_CUDA(cudaFuncSetAttribute(k_bwd_u12<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-  }
+  // the triangle kernels also hold a static 32 x 33 diagonal block, so the
+  // dynamic limit is raised whatever the front size
+  ELP_CUDA(cudaFuncSetAttribute(k_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+  ELP_CUDA(cudaFuncSetAttribute(k_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+  ELP_CUDA(cudaFuncSetAttribute(k_fwd_border<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
+  ELP_CUDA(cudaFuncSetAttribute(k_bwd_u12<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
   return ELP_OK;
 }
 
@@ -1352,7 +1364,7 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
     ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
     ELP_CUDA(cudaMemcpyAsync(w.inner.p, w.h_inner, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
     ELP_CUDA(cudaMemcpyAsync(w.scal.p, w.h_scal, sizeof(double) * S_used, cudaMemcpyHostToDevice, st));
-    k_vscale<<<gv, 256, 0, st>>>(w.r.p, w.Vb.p, vst, w.scal.p, n, w.inner.p);
+    PROF_LAUNCH(KC_KRYLOV, st, k_vscale<<<gv, 256, 0, st>>>(w.r.p, w.Vb.p, vst, w.scal.p, n, w.inner.p));
     for (int j = 0; j < RST; ++j) {
       ELP_CUDA(cudaEventRecord(w.ev[2], st));
       rc = precond(w.Vb.p + (int64_t)j * n, vst, w.inner.p);
@@ -1360,18 +1372,18 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
       ELP_CUDA(cudaEventRecord(w.ev[3], st));
       // Z_j = M^-1 V_j kept in FP64 (flexible GMRES: the update uses Z y, so
       // rounding of the front-precision solve never enters the Arnoldi relation)
-      k_unscale<V><<<gv, 256, 0, st>>>(z, w.dscale.p, n, w.Zb.p + (int64_t)j * n, zst, w.inner.p);
-      PROF_LAUNCH(KC_RESIDUAL, st, k_spmv<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n,
+      PROF_LAUNCH(KC_KRYLOV, st, k_unscale<V><<<gv, 256, 0, st>>>(z, w.dscale.p, n, w.Zb.p + (int64_t)j * n, zst, w.inner.p));
+      PROF_LAUNCH(KC_SPMV, st, k_spmv<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n,
                                                                  w.Zb.p + (int64_t)j * n, zst, w.wv.p, w.inner.p));
       const int nv = j + 1;
-      k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p);
-      k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd1.p, w.inner.p);
-      k_gs<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.hd1.p, w.wv.p, n, w.inner.p);
-      k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p);
-      k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd2.p, w.inner.p);
-      k_gs<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.hd2.p, w.wv.p, n, w.inner.p);
-      k_dots<<<gr, 256, 0, st>>>(w.wv.p, n, 0, 1, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p);
-      k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, 1, w.hnd.p, w.inner.p);
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd1.p, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_gs<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.hd1.p, w.wv.p, n, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd2.p, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_gs<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.hd2.p, w.wv.p, n, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gr, 256, 0, st>>>(w.wv.p, n, 0, 1, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, 1, w.hnd.p, w.inner.p));
       ELP_CUDA(cudaMemcpyAsync(w.h_h, w.hd1.p, sizeof(double2) * S_used * kMaxBasis, cudaMemcpyDeviceToHost, st));
       ELP_CUDA(cudaMemcpyAsync(w.h_h + S_used * kMaxBasis, w.hd2.p, sizeof(double2) * S_used * kMaxBasis,
                                cudaMemcpyDeviceToHost, st));
@@ -1416,7 +1428,7 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
         w.h_scal[s] = hn > 0 ? 1.0 / hn : 0.0;
       }
       ELP_CUDA(cudaMemcpyAsync(w.scal.p, w.h_scal, sizeof(double) * S_used, cudaMemcpyHostToDevice, st));
-      k_vscale<<<gv, 256, 0, st>>>(w.wv.p, w.Vb.p + (int64_t)(j + 1) * n, vst, w.scal.p, n, w.inner.p);
+      PROF_LAUNCH(KC_KRYLOV, st, k_vscale<<<gv, 256, 0, st>>>(w.wv.p, w.Vb.p + (int64_t)(j + 1) * n, vst, w.scal.p, n, w.inner.p));
       ELP_CUDA(cudaMemcpyAsync(w.inner.p, w.h_inner, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
       if (!more) break;
     }

@@ -16,6 +16,7 @@ namespace elp {
 enum KernelClass {
   KC_ASSEMBLE = 0, KC_DSCALE, KC_SCATTER, KC_PANEL, KC_BORDER, KC_UROW, KC_GEMM, KC_EXTEND_ADD,
   KC_FORWARD, KC_BACKWARD, KC_RESIDUAL, KC_NORMS, KC_RHS, KC_UPDATE, KC_VALUES, KC_GEMM_TC,
+  KC_SPMV, KC_FWD_BORDER, KC_BWD_U12, KC_KRYLOV,
   KC_COUNT
 };
 

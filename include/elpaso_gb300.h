@@ -232,13 +232,15 @@ int elp_residual_noalloc(elp_model* m, const double* omegas, int n_omega, const 
 /* Kernel classes, in the order of the arrays below:
  *  0 assemble, 1 dscale, 2 scatter, 3 panel, 4 border, 5 urow, 6 gemm,
  *  7 extend_add, 8 forward, 9 backward, 10 residual, 11 norms, 12 rhs,
- *  13 update, 14 values, 15 gemm_tc.
+ *  13 update, 14 values, 15 gemm_tc, 16 spmv, 17 fwd_border, 18 bwd_u12,
+ *  19 krylov (GMRES vector kernels).
  * No reference counterpart (the reference times whole phases with
  * cStopwatch, basics/watch/stopwatch.cpp:35-64). elp_profile(1) resets the
  * counters and records a CUDA event pair around every launch on its stream;
  * elp_profile(0) resets and counts launches only. */
 int elp_profile(int enable);
-int elp_profile_read(double* ms /* [16] */, int64_t* launches /* [16] */, int64_t* timed /* [16] */,
+#define ELP_PROFILE_CLASSES 20
+int elp_profile_read(double* ms /* [ELP_PROFILE_CLASSES] */, int64_t* launches, int64_t* timed,
                      int* n_classes);
 
 /* ---- serving loop (continuous batching over resident models) ------------ */
