@@ -21,6 +21,7 @@
 //    the correction is solved with the front-precision factors, and x is
 //    updated in FP64 until ||r||/||f|| <= tol.
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 #include <cmath>
 #include <cstring>
@@ -1069,16 +1070,18 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   static const bool use_tc = !(getenv("ELP_TC") && getenv("ELP_TC")[0] == '0');
   const bool tc = std::is_same<R, float>::value && use_tc;
   if (tc) {
-    static bool attr = false;
-    if (!attr) {
-      ELP_CUDA(cudaFuncSetAttribute(k_gemm_tc<NB, 32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)sizeof(TcSmem<32>)));
-      ELP_CUDA(cudaFuncSetAttribute(k_gemm_tc<NB, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)sizeof(TcSmem<32>)));
-      ELP_CUDA(cudaFuncSetAttribute(k_gemm_tc<NB, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)sizeof(TcSmem<64>)));
-      attr = true;
-    }
+    static std::once_flag once;
+    static cudaError_t e = cudaSuccess;
+    std::call_once(once, [] {
+      cudaError_t a = cudaFuncSetAttribute(k_gemm_tc<NB, 32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(TcSmem<32>));
+      cudaError_t b = cudaFuncSetAttribute(k_gemm_tc<NB, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(TcSmem<32>));
+      cudaError_t c = cudaFuncSetAttribute(k_gemm_tc<NB, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sizeof(TcSmem<64>));
+      e = a != cudaSuccess ? a : b != cudaSuccess ? b : c;
+    });
+    ELP_CUDA(e);
   }
   // mode: GM_COL / GM_ROW / GM_SCHUR; rows_c, cols_c: upper bounds of the C block over the level
   auto gemm = [&](int mode, int k, int rows_c, int cols_c) {
@@ -1200,13 +1203,29 @@ static int solve_smem(const Model& m) {
     set_error("front larger than the shared-memory solve buffer (max 227 KB)");
     return ELP_ERR_NOMEM;
   }
-  // the triangle kernels also hold a static 32 x 33 diagonal block, so the
-  // dynamic limit is raised whatever the front size
-  ELP_CUDA(cudaFuncSetAttribute(k_forward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-  ELP_CUDA(cudaFuncSetAttribute(k_backward<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-  ELP_CUDA(cudaFuncSetAttribute(k_fwd_border<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-  ELP_CUDA(cudaFuncSetAttribute(k_bwd_u12<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_need));
-  return ELP_OK;
+  // The limit is raised once per process to what the device allows: solves of
+  // different models run concurrently (server workers), and a per-model value
+  // set by one thread could lower the limit under another thread's launch.
+  static std::once_flag once;
+  static int rc = ELP_OK;
+  std::call_once(once, [] {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const void* fns[4] = {(const void*)k_forward<R>, (const void*)k_backward<R>, (const void*)k_fwd_border<R>,
+                          (const void*)k_bwd_u12<R>};
+    for (const void* fn : fns) {
+      cudaFuncAttributes a;
+      if (cudaFuncGetAttributes(&a, fn) != cudaSuccess ||
+          cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes) !=
+              cudaSuccess) {
+        cudaGetLastError();
+        rc = ELP_ERR_CUDA;
+      }
+    }
+  });
+  if (rc) set_error("could not raise the shared-memory limit of the solve kernels");
+  return rc;
 }
 
 template <class R>

@@ -190,6 +190,9 @@ struct elp_server {
             rc = ELP_ERR_CUDA;
         }
       }
+      if (rc && rc != ELP_ERR_NOMEM)  // the per-thread error text does not reach the caller's thread
+        fprintf(stderr, "[elp server] batch of %zu frequencies on model %d failed (%d): %s\n", items.size(), mi, rc,
+                get_error().c_str());
       lk.lock();
       for (size_t i = 0; i < items.size(); ++i) {
         auto it = reqs.find(items[i].rid);
