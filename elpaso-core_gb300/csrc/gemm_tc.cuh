@@ -1,21 +1,22 @@
 // Tensor-core (tcgen05, kind::tf32) complex Schur updates of FP32 fronts.
 //
-// C -= A B on sub-blocks of a column-major complex FP32 front, with the
-// complex product written as one real GEMM on real blocks:
-//   [C_re | C_im] = [A_re  A_im] . [[ B_re, B_im],
-//                                   [-B_im, B_re]]
-// and each real operand split into TF32 hi + lo parts (x = hi + lo, both
-// rounded to TF32), accumulating hi*hi + hi*lo + lo*hi in FP32 in tensor
-// memory: FP32-level products from three TF32 passes ("3xTF32").
+// C -= A B on sub-blocks of a column-major complex FP32 front, from four
+// real products accumulated in tensor memory,
+//   D_re = A_re B_re + (-A_im) B_im      (the minus is the negate-A bit)
+//   D_im = A_re B_im + A_im B_re,
+// with each real operand split into TF32 hi + lo parts (x = hi + lo, both
+// rounded to TF32) and hi*hi + hi*lo + lo*hi accumulated in FP32:
+// FP32-level products from three TF32 passes ("3xTF32").
 //
-// One CTA (256 threads) computes a 128 x NT complex tile: MMA M = 128 rows,
-// N = 2 NT real columns, K = 8 per instruction. Operands are converted in
-// registers and stored to shared memory in the canonical K-major,
-// no-swizzle layout (8-row x 16-byte core matrices; LBO = stride between
-// core matrices along K, SBO = stride between 8-row groups); thread 0 issues
-// the MMAs; tcgen05.commit arrives on an mbarrier that every thread waits on
-// (with an iteration bound) before the shared buffers are refilled or the
-// accumulator is read back with tcgen05.ld.
+// One CTA (256 threads) computes a 128 x NT complex tile: MMA M = 128, N = NT,
+// K = 8 per instruction. Operands are converted in registers and stored to
+// shared memory in the canonical K-major, no-swizzle layout (8-row x 16-byte
+// core matrices; LBO = stride between core matrices along K, SBO = stride
+// between 8-row groups); each warp writes whole core matrices, so the stores
+// are free of bank conflicts. Two shared-memory stages: while the MMAs of
+// chunk c run, the CTA stages chunk c + 1; tcgen05.commit arrives on the
+// stage's mbarrier, which is waited on (with an iteration bound) before that
+// stage is refilled and before the accumulator is read back with tcgen05.ld.
 //
 // TRANS = false: MMA rows are rows of C (GM_COL, GM_SCHUR);
 // TRANS = true:  MMA rows are columns of C (GM_ROW, whose C has only the 32
@@ -41,9 +42,11 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-// instruction descriptor: D = F32, A = B = TF32, both K-major, N >> 3, M >> 4
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// instruction descriptor: D = F32, A = B = TF32, both K-major, optional
+// negation of A (bit 13), N >> 3, M >> 4
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N, bool neg_a = false) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (neg_a ? (1u << 13) : 0u) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ uint32_t to_tf32(float x) {
@@ -107,23 +110,27 @@ __device__ __forceinline__ void ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// byte offset of (row, k) in a K-major no-swizzle tile with KT 32-bit elements per row
-__device__ __forceinline__ uint32_t kmajor_off(int row, int k, int KT) {
-  return (uint32_t)(((row >> 3) * (KT >> 2) + (k >> 2)) * 128 + (row & 7) * 16 + (k & 3) * 4);
-}
-
 }  // namespace tc
 
-constexpr int kTcKC = 16;               // complex K per chunk
-constexpr int kTcKT = 2 * kTcKC;        // real K per chunk (real and imaginary blocks)
+constexpr int kTcKC = 16;  // complex K per stage
 
+// one stage: planes [re_hi, re_lo, im_hi, im_lo] of A (128 x KC) and B (NT x KC)
+template <int NT>
+struct TcStage {
+  uint32_t a[4][128 * kTcKC];
+  uint32_t b[4][NT * kTcKC];
+};
 template <int NT>
 struct TcSmem {
-  uint32_t a_hi[128 * kTcKT], a_lo[128 * kTcKT];            // 128 rows x KT
-  uint32_t b_hi[2 * NT * kTcKT], b_lo[2 * NT * kTcKT];      // 2 NT rows x KT
-  uint64_t mbar;
+  TcStage<NT> st[2];
+  uint64_t mbar[2];
   uint32_t tmem_base;
 };
+
+// word index of (row, k) in a K-major no-swizzle tile with kTcKC words per row
+__device__ __forceinline__ int tc_word(int row, int k) {
+  return ((row >> 3) * (kTcKC >> 2) + (k >> 2)) * 32 + (row & 7) * 4 + (k & 3);
+}
 
 // C -= A B on one front's sub-block, FP32 complex, tcgen05 3xTF32.
 template <int NB, int NT, bool TRANS>
@@ -139,14 +146,13 @@ __global__ void __launch_bounds__(256) k_gemm_tc(LevelArgs L, float2* __restrict
   const int w = min(NB, p - k0);
   int ra, M, ca, N, K;
   if (!gemm_block(mode, p, m, k0, w, ra, M, ca, N, K)) return;
-  // MMA-row extent MR and MMA-column extent NC (complex)
-  const int MR = TRANS ? N : M, NC = TRANS ? M : N;
+  const int MR = TRANS ? N : M, NC = TRANS ? M : N;  // MMA rows / columns (complex)
   const int tiles_r = (MR + 127) / 128, tiles_c = (NC + NT - 1) / NT;
   const int ntiles = tiles_r * tiles_c;
-  if ((int)blockIdx.z >= ntiles) return;  // uniform per CTA
+  if ((int)blockIdx.z >= ntiles) return;  // uniform per CTA, before any TMEM allocation
   float2* F = arena + s * L.arena_size + L.foff[f];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  constexpr uint32_t kCols = 2 * NT < 32 ? 32 : 2 * NT;   // TMEM columns (power of two >= 32)
+  constexpr uint32_t kCols = 2 * NT;  // D_re | D_im, a power of two >= 32
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(&sm.tmem_base)),
                  "r"(kCols)
@@ -154,84 +160,107 @@ __global__ void __launch_bounds__(256) k_gemm_tc(LevelArgs L, float2* __restrict
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    tc::mbar_init(&sm.mbar, 1);
+    tc::mbar_init(&sm.mbar[0], 1);
+    tc::mbar_init(&sm.mbar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = sm.tmem_base;
-  constexpr uint32_t idesc = tc::idesc_tf32(128, 2 * NT);
-  uint32_t phase = 0;
+  constexpr uint32_t id_pos = tc::idesc_tf32(128, NT, false), id_neg = tc::idesc_tf32(128, NT, true);
+  constexpr uint32_t LBO = 128, SBO = (kTcKC / 4) * 128;
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
   bool ok = true;
+  // lane -> element of one 8 x 4 core matrix
+  const int cr = lane >> 2, ck = lane & 3;
   for (int tile = blockIdx.z; tile < ntiles && ok; tile += gridDim.z) {
-    const int i0 = (tile % tiles_r) * 128;   // MMA row origin
-    const int j0 = (tile / tiles_r) * NT;    // MMA column origin (complex)
-    for (int kc = 0; kc < K; kc += kTcKC) {
-      // ---- stage P (128 x KC complex) as [re | im] real blocks, hi/lo
-      for (int t = tid; t < 128 * kTcKC; t += 256) {
-        int i, k;
-        if (!TRANS) { i = t % 128; k = t / 128; }   // column-major source: i contiguous
-        else { k = t % kTcKC; i = t / kTcKC; }       // U row segments: k contiguous
+    const int i0 = (tile % tiles_r) * 128;
+    const int j0 = (tile / tiles_r) * NT;
+    int stage = 0, nchunks = (K + kTcKC - 1) / kTcKC;
+    for (int c = 0; c < nchunks && ok; ++c, stage ^= 1) {
+      const int kc = c * kTcKC;
+      if (pending[stage]) {  // the MMAs that read this stage two chunks ago
+        ok = tc::mbar_wait(&sm.mbar[stage], phase[stage]);
+        phase[stage] ^= 1u;
+        pending[stage] = false;
+        if (!ok) break;
+      }
+      TcStage<NT>& S = sm.st[stage];
+      // ---- A planes: 128 x KC, core matrices (16 row groups x 4 k groups) over 8 warps
+      for (int cm = warp; cm < 16 * (kTcKC / 4); cm += 8) {
+        const int i = (cm / (kTcKC / 4)) * 8 + cr, k = (cm % (kTcKC / 4)) * 4 + ck;
         float2 v = make_float2(0.f, 0.f);
-        if (i0 + i < MR && kc + k < K) {
-          v = !TRANS ? F[(int64_t)(kc + k) * m + ra + i0 + i]        // A = L[ra + i, k]
-                     : F[(int64_t)(ca + i0 + i) * m + kc + k];      // B^T: U[k, ca + i]
-        }
+        if (i0 + i < MR && kc + k < K)
+          v = !TRANS ? F[(int64_t)(kc + k) * m + ra + i0 + i]     // A = L[ra + i, k]
+                     : F[(int64_t)(ca + i0 + i) * m + kc + k];   // B^T: U[k, ca + i]
+        const int wd = tc_word(i, k);
         uint32_t h, l;
         tc::split_tf32(v.x, h, l);
-        sm.a_hi[tc::kmajor_off(i, k, kTcKT) >> 2] = h;
-        sm.a_lo[tc::kmajor_off(i, k, kTcKT) >> 2] = l;
+        S.a[0][wd] = h;
+        S.a[1][wd] = l;
         tc::split_tf32(v.y, h, l);
-        sm.a_hi[tc::kmajor_off(i, kTcKC + k, kTcKT) >> 2] = h;
-        sm.a_lo[tc::kmajor_off(i, kTcKC + k, kTcKT) >> 2] = l;
+        S.a[2][wd] = h;
+        S.a[3][wd] = l;
       }
-      // ---- stage Q (NT x KC complex) as [[re, -im], [im, re]] real blocks
-      for (int t = tid; t < NT * kTcKC; t += 256) {
-        int j, k;
-        if (!TRANS) { k = t % kTcKC; j = t / kTcKC; }  // U[k, ca + j]: k contiguous
-        else { j = t % NT; k = t / NT; }                 // A^T: L[ra + j, k]: j contiguous
+      // ---- B planes: NT x KC
+      for (int cm = warp; cm < (NT / 8) * (kTcKC / 4); cm += 8) {
+        const int j = (cm / (kTcKC / 4)) * 8 + cr, k = (cm % (kTcKC / 4)) * 4 + ck;
         float2 v = make_float2(0.f, 0.f);
-        if (j0 + j < NC && kc + k < K) {
-          v = !TRANS ? F[(int64_t)(ca + j0 + j) * m + kc + k]
-                     : F[(int64_t)(kc + k) * m + ra + j0 + j];
-        }
-        uint32_t rh, rl, ih, il, nh, nl;
-        tc::split_tf32(v.x, rh, rl);
-        tc::split_tf32(v.y, ih, il);
-        tc::split_tf32(-v.y, nh, nl);
-        sm.b_hi[tc::kmajor_off(j, k, kTcKT) >> 2] = rh;
-        sm.b_lo[tc::kmajor_off(j, k, kTcKT) >> 2] = rl;
-        sm.b_hi[tc::kmajor_off(j, kTcKC + k, kTcKT) >> 2] = nh;
-        sm.b_lo[tc::kmajor_off(j, kTcKC + k, kTcKT) >> 2] = nl;
-        sm.b_hi[tc::kmajor_off(NT + j, k, kTcKT) >> 2] = ih;
-        sm.b_lo[tc::kmajor_off(NT + j, k, kTcKT) >> 2] = il;
-        sm.b_hi[tc::kmajor_off(NT + j, kTcKC + k, kTcKT) >> 2] = rh;
-        sm.b_lo[tc::kmajor_off(NT + j, kTcKC + k, kTcKT) >> 2] = rl;
+        if (j0 + j < NC && kc + k < K)
+          v = !TRANS ? F[(int64_t)(ca + j0 + j) * m + kc + k]    // U[k, ca + j]
+                     : F[(int64_t)(kc + k) * m + ra + j0 + j];  // A^T: L[ra + j, k]
+        const int wd = tc_word(j, k);
+        uint32_t h, l;
+        tc::split_tf32(v.x, h, l);
+        S.b[0][wd] = h;
+        S.b[1][wd] = l;
+        tc::split_tf32(v.y, h, l);
+        S.b[2][wd] = h;
+        S.b[3][wd] = l;
       }
       tc::fence_async_smem();
       tc::fence_before();
       __syncthreads();
       tc::fence_after();
       if (tid == 0) {
-        const uint32_t lbo = 128, sbo = (kTcKT / 4) * 128;
-        const uint32_t ah = tc::smem_u32(sm.a_hi), al = tc::smem_u32(sm.a_lo);
-        const uint32_t bh = tc::smem_u32(sm.b_hi), bl = tc::smem_u32(sm.b_lo);
+        uint32_t a[4], b[4];
 #pragma unroll
-        for (int ks = 0; ks < kTcKT / 8; ++ks) {
-          const uint32_t ko = ks * 2 * 128;  // two core matrices per K = 8 step
-          const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-          tc::mma_tf32(tmem, tc::smem_desc(ah + ko, lbo, sbo), tc::smem_desc(bh + ko, lbo, sbo), idesc, acc);
-          tc::mma_tf32(tmem, tc::smem_desc(ah + ko, lbo, sbo), tc::smem_desc(bl + ko, lbo, sbo), idesc, 1u);
-          tc::mma_tf32(tmem, tc::smem_desc(al + ko, lbo, sbo), tc::smem_desc(bh + ko, lbo, sbo), idesc, 1u);
+        for (int q = 0; q < 4; ++q) { a[q] = tc::smem_u32(S.a[q]); b[q] = tc::smem_u32(S.b[q]); }
+        const uint32_t re = tmem, im = tmem + NT;
+#pragma unroll
+        for (int ks = 0; ks < kTcKC / 8; ++ks) {
+          const uint32_t o = ks * 2 * 128;  // two core matrices per K = 8 step
+          auto d = [&](uint32_t base) { return tc::smem_desc(base + o, LBO, SBO); };
+          const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
+          // D_re += A_re B_re - A_im B_im
+          tc::mma_tf32(re, d(a[0]), d(b[0]), id_pos, acc0);
+          tc::mma_tf32(re, d(a[0]), d(b[1]), id_pos, 1u);
+          tc::mma_tf32(re, d(a[1]), d(b[0]), id_pos, 1u);
+          tc::mma_tf32(re, d(a[2]), d(b[2]), id_neg, 1u);
+          tc::mma_tf32(re, d(a[2]), d(b[3]), id_neg, 1u);
+          tc::mma_tf32(re, d(a[3]), d(b[2]), id_neg, 1u);
+          // D_im += A_re B_im + A_im B_re
+          tc::mma_tf32(im, d(a[0]), d(b[2]), id_pos, acc0);
+          tc::mma_tf32(im, d(a[0]), d(b[3]), id_pos, 1u);
+          tc::mma_tf32(im, d(a[1]), d(b[2]), id_pos, 1u);
+          tc::mma_tf32(im, d(a[2]), d(b[0]), id_pos, 1u);
+          tc::mma_tf32(im, d(a[2]), d(b[1]), id_pos, 1u);
+          tc::mma_tf32(im, d(a[3]), d(b[0]), id_pos, 1u);
         }
-        tc::commit(&sm.mbar);
+        tc::commit(&sm.mbar[stage]);
       }
-      ok = tc::mbar_wait(&sm.mbar, phase);
-      phase ^= 1u;
-      tc::fence_after();
-      if (!ok) break;
+      pending[stage] = true;
     }
+    // drain both stages before reading the accumulator
+    for (int q = 0; q < 2 && ok; ++q)
+      if (pending[q]) {
+        ok = tc::mbar_wait(&sm.mbar[q], phase[q]);
+        phase[q] ^= 1u;
+        pending[q] = false;
+      }
+    tc::fence_after();
     if (!ok) break;
     // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, column half w / 4
     const int lg = warp & 3, half = warp >> 2;
