@@ -1,0 +1,127 @@
+"""elpasoC HDF5 model files -> ModelDesc, and reference solution files.
+
+Mirrors the parts of the reference's HDF5 parser that feed the frequency
+path (``ESC/misc/parser/femparserhdf5.cpp:202-499``; group names from
+``ESC/misc/hdf5/rulesh5.h:31-157``):
+
+* ``/Nodes/mtxFemNodes``: compound {Ids, xCoords, yCoords, zCoords};
+* ``/Elements/mtxFemElemGroup*``: rows (element id, node ids...), attributes
+  ``ElementType`` (DSG4 / Brick8 / Fluid8) and ``MaterialId``;
+* ``/Materials/*``: attributes ``Id``, ``MaterialType`` and the parameters as
+  strings (``E``, ``nu``, ``rho``, ``t``, ``eta``, ``type``, ``c``;
+  ``ESC/misc/hdf5/rulesh5.h:112-141``);
+* ``/NodeConstraints/*``: structural constraints with flags ``u1..u3``,
+  ``w1..w3`` and values ``valu*``/``valw*`` (reference DOF enum 0..5);
+* ``/NodeLoads/*``: ``point_force`` loads ``Fx, Fy, Fz`` at ``NodeId``;
+* ``/Analysis`` attributes ``start``, ``steps``, ``delta``: the frequency list.
+
+and the solution file elpasoC writes (``ESC/analysis/frequency/
+analysisfrequencybasic.cpp:184-262``): ``/Solution/State/vecFemStep{k}``
+complex vectors with ``FreqStep{k}`` attributes, ``/Solution/Maps/mtxDofMap``
+(node id, dof enum) per global row.
+
+Interface elements, element loads and nodal moments are not read (a model
+that has them raises ``NotImplementedError``).
+"""
+from __future__ import annotations
+
+import importlib.util
+import os
+
+import numpy as np
+
+try:
+    from . import h5lite
+except ImportError:  # loaded as a plain module
+    _spec = importlib.util.spec_from_file_location("h5lite", os.path.join(os.path.dirname(__file__), "h5lite.py"))
+    h5lite = importlib.util.module_from_spec(_spec)
+    _spec.loader.exec_module(h5lite)
+
+_ELEMENT_TYPES = {"Brick8": 1, "DSG4": 2, "Fluid8": 3}     # ELP_BRICK8, ELP_DSG4, ELP_FLUID8
+_MATERIAL_KINDS = {"STR_LIN_ELA_ISO_DIR": 1, "STR_LIN_VIS_ISO_DIR": 2, "AF_LIN_UAF_ISO_DIR": 3}
+_CONSTRAINT_DOFS = (("u1", 0), ("u2", 1), ("u3", 2), ("w1", 3), ("w2", 4), ("w3", 5))
+
+
+def _num(attrs, key, default=0.0):
+    v = attrs.get(key, default)
+    return float(v) if not isinstance(v, str) or v.strip() else default
+
+
+def read_model(path: str, model_desc_cls=None):
+    """Reads an elpasoC model file. Returns (ModelDesc, frequencies in Hz)."""
+    if model_desc_cls is None:
+        from . import ModelDesc as model_desc_cls  # noqa: N813
+    f = h5lite.File(path)
+    nodes = f["Nodes/mtxFemNodes"].read()
+    ids = nodes["Ids"].astype(np.int64)
+    order = np.argsort(ids, kind="stable")
+    ids = ids[order]
+    coords = np.stack([nodes["xCoords"], nodes["yCoords"], nodes["zCoords"]], axis=1)[order]
+    index = {int(v): i for i, v in enumerate(ids)}
+
+    mats, mat_index = [], {}
+    for name in sorted(f["Materials"].keys()):
+        a = f["Materials"][name].attrs
+        kind = _MATERIAL_KINDS.get(a["MaterialType"])
+        if kind is None:
+            raise NotImplementedError(f"material type {a['MaterialType']}")
+        mat_index[int(a["Id"])] = len(mats)
+        mats.append(dict(kind=kind, E=_num(a, "E"), nu=_num(a, "nu"), rho=_num(a, "rho"), t=_num(a, "t"),
+                         eta=_num(a, "eta"), visco_type=int(_num(a, "type", 1.0)) or 1, c=_num(a, "c")))
+
+    blocks = []
+    for name in sorted(f["Elements"].keys(), key=lambda s: int("".join(c for c in s if c.isdigit()) or 0)):
+        ds = f["Elements"][name]
+        typ = _ELEMENT_TYPES.get(ds.attrs["ElementType"])
+        if typ is None:
+            raise NotImplementedError(f"element type {ds.attrs['ElementType']}")
+        rows = ds.read().astype(np.int64)
+        conn = np.vectorize(index.__getitem__, otypes=[np.int64])(rows[:, 1:])
+        blocks.append((typ, mat_index[int(ds.attrs["MaterialId"])], conn.astype(np.int32)))
+
+    for grp in ("InterfaceElements", "NCInterfaceElements"):
+        if grp in f and int(f[grp].attrs.get("N", 0)):
+            raise NotImplementedError(f"{grp} are not read")
+
+    fnode, fdof, fval = [], [], []
+    if "NodeConstraints" in f:
+        for name in sorted(f["NodeConstraints"].keys()):
+            a = f["NodeConstraints"][name].attrs
+            if a.get("ConstraintType") != "structure":
+                raise NotImplementedError(f"constraint type {a.get('ConstraintType')}")
+            for key, dof in _CONSTRAINT_DOFS:
+                if int(a.get(key, 0)):
+                    fnode.append(index[int(a["NodeId"])])
+                    fdof.append(dof)
+                    fval.append(complex(float(a.get("val" + key, 0.0))))
+    lnode, lf = [], []
+    if "NodeLoads" in f:
+        for name in sorted(f["NodeLoads"].keys()):
+            a = f["NodeLoads"][name].attrs
+            if a.get("LoadType") != "point_force":
+                raise NotImplementedError(f"load type {a.get('LoadType')}")
+            lnode.append(index[int(a["NodeId"])])
+            lf.append([float(a["Fx"]), float(a["Fy"]), float(a["Fz"])])
+
+    an = f["Analysis"].attrs
+    freqs = float(an["start"]) + float(an["delta"]) * np.arange(int(an["steps"]))
+    desc = model_desc_cls(
+        node_ids=ids, coords=coords, materials=mats, blocks=blocks,
+        fixed=dict(node=np.array(fnode, np.int64), dof=np.array(fdof, np.int64), value=np.array(fval, complex)),
+        forces=dict(node=np.array(lnode, np.int64), f=np.array(lf).reshape(-1, 3)),
+        name=os.path.splitext(os.path.basename(path))[0])
+    return desc, freqs
+
+
+def read_solution(path: str):
+    """Reads an elpasoC solution file. Returns (freqs [k], x [k, n] complex,
+    dof_map [n, 2] of (node id, dof enum))."""
+    f = h5lite.File(path)
+    state = f["Solution/State"]
+    steps = sorted((int(k[len("vecFemStep"):]) for k in state.keys() if k.startswith("vecFemStep")))
+    freqs = np.array([float(state.attrs[f"FreqStep{k}"]) for k in steps])
+    xs = []
+    for k in steps:
+        v = state[f"vecFemStep{k}"].read()
+        xs.append(v["real"] + 1j * v["imag"])
+    return freqs, np.array(xs), f["Solution/Maps/mtxDofMap"].read().astype(np.int64)
