@@ -1,28 +1,36 @@
 // Tensor-core (tcgen05, kind::tf32) complex Schur updates of FP32 fronts.
 //
-// C -= A B on sub-blocks of a column-major complex FP32 front, from four
-// real products accumulated in tensor memory,
-//   D_re = A_re B_re + (-A_im) B_im      (the minus is the negate-A bit)
-//   D_im = A_re B_im + A_im B_re,
-// with each real operand split into TF32 hi + lo parts (x = hi + lo, both
-// rounded to TF32) and hi*hi + hi*lo + lo*hi accumulated in FP32:
-// FP32-level products from three TF32 passes ("3xTF32").
+// C -= A B on sub-blocks of a column-major complex FP32 front. Every real
+// operand x is split into TF32 parts x = hi + lo (both rounded to TF32) and
+// hi*hi + hi*lo + lo*hi is accumulated in FP32 ("3xTF32": FP32-level
+// products). The complex product is assembled from real MMAs with M = 128:
+//   [D_re | D_im] += A_re [B_re | B_im]        (one MMA of N = 2 NT)
+//    D_re         += (-A_im) B_im              (negate-A bit, N = NT)
+//    D_im         +=   A_im  B_re              (N = NT)
+// so a K = 8 step is 9 MMAs (3 products x 3 split terms).
 //
-// One CTA (256 threads) computes a 128 x NT complex tile: MMA M = 128, N = NT,
-// K = 8 per instruction. Operands are converted in registers and stored to
-// shared memory in the canonical K-major, no-swizzle layout (8-row x 16-byte
-// core matrices; LBO = stride between core matrices along K, SBO = stride
-// between 8-row groups); each warp writes whole core matrices, so the stores
-// are free of bank conflicts. Two shared-memory stages: while the MMAs of
-// chunk c run, the CTA stages chunk c + 1; tcgen05.commit arrives on the
-// stage's mbarrier, which is waited on (with an iteration bound) before that
-// stage is refilled and before the accumulator is read back with tcgen05.ld.
+// Operand placement (shared-memory bandwidth, not the tensor pipe, bounds a
+// 3xTF32 complex update whose operands all come from shared memory):
+//  * A (128 rows x KC) lives in TENSOR memory: each thread converts its row's
+//    values in registers and writes the four planes [re_hi, re_lo, im_hi,
+//    im_lo] with tcgen05.st; the MMAs read A from TMEM;
+//  * B (NT x KC, complex) lives in shared memory once, as the two planes hi
+//    and lo of the real 2NT x KC matrix [B_re ; B_im], in the canonical
+//    K-major no-swizzle layout (8-row x 16-byte core matrices, LBO = stride
+//    between core matrices along K, SBO = stride between 8-row groups); the
+//    N = NT MMAs address its B_re or B_im half by an SBO offset.
+// Two stages (TMEM columns for A, shared memory for B): while the MMAs of
+// chunk c run, the CTA converts and stores chunk c + 1 whose global loads
+// were issued during chunk c. tcgen05.commit arrives on the stage's
+// mbarrier, waited on (with an iteration bound) before the stage is refilled
+// and before the accumulator is read back with tcgen05.ld.
 //
 // TRANS = false: MMA rows are rows of C (GM_COL, GM_SCHUR);
 // TRANS = true:  MMA rows are columns of C (GM_ROW, whose C has only the 32
 //                panel rows), computing C^T -= B^T A^T.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 
 namespace elp {
 namespace tc {
@@ -60,12 +68,22 @@ __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) 
   lo = to_tf32(x - __uint_as_float(hi));
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+// D (TMEM) += A (TMEM, 128 lanes x 8 columns) * B (shared memory descriptor)
+__device__ __forceinline__ void mma_tf32_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t db, uint32_t idesc,
+                                            uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(da), "l"(db), "r"(idesc), "r"(acc));
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "r"(tmem_a), "l"(db), "r"(idesc), "r"(acc));
 }
+
+// the warp's 32 TMEM lanes (one per thread), 8 consecutive 32-bit columns
+__device__ __forceinline__ void st8(uint32_t taddr, const uint32_t* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(v[0]),
+               "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+               : "memory");
+}
+__device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void commit(uint64_t* mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
@@ -112,13 +130,15 @@ __device__ __forceinline__ void ld32(uint32_t taddr, float* v) {
 
 }  // namespace tc
 
-constexpr int kTcKC = 16;  // complex K per stage
+constexpr int kTcKC = 16;            // complex K per stage
+constexpr uint32_t kTcCols = 256;    // TMEM columns per CTA: D (2 NT) + A (2 stages x 4 planes x KC)
+constexpr int kTcSmemBytes = 100 * 1024;  // requested dynamic shared memory: caps residency at 2 CTAs
+                                          // per SM, so two 256-column TMEM allocations always fit
 
-// one stage: planes [re_hi, re_lo, im_hi, im_lo] of A (128 x KC) and B (NT x KC)
+// B planes of one stage: hi, lo of the real 2NT x KC matrix [B_re ; B_im]
 template <int NT>
 struct TcStage {
-  uint32_t a[4][128 * kTcKC];
-  uint32_t b[4][NT * kTcKC];
+  uint32_t b[2][2 * NT * kTcKC];
 };
 template <int NT>
 struct TcSmem {
@@ -134,8 +154,13 @@ __device__ __forceinline__ int tc_word(int row, int k) {
 
 // C -= A B on one front's sub-block, FP32 complex, tcgen05 3xTF32.
 template <int NB, int NT, bool TRANS>
-__global__ void __launch_bounds__(256) k_gemm_tc(LevelArgs L, float2* __restrict__ arena, int step, int mode,
-                                                 int* __restrict__ err) {
+__global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restrict__ arena, int step, int mode,
+                                                    int* __restrict__ err) {
+  static_assert(NT == 32 || NT == 64, "tile width");
+  static_assert(2 * NT + 2 * 4 * kTcKC <= (int)kTcCols, "TMEM budget");
+  static_assert(sizeof(TcSmem<NT>) <= kTcSmemBytes, "shared memory");
+  constexpr int BPT = NT * kTcKC / 256;  // B elements per thread and chunk
+  constexpr int TPJ = kTcKC / BPT;       // threads per B row (column of C) without TRANS
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
   TcSmem<NT>& sm = *reinterpret_cast<TcSmem<NT>*>(tc_smem_raw);
   const int f = L.list[blockIdx.x];
@@ -150,12 +175,12 @@ __global__ void __launch_bounds__(256) k_gemm_tc(LevelArgs L, float2* __restrict
   const int tiles_r = (MR + 127) / 128, tiles_c = (NC + NT - 1) / NT;
   const int ntiles = tiles_r * tiles_c;
   if ((int)blockIdx.z >= ntiles) return;  // uniform per CTA, before any TMEM allocation
-  float2* F = arena + s * L.arena_size + L.foff[f];
+  const float2* __restrict__ F = arena + s * L.arena_size + L.foff[f];
+  float2* Fw = arena + s * L.arena_size + L.foff[f];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  constexpr uint32_t kCols = 2 * NT;  // D_re | D_im, a power of two >= 32
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(&sm.tmem_base)),
-                 "r"(kCols)
+                 "r"(kTcCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -168,86 +193,132 @@ __global__ void __launch_bounds__(256) k_gemm_tc(LevelArgs L, float2* __restrict
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = sm.tmem_base;
-  constexpr uint32_t id_pos = tc::idesc_tf32(128, NT, false), id_neg = tc::idesc_tf32(128, NT, true);
+  const uint32_t tD = tmem, tA = tmem + 2 * NT;  // column offsets
+  constexpr uint32_t id_w = tc::idesc_tf32(128, 2 * NT, false);  // [D_re | D_im]
+  constexpr uint32_t id_p = tc::idesc_tf32(128, NT, false), id_n = tc::idesc_tf32(128, NT, true);
   constexpr uint32_t LBO = 128, SBO = (kTcKC / 4) * 128;
+  constexpr uint32_t half_off = (NT / 8) * SBO;  // bytes from [B_re] to [B_im] rows
   uint32_t phase[2] = {0u, 0u};
   bool pending[2] = {false, false};
   bool ok = true;
-  // lane -> element of one 8 x 4 core matrix
-  const int cr = lane >> 2, ck = lane & 3;
+  // A: thread = MMA row (TMEM lane) 32 (warp % 4) + lane, K half warp / 4
+  const int arow = 32 * (warp & 3) + lane, akh = (warp >> 2) * 8;
+  const uint32_t a_lane = (uint32_t)(32 * (warp & 3)) << 16;
   for (int tile = blockIdx.z; tile < ntiles && ok; tile += gridDim.z) {
     const int i0 = (tile % tiles_r) * 128;
     const int j0 = (tile / tiles_r) * NT;
-    int stage = 0, nchunks = (K + kTcKC - 1) / kTcKC;
-    for (int c = 0; c < nchunks && ok; ++c, stage ^= 1) {
+    const int nchunks = (K + kTcKC - 1) / kTcKC;
+    float2 av[8], bv[BPT];
+    // global loads of chunk c into registers (zero outside the block)
+    auto load = [&](int c) {
       const int kc = c * kTcKC;
+      const int i = i0 + arow;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int k = kc + akh + q;
+        av[q] = make_float2(0.f, 0.f);
+        if (i < MR && k < K)
+          av[q] = !TRANS ? F[(int64_t)k * m + ra + i]      // A = L[ra + i, k]
+                         : F[(int64_t)(ca + i) * m + k];   // B^T: U[k, ca + i]
+      }
+#pragma unroll
+      for (int q = 0; q < BPT; ++q) {
+        int j, k;
+        if (!TRANS) { j = tid / TPJ; k = (tid % TPJ) * BPT + q; }           // BPT consecutive k per thread
+        else { j = tid % NT; k = (tid / NT) + (256 / NT) * q; }            // consecutive j across lanes
+        j += j0;
+        k += kc;
+        bv[q] = make_float2(0.f, 0.f);
+        if (j < NC && k < K)
+          bv[q] = !TRANS ? F[(int64_t)(ca + j) * m + k]       // U[k, ca + j]
+                         : F[(int64_t)k * m + ra + j];       // A^T: L[ra + j, k]
+      }
+    };
+    load(0);
+    for (int c = 0; c < nchunks && ok; ++c) {
+      const int stage = c & 1;
       if (pending[stage]) {  // the MMAs that read this stage two chunks ago
-        ok = tc::mbar_wait(&sm.mbar[stage], phase[stage]);
+        ok = tc::mbar_wait(&sm.mbar[stage], phase[stage]);  // a failure is made uniform at the barrier below
         phase[stage] ^= 1u;
         pending[stage] = false;
-        if (!ok) break;
       }
-      TcStage<NT>& S = sm.st[stage];
-      // ---- A planes: 128 x KC, core matrices (16 row groups x 4 k groups) over 8 warps
-      for (int cm = warp; cm < 16 * (kTcKC / 4); cm += 8) {
-        const int i = (cm / (kTcKC / 4)) * 8 + cr, k = (cm % (kTcKC / 4)) * 4 + ck;
-        float2 v = make_float2(0.f, 0.f);
-        if (i0 + i < MR && kc + k < K)
-          v = !TRANS ? F[(int64_t)(kc + k) * m + ra + i0 + i]     // A = L[ra + i, k]
-                     : F[(int64_t)(ca + i0 + i) * m + kc + k];   // B^T: U[k, ca + i]
-        const int wd = tc_word(i, k);
-        uint32_t h, l;
-        tc::split_tf32(v.x, h, l);
-        S.a[0][wd] = h;
-        S.a[1][wd] = l;
-        tc::split_tf32(v.y, h, l);
-        S.a[2][wd] = h;
-        S.a[3][wd] = l;
+      tc::fence_after();
+      // ---- A planes into TMEM: columns tA + stage*64 + plane*16 + k
+      {
+        uint32_t h[4][8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          tc::split_tf32(av[q].x, h[0][q], h[1][q]);
+          tc::split_tf32(av[q].y, h[2][q], h[3][q]);
+        }
+        const uint32_t base = tA + stage * (4 * kTcKC) + akh + a_lane;
+#pragma unroll
+        for (int pl = 0; pl < 4; ++pl) tc::st8(base + pl * kTcKC, h[pl]);
       }
-      // ---- B planes: NT x KC
-      for (int cm = warp; cm < (NT / 8) * (kTcKC / 4); cm += 8) {
-        const int j = (cm / (kTcKC / 4)) * 8 + cr, k = (cm % (kTcKC / 4)) * 4 + ck;
-        float2 v = make_float2(0.f, 0.f);
-        if (j0 + j < NC && kc + k < K)
-          v = !TRANS ? F[(int64_t)(ca + j0 + j) * m + kc + k]    // U[k, ca + j]
-                     : F[(int64_t)(kc + k) * m + ra + j0 + j];  // A^T: L[ra + j, k]
-        const int wd = tc_word(j, k);
-        uint32_t h, l;
-        tc::split_tf32(v.x, h, l);
-        S.b[0][wd] = h;
-        S.b[1][wd] = l;
-        tc::split_tf32(v.y, h, l);
-        S.b[2][wd] = h;
-        S.b[3][wd] = l;
+      // ---- B planes into shared memory: rows j (re) and NT + j (im)
+      {
+        TcStage<NT>& S = sm.st[stage];
+        if (!TRANS) {  // BPT consecutive words of one core-matrix row: one vector store per plane
+          using VW = typename std::conditional<BPT == 4, uint4, uint2>::type;
+          const int j = tid / TPJ, kf = (tid % TPJ) * BPT;
+          VW hr, lr, hi, li;
+          uint32_t* H = &hr.x; uint32_t* Lr = &lr.x; uint32_t* Hi = &hi.x; uint32_t* Li = &li.x;
+#pragma unroll
+          for (int q = 0; q < BPT; ++q) {
+            tc::split_tf32(bv[q].x, H[q], Lr[q]);
+            tc::split_tf32(bv[q].y, Hi[q], Li[q]);
+          }
+          const int wr = tc_word(j, kf), wi = tc_word(NT + j, kf);
+          *reinterpret_cast<VW*>(&S.b[0][wr]) = hr;
+          *reinterpret_cast<VW*>(&S.b[1][wr]) = lr;
+          *reinterpret_cast<VW*>(&S.b[0][wi]) = hi;
+          *reinterpret_cast<VW*>(&S.b[1][wi]) = li;
+        } else {
+#pragma unroll
+          for (int q = 0; q < BPT; ++q) {
+            const int j = tid % NT, k = (tid / NT) + (256 / NT) * q;
+            uint32_t h, l;
+            tc::split_tf32(bv[q].x, h, l);
+            S.b[0][tc_word(j, k)] = h;
+            S.b[1][tc_word(j, k)] = l;
+            tc::split_tf32(bv[q].y, h, l);
+            S.b[0][tc_word(NT + j, k)] = h;
+            S.b[1][tc_word(NT + j, k)] = l;
+          }
+        }
       }
+      if (c + 1 < nchunks) load(c + 1);  // in flight during the MMAs of this chunk
+      tc::wait_st();
       tc::fence_async_smem();
       tc::fence_before();
-      __syncthreads();
+      ok = __syncthreads_and(ok);
       tc::fence_after();
+      if (!ok) break;
       if (tid == 0) {
-        uint32_t a[4], b[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) { a[q] = tc::smem_u32(S.a[q]); b[q] = tc::smem_u32(S.b[q]); }
-        const uint32_t re = tmem, im = tmem + NT;
+        const TcStage<NT>& S = sm.st[stage];
+        const uint32_t bh = tc::smem_u32(S.b[0]), bl = tc::smem_u32(S.b[1]);
+        const uint32_t a0 = tA + stage * (4 * kTcKC);
 #pragma unroll
         for (int ks = 0; ks < kTcKC / 8; ++ks) {
           const uint32_t o = ks * 2 * 128;  // two core matrices per K = 8 step
-          auto d = [&](uint32_t base) { return tc::smem_desc(base + o, LBO, SBO); };
+          const uint32_t a_rh = a0 + 0 * kTcKC + ks * 8, a_rl = a0 + 1 * kTcKC + ks * 8;
+          const uint32_t a_ih = a0 + 2 * kTcKC + ks * 8, a_il = a0 + 3 * kTcKC + ks * 8;
+          const uint64_t bh_re = tc::smem_desc(bh + o, LBO, SBO), bl_re = tc::smem_desc(bl + o, LBO, SBO);
+          const uint64_t bh_im = tc::smem_desc(bh + o + half_off, LBO, SBO);
+          const uint64_t bl_im = tc::smem_desc(bl + o + half_off, LBO, SBO);
           const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
-          // D_re += A_re B_re - A_im B_im
-          tc::mma_tf32(re, d(a[0]), d(b[0]), id_pos, acc0);
-          tc::mma_tf32(re, d(a[0]), d(b[1]), id_pos, 1u);
-          tc::mma_tf32(re, d(a[1]), d(b[0]), id_pos, 1u);
-          tc::mma_tf32(re, d(a[2]), d(b[2]), id_neg, 1u);
-          tc::mma_tf32(re, d(a[2]), d(b[3]), id_neg, 1u);
-          tc::mma_tf32(re, d(a[3]), d(b[2]), id_neg, 1u);
-          // D_im += A_re B_im + A_im B_re
-          tc::mma_tf32(im, d(a[0]), d(b[2]), id_pos, acc0);
-          tc::mma_tf32(im, d(a[0]), d(b[3]), id_pos, 1u);
-          tc::mma_tf32(im, d(a[1]), d(b[2]), id_pos, 1u);
-          tc::mma_tf32(im, d(a[2]), d(b[0]), id_pos, 1u);
-          tc::mma_tf32(im, d(a[2]), d(b[1]), id_pos, 1u);
-          tc::mma_tf32(im, d(a[3]), d(b[0]), id_pos, 1u);
+          // [D_re | D_im] += A_re [B_re | B_im]
+          tc::mma_tf32_ta(tD, a_rh, bh_re, id_w, acc0);
+          tc::mma_tf32_ta(tD, a_rh, bl_re, id_w, 1u);
+          tc::mma_tf32_ta(tD, a_rl, bh_re, id_w, 1u);
+          // D_re -= A_im B_im
+          tc::mma_tf32_ta(tD, a_ih, bh_im, id_n, 1u);
+          tc::mma_tf32_ta(tD, a_ih, bl_im, id_n, 1u);
+          tc::mma_tf32_ta(tD, a_il, bh_im, id_n, 1u);
+          // D_im += A_im B_re
+          tc::mma_tf32_ta(tD + NT, a_ih, bh_re, id_p, 1u);
+          tc::mma_tf32_ta(tD + NT, a_ih, bl_re, id_p, 1u);
+          tc::mma_tf32_ta(tD + NT, a_il, bh_re, id_p, 1u);
         }
         tc::commit(&sm.mbar[stage]);
       }
@@ -260,6 +331,7 @@ __global__ void __launch_bounds__(256) k_gemm_tc(LevelArgs L, float2* __restrict
         phase[q] ^= 1u;
         pending[q] = false;
       }
+    ok = __syncthreads_and(ok);  // every thread leaves the tile loop together
     tc::fence_after();
     if (!ok) break;
     // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, column half w / 4
@@ -267,15 +339,15 @@ __global__ void __launch_bounds__(256) k_gemm_tc(LevelArgs L, float2* __restrict
     if (half * 32 < NT) {
       float re[32], im[32];
       const uint32_t lane_base = (uint32_t)(32 * lg) << 16;
-      tc::ld32(tmem + lane_base + half * 32, re);
-      tc::ld32(tmem + lane_base + NT + half * 32, im);
+      tc::ld32(tD + lane_base + half * 32, re);
+      tc::ld32(tD + lane_base + NT + half * 32, im);
       const int i = i0 + 32 * lg + lane;  // MMA row
       if (i < MR) {
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
           const int j = j0 + half * 32 + q;  // MMA column (complex)
           if (j < NC) {
-            float2* dst = !TRANS ? F + (int64_t)(ca + j) * m + ra + i : F + (int64_t)(ca + i) * m + ra + j;
+            float2* dst = !TRANS ? Fw + (int64_t)(ca + j) * m + ra + i : Fw + (int64_t)(ca + i) * m + ra + j;
             float2 v = *dst;
             v.x -= re[q];
             v.y -= im[q];
@@ -288,10 +360,16 @@ __global__ void __launch_bounds__(256) k_gemm_tc(LevelArgs L, float2* __restrict
     __syncthreads();
     tc::fence_after();
   }
+  // a timed-out wait leaves MMAs possibly in flight: wait (bounded) for every
+  // committed stage before the TMEM is released
+  for (int q = 0; q < 2; ++q)
+    if (pending[q]) tc::mbar_wait(&sm.mbar[q], phase[q]);
   if (!ok && tid == 0) atomicExch(err, 1);
+  tc::fence_before();
   __syncthreads();
+  tc::fence_after();
   if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
   }
 }
 

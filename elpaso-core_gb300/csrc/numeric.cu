@@ -1074,11 +1074,11 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     static cudaError_t e = cudaSuccess;
     std::call_once(once, [] {
       cudaError_t a = cudaFuncSetAttribute(k_gemm_tc<NB, 32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)sizeof(TcSmem<32>));
+                                           kTcSmemBytes);
       cudaError_t b = cudaFuncSetAttribute(k_gemm_tc<NB, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)sizeof(TcSmem<32>));
+                                           kTcSmemBytes);
       cudaError_t c = cudaFuncSetAttribute(k_gemm_tc<NB, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)sizeof(TcSmem<64>));
+                                           kTcSmemBytes);
       e = a != cudaSuccess ? a : b != cudaSuccess ? b : c;
     });
     ELP_CUDA(e);
@@ -1090,13 +1090,13 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       if (mode == GM_SCHUR) {
         const int t = ((rows_c + 127) / 128) * ((cols_c + 63) / 64);
         dim3 g(L.count, S_used, (unsigned)std::min(65535, t));
-        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 64, false><<<g, 256, sizeof(TcSmem<64>), st>>>(L, fa, k, mode, w.tc_err.p));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 64, false><<<g, 256, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
       } else if (mode == GM_COL) {
         dim3 g(L.count, S_used, (unsigned)std::min(65535, (rows_c + 127) / 128));
-        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, false><<<g, 256, sizeof(TcSmem<32>), st>>>(L, fa, k, mode, w.tc_err.p));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, false><<<g, 256, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
       } else {
         dim3 g(L.count, S_used, (unsigned)std::min(65535, (cols_c + 127) / 128));
-        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, true><<<g, 256, sizeof(TcSmem<32>), st>>>(L, fa, k, mode, w.tc_err.p));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, true><<<g, 256, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
       }
       return;
     }
