@@ -19,11 +19,15 @@
 //    K-major no-swizzle layout (8-row x 16-byte core matrices, LBO = stride
 //    between core matrices along K, SBO = stride between 8-row groups); the
 //    N = NT MMAs address its B_re or B_im half by an SBO offset.
-// Two stages (TMEM columns for A, shared memory for B): while the MMAs of
-// chunk c run, the CTA converts and stores chunk c + 1 whose global loads
-// were issued during chunk c. tcgen05.commit arrives on the stage's
-// mbarrier, waited on (with an iteration bound) before the stage is refilled
-// and before the accumulator is read back with tcgen05.ld.
+// Pipeline: the raw complex operands go through a three-slot ring in shared
+// memory filled with cp.async (8-byte copies, zero-filled outside the
+// block) two chunks ahead, so no prefetched data sits in registers; each
+// chunk is then converted into the planes of one of two MMA stages (TMEM
+// columns for A, shared memory for B). tcgen05.commit arrives on the
+// stage's mbarrier, waited on by one thread (with an iteration bound) before
+// the stage is refilled and before the accumulator is read back with
+// tcgen05.ld. The raw rows are padded (A: 129, B: 18 complex per row) so the
+// copies and the conversion reads are free of bank conflicts.
 //
 // TRANS = false: MMA rows are rows of C (GM_COL, GM_SCHUR);
 // TRANS = true:  MMA rows are columns of C (GM_ROW, whose C has only the 32
@@ -130,19 +134,19 @@ __device__ __forceinline__ void ld32(uint32_t taddr, float* v) {
 
 }  // namespace tc
 
-constexpr int kTcKC = 16;            // complex K per stage
+constexpr int kTcKC = 16;            // complex K per chunk
+constexpr int kTcRing = 3;           // raw chunks in flight
+constexpr int kTcLdA = 129;          // raw A row stride (complex): [k][i], 128 rows + 1
+constexpr int kTcLdB = 18;           // raw B row stride (complex): [j][k], 16 k + 2
 constexpr uint32_t kTcCols = 256;    // TMEM columns per CTA: D (2 NT) + A (2 stages x 4 planes x KC)
-constexpr int kTcSmemBytes = 100 * 1024;  // requested dynamic shared memory: caps residency at 2 CTAs
+constexpr int kTcSmemBytes = 110 * 1024;  // requested dynamic shared memory: caps residency at 2 CTAs
                                           // per SM, so two 256-column TMEM allocations always fit
 
-// B planes of one stage: hi, lo of the real 2NT x KC matrix [B_re ; B_im]
-template <int NT>
-struct TcStage {
-  uint32_t b[2][2 * NT * kTcKC];
-};
 template <int NT>
 struct TcSmem {
-  TcStage<NT> st[2];
+  float2 rawA[kTcRing][kTcKC * kTcLdA];
+  float2 rawB[kTcRing][NT * kTcLdB];
+  uint32_t b[2][2][2 * NT * kTcKC];  // [stage][hi, lo] planes of the real 2NT x KC matrix [B_re ; B_im]
   uint64_t mbar[2];
   uint32_t tmem_base;
 };
@@ -152,6 +156,16 @@ __device__ __forceinline__ int tc_word(int row, int k) {
   return ((row >> 3) * (kTcKC >> 2) + (k >> 2)) * 32 + (row & 7) * 4 + (k & 3);
 }
 
+namespace tc {
+// 8-byte asynchronous global -> shared copy; zero-fills when !valid
+__device__ __forceinline__ void cp8(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 8 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait2() { asm volatile("cp.async.wait_group 2;" ::: "memory"); }
+}  // namespace tc
+
 // C -= A B on one front's sub-block, FP32 complex, tcgen05 3xTF32.
 template <int NB, int NT, bool TRANS>
 __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restrict__ arena, int step, int mode,
@@ -159,8 +173,9 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restr
   static_assert(NT == 32 || NT == 64, "tile width");
   static_assert(2 * NT + 2 * 4 * kTcKC <= (int)kTcCols, "TMEM budget");
   static_assert(sizeof(TcSmem<NT>) <= kTcSmemBytes, "shared memory");
+  static_assert(!TRANS || NT == 32, "transposed tiles are 32 wide");
   constexpr int BPT = NT * kTcKC / 256;  // B elements per thread and chunk
-  constexpr int TPJ = kTcKC / BPT;       // threads per B row (column of C) without TRANS
+  constexpr int TPJ = kTcKC / BPT;       // threads per B row in the conversion
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
   TcSmem<NT>& sm = *reinterpret_cast<TcSmem<NT>*>(tc_smem_raw);
   const int f = L.list[blockIdx.x];
@@ -175,8 +190,7 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restr
   const int tiles_r = (MR + 127) / 128, tiles_c = (NC + NT - 1) / NT;
   const int ntiles = tiles_r * tiles_c;
   if ((int)blockIdx.z >= ntiles) return;  // uniform per CTA, before any TMEM allocation
-  const float2* __restrict__ F = arena + s * L.arena_size + L.foff[f];
-  float2* Fw = arena + s * L.arena_size + L.foff[f];
+  float2* F = arena + s * L.arena_size + L.foff[f];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(&sm.tmem_base)),
@@ -199,104 +213,101 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restr
   constexpr uint32_t LBO = 128, SBO = (kTcKC / 4) * 128;
   constexpr uint32_t half_off = (NT / 8) * SBO;  // bytes from [B_re] to [B_im] rows
   uint32_t phase[2] = {0u, 0u};
-  bool pending[2] = {false, false};
+  bool pending[2] = {false, false};  // meaningful in thread 0, which alone waits on the mbarriers
   bool ok = true;
-  // A: thread = MMA row (TMEM lane) 32 (warp % 4) + lane, K half warp / 4
+  // conversion roles: A row (TMEM lane) 32 (warp % 4) + lane, K half warp / 4; B row j, first k kf
   const int arow = 32 * (warp & 3) + lane, akh = (warp >> 2) * 8;
   const uint32_t a_lane = (uint32_t)(32 * (warp & 3)) << 16;
+  const int bj = tid / TPJ, bkf = (tid % TPJ) * BPT;
   for (int tile = blockIdx.z; tile < ntiles && ok; tile += gridDim.z) {
     const int i0 = (tile % tiles_r) * 128;
     const int j0 = (tile / tiles_r) * NT;
     const int nchunks = (K + kTcKC - 1) / kTcKC;
-    float2 av[8], bv[BPT];
-    // global loads of chunk c into registers (zero outside the block)
-    auto load = [&](int c) {
-      const int kc = c * kTcKC;
-      const int i = i0 + arow;
+    // raw copies of chunk c into ring slot c % kTcRing (an empty group past the end)
+    auto issue = [&](int c) {
+      if (c < nchunks) {
+        const int kc = c * kTcKC;
+        float2* rA = sm.rawA[c % kTcRing];
+        float2* rB = sm.rawB[c % kTcRing];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int k = kc + akh + q;
-        av[q] = make_float2(0.f, 0.f);
-        if (i < MR && k < K)
-          av[q] = !TRANS ? F[(int64_t)k * m + ra + i]      // A = L[ra + i, k]
-                         : F[(int64_t)(ca + i) * m + k];   // B^T: U[k, ca + i]
-      }
+        for (int q = 0; q < 8; ++q) {  // A: 128 x 16
+          int i, k;
+          if (!TRANS) { i = tid % 128; k = tid / 128 + 2 * q; }     // lanes along rows of L
+          else { k = tid % 16; i = tid / 16 + 16 * q; }              // lanes along k of U
+          const bool v = i0 + i < MR && kc + k < K;
+          const float2* src = !v ? F
+                              : !TRANS ? F + (int64_t)(kc + k) * m + ra + i0 + i   // L[ra + i, k]
+                                       : F + (int64_t)(ca + i0 + i) * m + kc + k;  // U[k, ca + i]
+          tc::cp8(rA + k * kTcLdA + i, src, v);
+        }
 #pragma unroll
-      for (int q = 0; q < BPT; ++q) {
-        int j, k;
-        if (!TRANS) { j = tid / TPJ; k = (tid % TPJ) * BPT + q; }           // BPT consecutive k per thread
-        else { j = tid % NT; k = (tid / NT) + (256 / NT) * q; }            // consecutive j across lanes
-        j += j0;
-        k += kc;
-        bv[q] = make_float2(0.f, 0.f);
-        if (j < NC && k < K)
-          bv[q] = !TRANS ? F[(int64_t)(ca + j) * m + k]       // U[k, ca + j]
-                         : F[(int64_t)k * m + ra + j];       // A^T: L[ra + j, k]
+        for (int q = 0; q < BPT; ++q) {  // B: NT x 16
+          int j, k;
+          if (!TRANS) { k = tid % 16; j = tid / 16 + 16 * q; }       // lanes along k of U
+          else { j = tid % NT; k = tid / NT + (256 / NT) * q; }      // lanes along rows of L
+          const bool v = j0 + j < NC && kc + k < K;
+          const float2* src = !v ? F
+                              : !TRANS ? F + (int64_t)(ca + j0 + j) * m + kc + k   // U[k, ca + j]
+                                       : F + (int64_t)(kc + k) * m + ra + j0 + j;  // L[ra + j, k]
+          tc::cp8(rB + j * kTcLdB + k, src, v);
+        }
       }
+      tc::cp_commit();
     };
-    load(0);
-    for (int c = 0; c < nchunks && ok; ++c) {
-      const int stage = c & 1;
-      if (pending[stage]) {  // the MMAs that read this stage two chunks ago
-        ok = tc::mbar_wait(&sm.mbar[stage], phase[stage]);  // a failure is made uniform at the barrier below
+    issue(0);
+    issue(1);
+    for (int c = 0; c < nchunks; ++c) {
+      const int stage = c & 1, slot = c % kTcRing;
+      issue(c + 2);  // into the slot converted in iteration c - 1 (all threads passed its barrier)
+      tc::cp_wait2();  // this thread's copies of chunk c have landed
+      if (tid == 0 && pending[stage]) {  // the MMAs that read this stage two chunks ago
+        ok = tc::mbar_wait(&sm.mbar[stage], phase[stage]);
         phase[stage] ^= 1u;
         pending[stage] = false;
       }
+      tc::fence_before();
+      ok = __syncthreads_and(ok);  // chunk c visible to all, stage free (or a uniform failure)
       tc::fence_after();
+      if (!ok) break;
       // ---- A planes into TMEM: columns tA + stage*64 + plane*16 + k
       {
+        const float2* rA = sm.rawA[slot];
         uint32_t h[4][8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          tc::split_tf32(av[q].x, h[0][q], h[1][q]);
-          tc::split_tf32(av[q].y, h[2][q], h[3][q]);
+          const float2 v = rA[(akh + q) * kTcLdA + arow];
+          tc::split_tf32(v.x, h[0][q], h[1][q]);
+          tc::split_tf32(v.y, h[2][q], h[3][q]);
         }
         const uint32_t base = tA + stage * (4 * kTcKC) + akh + a_lane;
 #pragma unroll
         for (int pl = 0; pl < 4; ++pl) tc::st8(base + pl * kTcKC, h[pl]);
       }
-      // ---- B planes into shared memory: rows j (re) and NT + j (im)
+      // ---- B planes into shared memory: rows j (re) and NT + j (im), BPT consecutive k per thread
       {
-        TcStage<NT>& S = sm.st[stage];
-        if (!TRANS) {  // BPT consecutive words of one core-matrix row: one vector store per plane
-          using VW = typename std::conditional<BPT == 4, uint4, uint2>::type;
-          const int j = tid / TPJ, kf = (tid % TPJ) * BPT;
-          VW hr, lr, hi, li;
-          uint32_t* H = &hr.x; uint32_t* Lr = &lr.x; uint32_t* Hi = &hi.x; uint32_t* Li = &li.x;
+        using VW = typename std::conditional<BPT == 4, uint4, uint2>::type;
+        const float2* rB = sm.rawB[slot] + bj * kTcLdB + bkf;
+        VW hr, lr, hi, li;
+        uint32_t* H = &hr.x; uint32_t* Lr = &lr.x; uint32_t* Hi = &hi.x; uint32_t* Li = &li.x;
 #pragma unroll
-          for (int q = 0; q < BPT; ++q) {
-            tc::split_tf32(bv[q].x, H[q], Lr[q]);
-            tc::split_tf32(bv[q].y, Hi[q], Li[q]);
-          }
-          const int wr = tc_word(j, kf), wi = tc_word(NT + j, kf);
-          *reinterpret_cast<VW*>(&S.b[0][wr]) = hr;
-          *reinterpret_cast<VW*>(&S.b[1][wr]) = lr;
-          *reinterpret_cast<VW*>(&S.b[0][wi]) = hi;
-          *reinterpret_cast<VW*>(&S.b[1][wi]) = li;
-        } else {
-#pragma unroll
-          for (int q = 0; q < BPT; ++q) {
-            const int j = tid % NT, k = (tid / NT) + (256 / NT) * q;
-            uint32_t h, l;
-            tc::split_tf32(bv[q].x, h, l);
-            S.b[0][tc_word(j, k)] = h;
-            S.b[1][tc_word(j, k)] = l;
-            tc::split_tf32(bv[q].y, h, l);
-            S.b[0][tc_word(NT + j, k)] = h;
-            S.b[1][tc_word(NT + j, k)] = l;
-          }
+        for (int q = 0; q < BPT; ++q) {
+          const float2 v = rB[q];
+          tc::split_tf32(v.x, H[q], Lr[q]);
+          tc::split_tf32(v.y, Hi[q], Li[q]);
         }
+        const int wr = tc_word(bj, bkf), wi = tc_word(NT + bj, bkf);
+        *reinterpret_cast<VW*>(&sm.b[stage][0][wr]) = hr;
+        *reinterpret_cast<VW*>(&sm.b[stage][1][wr]) = lr;
+        *reinterpret_cast<VW*>(&sm.b[stage][0][wi]) = hi;
+        *reinterpret_cast<VW*>(&sm.b[stage][1][wi]) = li;
       }
-      if (c + 1 < nchunks) load(c + 1);  // in flight during the MMAs of this chunk
       tc::wait_st();
       tc::fence_async_smem();
       tc::fence_before();
-      ok = __syncthreads_and(ok);
+      __syncthreads();
       tc::fence_after();
-      if (!ok) break;
       if (tid == 0) {
-        const TcStage<NT>& S = sm.st[stage];
-        const uint32_t bh = tc::smem_u32(S.b[0]), bl = tc::smem_u32(S.b[1]);
+        const uint32_t bh = tc::smem_u32(sm.b[stage][0]), bl = tc::smem_u32(sm.b[stage][1]);
         const uint32_t a0 = tA + stage * (4 * kTcKC);
 #pragma unroll
         for (int ks = 0; ks < kTcKC / 8; ++ks) {
@@ -321,16 +332,19 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restr
           tc::mma_tf32_ta(tD + NT, a_il, bh_re, id_p, 1u);
         }
         tc::commit(&sm.mbar[stage]);
+        pending[stage] = true;
       }
-      pending[stage] = true;
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");  // no copy outlives the tile (empty groups past the end)
     // drain both stages before reading the accumulator
-    for (int q = 0; q < 2 && ok; ++q)
-      if (pending[q]) {
-        ok = tc::mbar_wait(&sm.mbar[q], phase[q]);
-        phase[q] ^= 1u;
-        pending[q] = false;
-      }
+    if (tid == 0)
+      for (int q = 0; q < 2 && ok; ++q)
+        if (pending[q]) {
+          ok = tc::mbar_wait(&sm.mbar[q], phase[q]);
+          phase[q] ^= 1u;
+          pending[q] = false;
+        }
+    tc::fence_before();
     ok = __syncthreads_and(ok);  // every thread leaves the tile loop together
     tc::fence_after();
     if (!ok) break;
@@ -347,7 +361,7 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restr
         for (int q = 0; q < 32; ++q) {
           const int j = j0 + half * 32 + q;  // MMA column (complex)
           if (j < NC) {
-            float2* dst = !TRANS ? Fw + (int64_t)(ca + j) * m + ra + i : Fw + (int64_t)(ca + i) * m + ra + j;
+            float2* dst = !TRANS ? F + (int64_t)(ca + j) * m + ra + i : F + (int64_t)(ca + i) * m + ra + j;
             float2 v = *dst;
             v.x -= re[q];
             v.y -= im[q];
@@ -360,10 +374,12 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restr
     __syncthreads();
     tc::fence_after();
   }
-  // a timed-out wait leaves MMAs possibly in flight: wait (bounded) for every
-  // committed stage before the TMEM is released
-  for (int q = 0; q < 2; ++q)
-    if (pending[q]) tc::mbar_wait(&sm.mbar[q], phase[q]);
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  // after a timed-out wait MMAs may still be in flight: wait (bounded) for
+  // every committed stage before the TMEM is released
+  if (tid == 0)
+    for (int q = 0; q < 2; ++q)
+      if (pending[q]) tc::mbar_wait(&sm.mbar[q], phase[q]);
   if (!ok && tid == 0) atomicExch(err, 1);
   tc::fence_before();
   __syncthreads();
