@@ -19,15 +19,23 @@
 //    K-major no-swizzle layout (8-row x 16-byte core matrices, LBO = stride
 //    between core matrices along K, SBO = stride between 8-row groups); the
 //    N = NT MMAs address its B_re or B_im half by an SBO offset.
-// Pipeline: the raw complex operands go through a three-slot ring in shared
-// memory filled with cp.async (8-byte copies, zero-filled outside the
-// block) two chunks ahead, so no prefetched data sits in registers; each
-// chunk is then converted into the planes of one of two MMA stages (TMEM
-// columns for A, shared memory for B). tcgen05.commit arrives on the
-// stage's mbarrier, waited on by one thread (with an iteration bound) before
-// the stage is refilled and before the accumulator is read back with
-// tcgen05.ld. The raw rows are padded (A: 129, B: 18 complex per row) so the
-// copies and the conversion reads are free of bank conflicts.
+// Warp roles (288 threads): warp 0 issues the MMAs (one elected thread);
+// warps 1..8 are converters. Converter warp w owns TMEM lane quarter w % 4
+// (the only lanes it may write) and K half (w - 1) / 4 of every A chunk, and
+// a fixed set of B elements. Each converter copies exactly the raw complex
+// values it will convert, with cp.async (8-byte copies, zero-filled outside
+// the block) into its own slots of a three-chunk ring in shared memory, so
+// the raw data needs no cross-thread synchronisation: a thread waits only for
+// its own copy groups. Two MMA stages (TMEM columns for A, shared memory for
+// B) are handed over with mbarriers, never with block barriers:
+//   full[s]  - 256 converter arrivals: stage s holds a converted chunk;
+//   empty[s] - tcgen05.commit of the MMAs that read stage s.
+// So the converters prepare chunk c + 1 while the tensor pipe runs chunk c,
+// whatever back-pressure the MMA issue meets. Every wait is bounded: a
+// timeout sets the error flag, and later waits of the CTA are skipped so it
+// finishes quickly (with meaningless values) instead of hanging. The CTA
+// synchronises only at tile ends: the epilogue (converter warps, tcgen05.ld
+// of the accumulator) must finish before the next tile overwrites it.
 //
 // TRANS = false: MMA rows are rows of C (GM_COL, GM_SCHUR);
 // TRANS = true:  MMA rows are columns of C (GM_ROW, whose C has only the 32
@@ -135,19 +143,18 @@ __device__ __forceinline__ void ld32(uint32_t taddr, float* v) {
 }  // namespace tc
 
 constexpr int kTcKC = 16;            // complex K per chunk
-constexpr int kTcRing = 3;           // raw chunks in flight
-constexpr int kTcLdA = 129;          // raw A row stride (complex): [k][i], 128 rows + 1
-constexpr int kTcLdB = 18;           // raw B row stride (complex): [j][k], 16 k + 2
+constexpr int kTcRing = 3;           // chunks in flight per converter thread
+constexpr int kTcThreads = 288;      // warp 0: MMA issue; warps 1..8: converters
 constexpr uint32_t kTcCols = 256;    // TMEM columns per CTA: D (2 NT) + A (2 stages x 4 planes x KC)
 constexpr int kTcSmemBytes = 110 * 1024;  // requested dynamic shared memory: caps residency at 2 CTAs
                                           // per SM, so two 256-column TMEM allocations always fit
 
 template <int NT>
 struct TcSmem {
-  float2 rawA[kTcRing][kTcKC * kTcLdA];
-  float2 rawB[kTcRing][NT * kTcLdB];
-  uint32_t b[2][2][2 * NT * kTcKC];  // [stage][hi, lo] planes of the real 2NT x KC matrix [B_re ; B_im]
-  uint64_t mbar[2];
+  static constexpr int BPT = NT * kTcKC / 256;  // B elements per converter and chunk
+  float2 raw[kTcRing][8 + BPT][256];            // [slot][element][converter]: conflict-free
+  uint32_t b[2][2][2 * NT * kTcKC];             // [stage][hi, lo] planes of the real 2NT x KC [B_re ; B_im]
+  uint64_t full[2], empty[2];
   uint32_t tmem_base;
 };
 
@@ -163,19 +170,22 @@ __device__ __forceinline__ void cp8(void* dst, const void* src, bool valid) {
                : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait2() { asm volatile("cp.async.wait_group 2;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_ring() { asm volatile("cp.async.wait_group %0;" ::"n"(kTcRing - 1) : "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(mbar)) : "memory");
+}
 }  // namespace tc
 
 // C -= A B on one front's sub-block, FP32 complex, tcgen05 3xTF32.
 template <int NB, int NT, bool TRANS>
-__global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restrict__ arena, int step, int mode,
-                                                    int* __restrict__ err) {
+__global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* __restrict__ arena, int step,
+                                                           int mode, int* __restrict__ err) {
   static_assert(NT == 32 || NT == 64, "tile width");
   static_assert(2 * NT + 2 * 4 * kTcKC <= (int)kTcCols, "TMEM budget");
   static_assert(sizeof(TcSmem<NT>) <= kTcSmemBytes, "shared memory");
   static_assert(!TRANS || NT == 32, "transposed tiles are 32 wide");
-  constexpr int BPT = NT * kTcKC / 256;  // B elements per thread and chunk
-  constexpr int TPJ = kTcKC / BPT;       // threads per B row in the conversion
+  constexpr int BPT = TcSmem<NT>::BPT;
+  constexpr int TPJ = kTcKC / BPT;  // converters per B row
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
   TcSmem<NT>& sm = *reinterpret_cast<TcSmem<NT>*>(tc_smem_raw);
   const int f = L.list[blockIdx.x];
@@ -199,8 +209,10 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restr
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    tc::mbar_init(&sm.mbar[0], 1);
-    tc::mbar_init(&sm.mbar[1], 1);
+    for (int q = 0; q < 2; ++q) {
+      tc::mbar_init(&sm.full[q], 256);
+      tc::mbar_init(&sm.empty[q], 1);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_before();
@@ -208,179 +220,172 @@ __global__ void __launch_bounds__(256, 2) k_gemm_tc(LevelArgs L, float2* __restr
   tc::fence_after();
   const uint32_t tmem = sm.tmem_base;
   const uint32_t tD = tmem, tA = tmem + 2 * NT;  // column offsets
-  constexpr uint32_t id_w = tc::idesc_tf32(128, 2 * NT, false);  // [D_re | D_im]
-  constexpr uint32_t id_p = tc::idesc_tf32(128, NT, false), id_n = tc::idesc_tf32(128, NT, true);
-  constexpr uint32_t LBO = 128, SBO = (kTcKC / 4) * 128;
-  constexpr uint32_t half_off = (NT / 8) * SBO;  // bytes from [B_re] to [B_im] rows
-  uint32_t phase[2] = {0u, 0u};
-  bool pending[2] = {false, false};  // meaningful in thread 0, which alone waits on the mbarriers
   bool ok = true;
-  // conversion roles: A row (TMEM lane) 32 (warp % 4) + lane, K half warp / 4; B row j, first k kf
-  const int arow = 32 * (warp & 3) + lane, akh = (warp >> 2) * 8;
+  int gc = 0;  // chunks processed by this CTA over all its tiles: stage gc & 1, phase (gc >> 1) & 1
+  // converter roles (warps 1..8): A row 32 (warp % 4) + lane, K half (warp - 1) / 4; B row bj, first k bkf
+  const int ct = tid - 32;
+  const int arow = 32 * (warp & 3) + lane, akh = ((warp - 1) >> 2) * 8;
   const uint32_t a_lane = (uint32_t)(32 * (warp & 3)) << 16;
-  const int bj = tid / TPJ, bkf = (tid % TPJ) * BPT;
-  for (int tile = blockIdx.z; tile < ntiles && ok; tile += gridDim.z) {
+  const int bj = ct / TPJ, bkf = (ct % TPJ) * BPT;
+  for (int tile = blockIdx.z; tile < ntiles; tile += gridDim.z) {
     const int i0 = (tile % tiles_r) * 128;
     const int j0 = (tile / tiles_r) * NT;
     const int nchunks = (K + kTcKC - 1) / kTcKC;
-    // raw copies of chunk c into ring slot c % kTcRing (an empty group past the end)
-    auto issue = [&](int c) {
-      if (c < nchunks) {
-        const int kc = c * kTcKC;
-        float2* rA = sm.rawA[c % kTcRing];
-        float2* rB = sm.rawB[c % kTcRing];
+    if (warp == 0) {
+      // ------------------------------------------------ MMA issue
+      if (lane == 0) {
+        constexpr uint32_t id_w = tc::idesc_tf32(128, 2 * NT, false);  // [D_re | D_im]
+        constexpr uint32_t id_p = tc::idesc_tf32(128, NT, false), id_n = tc::idesc_tf32(128, NT, true);
+        constexpr uint32_t LBO = 128, SBO = (kTcKC / 4) * 128;
+        constexpr uint32_t half_off = (NT / 8) * SBO;  // bytes from [B_re] to [B_im] rows
+        for (int c = 0; c < nchunks; ++c) {
+          const int g = gc + c, stage = g & 1;
+          if (ok) ok = tc::mbar_wait(&sm.full[stage], (g >> 1) & 1);
+          tc::fence_after();
+          const uint32_t bh = tc::smem_u32(sm.b[stage][0]), bl = tc::smem_u32(sm.b[stage][1]);
+          const uint32_t a0 = tA + stage * (4 * kTcKC);
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {  // A: 128 x 16
-          int i, k;
-          if (!TRANS) { i = tid % 128; k = tid / 128 + 2 * q; }     // lanes along rows of L
-          else { k = tid % 16; i = tid / 16 + 16 * q; }              // lanes along k of U
-          const bool v = i0 + i < MR && kc + k < K;
-          const float2* src = !v ? F
-                              : !TRANS ? F + (int64_t)(kc + k) * m + ra + i0 + i   // L[ra + i, k]
-                                       : F + (int64_t)(ca + i0 + i) * m + kc + k;  // U[k, ca + i]
-          tc::cp8(rA + k * kTcLdA + i, src, v);
-        }
-#pragma unroll
-        for (int q = 0; q < BPT; ++q) {  // B: NT x 16
-          int j, k;
-          if (!TRANS) { k = tid % 16; j = tid / 16 + 16 * q; }       // lanes along k of U
-          else { j = tid % NT; k = tid / NT + (256 / NT) * q; }      // lanes along rows of L
-          const bool v = j0 + j < NC && kc + k < K;
-          const float2* src = !v ? F
-                              : !TRANS ? F + (int64_t)(ca + j0 + j) * m + kc + k   // U[k, ca + j]
-                                       : F + (int64_t)(kc + k) * m + ra + j0 + j;  // L[ra + j, k]
-          tc::cp8(rB + j * kTcLdB + k, src, v);
+          for (int ks = 0; ks < kTcKC / 8; ++ks) {
+            const uint32_t o = ks * 2 * 128;  // two core matrices per K = 8 step
+            const uint32_t a_rh = a0 + 0 * kTcKC + ks * 8, a_rl = a0 + 1 * kTcKC + ks * 8;
+            const uint32_t a_ih = a0 + 2 * kTcKC + ks * 8, a_il = a0 + 3 * kTcKC + ks * 8;
+            const uint64_t bh_re = tc::smem_desc(bh + o, LBO, SBO), bl_re = tc::smem_desc(bl + o, LBO, SBO);
+            const uint64_t bh_im = tc::smem_desc(bh + o + half_off, LBO, SBO);
+            const uint64_t bl_im = tc::smem_desc(bl + o + half_off, LBO, SBO);
+            const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
+            // [D_re | D_im] += A_re [B_re | B_im]
+            tc::mma_tf32_ta(tD, a_rh, bh_re, id_w, acc0);
+            tc::mma_tf32_ta(tD, a_rh, bl_re, id_w, 1u);
+            tc::mma_tf32_ta(tD, a_rl, bh_re, id_w, 1u);
+            // D_re -= A_im B_im
+            tc::mma_tf32_ta(tD, a_ih, bh_im, id_n, 1u);
+            tc::mma_tf32_ta(tD, a_ih, bl_im, id_n, 1u);
+            tc::mma_tf32_ta(tD, a_il, bh_im, id_n, 1u);
+            // D_im += A_im B_re
+            tc::mma_tf32_ta(tD + NT, a_ih, bh_re, id_p, 1u);
+            tc::mma_tf32_ta(tD + NT, a_ih, bl_re, id_p, 1u);
+            tc::mma_tf32_ta(tD + NT, a_il, bh_re, id_p, 1u);
+          }
+          tc::commit(&sm.empty[stage]);
         }
       }
-      tc::cp_commit();
-    };
-    issue(0);
-    issue(1);
-    for (int c = 0; c < nchunks; ++c) {
-      const int stage = c & 1, slot = c % kTcRing;
-      issue(c + 2);  // into the slot converted in iteration c - 1 (all threads passed its barrier)
-      tc::cp_wait2();  // this thread's copies of chunk c have landed
-      if (tid == 0 && pending[stage]) {  // the MMAs that read this stage two chunks ago
-        ok = tc::mbar_wait(&sm.mbar[stage], phase[stage]);
-        phase[stage] ^= 1u;
-        pending[stage] = false;
+      __syncwarp();
+    } else {
+      // ------------------------------------------------ converters
+      // raw copies of this thread's elements of chunk c into ring slot c % kTcRing
+      auto issue = [&](int c) {
+        if (c < nchunks) {
+          const int kc = c * kTcKC;
+          const int i = i0 + arow;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int k = kc + akh + q;
+            const bool v = i < MR && k < K;
+            const float2* src = !v ? F
+                                : !TRANS ? F + (int64_t)k * m + ra + i      // A = L[ra + i, k]
+                                         : F + (int64_t)(ca + i) * m + k;   // B^T: U[k, ca + i]
+            tc::cp8(&sm.raw[c % kTcRing][q][ct], src, v);
+          }
+          const int j = j0 + bj;
+#pragma unroll
+          for (int q = 0; q < BPT; ++q) {
+            const int k = kc + bkf + q;
+            const bool v = j < NC && k < K;
+            const float2* src = !v ? F
+                                : !TRANS ? F + (int64_t)(ca + j) * m + k      // U[k, ca + j]
+                                         : F + (int64_t)k * m + ra + j;      // A^T: L[ra + j, k]
+            tc::cp8(&sm.raw[c % kTcRing][8 + q][ct], src, v);
+          }
+        }
+        tc::cp_commit();
+      };
+#pragma unroll
+      for (int c = 0; c < kTcRing; ++c) issue(c);
+      for (int c = 0; c < nchunks; ++c) {
+        const int g = gc + c, stage = g & 1, slot = c % kTcRing;
+        tc::cp_wait_ring();  // this thread's copies of chunk c have landed
+        float2 av[8], bv[BPT];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) av[q] = sm.raw[slot][q][ct];
+#pragma unroll
+        for (int q = 0; q < BPT; ++q) bv[q] = sm.raw[slot][8 + q][ct];
+        issue(c + kTcRing);  // the values are in registers: the slot can be refilled
+        // stage free: the MMAs of chunk g - 2 have completed
+        if (g >= 2 && ok) ok = tc::mbar_wait(&sm.empty[stage], ((g >> 1) + 1) & 1);
+        tc::fence_after();
+        {  // A planes into TMEM: columns tA + stage*64 + plane*16 + k
+          uint32_t h[4][8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            tc::split_tf32(av[q].x, h[0][q], h[1][q]);
+            tc::split_tf32(av[q].y, h[2][q], h[3][q]);
+          }
+          const uint32_t base = tA + stage * (4 * kTcKC) + akh + a_lane;
+#pragma unroll
+          for (int pl = 0; pl < 4; ++pl) tc::st8(base + pl * kTcKC, h[pl]);
+        }
+        {  // B planes: rows bj (re) and NT + bj (im), BPT consecutive k
+          using VW = typename std::conditional<BPT == 4, uint4, uint2>::type;
+          VW hr, lr, hi, li;
+          uint32_t* H = &hr.x; uint32_t* Lr = &lr.x; uint32_t* Hi = &hi.x; uint32_t* Li = &li.x;
+#pragma unroll
+          for (int q = 0; q < BPT; ++q) {
+            tc::split_tf32(bv[q].x, H[q], Lr[q]);
+            tc::split_tf32(bv[q].y, Hi[q], Li[q]);
+          }
+          const int wr = tc_word(bj, bkf), wi = tc_word(NT + bj, bkf);
+          *reinterpret_cast<VW*>(&sm.b[stage][0][wr]) = hr;
+          *reinterpret_cast<VW*>(&sm.b[stage][1][wr]) = lr;
+          *reinterpret_cast<VW*>(&sm.b[stage][0][wi]) = hi;
+          *reinterpret_cast<VW*>(&sm.b[stage][1][wi]) = li;
+        }
+        tc::wait_st();
+        tc::fence_async_smem();
+        tc::fence_before();
+        tc::mbar_arrive(&sm.full[stage]);
       }
-      tc::fence_before();
-      ok = __syncthreads_and(ok);  // chunk c visible to all, stage free (or a uniform failure)
+      asm volatile("cp.async.wait_all;" ::: "memory");  // only empty groups remain
+      // ---- epilogue: the accumulator is complete when the last chunk's commit has arrived
+      const int gl = gc + nchunks - 1;
+      if (ok) ok = tc::mbar_wait(&sm.empty[gl & 1], (gl >> 1) & 1);
       tc::fence_after();
-      if (!ok) break;
-      // ---- A planes into TMEM: columns tA + stage*64 + plane*16 + k
-      {
-        const float2* rA = sm.rawA[slot];
-        uint32_t h[4][8];
+      const int lg = warp & 3, half = (warp - 1) >> 2;
+      if (half * 32 < NT) {
+        float re[32], im[32];
+        const uint32_t lane_base = (uint32_t)(32 * lg) << 16;
+        tc::ld32(tD + lane_base + half * 32, re);
+        tc::ld32(tD + lane_base + NT + half * 32, im);
+        const int i = i0 + 32 * lg + lane;  // MMA row
+        if (ok && i < MR) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const float2 v = rA[(akh + q) * kTcLdA + arow];
-          tc::split_tf32(v.x, h[0][q], h[1][q]);
-          tc::split_tf32(v.y, h[2][q], h[3][q]);
-        }
-        const uint32_t base = tA + stage * (4 * kTcKC) + akh + a_lane;
-#pragma unroll
-        for (int pl = 0; pl < 4; ++pl) tc::st8(base + pl * kTcKC, h[pl]);
-      }
-      // ---- B planes into shared memory: rows j (re) and NT + j (im), BPT consecutive k per thread
-      {
-        using VW = typename std::conditional<BPT == 4, uint4, uint2>::type;
-        const float2* rB = sm.rawB[slot] + bj * kTcLdB + bkf;
-        VW hr, lr, hi, li;
-        uint32_t* H = &hr.x; uint32_t* Lr = &lr.x; uint32_t* Hi = &hi.x; uint32_t* Li = &li.x;
-#pragma unroll
-        for (int q = 0; q < BPT; ++q) {
-          const float2 v = rB[q];
-          tc::split_tf32(v.x, H[q], Lr[q]);
-          tc::split_tf32(v.y, Hi[q], Li[q]);
-        }
-        const int wr = tc_word(bj, bkf), wi = tc_word(NT + bj, bkf);
-        *reinterpret_cast<VW*>(&sm.b[stage][0][wr]) = hr;
-        *reinterpret_cast<VW*>(&sm.b[stage][1][wr]) = lr;
-        *reinterpret_cast<VW*>(&sm.b[stage][0][wi]) = hi;
-        *reinterpret_cast<VW*>(&sm.b[stage][1][wi]) = li;
-      }
-      tc::wait_st();
-      tc::fence_async_smem();
-      tc::fence_before();
-      __syncthreads();
-      tc::fence_after();
-      if (tid == 0) {
-        const uint32_t bh = tc::smem_u32(sm.b[stage][0]), bl = tc::smem_u32(sm.b[stage][1]);
-        const uint32_t a0 = tA + stage * (4 * kTcKC);
-#pragma unroll
-        for (int ks = 0; ks < kTcKC / 8; ++ks) {
-          const uint32_t o = ks * 2 * 128;  // two core matrices per K = 8 step
-          const uint32_t a_rh = a0 + 0 * kTcKC + ks * 8, a_rl = a0 + 1 * kTcKC + ks * 8;
-          const uint32_t a_ih = a0 + 2 * kTcKC + ks * 8, a_il = a0 + 3 * kTcKC + ks * 8;
-          const uint64_t bh_re = tc::smem_desc(bh + o, LBO, SBO), bl_re = tc::smem_desc(bl + o, LBO, SBO);
-          const uint64_t bh_im = tc::smem_desc(bh + o + half_off, LBO, SBO);
-          const uint64_t bl_im = tc::smem_desc(bl + o + half_off, LBO, SBO);
-          const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
-          // [D_re | D_im] += A_re [B_re | B_im]
-          tc::mma_tf32_ta(tD, a_rh, bh_re, id_w, acc0);
-          tc::mma_tf32_ta(tD, a_rh, bl_re, id_w, 1u);
-          tc::mma_tf32_ta(tD, a_rl, bh_re, id_w, 1u);
-          // D_re -= A_im B_im
-          tc::mma_tf32_ta(tD, a_ih, bh_im, id_n, 1u);
-          tc::mma_tf32_ta(tD, a_ih, bl_im, id_n, 1u);
-          tc::mma_tf32_ta(tD, a_il, bh_im, id_n, 1u);
-          // D_im += A_im B_re
-          tc::mma_tf32_ta(tD + NT, a_ih, bh_re, id_p, 1u);
-          tc::mma_tf32_ta(tD + NT, a_ih, bl_re, id_p, 1u);
-          tc::mma_tf32_ta(tD + NT, a_il, bh_re, id_p, 1u);
-        }
-        tc::commit(&sm.mbar[stage]);
-        pending[stage] = true;
-      }
-    }
-    asm volatile("cp.async.wait_all;" ::: "memory");  // no copy outlives the tile (empty groups past the end)
-    // drain both stages before reading the accumulator
-    if (tid == 0)
-      for (int q = 0; q < 2 && ok; ++q)
-        if (pending[q]) {
-          ok = tc::mbar_wait(&sm.mbar[q], phase[q]);
-          phase[q] ^= 1u;
-          pending[q] = false;
-        }
-    tc::fence_before();
-    ok = __syncthreads_and(ok);  // every thread leaves the tile loop together
-    tc::fence_after();
-    if (!ok) break;
-    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, column half w / 4
-    const int lg = warp & 3, half = warp >> 2;
-    if (half * 32 < NT) {
-      float re[32], im[32];
-      const uint32_t lane_base = (uint32_t)(32 * lg) << 16;
-      tc::ld32(tD + lane_base + half * 32, re);
-      tc::ld32(tD + lane_base + NT + half * 32, im);
-      const int i = i0 + 32 * lg + lane;  // MMA row
-      if (i < MR) {
-#pragma unroll
-        for (int q = 0; q < 32; ++q) {
-          const int j = j0 + half * 32 + q;  // MMA column (complex)
-          if (j < NC) {
-            float2* dst = !TRANS ? F + (int64_t)(ca + j) * m + ra + i : F + (int64_t)(ca + i) * m + ra + j;
-            float2 v = *dst;
-            v.x -= re[q];
-            v.y -= im[q];
-            *dst = v;
+          for (int q = 0; q < 32; ++q) {
+            const int j = j0 + half * 32 + q;  // MMA column (complex)
+            if (j < NC) {
+              float2* dst = !TRANS ? F + (int64_t)(ca + j) * m + ra + i : F + (int64_t)(ca + i) * m + ra + j;
+              float2 v = *dst;
+              v.x -= re[q];
+              v.y -= im[q];
+              *dst = v;
+            }
           }
         }
       }
     }
+    gc += nchunks;
+    // the accumulator is read before the next tile's first MMA overwrites it
     tc::fence_before();
-    __syncthreads();
+    ok = __syncthreads_and(ok);
     tc::fence_after();
   }
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  // after a timed-out wait MMAs may still be in flight: wait (bounded) for
-  // every committed stage before the TMEM is released
-  if (tid == 0)
-    for (int q = 0; q < 2; ++q)
-      if (pending[q]) tc::mbar_wait(&sm.mbar[q], phase[q]);
-  if (!ok && tid == 0) atomicExch(err, 1);
+  // every commit has been waited on by the epilogue (or a wait timed out, in which
+  // case the MMAs that may still run are waited for, bounded, before the release)
+  if (!ok && tid == 0) {
+    atomicExch(err, 1);
+    for (int q = 0; q < 2; ++q) {  // the last chunk committed on stage q
+      const int gq = ((gc - 1) & 1) == q ? gc - 1 : gc - 2;
+      if (gq >= 0) tc::mbar_wait(&sm.empty[q], (gq >> 1) & 1);
+    }
+  }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();

@@ -1090,13 +1090,13 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       if (mode == GM_SCHUR) {
         const int t = ((rows_c + 127) / 128) * ((cols_c + 63) / 64);
         dim3 g(L.count, S_used, (unsigned)std::min(65535, t));
-        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 64, false><<<g, 256, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 64, false><<<g, kTcThreads, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
       } else if (mode == GM_COL) {
         dim3 g(L.count, S_used, (unsigned)std::min(65535, (rows_c + 127) / 128));
-        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, false><<<g, 256, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, false><<<g, kTcThreads, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
       } else {
         dim3 g(L.count, S_used, (unsigned)std::min(65535, (cols_c + 127) / 128));
-        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, true><<<g, 256, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, true><<<g, kTcThreads, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
       }
       return;
     }
