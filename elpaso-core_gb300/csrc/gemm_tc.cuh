@@ -28,7 +28,7 @@
 // the raw data needs no cross-thread synchronisation: a thread waits only for
 // its own copy groups. Two MMA stages (TMEM columns for A, shared memory for
 // B) are handed over with mbarriers, never with block barriers:
-//   full[s]  - 256 converter arrivals: stage s holds a converted chunk;
+//   full[s]  - one arrival per converter warp: stage s holds a converted chunk;
 //   empty[s] - tcgen05.commit of the MMAs that read stage s.
 // So the converters prepare chunk c + 1 while the tensor pipe runs chunk c,
 // whatever back-pressure the MMA issue meets. Every wait is bounded: a
@@ -125,19 +125,16 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
+__device__ __forceinline__ void ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 }  // namespace tc
@@ -210,7 +207,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
   }
   if (tid == 0) {
     for (int q = 0; q < 2; ++q) {
-      tc::mbar_init(&sm.full[q], 256);
+      tc::mbar_init(&sm.full[q], 8);  // one arrival per converter warp
       tc::mbar_init(&sm.empty[q], 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -310,8 +307,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
 #pragma unroll
         for (int q = 0; q < BPT; ++q) bv[q] = sm.raw[slot][8 + q][ct];
         issue(c + kTcRing);  // the values are in registers: the slot can be refilled
-        // stage free: the MMAs of chunk g - 2 have completed
-        if (g >= 2 && ok) ok = tc::mbar_wait(&sm.empty[stage], ((g >> 1) + 1) & 1);
+        // stage free: the MMAs of chunk g - 2 have completed (one lane polls, the warp follows)
+        if (g >= 2) {
+          if (lane == 0 && ok) ok = tc::mbar_wait(&sm.empty[stage], ((g >> 1) + 1) & 1);
+          __syncwarp();
+        }
         tc::fence_after();
         {  // A planes into TMEM: columns tA + stage*64 + plane*16 + k
           uint32_t h[4][8];
@@ -342,31 +342,35 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
         tc::wait_st();
         tc::fence_async_smem();
         tc::fence_before();
-        tc::mbar_arrive(&sm.full[stage]);
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&sm.full[stage]);
       }
       asm volatile("cp.async.wait_all;" ::: "memory");  // only empty groups remain
       // ---- epilogue: the accumulator is complete when the last chunk's commit has arrived
       const int gl = gc + nchunks - 1;
-      if (ok) ok = tc::mbar_wait(&sm.empty[gl & 1], (gl >> 1) & 1);
+      if (lane == 0 && ok) ok = tc::mbar_wait(&sm.empty[gl & 1], (gl >> 1) & 1);
+      __syncwarp();
       tc::fence_after();
       const int lg = warp & 3, half = (warp - 1) >> 2;
       if (half * 32 < NT) {
-        float re[32], im[32];
         const uint32_t lane_base = (uint32_t)(32 * lg) << 16;
-        tc::ld32(tD + lane_base + half * 32, re);
-        tc::ld32(tD + lane_base + NT + half * 32, im);
         const int i = i0 + 32 * lg + lane;  // MMA row
-        if (ok && i < MR) {
 #pragma unroll
-          for (int q = 0; q < 32; ++q) {
-            const int j = j0 + half * 32 + q;  // MMA column (complex)
-            if (j < NC) {
-              float2* dst = !TRANS ? F + (int64_t)(ca + j) * m + ra + i : F + (int64_t)(ca + i) * m + ra + j;
-              float2 v = *dst;
-              v.x -= re[q];
-              v.y -= im[q];
-              *dst = v;
-            }
+        for (int part = 0; part < 2; ++part) {  // 16 columns at a time: loads first, then stores
+          const int jb = j0 + half * 32 + part * 16;
+          float re[16], im[16];
+          tc::ld16(tD + lane_base + half * 32 + part * 16, re);
+          tc::ld16(tD + lane_base + NT + half * 32 + part * 16, im);
+          if (ok && i < MR) {
+            float2* dst0 = !TRANS ? F + (int64_t)(ca + jb) * m + ra + i : F + (int64_t)(ca + i) * m + ra + jb;
+            const int64_t dq = !TRANS ? (int64_t)m : 1;
+            float2 cv[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+              if (jb + q < NC) cv[q] = dst0[q * dq];
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+              if (jb + q < NC) dst0[q * dq] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
           }
         }
       }
