@@ -170,8 +170,10 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
     }
     __syncthreads();
     const int pr = s_piv;
+    // swap within the panel columns only; k_laswp applies the panel's swaps to
+    // every other column of the front afterwards, in one parallel pass
     if (pr != j)
-      for (int c = tid; c < m; c += blockDim.x) {
+      for (int c = k0 + tid; c < k0 + w; c += blockDim.x) {
         V t = F[(int64_t)c * m + j];
         F[(int64_t)c * m + j] = F[(int64_t)c * m + pr];
         F[(int64_t)c * m + pr] = t;
@@ -191,10 +193,20 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
     for (int c = j + 1 + tid; c < k0 + w; c += blockDim.x) prow[c - k0] = F[(int64_t)c * m + j];
     __syncthreads();
     const V inv = cinv(d);
+    const int cj = j - k0;  // panel column of the pivot
     for (int r = j + 1 + tid; r < p; r += blockDim.x) {
-      V l = cmul(F[(int64_t)j * m + r], inv);
+      const V l = cmul(F[(int64_t)j * m + r], inv);
       F[(int64_t)j * m + r] = l;
-      for (int c = j + 1; c < k0 + w; ++c) F[(int64_t)c * m + r] = cfms(F[(int64_t)c * m + r], l, prow[c - k0]);
+#pragma unroll
+      for (int h = 0; h < NB; h += 16) {  // the row's panel entries right of the pivot, 16 loads together
+        V a[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (h + c > cj && h + c < w) a[c] = F[(int64_t)(k0 + h + c) * m + r];
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (h + c > cj && h + c < w) F[(int64_t)(k0 + h + c) * m + r] = cfms(a[c], l, prow[h + c]);
+      }
     }
     __syncthreads();
   }
@@ -203,6 +215,58 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
     atomicMax(stats + 4 * s + 1, (unsigned long long)__double_as_longlong((double)pmax));
     // min |u_jj| stored as bits of 1/|u_jj| max
     atomicMax(stats + 4 * s + 2, (unsigned long long)__double_as_longlong(1.0 / (double)pmin));
+  }
+}
+
+// Row interchanges of one panel applied to every column outside it (LAPACK's
+// laswp): the panel's w swaps (j, pv[j]), j = k0..k0+w-1, touch at most 2w
+// rows; their net effect is new[row_i] = old[src_i] over that row list, built
+// once per CTA in shared memory, then every thread moves its column's touched
+// rows with independent loads followed by the stores.
+template <class R, int NB>
+__global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T* __restrict__ arena,
+                                               const int32_t* __restrict__ perm, int step) {
+  using V = typename Vec2<R>::T;
+  const int f = L.list[blockIdx.x];
+  const int s = blockIdx.y;
+  const int p = L.fp[f], m = p + L.fb[f];
+  const int k0 = step * NB;
+  if (k0 >= p) return;
+  const int w = min(NB, p - k0);
+  if ((int)blockIdx.z * (int)blockDim.x >= m - w) return;
+  __shared__ int rows[2 * NB], src[2 * NB];
+  __shared__ int nrows;
+  const int32_t* pv = perm + s * L.n + L.piv_off[f];
+  if (threadIdx.x == 0) {
+    int n = 0;
+    for (int j = 0; j < w; ++j) { rows[n] = k0 + j; src[n] = k0 + j; ++n; }
+    for (int j = 0; j < w; ++j) {
+      const int r = pv[k0 + j];
+      int a = -1, b = -1;
+      for (int q = 0; q < n; ++q) {
+        if (rows[q] == k0 + j) a = q;
+        if (rows[q] == r) b = q;
+      }
+      if (b < 0) { rows[n] = r; src[n] = r; b = n++; }
+      const int t = src[a]; src[a] = src[b]; src[b] = t;
+    }
+    nrows = n;
+  }
+  __syncthreads();
+  const int n = nrows;
+  int c = blockIdx.z * blockDim.x + threadIdx.x;  // index over the columns outside the panel
+  if (c >= m - w) return;
+  if (c >= k0) c += w;
+  V* col = arena + s * L.arena_size + L.foff[f] + (int64_t)c * m;
+#pragma unroll
+  for (int h = 0; h < 2 * NB; h += NB) {  // NB rows at a time: loads first, then stores
+    V v[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q)
+      if (h + q < n) v[q] = col[src[h + q]];
+#pragma unroll
+    for (int q = 0; q < NB; ++q)
+      if (h + q < n) col[rows[h + q]] = v[q];
   }
 }
 
@@ -400,12 +464,20 @@ __global__ void __launch_bounds__(256) k_extend_add(const int32_t* __restrict__ 
   const V* C = arena + s * arena_size + foff[c];
   V* PF = arena + s * arena_size + foff[P];
   const int32_t* mp = pmap + map_off[c];
-  for (int j = blockIdx.z; j < bc; j += gridDim.z) {
-    const int64_t pcol = (int64_t)mp[j] * mP;
-    const V* src = C + (int64_t)(pc + j) * mc + pc;
-    for (int i = threadIdx.x; i < bc; i += blockDim.x) {
-      V* d = PF + pcol + mp[i];
-      *d = cadd(*d, src[i]);
+  for (int i = threadIdx.x; i < bc; i += blockDim.x) {
+    const int pi = mp[i];
+    // 4 columns per pass: their loads are independent and in flight together
+    for (int j = blockIdx.z * 4; j < bc; j += gridDim.z * 4) {
+      V sv[4], dv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (j + q < bc) {
+          sv[q] = C[(int64_t)(pc + j + q) * mc + pc + i];
+          dv[q] = PF[(int64_t)mp[j + q] * mP + pi];
+        }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (j + q < bc) PF[(int64_t)mp[j + q] * mP + pi] = cadd(dv[q], sv[q]);
     }
   }
 }
@@ -479,8 +551,13 @@ __global__ void __launch_bounds__(256) k_forward(SolveArgs S, const typename Vec
     }
     __syncthreads();
     for (int r = j0 + jw + tid; r < p; r += blockDim.x) {
+      V a[32];  // all loads of the row first: one memory latency per row, not 32
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj) a[jj] = jj < jw ? F[(int64_t)(j0 + jj) * m + r] : cmk<V>(0.0, 0.0);
       V t = w[r];
-      for (int jj = 0; jj < jw; ++jj) t = cfms(t, F[(int64_t)(j0 + jj) * m + r], w[j0 + jj]);
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj)
+        if (jj < jw) t = cfms(t, a[jj], w[j0 + jj]);
       w[r] = t;
     }
     __syncthreads();
@@ -515,13 +592,12 @@ __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename 
   V t = *dst;
   const V* col = F + p + i;
   int j = 0;
-  for (; j + 4 <= p; j += 4) {
-    V a0 = col[(int64_t)(j + 0) * m], a1 = col[(int64_t)(j + 1) * m];
-    V a2 = col[(int64_t)(j + 2) * m], a3 = col[(int64_t)(j + 3) * m];
-    t = cfms(t, a0, y[j + 0]);
-    t = cfms(t, a1, y[j + 1]);
-    t = cfms(t, a2, y[j + 2]);
-    t = cfms(t, a3, y[j + 3]);
+  for (; j + 16 <= p; j += 16) {  // 16 independent loads in flight per thread
+    V a[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) a[q] = col[(int64_t)(j + q) * m];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) t = cfms(t, a[q], y[j + q]);
   }
   for (; j < p; ++j) t = cfms(t, col[(int64_t)j * m], y[j]);
   *dst = t;
@@ -550,13 +626,12 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   V t = zs[I[r]];
   const V* row = F + (int64_t)p * m + r;
   int i = 0;
-  for (; i + 4 <= b; i += 4) {
-    V a0 = row[(int64_t)(i + 0) * m], a1 = row[(int64_t)(i + 1) * m];
-    V a2 = row[(int64_t)(i + 2) * m], a3 = row[(int64_t)(i + 3) * m];
-    t = cfms(t, a0, xb[i + 0]);
-    t = cfms(t, a1, xb[i + 1]);
-    t = cfms(t, a2, xb[i + 2]);
-    t = cfms(t, a3, xb[i + 3]);
+  for (; i + 16 <= b; i += 16) {  // 16 independent loads in flight per thread
+    V a[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) a[q] = row[(int64_t)(i + q) * m];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) t = cfms(t, a[q], xb[i + q]);
   }
   for (; i < b; ++i) t = cfms(t, row[(int64_t)i * m], xb[i]);
   tb[s * S.n + S.piv_off[f] + r] = t;
@@ -602,8 +677,13 @@ __global__ void __launch_bounds__(256) k_backward(SolveArgs S, const typename Ve
     }
     __syncthreads();
     for (int r = tid; r < j0; r += blockDim.x) {
+      V a[32];  // all loads of the row first: one memory latency per row, not 32
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj) a[jj] = jj < jw ? F[(int64_t)(j0 + jj) * m + r] : cmk<V>(0.0, 0.0);
       V t = w[r];
-      for (int jj = 0; jj < jw; ++jj) t = cfms(t, F[(int64_t)(j0 + jj) * m + r], w[j0 + jj]);
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj)
+        if (jj < jw) t = cfms(t, a[jj], w[j0 + jj]);
       w[r] = t;
     }
     __syncthreads();
@@ -1123,6 +1203,10 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       if (k > 0) gemm(GM_COL, k, rows, NB);     // panel columns from all previous panels
       dim3 g1(LV.count, S_used);
       PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB><<<g1, 256, 0, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p));
+      {
+        dim3 gl(LV.count, S_used, (unsigned)std::min(65535, (LV.max_m + 255) / 256));
+        PROF_LAUNCH(KC_PANEL, st, k_laswp<R, NB><<<gl, 256, 0, st>>>(L, arena, w.perm.p, k));
+      }
       if (LV.max_b > 0) {
         dim3 g2(LV.count, S_used, (unsigned)std::min(65535, (LV.max_b + 127) / 128));
         PROF_LAUNCH(KC_BORDER, st, k_border<R, NB><<<g2, 128, 0, st>>>(L, arena, k));
@@ -1136,7 +1220,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     if (LV.max_b > 0) gemm(GM_SCHUR, 0, LV.max_b, LV.max_b);  // Schur complement, depth p
     for (size_t k = 0; k < LV.ea_count.size(); ++k) {
       if (!LV.ea_count[k]) continue;
-      dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, LV.ea_max_b));
+      dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, (LV.ea_max_b + 3) / 4));  // 4 columns per pass
       PROF_LAUNCH(KC_EXTEND_ADD, st, k_extend_add<R><<<g5, 256, 0, st>>>(D.ea_list.p + LV.ea_start[k], D.f_p.p, D.f_b.p, D.f_parent.p, D.f_map_off.p,
                                           D.f_off.p, D.parent_map.p, arena, D.arena));
     }
