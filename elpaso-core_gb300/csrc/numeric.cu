@@ -221,8 +221,9 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
 // Row interchanges of one panel applied to every column outside it (LAPACK's
 // laswp): the panel's w swaps (j, pv[j]), j = k0..k0+w-1, touch at most 2w
 // rows; their net effect is new[row_i] = old[src_i] over that row list, built
-// once per CTA in shared memory, then every thread moves its column's touched
-// rows with independent loads followed by the stores.
+// once per CTA in shared memory. FP32: every thread loads all of its column's
+// touched rows, then stores them (one memory latency per column); FP64: the
+// swaps in order.
 template <class R, int NB>
 __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T* __restrict__ arena,
                                                const int32_t* __restrict__ perm, int step) {
@@ -258,15 +259,26 @@ __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T*
   if (c >= m - w) return;
   if (c >= k0) c += w;
   V* col = arena + s * L.arena_size + L.foff[f] + (int64_t)c * m;
+  if (sizeof(R) == 4) {
+    // every source is loaded before any row is written: a source row may be
+    // another entry's destination
+    V v[2 * NB];
 #pragma unroll
-  for (int h = 0; h < 2 * NB; h += NB) {  // NB rows at a time: loads first, then stores
-    V v[NB];
+    for (int q = 0; q < 2 * NB; ++q)
+      if (q < n) v[q] = col[src[q]];
 #pragma unroll
-    for (int q = 0; q < NB; ++q)
-      if (h + q < n) v[q] = col[src[h + q]];
-#pragma unroll
-    for (int q = 0; q < NB; ++q)
-      if (h + q < n) col[rows[h + q]] = v[q];
+    for (int q = 0; q < 2 * NB; ++q)
+      if (q < n) col[rows[q]] = v[q];
+  } else {
+    // FP64 (2 NB complex doubles would not fit in registers): the swaps in order
+    for (int j = 0; j < w; ++j) {
+      const int r = pv[k0 + j];
+      if (r != k0 + j) {
+        const V t = col[k0 + j];
+        col[k0 + j] = col[r];
+        col[r] = t;
+      }
+    }
   }
 }
 
