@@ -62,36 +62,44 @@ int scratch_address(NoAllocScratch** out) {
   return ELP_OK;
 }
 
-// r = f - A x per row (warp per row) and per-block |r|^2, |f|^2 into the scratch
+// r = f - A x per row (kRowLanes lanes per row, as the solve path's
+// k_residual) and per-block |r|^2, |f|^2 into the scratch
 __global__ void k_noalloc_residual(CombineArgs A, NoAllocScratch* sc, const int32_t* __restrict__ row_ptr,
                                    const int32_t* __restrict__ col_idx, int64_t n, const double2* __restrict__ x,
                                    const double2* __restrict__ f, double2* __restrict__ r) {
   const int s = blockIdx.y;
   const Coef c = sc->coef[s];
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
   const double2* xs = x + s * n;
   double rr = 0.0, ff = 0.0;
+  constexpr int RPW = 32 / kRowLanes;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = warp; i < n; i += nwarps) {
+  for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {  // warp-uniform bound
+    const int64_t i = base + lane / kRowLanes;
     DD sx{0.0, 0.0}, sy{0.0, 0.0};
-    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
-      double2 a = combine(A, c, q);
-      double2 v = xs[col_idx[q]];
-      dd_fma(sx, a.x, v.x);
-      dd_fma(sx, -a.y, v.y);
-      dd_fma(sy, a.x, v.y);
-      dd_fma(sy, a.y, v.x);
-    }
-    sx = dd_warp_sum(sx);
-    sy = dd_warp_sum(sy);
-    if (lane == 0) {
+    if (i < n)
+      for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
+        double2 a = combine(A, c, q);
+        double2 v = xs[col_idx[q]];
+        dd_fma(sx, a.x, v.x);
+        dd_fma(sx, -a.y, v.y);
+        dd_fma(sy, a.x, v.y);
+        dd_fma(sy, a.y, v.x);
+      }
+    sx = row_sum(sx);
+    sy = row_sum(sy);
+    if (i < n && sub == 0) {
       double2 fi = f[s * n + i];
       double2 ri = make_double2(dd_residual(fi.x, sx), dd_residual(fi.y, sy));
       r[s * n + i] = ri;
       rr += ri.x * ri.x + ri.y * ri.y;
       ff += fi.x * fi.x + fi.y * fi.y;
     }
+  }
+  for (int o = 16; o; o >>= 1) {
+    rr += __shfl_xor_sync(0xffffffffu, rr, o);
+    ff += __shfl_xor_sync(0xffffffffu, ff, o);
   }
   __shared__ double red[2][32];
   const int wid = threadIdx.x >> 5;

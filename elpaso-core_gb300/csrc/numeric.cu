@@ -235,21 +235,27 @@ __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T*
   if (k0 >= p) return;
   const int w = min(NB, p - k0);
   if ((int)blockIdx.z * (int)blockDim.x >= m - w) return;
-  __shared__ int rows[2 * NB], src[2 * NB];
+  __shared__ int rows[2 * NB], src[2 * NB], spv[NB];
   __shared__ int nrows;
   const int32_t* pv = perm + s * L.n + L.piv_off[f];
-  if (threadIdx.x == 0) {
-    int n = 0;
-    for (int j = 0; j < w; ++j) { rows[n] = k0 + j; src[n] = k0 + j; ++n; }
+  const int tid = threadIdx.x;
+  if (tid < w) spv[tid] = pv[k0 + tid];
+  // most panels interchange no rows at all
+  if (!__syncthreads_or(tid < w && spv[tid] != k0 + tid)) return;
+  if (tid == 0) {
+    // panel rows sit at list position row - k0; rows below the panel are appended
+    int n = w;
+    for (int j = 0; j < w; ++j) { rows[j] = k0 + j; src[j] = k0 + j; }
     for (int j = 0; j < w; ++j) {
-      const int r = pv[k0 + j];
-      int a = -1, b = -1;
-      for (int q = 0; q < n; ++q) {
-        if (rows[q] == k0 + j) a = q;
-        if (rows[q] == r) b = q;
+      const int r = spv[j];
+      int b = r - k0;
+      if (b >= w) {
+        b = -1;
+        for (int q = w; q < n; ++q)
+          if (rows[q] == r) b = q;
+        if (b < 0) { rows[n] = r; src[n] = r; b = n++; }
       }
-      if (b < 0) { rows[n] = r; src[n] = r; b = n++; }
-      const int t = src[a]; src[a] = src[b]; src[b] = t;
+      const int t = src[j]; src[j] = src[b]; src[b] = t;
     }
     nrows = n;
   }
@@ -272,7 +278,7 @@ __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T*
   } else {
     // FP64 (2 NB complex doubles would not fit in registers): the swaps in order
     for (int j = 0; j < w; ++j) {
-      const int r = pv[k0 + j];
+      const int r = spv[j];
       if (r != k0 + j) {
         const V t = col[k0 + j];
         col[k0 + j] = col[r];
@@ -705,37 +711,48 @@ __global__ void __launch_bounds__(256) k_backward(SolveArgs S, const typename Ve
 
 // ------------------------------------------------------------- refinement (FP64)
 // r = f - A x (unscaled A, BC rows included); partial sums of |r|^2 and |f|^2
+// kRowLanes lanes per row; the row loop bound is warp-uniform so every lane
+// reaches every shuffle. With x_zero the residual is f itself (no product).
 __global__ void k_residual(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ row_ptr,
                            const int32_t* __restrict__ col_idx, int64_t n, const double2* __restrict__ x,
                            const double2* __restrict__ f, double2* __restrict__ r, double* __restrict__ partial,
-                           int nparts, const int* __restrict__ active) {
+                           int nparts, const int* __restrict__ active, int x_zero) {
   const int s = blockIdx.y;
   if (!active[s]) return;
   const Coef c = coef[s];
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
   const double2* xs = x + s * n;
   double rr = 0.0, ff = 0.0;
+  constexpr int RPW = 32 / kRowLanes;  // rows per warp
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = warp; i < n; i += nwarps) {
+  for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
+    const int64_t i = base + lane / kRowLanes;
     DD sx{0.0, 0.0}, sy{0.0, 0.0};
-    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
-      double2 a = combine(A, c, q);
-      double2 v = xs[col_idx[q]];
-      dd_fma(sx, a.x, v.x);
-      dd_fma(sx, -a.y, v.y);
-      dd_fma(sy, a.x, v.y);
-      dd_fma(sy, a.y, v.x);
+    if (i < n && !x_zero)
+      for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
+        double2 a = combine(A, c, q);
+        double2 v = xs[col_idx[q]];
+        dd_fma(sx, a.x, v.x);
+        dd_fma(sx, -a.y, v.y);
+        dd_fma(sy, a.x, v.y);
+        dd_fma(sy, a.y, v.x);
+      }
+    if (!x_zero) {
+      sx = row_sum(sx);
+      sy = row_sum(sy);
     }
-    sx = dd_warp_sum(sx);
-    sy = dd_warp_sum(sy);
-    if (lane == 0) {
+    if (i < n && sub == 0) {
       double2 fi = f[s * n + i];
-      double2 ri = make_double2(dd_residual(fi.x, sx), dd_residual(fi.y, sy));
+      double2 ri = x_zero ? fi : make_double2(dd_residual(fi.x, sx), dd_residual(fi.y, sy));
       r[s * n + i] = ri;
       rr += ri.x * ri.x + ri.y * ri.y;
       ff += fi.x * fi.x + fi.y * fi.y;
     }
+  }
+  for (int o = 16; o; o >>= 1) {
+    rr += __shfl_xor_sync(0xffffffffu, rr, o);
+    ff += __shfl_xor_sync(0xffffffffu, ff, o);
   }
   __shared__ double red[2][32];
   const int wid = threadIdx.x >> 5;
@@ -780,24 +797,29 @@ __global__ void k_rhs(CombineArgs A, const Coef* __restrict__ coef, const int32_
                       const double* __restrict__ dscale, int64_t n, V* __restrict__ z, const int* __restrict__ active) {
   const int s = blockIdx.y;
   if (!active[s]) return;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
   const double2* rs = r + s * sstride;
+  constexpr int RPW = 32 / kRowLanes;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = warp; i < n; i += nwarps) {
+  for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
+    const int64_t i = base + lane / kRowLanes;
     double sx = 0.0, sy = 0.0;
-    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
-      if (!(A.cls[q] & CLS_BC_COLUMN)) continue;
-      double2 a = combine(A, coef[s], q);
-      double2 v = rs[col_idx[q]];
-      sx += a.x * v.x - a.y * v.y;
-      sy += a.x * v.y + a.y * v.x;
+    bool lift = false;  // entries in Dirichlet columns: lifted to the right-hand side
+    if (i < n)
+      for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
+        if (!(A.cls[q] & CLS_BC_COLUMN)) continue;
+        lift = true;
+        double2 a = combine(A, coef[s], q);
+        double2 v = rs[col_idx[q]];
+        sx += a.x * v.x - a.y * v.y;
+        sy += a.x * v.y + a.y * v.x;
+      }
+    if (__any_sync(0xffffffffu, lift)) {  // most rows touch no Dirichlet column
+      sx = row_sum(sx);
+      sy = row_sum(sy);
     }
-    for (int o = 16; o; o >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, o);
-      sy += __shfl_xor_sync(0xffffffffu, sy, o);
-    }
-    if (lane == 0) {
+    if (i < n && sub == 0) {
       const double d = dscale[s * n + i];
       const double2 v = rs[i];
       z[s * n + i] = cmk<V>((v.x - sx) * d, (v.y - sy) * d);
@@ -835,23 +857,24 @@ __global__ void k_spmv(CombineArgs A, const Coef* __restrict__ coef, const int32
   const int s = blockIdx.y;
   if (!active[s]) return;
   const Coef c = coef[s];
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
   const double2* us = u + s * ustride;
+  constexpr int RPW = 32 / kRowLanes;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = warp; i < n; i += nwarps) {
+  for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
+    const int64_t i = base + lane / kRowLanes;
     double sx = 0.0, sy = 0.0;
-    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
-      double2 a = combine(A, c, q);
-      double2 v = us[col_idx[q]];
-      sx += a.x * v.x - a.y * v.y;
-      sy += a.x * v.y + a.y * v.x;
-    }
-    for (int o = 16; o; o >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, o);
-      sy += __shfl_xor_sync(0xffffffffu, sy, o);
-    }
-    if (lane == 0) w[s * n + i] = make_double2(sx, sy);
+    if (i < n)
+      for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
+        double2 a = combine(A, c, q);
+        double2 v = us[col_idx[q]];
+        sx += a.x * v.x - a.y * v.y;
+        sy += a.x * v.y + a.y * v.x;
+      }
+    sx = row_sum(sx);
+    sy = row_sum(sy);
+    if (i < n && sub == 0) w[s * n + i] = make_double2(sx, sy);
   }
 }
 
@@ -1346,7 +1369,7 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
   float solve_ms = 0.f, refine_ms = 0.f;
   // initial residual r = f (x = 0)
   PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p, w.r.p, w.partial.p,
-                                 w.nparts, w.active.p));
+                                 w.nparts, w.active.p, 1));
   for (it = 0; it < max_iter; ++it) {
     ELP_CUDA(cudaEventRecord(w.ev[2], st));
     PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, w.r.p, n, w.dscale.p, n, reinterpret_cast<V*>(w.z.p), w.active.p));
@@ -1355,7 +1378,7 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
     PROF_LAUNCH(KC_UPDATE, st, k_update<V><<<gv, 256, 0, st>>>(w.x.p, w.dscale.p, n, reinterpret_cast<const V*>(w.z.p), w.active.p));
     ELP_CUDA(cudaEventRecord(w.ev[3], st));
     PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p, w.r.p, w.partial.p,
-                                   w.nparts, w.active.p));
+                                   w.nparts, w.active.p, 0));
     PROF_LAUNCH(KC_NORMS, st, k_norms<<<S_used, 256, 0, st>>>(w.partial.p, w.nparts, w.norms.p, w.active.p));
     ELP_CUDA(cudaMemcpyAsync(w.h_norms, w.norms.p, sizeof(double) * 2 * S_used, cudaMemcpyDeviceToHost, st));
     ELP_CUDA(cudaEventRecord(w.ev[4], st));
@@ -1437,9 +1460,9 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
   V* z = reinterpret_cast<V*>(w.z.p);
   static const bool trace = getenv("ELP_TRACE") != nullptr;
   std::vector<double> fn(S_used), rel(S_used);
-  auto residual = [&]() -> int {
+  auto residual = [&](int x_zero) -> int {
     PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p,
-                                                                   w.r.p, w.partial.p, w.nparts, w.active.p));
+                                                                   w.r.p, w.partial.p, w.nparts, w.active.p, x_zero));
     PROF_LAUNCH(KC_NORMS, st, k_norms<<<S_used, 256, 0, st>>>(w.partial.p, w.nparts, w.norms.p, w.active.p));
     ELP_CUDA(cudaMemcpyAsync(w.h_norms, w.norms.p, sizeof(double) * 2 * S_used, cudaMemcpyDeviceToHost, st));
     ELP_CUDA(cudaStreamSynchronize(st));
@@ -1454,7 +1477,7 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
     PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, src, sstride, w.dscale.p, n, z, mask));
     return solve_sweep<R>(m, w, S_used, st, mask);
   };
-  rc = residual();
+  rc = residual(1);  // x = 0
   if (rc) return rc;
   std::vector<std::vector<cd>> H(S_used, std::vector<cd>((RST + 1) * RST));
   std::vector<std::vector<cd>> g(S_used, std::vector<cd>(RST + 1)), sn(S_used, std::vector<cd>(RST));
@@ -1565,7 +1588,7 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
     }
     ELP_CUDA(cudaMemcpyAsync(w.ydev.p, w.h_y, sizeof(double2) * S_used * kMaxBasis, cudaMemcpyHostToDevice, st));
     PROF_LAUNCH(KC_UPDATE, st, k_combo<<<gv, 256, 0, st>>>(w.Zb.p, zst, n, nvmax, w.ydev.p, w.x.p, n, w.active.p));
-    rc = residual();
+    rc = residual(0);
     if (rc) return rc;
   }
   ELP_CUDA(cudaGetLastError());

@@ -85,6 +85,26 @@ __device__ __forceinline__ DD dd_warp_sum(DD v) {
   }
   return v;
 }
+// FP64 row kernels give each CSR row kRowLanes lanes (rows hold ~10-40
+// entries); FP64 instructions are scarce on this part, so a full warp and a
+// five-level reduction per row would waste most of them.
+constexpr int kRowLanes = 8;
+
+// the kRowLanes-lane group of a row: sum over the group (xor shuffles stay inside it)
+__device__ __forceinline__ double row_sum(double v) {
+  for (int o = kRowLanes / 2; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ DD row_sum(DD v) {
+  for (int o = kRowLanes / 2; o; o >>= 1) {
+    DD w;
+    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    dd_merge(v, w);
+  }
+  return v;
+}
+
 // f - (a.hi + a.lo), rounded once
 __device__ __forceinline__ double dd_residual(double f, const DD& a) {
   DD s{f, 0.0};
