@@ -124,32 +124,64 @@ struct LevelArgs {
   int64_t n;
 };
 
+constexpr int kPanelSmemBytes = 200 * 1024;  // panel rows held in shared memory when they fit
+
+// swap map of one panel per (front of the level, slot): [n, rows[2 NB], src[2 NB]],
+// n = 0 when the panel interchanged no rows
+template <int NB>
+__host__ __device__ constexpr int swapmap_ints() { return 1 + 4 * NB; }
+
+// Panel factorisation (columns k0..k0+w-1, fully summed rows k0..p-1) with
+// partial pivoting restricted to the fully summed rows and a static pivot
+// floor. The panel lives in shared memory when its rows fit (one load and
+// one store of the panel instead of a memory round trip per column step),
+// else it is factorised in place. Row interchanges are applied here to the
+// panel columns only; the panel's net permutation of rows (at most 2 w rows)
+// is written as a swap map that k_laswp applies to every other column.
 template <class R, int NB>
 __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T* __restrict__ arena,
                                                int32_t* __restrict__ perm, int step, R tiny,
-                                               unsigned long long* __restrict__ stats) {
+                                               unsigned long long* __restrict__ stats, int32_t* __restrict__ swapmap,
+                                               int cap_rows) {
   using V = typename Vec2<R>::T;
+  extern __shared__ unsigned char psm_raw[];
   const int f = L.list[blockIdx.x];
   const int s = blockIdx.y;
   const int p = L.fp[f], m = p + L.fb[f];
   const int k0 = step * NB;
   if (k0 >= p) return;
   const int w = min(NB, p - k0);
+  const int rows = p - k0;
   V* F = arena + s * L.arena_size + L.foff[f];
   int32_t* pv = perm + s * L.n + L.piv_off[f];
   __shared__ R red_v[8];
   __shared__ int red_i[8];
   __shared__ V prow[NB];
-  __shared__ int s_piv;
+  __shared__ int s_piv, spiv[NB];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const bool in_smem = rows <= cap_rows;
+  V* P;       // P[c * ld + r] = F[(k0 + c) * m + k0 + r]
+  int64_t ld;
+  if (in_smem) {
+    P = reinterpret_cast<V*>(psm_raw);
+    ld = rows;
+    for (int t = tid; t < rows * w; t += blockDim.x) {
+      const int c = t / rows, r = t - c * rows;
+      P[t] = F[(int64_t)(k0 + c) * m + k0 + r];
+    }
+    __syncthreads();
+  } else {
+    P = F + (int64_t)k0 * m + k0;
+    ld = m;
+  }
   int nstatic = 0;
   R pmax = 0, pmin = (R)1e30;
-  for (int j = k0; j < k0 + w; ++j) {
-    // ---- pivot search over the fully summed rows j..p-1
+  for (int j = 0; j < w; ++j) {
+    // ---- pivot search over the fully summed rows j..rows-1
     R best = -1;
     int bi = j;  // stays in range even when the whole column is NaN
-    for (int r = j + tid; r < p; r += blockDim.x) {
-      R a = cabs2(F[(int64_t)j * m + r]);
+    for (int r = j + tid; r < rows; r += blockDim.x) {
+      R a = cabs2(P[j * ld + r]);
       if (a > best) { best = a; bi = r; }
     }
     for (int o = 16; o; o >>= 1) {
@@ -164,69 +196,94 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
       int i0 = red_i[0];
       for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
         if (red_v[q] > b0 || (red_v[q] == b0 && red_i[q] < i0)) { b0 = red_v[q]; i0 = red_i[q]; }
-      if (i0 < j || i0 >= p) i0 = j;
+      if (i0 < j || i0 >= rows) i0 = j;
       s_piv = i0;
-      pv[j] = i0;
+      spiv[j] = k0 + i0;
+      pv[k0 + j] = k0 + i0;
     }
     __syncthreads();
     const int pr = s_piv;
-    // swap within the panel columns only; k_laswp applies the panel's swaps to
-    // every other column of the front afterwards, in one parallel pass
     if (pr != j)
-      for (int c = k0 + tid; c < k0 + w; c += blockDim.x) {
-        V t = F[(int64_t)c * m + j];
-        F[(int64_t)c * m + j] = F[(int64_t)c * m + pr];
-        F[(int64_t)c * m + pr] = t;
+      for (int c = tid; c < w; c += blockDim.x) {
+        V t = P[c * ld + j];
+        P[c * ld + j] = P[c * ld + pr];
+        P[c * ld + pr] = t;
       }
     __syncthreads();
-    V d = F[(int64_t)j * m + j];
+    V d = P[j * ld + j];
     R ad = sqrt(cabs2(d));
-    if (!(ad >= tiny)) {  // static pivot floor (also catches NaN)
+    if (!(ad >= tiny)) {  // static pivot floor (also catches NaN); uniform over the CTA
       d = cmk<V>((double)tiny, 0.0);
       ad = tiny;
       ++nstatic;
       __syncthreads();
-      if (tid == 0) F[(int64_t)j * m + j] = d;
+      if (tid == 0) P[j * ld + j] = d;
     }
     pmax = ad > pmax ? ad : pmax;
     pmin = ad < pmin ? ad : pmin;
-    for (int c = j + 1 + tid; c < k0 + w; c += blockDim.x) prow[c - k0] = F[(int64_t)c * m + j];
+    for (int c = j + 1 + tid; c < w; c += blockDim.x) prow[c] = P[c * ld + j];
     __syncthreads();
     const V inv = cinv(d);
-    const int cj = j - k0;  // panel column of the pivot
-    for (int r = j + 1 + tid; r < p; r += blockDim.x) {
-      const V l = cmul(F[(int64_t)j * m + r], inv);
-      F[(int64_t)j * m + r] = l;
+    for (int r = j + 1 + tid; r < rows; r += blockDim.x) {
+      const V l = cmul(P[j * ld + r], inv);
+      P[j * ld + r] = l;
 #pragma unroll
       for (int h = 0; h < NB; h += 16) {  // the row's panel entries right of the pivot, 16 loads together
         V a[16];
 #pragma unroll
         for (int c = 0; c < 16; ++c)
-          if (h + c > cj && h + c < w) a[c] = F[(int64_t)(k0 + h + c) * m + r];
+          if (h + c > j && h + c < w) a[c] = P[(h + c) * ld + r];
 #pragma unroll
         for (int c = 0; c < 16; ++c)
-          if (h + c > cj && h + c < w) F[(int64_t)(k0 + h + c) * m + r] = cfms(a[c], l, prow[h + c]);
+          if (h + c > j && h + c < w) P[(h + c) * ld + r] = cfms(a[c], l, prow[h + c]);
       }
     }
     __syncthreads();
   }
+  if (in_smem)
+    for (int t = tid; t < rows * w; t += blockDim.x) {
+      const int c = t / rows, r = t - c * rows;
+      F[(int64_t)(k0 + c) * m + k0 + r] = P[t];
+    }
   if (tid == 0) {
     if (nstatic) atomicAdd(stats + 4 * s + 0, (unsigned long long)nstatic);
     atomicMax(stats + 4 * s + 1, (unsigned long long)__double_as_longlong((double)pmax));
     // min |u_jj| stored as bits of 1/|u_jj| max
     atomicMax(stats + 4 * s + 2, (unsigned long long)__double_as_longlong(1.0 / (double)pmin));
+    // swap map: panel rows sit at list position row - k0, rows below the panel are appended
+    int32_t* mp = swapmap + ((int64_t)blockIdx.x * gridDim.y + s) * swapmap_ints<NB>();
+    int32_t* mrows = mp + 1;
+    int32_t* msrc = mp + 1 + 2 * NB;
+    int n = w;
+    bool any = false;
+    for (int j = 0; j < w; ++j) { mrows[j] = k0 + j; msrc[j] = k0 + j; }
+    for (int j = 0; j < w; ++j) {
+      const int r = spiv[j];
+      if (r == k0 + j) continue;
+      any = true;
+      int b = r - k0;
+      if (b >= w) {
+        b = -1;
+        for (int q = w; q < n; ++q)
+          if (mrows[q] == r) b = q;
+        if (b < 0) { mrows[n] = r; msrc[n] = r; b = n++; }
+      }
+      const int t = msrc[j]; msrc[j] = msrc[b]; msrc[b] = t;
+    }
+    mp[0] = any ? n : 0;
   }
 }
 
 // Row interchanges of one panel applied to every column outside it (LAPACK's
-// laswp): the panel's w swaps (j, pv[j]), j = k0..k0+w-1, touch at most 2w
-// rows; their net effect is new[row_i] = old[src_i] over that row list, built
-// once per CTA in shared memory. FP32: every thread loads all of its column's
-// touched rows, then stores them (one memory latency per column); FP64: the
-// swaps in order.
+// laswp), from the panel's swap map (new[rows_i] = old[src_i], at most 2 w
+// rows). FP32: every thread loads all of its column's touched rows, then
+// stores them (a source row may be another entry's destination); FP64 (2 NB
+// complex doubles would not fit in registers): the panel's swaps replayed in
+// order.
 template <class R, int NB>
 __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T* __restrict__ arena,
-                                               const int32_t* __restrict__ perm, int step) {
+                                               const int32_t* __restrict__ perm, const int32_t* __restrict__ swapmap,
+                                               int step) {
   using V = typename Vec2<R>::T;
   const int f = L.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -235,39 +292,19 @@ __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T*
   if (k0 >= p) return;
   const int w = min(NB, p - k0);
   if ((int)blockIdx.z * (int)blockDim.x >= m - w) return;
+  const int32_t* mp = swapmap + ((int64_t)blockIdx.x * gridDim.y + s) * swapmap_ints<NB>();
+  const int n = mp[0];
+  if (n == 0) return;  // no interchange in this panel
   __shared__ int rows[2 * NB], src[2 * NB], spv[NB];
-  __shared__ int nrows;
-  const int32_t* pv = perm + s * L.n + L.piv_off[f];
   const int tid = threadIdx.x;
-  if (tid < w) spv[tid] = pv[k0 + tid];
-  // most panels interchange no rows at all
-  if (!__syncthreads_or(tid < w && spv[tid] != k0 + tid)) return;
-  if (tid == 0) {
-    // panel rows sit at list position row - k0; rows below the panel are appended
-    int n = w;
-    for (int j = 0; j < w; ++j) { rows[j] = k0 + j; src[j] = k0 + j; }
-    for (int j = 0; j < w; ++j) {
-      const int r = spv[j];
-      int b = r - k0;
-      if (b >= w) {
-        b = -1;
-        for (int q = w; q < n; ++q)
-          if (rows[q] == r) b = q;
-        if (b < 0) { rows[n] = r; src[n] = r; b = n++; }
-      }
-      const int t = src[j]; src[j] = src[b]; src[b] = t;
-    }
-    nrows = n;
-  }
+  if (tid < n) { rows[tid] = mp[1 + tid]; src[tid] = mp[1 + 2 * NB + tid]; }
+  if (tid < w) spv[tid] = perm[s * L.n + L.piv_off[f] + k0 + tid];
   __syncthreads();
-  const int n = nrows;
-  int c = blockIdx.z * blockDim.x + threadIdx.x;  // index over the columns outside the panel
+  int c = blockIdx.z * blockDim.x + tid;  // index over the columns outside the panel
   if (c >= m - w) return;
   if (c >= k0) c += w;
   V* col = arena + s * L.arena_size + L.foff[f] + (int64_t)c * m;
   if (sizeof(R) == 4) {
-    // every source is loaded before any row is written: a source row may be
-    // another entry's destination
     V v[2 * NB];
 #pragma unroll
     for (int q = 0; q < 2 * NB; ++q)
@@ -276,7 +313,6 @@ __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T*
     for (int q = 0; q < 2 * NB; ++q)
       if (q < n) col[rows[q]] = v[q];
   } else {
-    // FP64 (2 NB complex doubles would not fit in registers): the swaps in order
     for (int j = 0; j < w; ++j) {
       const int r = spv[j];
       if (r != k0 + j) {
@@ -1118,6 +1154,11 @@ int workspace_ensure(Model& m, int precision, int slots) {
   ELP_CUDA(w.partial.alloc((size_t)slots * w.nparts * 2));
   ELP_CUDA(w.active.alloc(slots));
   ELP_CUDA(w.stats.alloc(4 * (size_t)slots));
+  {
+    int max_count = 1;
+    for (const auto& LV : D.levels) max_count = std::max(max_count, LV.count);
+    ELP_CUDA(w.swapmap.alloc((size_t)max_count * slots * swapmap_ints<32>()));
+  }
   ELP_CUDA(w.tc_err.alloc(1));
   ELP_CUDA(cudaMemset(w.tc_err.p, 0, sizeof(int)));
   ELP_CUDA(cudaMallocHost((void**)&w.h_coef, sizeof(Coef) * slots));
@@ -1198,6 +1239,15 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     });
     ELP_CUDA(e);
   }
+  const int panel_cap = kPanelSmemBytes / (NB * (int)sizeof(V));  // panel rows held in shared memory
+  {
+    static std::once_flag once;
+    static cudaError_t e = cudaSuccess;
+    std::call_once(once, [] {
+      e = cudaFuncSetAttribute(k_panel<R, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPanelSmemBytes);
+    });
+    ELP_CUDA(e);
+  }
   // mode: GM_COL / GM_ROW / GM_SCHUR; rows_c, cols_c: upper bounds of the C block over the level
   auto gemm = [&](int mode, int k, int rows_c, int cols_c) {
     if (tc) {
@@ -1237,10 +1287,13 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       const int rest = LV.max_m - k * NB - 1;   // columns right of the panel (upper bound)
       if (k > 0) gemm(GM_COL, k, rows, NB);     // panel columns from all previous panels
       dim3 g1(LV.count, S_used);
-      PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB><<<g1, 256, 0, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p));
       {
+        const int rows_max = LV.max_p - k * NB;
+        const size_t psm = (size_t)std::min(rows_max, panel_cap) * NB * sizeof(V);
+        PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB><<<g1, 256, psm, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p,
+                                                                      w.swapmap.p, panel_cap));
         dim3 gl(LV.count, S_used, (unsigned)std::min(65535, (LV.max_m + 255) / 256));
-        PROF_LAUNCH(KC_PANEL, st, k_laswp<R, NB><<<gl, 256, 0, st>>>(L, arena, w.perm.p, k));
+        PROF_LAUNCH(KC_PANEL, st, k_laswp<R, NB><<<gl, 256, 0, st>>>(L, arena, w.perm.p, w.swapmap.p, k));
       }
       if (LV.max_b > 0) {
         dim3 g2(LV.count, S_used, (unsigned)std::min(65535, (LV.max_b + 127) / 128));

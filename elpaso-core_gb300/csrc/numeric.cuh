@@ -150,6 +150,7 @@ struct Workspace {
   DevBuf<int> active;             // slots
   DevBuf<unsigned long long> stats;  // slots x 4: static pivots, max|u_jj| bits, min|u_jj| bits, max|a|
   DevBuf<int> tc_err;                // set when a tensor-core wait ran out
+  DevBuf<int32_t> swapmap;           // per (front of a level, slot): a panel's row interchanges
   Coef* h_coef = nullptr;         // pinned host staging
   double* h_norms = nullptr;
   int* h_active = nullptr;
