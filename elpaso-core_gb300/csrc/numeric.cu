@@ -133,12 +133,13 @@ __host__ __device__ constexpr int swapmap_ints() { return 1 + 4 * NB; }
 
 // Panel factorisation (columns k0..k0+w-1, fully summed rows k0..p-1) with
 // partial pivoting restricted to the fully summed rows and a static pivot
-// floor. The panel lives in shared memory when its rows fit (one load and
-// one store of the panel instead of a memory round trip per column step),
-// else it is factorised in place. Row interchanges are applied here to the
+// floor. SMEM = true handles the fronts whose panel rows fit in shared memory
+// (one load and one store of the panel instead of a memory round trip per
+// column step; few registers, so many CTAs share an SM); SMEM = false the
+// others, factorised in place with each row's loads issued together. Row interchanges are applied here to the
 // panel columns only; the panel's net permutation of rows (at most 2 w rows)
 // is written as a swap map that k_laswp applies to every other column.
-template <class R, int NB>
+template <class R, int NB, bool SMEM>
 __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T* __restrict__ arena,
                                                int32_t* __restrict__ perm, int step, R tiny,
                                                unsigned long long* __restrict__ stats, int32_t* __restrict__ swapmap,
@@ -159,7 +160,8 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
   __shared__ V prow[NB];
   __shared__ int s_piv, spiv[NB];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const bool in_smem = rows <= cap_rows;
+  if ((rows <= cap_rows) != SMEM) return;  // the other variant's front (uniform per CTA)
+  constexpr bool in_smem = SMEM;
   V* P;       // P[c * ld + r] = F[(k0 + c) * m + k0 + r]
   int64_t ld;
   if (in_smem) {
@@ -227,15 +229,19 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
     for (int r = j + 1 + tid; r < rows; r += blockDim.x) {
       const V l = cmul(P[j * ld + r], inv);
       P[j * ld + r] = l;
+      if (in_smem) {
+        for (int c = j + 1; c < w; ++c) P[c * ld + r] = cfms(P[c * ld + r], l, prow[c]);
+      } else {
 #pragma unroll
-      for (int h = 0; h < NB; h += 16) {  // the row's panel entries right of the pivot, 16 loads together
-        V a[16];
+        for (int h = 0; h < NB; h += 16) {  // the row's panel entries right of the pivot, 16 loads together
+          V a[16];
 #pragma unroll
-        for (int c = 0; c < 16; ++c)
-          if (h + c > j && h + c < w) a[c] = P[(h + c) * ld + r];
+          for (int c = 0; c < 16; ++c)
+            if (h + c > j && h + c < w) a[c] = P[(h + c) * ld + r];
 #pragma unroll
-        for (int c = 0; c < 16; ++c)
-          if (h + c > j && h + c < w) P[(h + c) * ld + r] = cfms(a[c], l, prow[h + c]);
+          for (int c = 0; c < 16; ++c)
+            if (h + c > j && h + c < w) P[(h + c) * ld + r] = cfms(a[c], l, prow[h + c]);
+        }
       }
     }
     __syncthreads();
@@ -275,15 +281,15 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
 }
 
 // Row interchanges of one panel applied to every column outside it (LAPACK's
-// laswp), from the panel's swap map (new[rows_i] = old[src_i], at most 2 w
-// rows). FP32: every thread loads all of its column's touched rows, then
-// stores them (a source row may be another entry's destination); FP64 (2 NB
-// complex doubles would not fit in registers): the panel's swaps replayed in
-// order.
+// laswp), from the panel's swap map (new[rows_i] = old[src_i], at most 2 NB
+// rows). A warp moves one column: lane i handles list entries i and i + 32;
+// all loads come before __syncwarp and all stores after it, since a source
+// row may be another entry's destination. A CTA covers kLaswpCols columns.
+constexpr int kLaswpCols = 64;
 template <class R, int NB>
 __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T* __restrict__ arena,
-                                               const int32_t* __restrict__ perm, const int32_t* __restrict__ swapmap,
-                                               int step) {
+                                               const int32_t* __restrict__ swapmap, int step) {
+  static_assert(NB <= 32, "two list entries per lane");
   using V = typename Vec2<R>::T;
   const int f = L.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -291,36 +297,25 @@ __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T*
   const int k0 = step * NB;
   if (k0 >= p) return;
   const int w = min(NB, p - k0);
-  if ((int)blockIdx.z * (int)blockDim.x >= m - w) return;
+  const int c0 = blockIdx.z * kLaswpCols;
+  if (c0 >= m - w) return;
   const int32_t* mp = swapmap + ((int64_t)blockIdx.x * gridDim.y + s) * swapmap_ints<NB>();
   const int n = mp[0];
   if (n == 0) return;  // no interchange in this panel
-  __shared__ int rows[2 * NB], src[2 * NB], spv[NB];
-  const int tid = threadIdx.x;
-  if (tid < n) { rows[tid] = mp[1 + tid]; src[tid] = mp[1 + 2 * NB + tid]; }
-  if (tid < w) spv[tid] = perm[s * L.n + L.piv_off[f] + k0 + tid];
-  __syncthreads();
-  int c = blockIdx.z * blockDim.x + tid;  // index over the columns outside the panel
-  if (c >= m - w) return;
-  if (c >= k0) c += w;
-  V* col = arena + s * L.arena_size + L.foff[f] + (int64_t)c * m;
-  if (sizeof(R) == 4) {
-    V v[2 * NB];
-#pragma unroll
-    for (int q = 0; q < 2 * NB; ++q)
-      if (q < n) v[q] = col[src[q]];
-#pragma unroll
-    for (int q = 0; q < 2 * NB; ++q)
-      if (q < n) col[rows[q]] = v[q];
-  } else {
-    for (int j = 0; j < w; ++j) {
-      const int r = spv[j];
-      if (r != k0 + j) {
-        const V t = col[k0 + j];
-        col[k0 + j] = col[r];
-        col[r] = t;
-      }
-    }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int r0 = lane < n ? mp[1 + lane] : 0, s0 = lane < n ? mp[1 + 2 * NB + lane] : 0;
+  const int r1 = lane + 32 < n ? mp[1 + lane + 32] : 0, s1 = lane + 32 < n ? mp[1 + 2 * NB + lane + 32] : 0;
+  V* F = arena + s * L.arena_size + L.foff[f];
+  for (int cc = c0 + wid; cc < min(c0 + kLaswpCols, m - w); cc += blockDim.x >> 5) {
+    const int c = cc < k0 ? cc : cc + w;  // columns outside the panel
+    V* col = F + (int64_t)c * m;
+    V v0, v1;
+    if (lane < n) v0 = col[s0];
+    if (lane + 32 < n) v1 = col[s1];
+    __syncwarp();
+    if (lane < n) col[r0] = v0;
+    if (lane + 32 < n) col[r1] = v1;
+    __syncwarp();
   }
 }
 
@@ -1244,7 +1239,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     static std::once_flag once;
     static cudaError_t e = cudaSuccess;
     std::call_once(once, [] {
-      e = cudaFuncSetAttribute(k_panel<R, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPanelSmemBytes);
+      e = cudaFuncSetAttribute(k_panel<R, NB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPanelSmemBytes);
     });
     ELP_CUDA(e);
   }
@@ -1290,10 +1285,13 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       {
         const int rows_max = LV.max_p - k * NB;
         const size_t psm = (size_t)std::min(rows_max, panel_cap) * NB * sizeof(V);
-        PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB><<<g1, 256, psm, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p,
-                                                                      w.swapmap.p, panel_cap));
-        dim3 gl(LV.count, S_used, (unsigned)std::min(65535, (LV.max_m + 255) / 256));
-        PROF_LAUNCH(KC_PANEL, st, k_laswp<R, NB><<<gl, 256, 0, st>>>(L, arena, w.perm.p, w.swapmap.p, k));
+        PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB, true><<<g1, 256, psm, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p,
+                                                                            w.swapmap.p, panel_cap));
+        if (rows_max > panel_cap)  // fronts whose panel rows exceed shared memory
+          PROF_LAUNCH(KC_PANEL, st, k_panel<R, NB, false><<<g1, 256, 0, st>>>(L, arena, w.perm.p, k, tiny, w.stats.p,
+                                                                             w.swapmap.p, panel_cap));
+        dim3 gl(LV.count, S_used, (unsigned)std::min(65535, (LV.max_m + kLaswpCols - 1) / kLaswpCols));
+        PROF_LAUNCH(KC_PANEL, st, k_laswp<R, NB><<<gl, 256, 0, st>>>(L, arena, w.swapmap.p, k));
       }
       if (LV.max_b > 0) {
         dim3 g2(LV.count, S_used, (unsigned)std::min(65535, (LV.max_b + 127) / 128));
