@@ -184,6 +184,108 @@ def assembly_measurement(elp, meshes, n_cube=100, repeats=5):
     return out
 
 
+def _server_stream(elp, srv, reqs, rate=None, timeout_s=600.0):
+    """Submits `reqs` [(model id, n dofs, omegas)] all at once (rate None) or
+    as a Poisson stream of `rate` requests/s, and collects every result.
+    Returns (per-request results, wall seconds from the first submission)."""
+    import threading
+    rng = np.random.default_rng(20260101 + 17)
+    gaps = rng.exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
+    results, outs = [], []
+    done = threading.Event()
+
+    def collect():
+        for _ in range(len(reqs)):
+            results.append(srv.wait(timeout_s * 1e3))
+        done.set()
+
+    t0 = time.perf_counter()
+    th = threading.Thread(target=collect, daemon=True)
+    th.start()
+    t_next = t0
+    for (mid, n, oms), gap in zip(reqs, gaps):
+        t_next += gap
+        delay = t_next - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        x = np.zeros((len(oms), n), np.complex128)
+        outs.append(x)
+        srv.submit(mid, oms, x)
+    done.wait(timeout_s)
+    th.join(1.0)
+    return results, time.perf_counter() - t0
+
+
+def serving_measurement(elp, meshes, n_stream=96, n_probe=48):
+    """Latency under load through the C-ABI serving loop (elp_server_*): a
+    bounded sample of the 5k-500k DOF request stream. Five resident models
+    (Brick8 cubes, a DSG4 plate and plate-cavity models, 6.6k-85k DOFs),
+    requests of 1-16 frequencies from U(1, 500) Hz on a uniformly chosen
+    model. Capacity = requests/s of a saturating burst of `n_probe` requests;
+    then a Poisson stream of `n_stream` requests at 80% of that capacity.
+    Latency = request arrival -> last frequency returned (server clock)."""
+    descs = [meshes.cube(12), meshes.plate(80, 80, 0.5, 0.5, 0.003), meshes.plate_cavity(40, 27, 20, 0.6, 0.4, 0.3),
+             meshes.cube(24), meshes.plate_cavity()]
+    models = [elp.Model(d).assemble().analyse() for d in descs]
+    ns = [m.n for m in models]
+    srv = elp.Server(hbm_budget_bytes=160 << 30, max_inflight=4, precision=elp.MIXED, tol=TOL, omega_batch=16)
+    mids = [srv.add_model(m) for m in models]
+    rng = np.random.default_rng(20260101 + 5)
+
+    def make(k):
+        out = []
+        for _ in range(k):
+            i = int(rng.integers(len(mids)))
+            oms = 2 * np.pi * rng.uniform(1.0, 500.0, int(rng.integers(1, 17)))
+            out.append((mids[i], ns[i], oms))
+        return out
+
+    _server_stream(elp, srv, [(mids[i], ns[i], 2 * np.pi * np.array([50.0, 300.0])) for i in range(len(mids))])
+    probe = make(n_probe)
+    res_p, t_p = _server_stream(elp, srv, probe)
+    cap = n_probe / t_p
+    stream = make(n_stream)
+    res, t_s = _server_stream(elp, srv, stream, rate=0.8 * cap)
+    lat = np.array([r["latency_ms"] for r in res])
+    ok = all(r["status"] == 0 for r in res + res_p)
+    solves = sum(len(q[2]) for q in stream)
+    srv.close()
+    for m in models:
+        m.close()
+    return {"models_dofs": ns, "requests": len(res), "omegas_per_request": "U{1..16}",
+            "capacity_req_s": cap, "capacity_solves_s": sum(len(q[2]) for q in probe) / t_p,
+            "offered_req_s": 0.8 * cap, "achieved_solves_s": solves / t_s,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "max": float(lat.max()), "mean": float(lat.mean())},
+            "all_status_ok": ok, "max_rel_residual": max(r["max_rel_residual"] for r in res + res_p),
+            "server": "max_inflight 4, omega_batch 16, HBM budget 160 GiB, mixed precision"}
+
+
+def batched_plates_measurement(elp, meshes, count=256, n_omega=32):
+    """The batched-plates workload: `count` simply supported DSG4 plates m x m,
+    m ~ U{10..80} (363-19,683 DOFs), t ~ U(1, 5) mm, each with n_omega
+    frequencies from U(10, 400) Hz, all submitted at once to the serving loop.
+    Models are created, assembled and analysed before the timed region."""
+    descs = meshes.batched_plates(count)
+    models = [elp.Model(d).assemble().analyse() for d in descs]
+    srv = elp.Server(hbm_budget_bytes=160 << 30, max_inflight=4, precision=elp.MIXED, tol=TOL, omega_batch=n_omega)
+    mids = [srv.add_model(m) for m in models]
+    rng = np.random.default_rng(20260101 + 4)
+    reqs = [(mid, m.n, 2 * np.pi * rng.uniform(10.0, 400.0, n_omega)) for mid, m in zip(mids, models)]
+    _server_stream(elp, srv, reqs[:4])  # first-touch workspaces of the server threads
+    res, t = _server_stream(elp, srv, reqs)
+    ok = all(r["status"] == 0 for r in res)
+    out = {"models": count, "dofs_range": [min(m.n for m in models), max(m.n for m in models)],
+           "solves": count * n_omega, "seconds": t, "solves_s": count * n_omega / t, "all_status_ok": ok,
+           "max_rel_residual": max(r["max_rel_residual"] for r in res),
+           "latency_ms": {"p50": float(np.percentile([r["latency_ms"] for r in res], 50)),
+                          "p99": float(np.percentile([r["latency_ms"] for r in res], 99))}}
+    srv.close()
+    for m in models:
+        m.close()
+    return out
+
+
 def run_ours(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -307,6 +409,10 @@ def run_ours(args):
     asm100 = None
     if rank == 0 and not args.no_assembly:
         asm100 = assembly_measurement(elp, meshes)
+    serving = plates = None
+    if rank == 0 and not args.no_serving:
+        serving = serving_measurement(elp, meshes)
+        plates = batched_plates_measurement(elp, meshes)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(importlib.import_module("elpaso_core_gb300.meshes"), args)
@@ -331,6 +437,8 @@ def run_ours(args):
             "assembly": {"kernel_ms": asm_best, "elements": info["n_elements"], "host_create_s": t_create,
                          "symbolic_s": t_sym},
             "assembly_solid_cube_100": asm100,
+            "serving": serving,
+            "batched_plates": plates,
             "clocks": clk,
             "cpu_baseline": cpu,
         }
@@ -369,6 +477,7 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-assembly", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

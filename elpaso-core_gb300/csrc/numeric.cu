@@ -1118,6 +1118,30 @@ int device_upload_symbolic(Model& m) {
   return ELP_OK;
 }
 
+constexpr int kGmresRestart = 24;  // GMRES(24) of the mixed path
+
+// Device bytes of the workspace `workspace_ensure` (+ the GMRES buffers of the
+// mixed path) allocates for `slots` frequencies; the serving loop admits
+// models against this figure, so it mirrors those allocations.
+int64_t workspace_bytes(const Model& m, int precision, int slots) {
+  if (!m.dsym) return 0;
+  const DeviceSymbolic& D = *m.dsym;
+  const int64_t n = m.n, S = slots;
+  const int64_t elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
+  const int64_t nparts = std::min<int64_t>(1024, (n + 255) / 256);
+  int64_t max_count = 1;
+  for (const auto& LV : D.levels) max_count = std::max<int64_t>(max_count, LV.count);
+  int64_t b = S * (D.arena + std::max<int64_t>(1, D.cb_total) + 2 * n) * elem;  // arena, cb, z, tb
+  b += S * n * (4 + 8 + 3 * 16);                                               // perm, dscale, x, r, f
+  b += S * (int64_t)(sizeof(Coef) + 16 + nparts * 16 + 4 + 32) + 4;            // coef, norms, partials, flags
+  b += max_count * S * swapmap_ints<32>() * 4;
+  if (precision == ELP_MIXED) {
+    const int64_t rst = kGmresRestart;
+    b += S * ((2 * rst + 2) * n * 16 + (int64_t)kMaxBasis * 16 * (4 + nparts) + 8 + 4);  // Vb, Zb, wv, Hessenberg
+  }
+  return b;
+}
+
 int workspace_ensure(Model& m, int precision, int slots) {
   std::unique_ptr<Workspace>& W = m.ws[precision];
   if (W && W->slots >= slots) return ELP_OK;
@@ -1494,7 +1518,7 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
   CombineArgs A = combine_args(m);
   int rc0 = solve_smem<R>(m);
   if (rc0) return rc0;
-  const int RST = 24;
+  const int RST = kGmresRestart;
   int rc = gmres_alloc(w, n, w.slots, RST);
   if (rc) return rc;
   const int64_t vst = (int64_t)(RST + 1) * n;  // slot stride of the Arnoldi basis V

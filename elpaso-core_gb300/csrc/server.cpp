@@ -62,11 +62,12 @@ struct ModelSlot {
   std::deque<int64_t> queue;     // requests with unscheduled frequencies
 };
 
+// device bytes of a resident model: value arrays (VK, VM, per-group VK,
+// col_idx, class, arena offsets) + per-row data + its solve workspace
 int64_t model_bytes(const Model& m, int precision, int slots) {
-  const int64_t elem = precision == ELP_MIXED ? 8 : 16;
-  int64_t b = m.nnz * (8 + 8 + 4 + 1 + 8) + m.n * 64;
-  if (m.dsym) b += (int64_t)slots * (m.dsym->arena * elem + m.dsym->cb_total * elem + m.n * (elem + 3 * 16 + 12));
-  return b;
+  const int64_t groups = std::max<int64_t>(1, (int64_t)m.groups.size());
+  int64_t b = m.nnz * (8 + 8 + 8 * (groups - 1) + 4 + 1 + 8) + m.n * 64;
+  return b + workspace_bytes(m, precision, slots);
 }
 
 }  // namespace
