@@ -216,6 +216,14 @@ def _server_stream(elp, srv, reqs, rate=None, timeout_s=600.0):
     return results, time.perf_counter() - t0
 
 
+def _status_counts(res):
+    """{status: count} over request results (0 = every frequency at the target)."""
+    out = {}
+    for r in res:
+        out[str(r["status"])] = out.get(str(r["status"]), 0) + 1
+    return out
+
+
 def serving_measurement(elp, meshes, n_stream=96, n_probe=48):
     """Latency under load through the C-ABI serving loop (elp_server_*): a
     bounded sample of the 5k-500k DOF request stream. Five resident models
@@ -247,7 +255,6 @@ def serving_measurement(elp, meshes, n_stream=96, n_probe=48):
     stream = make(n_stream)
     res, t_s = _server_stream(elp, srv, stream, rate=0.8 * cap)
     lat = np.array([r["latency_ms"] for r in res])
-    ok = all(r["status"] == 0 for r in res + res_p)
     solves = sum(len(q[2]) for q in stream)
     srv.close()
     for m in models:
@@ -257,7 +264,8 @@ def serving_measurement(elp, meshes, n_stream=96, n_probe=48):
             "offered_req_s": 0.8 * cap, "achieved_solves_s": solves / t_s,
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "max": float(lat.max()), "mean": float(lat.mean())},
-            "all_status_ok": ok, "max_rel_residual": max(r["max_rel_residual"] for r in res + res_p),
+            "request_status": _status_counts(res + res_p),
+            "max_rel_residual": max(r["max_rel_residual"] for r in res + res_p),
             "server": "max_inflight 4, omega_batch 16, HBM budget 160 GiB, mixed precision"}
 
 
@@ -274,10 +282,12 @@ def batched_plates_measurement(elp, meshes, count=256, n_omega=32):
     reqs = [(mid, m.n, 2 * np.pi * rng.uniform(10.0, 400.0, n_omega)) for mid, m in zip(mids, models)]
     _server_stream(elp, srv, reqs[:4])  # first-touch workspaces of the server threads
     res, t = _server_stream(elp, srv, reqs)
-    ok = all(r["status"] == 0 for r in res)
     out = {"models": count, "dofs_range": [min(m.n for m in models), max(m.n for m in models)],
-           "solves": count * n_omega, "seconds": t, "solves_s": count * n_omega / t, "all_status_ok": ok,
+           "solves": count * n_omega, "seconds": t, "solves_s": count * n_omega / t,
+           "request_status": _status_counts(res),
            "max_rel_residual": max(r["max_rel_residual"] for r in res),
+           "note": "status 6 = a frequency whose FP64 rounding floor eps |||A| |x||| / ||f|| exceeds 1e-10 "
+                   "(no FP64 solution reaches the target there); its residual is reported as reached",
            "latency_ms": {"p50": float(np.percentile([r["latency_ms"] for r in res], 50)),
                           "p99": float(np.percentile([r["latency_ms"] for r in res], 99))}}
     srv.close()
