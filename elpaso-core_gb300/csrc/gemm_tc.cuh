@@ -22,11 +22,12 @@
 // Warp roles (288 threads): warp 0 issues the MMAs (one elected thread);
 // warps 1..8 are converters. Converter warp w owns TMEM lane quarter w % 4
 // (the only lanes it may write) and K half (w - 1) / 4 of every A chunk, and
-// a fixed set of B elements. Each converter copies exactly the raw complex
-// values it will convert, with cp.async (8-byte copies, zero-filled outside
-// the block) into its own slots of a three-chunk ring in shared memory, so
-// the raw data needs no cross-thread synchronisation: a thread waits only for
-// its own copy groups. Two MMA stages (TMEM columns for A, shared memory for
+// a fixed set of B elements. The raw complex values go with cp.async (8-byte
+// copies, zero-filled outside the block) into the converters' slots of a
+// three-chunk ring in shared memory: each converter copies its own values
+// (no cross-thread synchronisation: a thread waits only for its own copy
+// groups), except the transposed A, which a warp copies together (lanes
+// along the contiguous k) and hands over with __syncwarp. Two MMA stages (TMEM columns for A, shared memory for
 // B) are handed over with mbarriers, never with block barriers:
 //   full[s]  - one arrival per converter warp: stage s holds a converted chunk;
 //   empty[s] - tcgen05.commit of the MMAs that read stage s.
@@ -270,28 +271,42 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
     } else {
       // ------------------------------------------------ converters
       // raw copies of this thread's elements of chunk c into ring slot c % kTcRing
+      // copy addresses as 32-bit element offsets from the front base (a front has < 2^31
+      // entries), advanced per chunk; bounds are checked only where a chunk crosses K
+      const int mK = m * kTcKC;
+      const int wrow0 = 32 * (warp & 3), wct0 = 32 * (warp - 1), kq = lane & 7;
+      const bool arow_ok = i0 + arow < MR, bj_ok = j0 + bj < NC;
+      const int a_base = !TRANS ? akh * m + ra + i0 + arow                              // L[ra + i, k]
+                                : (ca + i0 + wrow0 + (lane >> 3)) * m + akh + kq;       // U[k, ca + i]
+      const int b_base = !TRANS ? (ca + j0 + bj) * m + bkf                              // U[k, ca + j]
+                                : bkf * m + ra + j0 + bj;                               // L[ra + j, k]
       auto issue = [&](int c) {
         if (c < nchunks) {
           const int kc = c * kTcKC;
-          const int i = i0 + arow;
+          const bool full = kc + kTcKC <= K;
+          float2(*slot)[256] = sm.raw[c % kTcRing];
+          if (!TRANS) {
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int k = kc + akh + q;
-            const bool v = i < MR && k < K;
-            const float2* src = !v ? F
-                                : !TRANS ? F + (int64_t)k * m + ra + i      // A = L[ra + i, k]
-                                         : F + (int64_t)(ca + i) * m + k;   // B^T: U[k, ca + i]
-            tc::cp8(&sm.raw[c % kTcRing][q][ct], src, v);
+            for (int q = 0; q < 8; ++q) {  // lanes along rows of L: coalesced
+              const bool v = arow_ok && (full || kc + akh + q < K);
+              tc::cp8(&slot[q][ct], F + (v ? a_base + c * mK + q * m : 0), v);
+            }
+          } else {
+            // B^T rows are U columns: a lane's own 8 values are 64 contiguous bytes of one column,
+            // so the warp copies its 32 rows x 8 k together, lanes along k (4 rows per copy), into
+            // the slots of the lanes that convert them
+#pragma unroll
+            for (int it = 0; it < 8; ++it) {
+              const int rr = (lane >> 3) + 4 * it;
+              const bool v = i0 + wrow0 + rr < MR && (full || kc + akh + kq < K);
+              tc::cp8(&slot[kq][wct0 + rr], F + (v ? a_base + 4 * it * m + kc : 0), v);
+            }
           }
-          const int j = j0 + bj;
 #pragma unroll
           for (int q = 0; q < BPT; ++q) {
-            const int k = kc + bkf + q;
-            const bool v = j < NC && k < K;
-            const float2* src = !v ? F
-                                : !TRANS ? F + (int64_t)(ca + j) * m + k      // U[k, ca + j]
-                                         : F + (int64_t)k * m + ra + j;      // A^T: L[ra + j, k]
-            tc::cp8(&sm.raw[c % kTcRing][8 + q][ct], src, v);
+            const bool v = bj_ok && (full || kc + bkf + q < K);
+            const int off = !TRANS ? b_base + kc + q : b_base + c * mK + q * m;
+            tc::cp8(&slot[8 + q][ct], F + (v ? off : 0), v);
           }
         }
         tc::cp_commit();
@@ -301,11 +316,13 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
       for (int c = 0; c < nchunks; ++c) {
         const int g = gc + c, stage = g & 1, slot = c % kTcRing;
         tc::cp_wait_ring();  // this thread's copies of chunk c have landed
+        if (TRANS) __syncwarp();  // ... and its warp's: some of its A values were copied by other lanes
         float2 av[8], bv[BPT];
 #pragma unroll
         for (int q = 0; q < 8; ++q) av[q] = sm.raw[slot][q][ct];
 #pragma unroll
         for (int q = 0; q < BPT; ++q) bv[q] = sm.raw[slot][8 + q][ct];
+        if (TRANS) __syncwarp();  // every lane has read the slot before any lane refills it
         issue(c + kTcRing);  // the values are in registers: the slot can be refilled
         // stage free: the MMAs of chunk g - 2 have completed (one lane polls, the warp follows)
         if (g >= 2) {
