@@ -152,6 +152,7 @@ struct TcSmem {
   static constexpr int BPT = NT * kTcKC / 256;  // B elements per converter and chunk
   float2 raw[kTcRing][8 + BPT][256];            // [slot][element][converter]: conflict-free
   uint32_t b[2][2][2 * NT * kTcKC];             // [stage][hi, lo] planes of the real 2NT x KC [B_re ; B_im]
+  float ep[NT == 32 ? 4 : 1][2][32][17];        // transposed epilogue: re, im of 32 rows x 16 columns per warp
   uint64_t full[2], empty[2];
   uint32_t tmem_base;
 };
@@ -224,7 +225,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
   const int ct = tid - 32;
   const int arow = 32 * (warp & 3) + lane, akh = ((warp - 1) >> 2) * 8;
   const uint32_t a_lane = (uint32_t)(32 * (warp & 3)) << 16;
-  const int bj = ct / TPJ, bkf = (ct % TPJ) * BPT;
+  // B row bj and first k bkf of each converter: BPT consecutive k per thread; transposed
+  // (B^T = L rows, contiguous along j) a warp owns all 32 rows for BPT k, so copies are 256 B runs
+  const int bj = !TRANS ? ct / TPJ : ct % NT, bkf = !TRANS ? (ct % TPJ) * BPT : (ct / NT) * BPT;
   for (int tile = blockIdx.z; tile < ntiles; tile += gridDim.z) {
     const int i0 = (tile % tiles_r) * 128;
     const int j0 = (tile / tiles_r) * NT;
@@ -375,19 +378,50 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
 #pragma unroll
         for (int part = 0; part < 2; ++part) {  // 16 columns at a time: loads first, then stores
           const int jb = j0 + half * 32 + part * 16;
-          float re[16], im[16];
-          tc::ld16(tD + lane_base + half * 32 + part * 16, re);
-          tc::ld16(tD + lane_base + NT + half * 32 + part * 16, im);
-          if (ok && i < MR) {
-            float2* dst0 = !TRANS ? F + (int64_t)(ca + jb) * m + ra + i : F + (int64_t)(ca + i) * m + ra + jb;
-            const int64_t dq = !TRANS ? (int64_t)m : 1;
-            float2 cv[16];
+          if (!TRANS) {  // lanes along rows of C: coalesced
+            float re[16], im[16];
+            tc::ld16(tD + lane_base + half * 32 + part * 16, re);
+            tc::ld16(tD + lane_base + NT + half * 32 + part * 16, im);
+            if (ok && i < MR) {
+              float2* dst0 = F + (int64_t)(ca + jb) * m + ra + i;
+              float2 cv[16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q)
-              if (jb + q < NC) cv[q] = dst0[q * dq];
+              for (int q = 0; q < 16; ++q)
+                if (jb + q < NC) cv[q] = dst0[(int64_t)q * m];
 #pragma unroll
-            for (int q = 0; q < 16; ++q)
-              if (jb + q < NC) dst0[q * dq] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+              for (int q = 0; q < 16; ++q)
+                if (jb + q < NC) dst0[(int64_t)q * m] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+            }
+          } else {
+            // C^T: the MMA row i is a column of C, contiguous along j; the warp's 32 x 16 block
+            // goes through shared memory so that a half-warp writes 16 contiguous entries
+            float(*ep)[32][17] = sm.ep[lg];
+#pragma unroll
+            for (int c2 = 0; c2 < 2; ++c2) {  // re, then im: 16 accumulator values live at a time
+              float v[16];
+              tc::ld16(tD + lane_base + c2 * NT + half * 32 + part * 16, v);
+#pragma unroll
+              for (int q = 0; q < 16; ++q) ep[c2][lane][q] = v[q];
+            }
+            __syncwarp();
+            const int jj = lane & 15, r0 = lane >> 4;
+#pragma unroll
+            for (int t0 = 0; t0 < 16; t0 += 8) {  // 8 rows per half-warp at a time: loads, then stores
+              float2 cv[8];
+#pragma unroll
+              for (int t = 0; t < 8; ++t) {
+                const int ii = i0 + 32 * lg + 2 * (t0 + t) + r0;
+                if (ok && ii < MR && jb + jj < NC) cv[t] = F[(int64_t)(ca + ii) * m + ra + jb + jj];
+              }
+#pragma unroll
+              for (int t = 0; t < 8; ++t) {
+                const int r = 2 * (t0 + t) + r0, ii = i0 + 32 * lg + r;
+                if (ok && ii < MR && jb + jj < NC)
+                  F[(int64_t)(ca + ii) * m + ra + jb + jj] =
+                      make_float2(cv[t].x - ep[0][r][jj], cv[t].y - ep[1][r][jj]);
+              }
+            }
+            __syncwarp();  // the staging block is rewritten by the next part
           }
         }
       }
