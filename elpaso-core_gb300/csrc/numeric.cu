@@ -56,6 +56,12 @@ template <class V> __device__ __forceinline__ V cfms(V a, V b, V c) {
   a.y -= b.x * c.y + b.y * c.x;
   return a;
 }
+// c + a * b
+template <class V> __device__ __forceinline__ V cfma(V a, V b, V c) {
+  c.x += a.x * b.x - a.y * b.y;
+  c.y += a.x * b.y + a.y * b.x;
+  return c;
+}
 template <class V> __device__ __forceinline__ auto cabs2(V a) -> decltype(a.x) { return a.x * a.x + a.y * a.y; }
 template <class V> __device__ __forceinline__ V cinv(V a) {
   auto d = a.x * a.x + a.y * a.y;
@@ -544,7 +550,7 @@ struct SolveArgs {
 };
 
 template <class R>
-__global__ void __launch_bounds__(256) k_forward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
+__global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                  const int32_t* __restrict__ perm, typename Vec2<R>::T* __restrict__ z,
                                                  typename Vec2<R>::T* __restrict__ cb) {
   using V = typename Vec2<R>::T;
@@ -617,7 +623,9 @@ __global__ void __launch_bounds__(256) k_forward(SolveArgs S, const typename Vec
   }
 }
 
-// border rows of the forward step: cb -= L21 y_p, rows split across CTAs
+// border rows of the forward step: cb -= L21 y_p. A CTA takes 32 border rows
+// (lane = row, loads coalesced along the column); its 8 warps split the p
+// columns and their partial sums are added in a fixed order.
 template <class R>
 __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                     const typename Vec2<R>::T* __restrict__ z,
@@ -625,34 +633,47 @@ __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename 
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
   V* y = reinterpret_cast<V*>(smraw);
+  __shared__ V part[8][32];
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
   if (!S.active[s]) return;
   const int p = S.fp[f], b = S.fb[f], m = p + b;
-  if (blockIdx.z * blockDim.x >= (unsigned)b) return;
+  if ((int)blockIdx.z * 32 >= b) return;
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   const V* zs = z + s * S.n;
   for (int k = threadIdx.x; k < p; k += blockDim.x) y[k] = zs[I[k]];
   __syncthreads();
-  const int i = blockIdx.z * blockDim.x + threadIdx.x;
-  if (i >= b) return;
-  V* dst = cb + s * S.cb_total + S.cb_off[f] + i;
-  V t = *dst;
-  const V* col = F + p + i;
-  int j = 0;
-  for (; j + 16 <= p; j += 16) {  // 16 independent loads in flight per thread
-    V a[16];
+  const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
+  const int i = blockIdx.z * 32 + lane;
+  V t = cmk<V>(0.0, 0.0);
+  if (i < b) {
+    const V* col = F + p + i;
+    const int j_lo = (p * wv) / 8, j_hi = (p * (wv + 1)) / 8;
+    int j = j_lo;
+    for (; j + 16 <= j_hi; j += 16) {  // 16 independent loads in flight per thread
+      V a[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) a[q] = col[(int64_t)(j + q) * m];
+      for (int q = 0; q < 16; ++q) a[q] = col[(int64_t)(j + q) * m];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) t = cfms(t, a[q], y[j + q]);
+      for (int q = 0; q < 16; ++q) t = cfma(a[q], y[j + q], t);
+    }
+    for (; j < j_hi; ++j) t = cfma(col[(int64_t)j * m], y[j], t);
   }
-  for (; j < p; ++j) t = cfms(t, col[(int64_t)j * m], y[j]);
-  *dst = t;
+  part[wv][lane] = t;
+  __syncthreads();
+  if (wv == 0 && i < b) {
+    V sum = part[0][lane];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) sum = cadd(sum, part[q][lane]);
+    V* dst = cb + s * S.cb_total + S.cb_off[f] + i;
+    *dst = csub(*dst, sum);
+  }
 }
 
-// pivot rows of the backward step: t = y_p - U12 x_b, rows split across CTAs
+// pivot rows of the backward step: t = y_p - U12 x_b. A CTA takes 32 pivot
+// rows (lane = row); its 8 warps split the b border columns, partial sums
+// added in a fixed order.
 template <class R>
 __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                  const typename Vec2<R>::T* __restrict__ z,
@@ -660,34 +681,45 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
   V* xb = reinterpret_cast<V*>(smraw);
+  __shared__ V part[8][32];
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
   if (!S.active[s]) return;
   const int p = S.fp[f], b = S.fb[f], m = p + b;
-  if (blockIdx.z * blockDim.x >= (unsigned)p) return;
+  if ((int)blockIdx.z * 32 >= p) return;
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   const V* zs = z + s * S.n;
   for (int k = threadIdx.x; k < b; k += blockDim.x) xb[k] = zs[I[p + k]];
   __syncthreads();
-  const int r = blockIdx.z * blockDim.x + threadIdx.x;
-  if (r >= p) return;
-  V t = zs[I[r]];
-  const V* row = F + (int64_t)p * m + r;
-  int i = 0;
-  for (; i + 16 <= b; i += 16) {  // 16 independent loads in flight per thread
-    V a[16];
+  const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
+  const int r = blockIdx.z * 32 + lane;
+  V t = cmk<V>(0.0, 0.0);
+  if (r < p) {
+    const V* row = F + (int64_t)p * m + r;
+    const int i_lo = (b * wv) / 8, i_hi = (b * (wv + 1)) / 8;
+    int i = i_lo;
+    for (; i + 16 <= i_hi; i += 16) {  // 16 independent loads in flight per thread
+      V a[16];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) a[q] = row[(int64_t)(i + q) * m];
+      for (int q = 0; q < 16; ++q) a[q] = row[(int64_t)(i + q) * m];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) t = cfms(t, a[q], xb[i + q]);
+      for (int q = 0; q < 16; ++q) t = cfma(a[q], xb[i + q], t);
+    }
+    for (; i < i_hi; ++i) t = cfma(row[(int64_t)i * m], xb[i], t);
   }
-  for (; i < b; ++i) t = cfms(t, row[(int64_t)i * m], xb[i]);
-  tb[s * S.n + S.piv_off[f] + r] = t;
+  part[wv][lane] = t;
+  __syncthreads();
+  if (wv == 0 && r < p) {
+    V sum = part[0][lane];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) sum = cadd(sum, part[q][lane]);
+    tb[s * S.n + S.piv_off[f] + r] = csub(zs[I[r]], sum);
+  }
 }
 
 template <class R>
-__global__ void __launch_bounds__(256) k_backward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
+__global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                   typename Vec2<R>::T* __restrict__ z,
                                                   const typename Vec2<R>::T* __restrict__ tb) {
   using V = typename Vec2<R>::T;
@@ -1339,6 +1371,11 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   return ELP_OK;
 }
 
+// threads of a pivot-block solve CTA: few for the many small fronts of the
+// lower levels (more CTAs per SM), many for the few large fronts at the top
+// (more rows of the trailing update in flight)
+static int solve_threads(int max_p) { return max_p <= 128 ? 128 : max_p >= 512 ? 512 : 256; }
+
 template <class R>
 static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, const int* mask) {
   using V = typename Vec2<R>::T;
@@ -1367,9 +1404,9 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
     size_t sm = (size_t)LV.max_m * sizeof(V);
-    PROF_LAUNCH(KC_FORWARD, st, k_forward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, w.perm.p, z, cb));
+    PROF_LAUNCH(KC_FORWARD, st, k_forward<R><<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, w.perm.p, z, cb));
     if (LV.max_b > 0) {
-      const unsigned chunks = (unsigned)((LV.max_b + 255) / 256);
+      const unsigned chunks = (unsigned)((LV.max_b + 31) / 32);
       PROF_LAUNCH(KC_FWD_BORDER, st, k_fwd_border<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)LV.max_p * sizeof(V), st>>>(
                                       S, arena, z, cb));
     }
@@ -1379,11 +1416,11 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     const auto& LV = D.levels[l];
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
-    const unsigned chunks = (unsigned)((LV.max_p + 255) / 256);
+    const unsigned chunks = (unsigned)((LV.max_p + 31) / 32);
     PROF_LAUNCH(KC_BWD_U12, st, k_bwd_u12<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)std::max(1, LV.max_b) * sizeof(V), st>>>(
                                      S, arena, z, tb));
     size_t sm = (size_t)LV.max_p * sizeof(V);
-    PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), 256, sm, st>>>(S, arena, z, tb));
+    PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, z, tb));
   }
   ELP_CUDA(cudaGetLastError());
   return ELP_OK;
