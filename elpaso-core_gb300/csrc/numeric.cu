@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(256) k_laswp(LevelArgs L, typename Vec2<R>::T*
 
 // L21 of the panel: rows p..m-1, panel columns (row-wise triangular solve with U of the panel)
 template <class R, int NB>
-__global__ void __launch_bounds__(128) k_border(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_border(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
   using V = typename Vec2<R>::T;
   const int f = L.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -350,14 +350,15 @@ __global__ void __launch_bounds__(128) k_border(LevelArgs L, typename Vec2<R>::T
 #pragma unroll
     for (int j = 0; j < NB; ++j)
       if (j < w) v[j] = F[(int64_t)(k0 + j) * m + r];
+    // column-oriented: once v[i] is final, every later v[j] is updated independently
+    // (critical path of NB steps instead of a chain of NB^2/2 dependent FMAs)
 #pragma unroll
-    for (int j = 0; j < NB; ++j) {
-      if (j < w) {
-        V t = v[j];
+    for (int i = 0; i < NB; ++i) {
+      if (i < w) {
+        v[i] = cmul(v[i], dinv[i]);
 #pragma unroll
-        for (int i = 0; i < NB; ++i)
-          if (i < j) t = cfms(t, v[i], U[i][j]);
-        v[j] = cmul(t, dinv[j]);
+        for (int j = i + 1; j < NB; ++j)
+          if (j < w) v[j] = cfms(v[j], v[i], U[i][j]);
       }
     }
 #pragma unroll
@@ -368,7 +369,7 @@ __global__ void __launch_bounds__(128) k_border(LevelArgs L, typename Vec2<R>::T
 
 // U12 of the panel rows: columns k0+w..m-1, unit-lower solve with L of the panel
 template <class R, int NB>
-__global__ void __launch_bounds__(128) k_urow(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_urow(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
   using V = typename Vec2<R>::T;
   const int f = L.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -389,14 +390,13 @@ __global__ void __launch_bounds__(128) k_urow(LevelArgs L, typename Vec2<R>::T* 
 #pragma unroll
     for (int j = 0; j < NB; ++j)
       if (j < w) v[j] = col[j];
+    // column-oriented (unit lower): once v[i] is final, every later v[j] is updated independently
 #pragma unroll
-    for (int j = 1; j < NB; ++j) {
-      if (j < w) {
-        V t = v[j];
+    for (int i = 0; i < NB; ++i) {
+      if (i < w) {
 #pragma unroll
-        for (int i = 0; i < NB; ++i)
-          if (i < j) t = cfms(t, Lp[j][i], v[i]);
-        v[j] = t;
+        for (int j = i + 1; j < NB; ++j)
+          if (j < w) v[j] = cfms(v[j], Lp[j][i], v[i]);
       }
     }
 #pragma unroll
