@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_border(LevelArg
 
 // U12 of the panel rows: columns k0+w..m-1, unit-lower solve with L of the panel
 template <class R, int NB>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_urow(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
+__global__ void __launch_bounds__(128) k_urow(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
   using V = typename Vec2<R>::T;
   const int f = L.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -390,13 +390,14 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_urow(LevelArgs 
 #pragma unroll
     for (int j = 0; j < NB; ++j)
       if (j < w) v[j] = col[j];
-    // column-oriented (unit lower): once v[i] is final, every later v[j] is updated independently
 #pragma unroll
-    for (int i = 0; i < NB; ++i) {
-      if (i < w) {
+    for (int j = 1; j < NB; ++j) {
+      if (j < w) {
+        V t = v[j];
 #pragma unroll
-        for (int j = i + 1; j < NB; ++j)
-          if (j < w) v[j] = cfms(v[j], Lp[j][i], v[i]);
+        for (int i = 0; i < NB; ++i)
+          if (i < j) t = cfms(t, Lp[j][i], v[i]);
+        v[j] = t;
       }
     }
 #pragma unroll
