@@ -326,7 +326,6 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
 #pragma unroll
         for (int q = 0; q < BPT; ++q) bv[q] = sm.raw[slot][8 + q][ct];
         if (TRANS) __syncwarp();  // every lane has read the slot before any lane refills it
-        issue(c + kTcRing);  // the values are in registers: the slot can be refilled
         // stage free: the MMAs of chunk g - 2 have completed (one lane polls, the warp follows)
         if (g >= 2) {
           if (lane == 0 && ok) ok = tc::mbar_wait(&sm.empty[stage], ((g >> 1) + 1) & 1);
@@ -364,6 +363,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
         tc::fence_before();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&sm.full[stage]);
+        // refill the slot read above (its values are in registers), off the path to the MMA warp
+        issue(c + kTcRing);
       }
       asm volatile("cp.async.wait_all;" ::: "memory");  // only empty groups remain
       // ---- epilogue: the accumulator is complete when the last chunk's commit has arrived
