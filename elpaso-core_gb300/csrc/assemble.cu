@@ -96,6 +96,18 @@ __device__ __forceinline__ int find_col(const int32_t* __restrict__ row_ptr,
   return -1;
 }
 
+// CSR index of (row0 + i, col) given p0 = index of (row0, col): the rows of one
+// node usually share their column list, so the same offset is tried first
+// (one load) before a search.
+__device__ __forceinline__ int sibling_col(const int32_t* __restrict__ row_ptr,
+                                           const int32_t* __restrict__ col_idx, int row0, int p0, int i, int col) {
+  if (p0 < 0) return find_col(row_ptr, col_idx, row0 + i, col);
+  const int lo = __ldg(row_ptr + row0 + i), hi = __ldg(row_ptr + row0 + i + 1);
+  const int p = lo + (p0 - __ldg(row_ptr + row0));
+  if (p < hi && __ldg(col_idx + p) == col) return p;
+  return find_col(row_ptr, col_idx, row0 + i, col);
+}
+
 __device__ __forceinline__ void add_at(double* v, int p, double x) {
   if (p >= 0 && x != 0.0) atomicAdd(v + p, x);
 }
@@ -219,17 +231,19 @@ __device__ void hex_item(const AsmArgs& A, int64_t item, double (*sg)[8][8][3], 
           for (int j = 0; j < 3; ++j) Kb[i][j] = mt.lam * P[i][j] + mt.mu * P[j][i] + (i == j ? mt.mu * tr : 0.0);
         const double mv = mt.rho * mm;
         double* VKt = mt.group == 0 ? A.VK : A.VKg + (int64_t)(mt.group - 1) * A.nnz;
+        const int pa0 = find_col(A.row_ptr, A.col_idx, ra, rb);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          int p = find_col(A.row_ptr, A.col_idx, ra + i, rb);
+          int p = i == 0 ? pa0 : sibling_col(A.row_ptr, A.col_idx, ra, pa0, i, rb);
 #pragma unroll
           for (int j = 0; j < 3; ++j) add_at(VKt, p + j, Kb[i][j]);
           add_at(A.VM, p + i, mv);
         }
         if (a != b) {
+          const int pb0 = find_col(A.row_ptr, A.col_idx, rb, ra);
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
-            int p = find_col(A.row_ptr, A.col_idx, rb + j, ra);
+            int p = j == 0 ? pb0 : sibling_col(A.row_ptr, A.col_idx, rb, pb0, j, ra);
 #pragma unroll
             for (int i = 0; i < 3; ++i) add_at(VKt, p + i, Kb[i][j]);
             add_at(A.VM, p + j, mv);
