@@ -482,26 +482,32 @@ __device__ void interface_quad(const AsmArgs& A, int64_t q) {
 }
 
 // ---------------------------------------------------------------- kernel
-__global__ void __launch_bounds__(kThreads) assemble_kernel(AsmArgs A) {
+// Brick8 / Fluid8 items (8 elements per CTA); register-light, so two CTAs
+// share an SM.
+__global__ void __launch_bounds__(kThreads, 2) assemble_hex_kernel(AsmArgs A) {
   __shared__ double sg[kHexPerItem][8][8][3];
   __shared__ double sw[kHexPerItem][8];
   __shared__ int srow[kHexPerItem][8];
   __shared__ int smat[kHexPerItem];
-  const int64_t total = A.items_brick + A.items_fluid + A.items_plate + A.items_iface;
+  const int64_t total = A.items_brick + A.items_fluid;
   for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
-    int64_t r = it;
-    if (r < A.items_brick) { hex_item<0>(A, r, sg, sw, srow, smat); continue; }
-    r -= A.items_brick;
-    if (r < A.items_fluid) { hex_item<1>(A, r, sg, sw, srow, smat); continue; }
-    r -= A.items_fluid;
-    if (r < A.items_plate) {
-      int64_t e = r * kThreads + threadIdx.x;
+    if (it < A.items_brick) hex_item<0>(A, it, sg, sw, srow, smat);
+    else hex_item<1>(A, it - A.items_brick, sg, sw, srow, smat);
+  }
+}
+
+// DSG4 plates and interface quads, one element per thread (the 12 x 12
+// element matrix lives in registers).
+__global__ void __launch_bounds__(kThreads) assemble_quad_kernel(AsmArgs A) {
+  const int64_t total = A.items_plate + A.items_iface;
+  for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
+    if (it < A.items_plate) {
+      int64_t e = it * kThreads + threadIdx.x;
       if (e < A.n_plate) plate_element(A, e);
-      continue;
+    } else {
+      int64_t q = (it - A.items_plate) * kThreads + threadIdx.x;
+      if (q < A.n_iface) interface_quad(A, q);
     }
-    r -= A.items_plate;
-    int64_t q = r * kThreads + threadIdx.x;
-    if (q < A.n_iface) interface_quad(A, q);
   }
 }
 
@@ -668,18 +674,19 @@ int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms) {
   A.items_plate = (D.n_plate + kThreads - 1) / kThreads;
   A.items_iface = (D.n_iface + kThreads - 1) / kThreads;
   A.flags = D.flags.p;
-  const int64_t total = A.items_brick + A.items_fluid + A.items_plate + A.items_iface;
-  int sms = 0, per_sm = 0;
+  int sms = 0, per_hex = 0, per_quad = 0;
   ELP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D.device));
-  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, assemble_kernel, kThreads, 0));
-  if (per_sm < 1) per_sm = 1;
-  int64_t grid = (int64_t)sms * per_sm;
-  if (grid > total) grid = total;
+  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_hex, assemble_hex_kernel, kThreads, 0));
+  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_quad, assemble_quad_kernel, kThreads, 0));
+  // persistent grids: one resident wave over the items of each kernel
+  const int64_t g_hex = std::min<int64_t>((int64_t)sms * std::max(1, per_hex), A.items_brick + A.items_fluid);
+  const int64_t g_quad = std::min<int64_t>((int64_t)sms * std::max(1, per_quad), A.items_plate + A.items_iface);
   cudaEvent_t e0, e1;
   ELP_CUDA(cudaEventCreate(&e0));
   ELP_CUDA(cudaEventCreate(&e1));
   ELP_CUDA(cudaEventRecord(e0, stream));
-  if (grid > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, assemble_kernel<<<(unsigned)grid, kThreads, 0, stream>>>(A));
+  if (g_hex > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, assemble_hex_kernel<<<(unsigned)g_hex, kThreads, 0, stream>>>(A));
+  if (g_quad > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, assemble_quad_kernel<<<(unsigned)g_quad, kThreads, 0, stream>>>(A));
   ELP_CUDA(cudaGetLastError());
   ELP_CUDA(cudaEventRecord(e1, stream));
   ELP_CUDA(cudaEventSynchronize(e1));
