@@ -482,9 +482,9 @@ __device__ void interface_quad(const AsmArgs& A, int64_t q) {
 }
 
 // ---------------------------------------------------------------- kernel
-// Brick8 / Fluid8 items (8 elements per CTA); register-light, so two CTAs
+// Brick8 / Fluid8 items (8 elements per CTA); register-light, so three CTAs
 // share an SM.
-__global__ void __launch_bounds__(kThreads, 2) assemble_hex_kernel(AsmArgs A) {
+__global__ void __launch_bounds__(kThreads, 3) assemble_hex_kernel(AsmArgs A) {
   __shared__ double sg[kHexPerItem][8][8][3];
   __shared__ double sw[kHexPerItem][8];
   __shared__ int srow[kHexPerItem][8];
