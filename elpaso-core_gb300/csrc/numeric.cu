@@ -367,10 +367,16 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_border(LevelArg
   }
 }
 
-// U12 of the panel rows: columns k0+w..m-1, unit-lower solve with L of the panel
+// U12 of the panel rows: columns k0+w..m-1, unit-lower solve with L of the panel.
+// The w x kUrowCols block goes through shared memory: loaded and stored with
+// lanes along the panel rows (contiguous), solved by one thread per column.
+template <class R>
+__host__ __device__ constexpr int urow_cols() { return sizeof(R) == 4 ? 128 : 32; }
+
 template <class R, int NB>
 __global__ void __launch_bounds__(128) k_urow(LevelArgs L, typename Vec2<R>::T* __restrict__ arena, int step) {
   using V = typename Vec2<R>::T;
+  constexpr int TC = urow_cols<R>();
   const int f = L.list[blockIdx.x];
   const int s = blockIdx.y;
   const int p = L.fp[f], m = p + L.fb[f];
@@ -379,30 +385,43 @@ __global__ void __launch_bounds__(128) k_urow(LevelArgs L, typename Vec2<R>::T* 
   const int w = min(NB, p - k0);
   V* F = arena + s * L.arena_size + L.foff[f];
   __shared__ V Lp[NB][NB + 1];
+  __shared__ V tile[TC][NB + 1];  // [column][panel row]
   for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
     int i = t % w, j = t / w;
     if (i > j) Lp[i][j] = F[(int64_t)(k0 + j) * m + k0 + i];
   }
-  __syncthreads();
-  for (int c = k0 + w + blockIdx.z * blockDim.x + threadIdx.x; c < m; c += gridDim.z * blockDim.x) {
-    V v[NB];
-    V* col = F + (int64_t)c * m + k0;
-#pragma unroll
-    for (int j = 0; j < NB; ++j)
-      if (j < w) v[j] = col[j];
-#pragma unroll
-    for (int j = 1; j < NB; ++j) {
-      if (j < w) {
-        V t = v[j];
-#pragma unroll
-        for (int i = 0; i < NB; ++i)
-          if (i < j) t = cfms(t, Lp[j][i], v[i]);
-        v[j] = t;
-      }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int cb = k0 + w + blockIdx.z * TC; cb < m; cb += gridDim.z * TC) {
+    for (int cc = wid; cc < TC; cc += nw) {
+      const int c = cb + cc;
+      if (c < m && lane < w) tile[cc][lane] = F[(int64_t)c * m + k0 + lane];
     }
+    __syncthreads();
+    if ((int)threadIdx.x < TC && cb + (int)threadIdx.x < m) {
+      V v[NB];
 #pragma unroll
-    for (int j = 0; j < NB; ++j)
-      if (j < w) col[j] = v[j];
+      for (int j = 0; j < NB; ++j)
+        if (j < w) v[j] = tile[threadIdx.x][j];
+#pragma unroll
+      for (int j = 1; j < NB; ++j) {
+        if (j < w) {
+          V t = v[j];
+#pragma unroll
+          for (int i = 0; i < NB; ++i)
+            if (i < j) t = cfms(t, Lp[j][i], v[i]);
+          v[j] = t;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < NB; ++j)
+        if (j < w) tile[threadIdx.x][j] = v[j];
+    }
+    __syncthreads();
+    for (int cc = wid; cc < TC; cc += nw) {
+      const int c = cb + cc;
+      if (c < m && lane < w) F[(int64_t)c * m + k0 + lane] = tile[cc][lane];
+    }
+    __syncthreads();
   }
 }
 
@@ -1357,6 +1376,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       if (rest > 0) {
         if (k > 0) gemm(GM_ROW, k, NB, rest);  // pivot rows right of the panel from all previous panels
         dim3 g3(LV.count, S_used, (unsigned)std::min(65535, (rest + 127) / 128));
+        g3.z = (unsigned)std::min(65535, (rest + urow_cols<R>() - 1) / urow_cols<R>());
         PROF_LAUNCH(KC_UROW, st, k_urow<R, NB><<<g3, 128, 0, st>>>(L, arena, k));
       }
     }
