@@ -421,7 +421,7 @@ def run_ours(args):
 
     asm100 = None
     if rank == 0 and not args.no_assembly:
-        asm100 = assembly_measurement(elp, meshes)
+        asm100 = assembly_measurement(elp, meshes, n_cube=args.assembly_n)
     serving = plates = None
     if rank == 0 and not args.no_serving:
         serving = serving_measurement(elp, meshes)
@@ -450,7 +450,7 @@ def run_ours(args):
             "roofline": roof,
             "assembly": {"kernel_ms": asm_best, "elements": info["n_elements"], "host_create_s": t_create,
                          "symbolic_s": t_sym},
-            "assembly_solid_cube_100": asm100,
+            "assembly_solid_cube": asm100,
             "serving": serving,
             "batched_plates": plates,
             "clocks": clk,
@@ -492,6 +492,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-assembly", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--assembly-n", type=int, default=100, help="edge of the Brick8 cube of the assembly measurement")
     ap.add_argument("--cpu-budget-s", type=float, default=30.0)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
