@@ -450,4 +450,236 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
   }
 }
 
+// ===================================================================== Schur update from packed operands
+//
+// The Schur complement update GM_SCHUR (C = F[p:m, p:m] -= L21 U12, depth p)
+// reads operands that are final once the level's panels are done, so they are
+// split into TF32 planes ONCE per level (k_pack_schur) in the exact
+// shared-memory layout the MMAs read (K-major, no swizzle, 16-deep chunks):
+//   A block (tile row tr, chunk c): L21 rows 128 tr.., 4 planes re_hi, re_lo,
+//     im_hi, im_lo of 128 x 16 words (32 KB);
+//   B block (tile col tc, chunk c): U12 columns 128 tc.., 4 planes of 256 x 16
+//     words: W1 = [B_re ; B_im] hi, lo and W2 = [-B_im ; B_re] hi, lo (64 KB).
+// k_schur_tc then needs no converter threads: one thread issues two 1D bulk
+// copies (cp.async.bulk, completing on an mbarrier with a byte count) per
+// chunk into a two-stage ring, one thread issues the MMAs, all eight warps
+// run the epilogue. A 128 x 128 complex tile is
+//   [D_re | D_im] += A_re W1 + A_im W2    (6 MMAs of N = 256 per K = 8 step,
+// 3xTF32: hi*hi + hi*lo + lo*hi), accumulated in 256 TMEM columns.
+constexpr int kSchurTile = 128;                  // complex rows and columns of a tile
+constexpr int64_t kSchurABlock = 4 * 128 * kTcKC * 4;
+constexpr int64_t kSchurBBlock = 4 * 256 * kTcKC * 4;
+constexpr uint32_t kSchurCols = 256;
+
+struct SchurStage {
+  uint32_t a[4][128 * kTcKC];
+  uint32_t b[4][256 * kTcKC];
+};
+struct SchurSmem {
+  SchurStage st[2];
+  uint64_t full[2], empty[2];
+  uint32_t tmem_base;
+};
+constexpr int kSchurSmemBytes = (int)((sizeof(SchurSmem) + 1023) / 1024 * 1024);
+
+namespace tc {
+__device__ __forceinline__ void mma_tf32_ss(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(
+                   smem_u32(mbar)), "r"(bytes)
+               : "memory");
+}
+// 1D bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+}  // namespace tc
+
+// Packs L21 and U12 of every front of a level and every frequency slot.
+// Grid: (fronts, slots, blocks); a CTA of 256 threads writes one block.
+template <int NB>
+__global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* __restrict__ arena,
+                                                    uint32_t* __restrict__ pack, const int64_t* __restrict__ pack_base,
+                                                    int64_t slot_bytes) {
+  const int f = L.list[blockIdx.x];
+  const int s = blockIdx.y;
+  const int p = L.fp[f], b = L.fb[f], m = p + b;
+  if (p == 0 || b == 0) return;
+  const int tiles = (b + kSchurTile - 1) / kSchurTile, nch = (p + kTcKC - 1) / kTcKC;
+  const int nA = tiles * nch;
+  int blk = blockIdx.z;
+  if (blk >= 2 * nA) return;
+  const float2* F = arena + s * L.arena_size + L.foff[f];
+  char* base = reinterpret_cast<char*>(pack) + s * slot_bytes + pack_base[f];
+  if (blk < nA) {
+    const int tr = blk / nch, c = blk % nch;
+    uint32_t* P = reinterpret_cast<uint32_t*>(base + (int64_t)blk * kSchurABlock);
+    for (int t = threadIdx.x; t < 128 * kTcKC; t += blockDim.x) {
+      const int ii = t % 128, kk = t / 128;  // lanes along the rows of L21: coalesced
+      const int i = tr * 128 + ii, k = c * kTcKC + kk;
+      const float2 v = (i < b && k < p) ? F[(int64_t)k * m + p + i] : make_float2(0.f, 0.f);
+      const int wd = tc_word(ii, kk);
+      uint32_t h, l;
+      tc::split_tf32(v.x, h, l);
+      P[0 * 128 * kTcKC + wd] = h;
+      P[1 * 128 * kTcKC + wd] = l;
+      tc::split_tf32(v.y, h, l);
+      P[2 * 128 * kTcKC + wd] = h;
+      P[3 * 128 * kTcKC + wd] = l;
+    }
+  } else {
+    blk -= nA;
+    const int tcol = blk / nch, c = blk % nch;
+    uint32_t* P = reinterpret_cast<uint32_t*>(base + (int64_t)nA * kSchurABlock + (int64_t)blk * kSchurBBlock);
+    constexpr int PL = 256 * kTcKC;  // words per plane
+    for (int t = threadIdx.x; t < 128 * kTcKC; t += blockDim.x) {
+      const int kk = t % kTcKC, jj = t / kTcKC;  // lanes along k: contiguous in a U12 column
+      const int j = tcol * 128 + jj, k = c * kTcKC + kk;
+      const float2 v = (j < b && k < p) ? F[(int64_t)(p + j) * m + k] : make_float2(0.f, 0.f);
+      uint32_t rh, rl, ih, il;
+      tc::split_tf32(v.x, rh, rl);
+      tc::split_tf32(v.y, ih, il);
+      const int w_re = tc_word(jj, kk), w_im = tc_word(128 + jj, kk);
+      P[0 * PL + w_re] = rh;  // W1 = [B_re ; B_im]
+      P[1 * PL + w_re] = rl;
+      P[0 * PL + w_im] = ih;
+      P[1 * PL + w_im] = il;
+      P[2 * PL + w_re] = ih ^ 0x80000000u;  // W2 = [-B_im ; B_re] (negation is exact)
+      P[3 * PL + w_re] = il ^ 0x80000000u;
+      P[2 * PL + w_im] = rh;
+      P[3 * PL + w_im] = rl;
+    }
+  }
+}
+
+// C -= L21 U12 for one 128 x 128 complex tile of one front and frequency.
+template <int NB>
+__global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __restrict__ arena,
+                                                     const uint32_t* __restrict__ pack,
+                                                     const int64_t* __restrict__ pack_base, int64_t slot_bytes,
+                                                     int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char schur_smem_raw[];
+  SchurSmem& sm = *reinterpret_cast<SchurSmem*>(schur_smem_raw);
+  const int f = L.list[blockIdx.x];
+  const int s = blockIdx.y;
+  const int p = L.fp[f], b = L.fb[f], m = p + b;
+  if (p == 0 || b == 0) return;
+  const int tiles = (b + kSchurTile - 1) / kSchurTile, nch = (p + kTcKC - 1) / kTcKC;
+  if ((int)blockIdx.z >= tiles * tiles) return;  // uniform per CTA, before any TMEM allocation
+  const int tr = blockIdx.z % tiles, tcol = blockIdx.z / tiles;
+  const char* base = reinterpret_cast<const char*>(pack) + s * slot_bytes + pack_base[f];
+  const char* Ab = base + (int64_t)(tr * nch) * kSchurABlock;
+  const char* Bb = base + (int64_t)tiles * nch * kSchurABlock + (int64_t)(tcol * nch) * kSchurBBlock;
+  float2* F = arena + s * L.arena_size + L.foff[f];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(&sm.tmem_base)),
+                 "r"(kSchurCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int q = 0; q < 2; ++q) {
+      tc::mbar_init(&sm.full[q], 1);
+      tc::mbar_init(&sm.empty[q], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = sm.tmem_base;
+  bool ok = true;
+  int issued = 0;  // chunks whose copies the producer issued (thread 0)
+  if (tid == 0) {
+    // ------------------------------------------------ producer
+    for (int c = 0; c < nch; ++c) {
+      const int st = c & 1;
+      if (c >= 2 && ok) ok = tc::mbar_wait(&sm.empty[st], ((c >> 1) + 1) & 1);  // MMAs of chunk c - 2 done
+      tc::mbar_expect_tx(&sm.full[st], (uint32_t)(kSchurABlock + kSchurBBlock));
+      tc::bulk_g2s(&sm.st[st].a[0][0], Ab + (int64_t)c * kSchurABlock, (uint32_t)kSchurABlock, &sm.full[st]);
+      tc::bulk_g2s(&sm.st[st].b[0][0], Bb + (int64_t)c * kSchurBBlock, (uint32_t)kSchurBBlock, &sm.full[st]);
+      issued = c + 1;
+    }
+  } else if (tid == 32) {
+    // ------------------------------------------------ MMA issue
+    constexpr uint32_t idesc = tc::idesc_tf32(128, 256, false);
+    constexpr uint32_t LBO = 128, SBO = (kTcKC / 4) * 128;
+    for (int c = 0; c < nch; ++c) {
+      const int st = c & 1;
+      if (ok) ok = tc::mbar_wait(&sm.full[st], (c >> 1) & 1);
+      tc::fence_after();
+      uint32_t a[4], w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[q] = tc::smem_u32(sm.st[st].a[q]);
+        w[q] = tc::smem_u32(sm.st[st].b[q]);
+      }
+#pragma unroll
+      for (int ks = 0; ks < kTcKC / 8; ++ks) {
+        const uint32_t o = ks * 2 * 128;  // two core matrices per K = 8 step
+        auto d = [&](uint32_t x) { return tc::smem_desc(x + o, LBO, SBO); };
+        const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
+        tc::mma_tf32_ss(tmem, d(a[0]), d(w[0]), idesc, acc0);  // A_re_hi W1_hi
+        tc::mma_tf32_ss(tmem, d(a[0]), d(w[1]), idesc, 1u);    // A_re_hi W1_lo
+        tc::mma_tf32_ss(tmem, d(a[1]), d(w[0]), idesc, 1u);    // A_re_lo W1_hi
+        tc::mma_tf32_ss(tmem, d(a[2]), d(w[2]), idesc, 1u);    // A_im_hi W2_hi
+        tc::mma_tf32_ss(tmem, d(a[2]), d(w[3]), idesc, 1u);    // A_im_hi W2_lo
+        tc::mma_tf32_ss(tmem, d(a[3]), d(w[2]), idesc, 1u);    // A_im_lo W2_hi
+      }
+      tc::commit(&sm.empty[st]);
+    }
+  }
+  // every warp: the accumulator is complete when the last chunk's commit has arrived
+  const int gl = nch - 1;
+  if (lane == 0 && ok) ok = tc::mbar_wait(&sm.empty[gl & 1], (gl >> 1) & 1);
+  __syncwarp();
+  tc::fence_after();
+  ok = __syncthreads_and(ok);
+  if (ok) {
+    const int lg = warp & 3, half = warp >> 2;  // TMEM lane quarter, 64-column half of the tile
+    const uint32_t lane_base = (uint32_t)(32 * lg) << 16;
+    const int i = tr * kSchurTile + 32 * lg + lane;  // row of C (within the border block)
+#pragma unroll
+    for (int part = 0; part < 4; ++part) {  // 16 complex columns at a time: loads first, then stores
+      const int jb = tcol * kSchurTile + half * 64 + part * 16;
+      float re[16], im[16];
+      tc::ld16(tmem + lane_base + half * 64 + part * 16, re);
+      tc::ld16(tmem + lane_base + 128 + half * 64 + part * 16, im);
+      if (i < b) {
+        float2* dst0 = F + (int64_t)(p + jb) * m + p + i;
+        float2 cv[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+          if (jb + q < b) cv[q] = dst0[(int64_t)q * m];
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+          if (jb + q < b) dst0[(int64_t)q * m] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+      }
+    }
+  } else if (tid == 0) {
+    // a wait ran out: copies or MMAs of the last chunks may still be in flight;
+    // wait (bounded) for their barriers before the shared memory and TMEM go away
+    atomicExch(err, 1);
+    for (int c = (issued > 2 ? issued - 2 : 0); c < issued; ++c) {
+      tc::mbar_wait(&sm.full[c & 1], (c >> 1) & 1);
+      tc::mbar_wait(&sm.empty[c & 1], (c >> 1) & 1);
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kSchurCols) : "memory");
+  }
+}
+
 }  // namespace elp

@@ -1161,6 +1161,26 @@ int device_upload_symbolic(Model& m) {
       L.ea_count[k] = (int)ea.size() - L.ea_start[k];
     }
   }
+  // packed Schur operands (mixed path): per front with p, b > 0, tiles x chunks
+  // blocks of A (L21, kSchurABlock bytes) then of B (U12, kSchurBBlock bytes)
+  std::vector<int64_t> pbase(T, 0);
+  D.pack_max = 0;
+  for (int l = 0; l < S.n_levels; ++l) {
+    auto& L = D.levels[l];
+    int64_t off = 0;
+    for (int t : S.level_fronts[l]) {
+      pbase[t] = off;
+      if (p[t] > 0 && b[t] > 0) {
+        const int64_t tiles = (b[t] + kSchurTile - 1) / kSchurTile, nch = (p[t] + kTcKC - 1) / kTcKC;
+        off += tiles * nch * (kSchurABlock + kSchurBBlock);
+        L.pack_blocks = std::max<int>(L.pack_blocks, (int)(2 * tiles * nch));
+        L.schur_tiles = std::max<int>(L.schur_tiles, (int)(tiles * tiles));
+      }
+    }
+    L.pack_bytes = off;
+    D.pack_max = std::max(D.pack_max, off);
+  }
+  ELP_CUDA(D.pack_base.upload(pbase));
   ELP_CUDA(D.level_list.upload(ll));
   ELP_CUDA(D.ea_list.upload(ea));
   D.n_fronts = T;
@@ -1188,6 +1208,7 @@ int64_t workspace_bytes(const Model& m, int precision, int slots) {
   b += S * (int64_t)(sizeof(Coef) + 16 + nparts * 16 + 4 + 32) + 4;            // coef, norms, partials, flags
   b += max_count * S * swapmap_ints<32>() * 4;
   if (precision == ELP_MIXED) {
+    b += S * D.pack_max;
     const int64_t rst = kGmresRestart;
     b += S * ((2 * rst + 2) * n * 16 + (int64_t)kMaxBasis * 16 * (4 + nparts) + 8 + 4);  // Vb, Zb, wv, Hessenberg
   }
@@ -1232,6 +1253,7 @@ int workspace_ensure(Model& m, int precision, int slots) {
   }
   ELP_CUDA(w.tc_err.alloc(1));
   ELP_CUDA(cudaMemset(w.tc_err.p, 0, sizeof(int)));
+  if (precision == ELP_MIXED && D.pack_max > 0) ELP_CUDA(w.pack.alloc((size_t)slots * D.pack_max));
   ELP_CUDA(cudaMallocHost((void**)&w.h_coef, sizeof(Coef) * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_norms, sizeof(double) * 2 * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_active, sizeof(int) * slots));
@@ -1295,6 +1317,8 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   const R tiny = sizeof(R) == 8 ? (R)1e-10 : (R)1e-6;
   // FP32 fronts: Schur updates on the tensor cores (tcgen05, 3xTF32) unless ELP_TC=0
   static const bool use_tc = !(getenv("ELP_TC") && getenv("ELP_TC")[0] == '0');
+  // Schur complement from packed operands (k_schur_tc) unless ELP_TC_PACK=0
+  static const bool use_pack = !(getenv("ELP_TC_PACK") && getenv("ELP_TC_PACK")[0] == '0');
   const bool tc = std::is_same<R, float>::value && use_tc;
   if (tc) {
     static std::once_flag once;
@@ -1306,7 +1330,9 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
                                            kTcSmemBytes);
       cudaError_t c = cudaFuncSetAttribute(k_gemm_tc<NB, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            kTcSmemBytes);
-      e = a != cudaSuccess ? a : b != cudaSuccess ? b : c;
+      cudaError_t d = cudaFuncSetAttribute(k_schur_tc<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           kSchurSmemBytes);
+      e = a != cudaSuccess ? a : b != cudaSuccess ? b : c != cudaSuccess ? c : d;
     });
     ELP_CUDA(e);
   }
@@ -1380,7 +1406,20 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
         PROF_LAUNCH(KC_UROW, st, k_urow<R, NB><<<g3, 128, 0, st>>>(L, arena, k));
       }
     }
-    if (LV.max_b > 0) gemm(GM_SCHUR, 0, LV.max_b, LV.max_b);  // Schur complement, depth p
+    if (LV.max_b > 0) {  // Schur complement, depth p
+      if (tc && use_pack && w.pack.p) {
+        // operands split into TF32 planes once, then bulk-copied by the MMA kernel
+        float2* fa = reinterpret_cast<float2*>(arena);
+        uint32_t* pk = reinterpret_cast<uint32_t*>(w.pack.p);
+        dim3 gp(LV.count, S_used, (unsigned)LV.pack_blocks);
+        PROF_LAUNCH(KC_GEMM_TC, st, k_pack_schur<NB><<<gp, 256, 0, st>>>(L, fa, pk, D.pack_base.p, LV.pack_bytes));
+        dim3 gs(LV.count, S_used, (unsigned)LV.schur_tiles);
+        PROF_LAUNCH(KC_GEMM_TC, st, k_schur_tc<NB><<<gs, 256, kSchurSmemBytes, st>>>(L, fa, pk, D.pack_base.p,
+                                                                                      LV.pack_bytes, w.tc_err.p));
+      } else {
+        gemm(GM_SCHUR, 0, LV.max_b, LV.max_b);
+      }
+    }
     for (size_t k = 0; k < LV.ea_count.size(); ++k) {
       if (!LV.ea_count[k]) continue;
       dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, (LV.ea_max_b + 3) / 4));  // 4 columns per pass

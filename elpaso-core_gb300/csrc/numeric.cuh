@@ -126,11 +126,16 @@ struct DeviceSymbolic {
     int max_p = 0, max_m = 0, max_b = 0;
     std::vector<int> ea_start, ea_count;   // per child slot
     int ea_max_b = 0;
+    int64_t pack_bytes = 0;   // packed Schur operands of the level, per frequency slot
+    int pack_blocks = 0;      // most packed blocks of one front of the level
+    int schur_tiles = 0;      // most 128 x 128 Schur tiles of one front of the level
   };
   std::vector<Level> levels;
   int n_fronts = 0;
   int64_t arena = 0, cb_total = 0;
   int max_front = 0;
+  DevBuf<int64_t> pack_base;      // per front: byte offset of its packed Schur operands within its level
+  int64_t pack_max = 0;           // largest level pack_bytes
 };
 
 struct Workspace {
@@ -151,6 +156,7 @@ struct Workspace {
   DevBuf<unsigned long long> stats;  // slots x 4: static pivots, max|u_jj| bits, min|u_jj| bits, max|a|
   DevBuf<int> tc_err;                // set when a tensor-core wait ran out
   DevBuf<int32_t> swapmap;           // per (front of a level, slot): a panel's row interchanges
+  DevBuf<char> pack;                 // mixed path: packed TF32 split Schur operands of one level
   Coef* h_coef = nullptr;         // pinned host staging
   double* h_norms = nullptr;
   int* h_active = nullptr;
