@@ -25,6 +25,7 @@
 #include <type_traits>
 #include <cmath>
 #include <cstring>
+#include <string>
 
 #include "numeric.cuh"
 #include "prof.cuh"
@@ -1178,7 +1179,8 @@ int device_upload_symbolic(Model& m) {
       }
     }
     L.pack_bytes = off;
-    D.pack_max = std::max(D.pack_max, off);
+    static const bool pack_all_levels = getenv("ELP_TC_PACK") && std::string(getenv("ELP_TC_PACK")) == "all";
+    if (pack_all_levels || packed_schur_level(L)) D.pack_max = std::max(D.pack_max, off);
   }
   ELP_CUDA(D.pack_base.upload(pbase));
   ELP_CUDA(D.level_list.upload(ll));
@@ -1317,8 +1319,11 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   const R tiny = sizeof(R) == 8 ? (R)1e-10 : (R)1e-6;
   // FP32 fronts: Schur updates on the tensor cores (tcgen05, 3xTF32) unless ELP_TC=0
   static const bool use_tc = !(getenv("ELP_TC") && getenv("ELP_TC")[0] == '0');
-  // Schur complement from packed operands (k_schur_tc) unless ELP_TC_PACK=0
-  static const bool use_pack = !(getenv("ELP_TC_PACK") && getenv("ELP_TC_PACK")[0] == '0');
+  // Schur complement from packed operands (k_schur_tc) on the levels that gain from it;
+  // ELP_TC_PACK=0 never, ELP_TC_PACK=all on every level (tests of small models)
+  static const char* pack_env = getenv("ELP_TC_PACK");
+  static const bool use_pack = !(pack_env && pack_env[0] == '0');
+  static const bool pack_all = pack_env && std::string(pack_env) == "all";
   const bool tc = std::is_same<R, float>::value && use_tc;
   if (tc) {
     static std::once_flag once;
@@ -1407,8 +1412,10 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       }
     }
     if (LV.max_b > 0) {  // Schur complement, depth p
-      if (tc && use_pack && w.pack.p) {
-        // operands split into TF32 planes once, then bulk-copied by the MMA kernel
+      // few, large fronts (the top of the tree): operands split into TF32 planes once,
+      // then bulk-copied by the MMA kernel (k_schur_tc); below, the converter kernel wins
+      // (128-wide tiles waste work on short borders and the pack pass does not pay off)
+      if (tc && use_pack && w.pack.p && (pack_all || packed_schur_level(LV))) {
         float2* fa = reinterpret_cast<float2*>(arena);
         uint32_t* pk = reinterpret_cast<uint32_t*>(w.pack.p);
         dim3 gp(LV.count, S_used, (unsigned)LV.pack_blocks);

@@ -135,8 +135,12 @@ struct DeviceSymbolic {
   int64_t arena = 0, cb_total = 0;
   int max_front = 0;
   DevBuf<int64_t> pack_base;      // per front: byte offset of its packed Schur operands within its level
-  int64_t pack_max = 0;           // largest level pack_bytes
+  int64_t pack_max = 0;           // largest pack_bytes of a level that uses the packed Schur update
 };
+
+// The packed-operand Schur update pays off for the few, large fronts at the
+// top of the tree; lower levels keep the converter kernel.
+inline bool packed_schur_level(const DeviceSymbolic::Level& L) { return L.count <= 8 && L.max_b >= 1024; }
 
 struct Workspace {
   int precision = 0;              // ELP_FP64_PLAIN / ELP_MIXED

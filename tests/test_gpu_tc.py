@@ -8,7 +8,8 @@ to the 1e-10 relative residual, the tensor-core factors needing at most
 term and rounds the lo parts to TF32, so its products are a few times less
 accurate than FP32; that shows only at the most ill-conditioned, lowest
 frequencies). Each variant runs in its own process because the switch is
-read once per process.
+read once per process. The packed-operand Schur kernel is checked the same
+way with ELP_TC_PACK=all (every level through it).
 """
 import json
 import os
@@ -43,10 +44,27 @@ def _run(tc):
     return json.loads(p.stdout.strip().splitlines()[-1])
 
 
-def test_tensor_core_updates_match_simt_convergence():
-    tc, simt = _run("1"), _run("0")
+def _run_env(**env):
+    p = subprocess.run([sys.executable, "-c", PROBE], env=dict(os.environ, **env), capture_output=True, text=True,
+                       timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    return json.loads(p.stdout.strip().splitlines()[-1])
+
+
+def _close(tc, simt):
     for name in tc:
         for (it_a, res_a), (it_b, res_b) in zip(tc[name], simt[name]):
             assert res_a <= 1e-10 and res_b <= 1e-10
             assert it_a <= it_b + 2 + it_b // 2, (name, tc[name], simt[name])
             assert it_b <= it_a + 2 + it_a // 2, (name, tc[name], simt[name])
+
+
+def test_tensor_core_updates_match_simt_convergence():
+    _close(_run("1"), _run("0"))
+
+
+def test_packed_schur_updates_match_simt_convergence():
+    """The packed-operand Schur kernel (k_schur_tc) runs only on the top
+    levels of large models; ELP_TC_PACK=all puts every level of these small
+    models through it."""
+    _close(_run_env(ELP_TC="1", ELP_TC_PACK="all"), _run("0"))
