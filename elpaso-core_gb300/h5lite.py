@@ -20,6 +20,14 @@ HDF5 File Format Specification (version 2.0 document, sections II-IV):
 
 Anything else (chunked or filtered storage, v2 object headers, dense
 attribute storage, variable-length types) raises ``NotImplementedError``.
+
+``Writer`` produces files in the same subset (superblock 0, v1 object
+headers, symbol-table groups with full-size v1 B-tree nodes of K = 16 and
+symbol nodes of K = 4 -- up to 8,192 links per group --, contiguous datasets
+of float64 / int32 / int64 / complex128 stored as the compound {real, imag},
+scalar int64 / float64 / fixed-length string attributes). The image this was
+built in has no HDF5 library, so files are checked by a round trip through
+``File`` only.
 """
 from __future__ import annotations
 
@@ -324,3 +332,211 @@ def walk(node, prefix=""):
             path = f"{prefix}/{k}"
             yield path, child
             yield from walk(child, path)
+
+
+# ============================================================================ writer
+_GROUP_LEAF_K = 4        # symbol table node: up to 2K = 8 links
+_GROUP_INTERNAL_K = 16   # v1 B-tree node: up to 2K = 32 children
+
+
+def _pad8(b: bytes) -> bytes:
+    return b + b"\0" * ((-len(b)) % 8)
+
+
+def _dt_float64() -> bytes:
+    # class 1 (floating point), version 1; little endian, IEEE: sign bit 63,
+    # exponent 52..62 (bias 1023), mantissa 0..51, implied msb (normalisation 2)
+    return bytes([0x11, 0x20, 63, 0]) + struct.pack("<I", 8) + struct.pack("<HHBBBBI", 0, 64, 52, 11, 0, 52, 1023)
+
+
+def _dt_int(size: int) -> bytes:
+    # class 0 (fixed point), version 1, little endian, signed
+    return bytes([0x10, 0x08, 0, 0]) + struct.pack("<I", size) + struct.pack("<HH", 0, 8 * size)
+
+
+def _dt_string(size: int) -> bytes:
+    # class 3 (string), version 1, null terminated, ASCII
+    return bytes([0x13, 0x00, 0, 0]) + struct.pack("<I", size)
+
+
+def _dt_complex() -> bytes:
+    # class 6 (compound), version 1, two float64 members "real" and "imag"
+    out = bytes([0x16, 2, 0, 0]) + struct.pack("<I", 16)
+    for name, off in (("real", 0), ("imag", 8)):
+        out += _pad8(name.encode() + b"\0") + struct.pack("<I", off) + bytes(4) + bytes(4) + bytes(4) + bytes(16)
+        out += _dt_float64()
+    return out
+
+
+def _dtype_message(dt: np.dtype) -> bytes:
+    if dt == np.float64:
+        return _dt_float64()
+    if dt == np.complex128:
+        return _dt_complex()
+    if dt == np.int32:
+        return _dt_int(4)
+    if dt == np.int64:
+        return _dt_int(8)
+    raise NotImplementedError(f"dataset type {dt}")
+
+
+def _dataspace(shape) -> bytes:
+    return bytes([1, len(shape), 0, 0]) + bytes(4) + b"".join(struct.pack("<Q", d) for d in shape)
+
+
+class Writer:
+    """Builds an HDF5 file in memory; ``close()`` writes it.
+
+        w = Writer(path)
+        w.dataset("/Solution/State/vecFemStep1", x)        # groups made on the way
+        w.attr("/Solution/State", "FreqStep1", "10.000000")
+        w.close()
+    """
+
+    def __init__(self, path: str):
+        self.path = path
+        self.root = {"children": {}, "attrs": []}
+
+    def _group(self, path: str):
+        node = self.root
+        for part in [p for p in path.split("/") if p]:
+            ch = node["children"]
+            if part not in ch:
+                ch[part] = {"children": {}, "attrs": []}
+            node = ch[part]
+            if "data" in node:
+                raise ValueError(f"{path}: {part} is a dataset")
+        return node
+
+    def group(self, path: str):
+        self._group(path)
+        return self
+
+    def dataset(self, path: str, data):
+        parts = [p for p in path.split("/") if p]
+        parent = self._group("/".join(parts[:-1]))
+        arr = np.ascontiguousarray(data)
+        if arr.dtype not in (np.float64, np.complex128, np.int32, np.int64):
+            raise NotImplementedError(f"dataset type {arr.dtype}")
+        parent["children"][parts[-1]] = {"data": arr, "attrs": []}
+        return self
+
+    def attr(self, path: str, name: str, value):
+        parts = [p for p in path.split("/") if p]
+        node = self.root
+        for part in parts:
+            node = node["children"][part]
+        node["attrs"].append((name, value))
+        return self
+
+    # ------------------------------------------------------------ layout
+    def close(self):
+        self._buf = bytearray(96)  # superblock placeholder
+        root_ohdr, root_btree, root_heap = self._write_group(self.root)
+        eof = len(self._buf)
+        sb = bytearray(_SIG + bytes([0, 0, 0, 0, 0, 8, 8, 0]))
+        sb += struct.pack("<HHI", _GROUP_LEAF_K, _GROUP_INTERNAL_K, 0)
+        sb += struct.pack("<QQQQ", 0, _UNDEF, eof, _UNDEF)
+        sb += struct.pack("<QQII", 0, root_ohdr, 1, 0) + struct.pack("<QQ", root_btree, root_heap)
+        assert len(sb) == 96
+        self._buf[0:96] = sb
+        with open(self.path, "wb") as fh:
+            fh.write(bytes(self._buf))
+
+    def _alloc(self, data: bytes) -> int:
+        while len(self._buf) % 8:
+            self._buf += b"\0"
+        addr = len(self._buf)
+        self._buf += data
+        return addr
+
+    def _object_header(self, messages) -> int:
+        body = b""
+        for mtype, data in messages:
+            data = _pad8(data)
+            body += struct.pack("<HHB3x", mtype, len(data), 0) + data
+        head = struct.pack("<BBHII", 1, 0, len(messages), 1, len(body)) + bytes(4)
+        return self._alloc(head + body)
+
+    def _attr_message(self, name: str, value) -> bytes:
+        if isinstance(value, str):
+            raw = value.encode() + b"\0"
+            dt, data = _dt_string(len(raw)), raw
+        elif isinstance(value, (bool, int, np.integer)):
+            dt, data = _dt_int(8), struct.pack("<q", int(value))
+        elif isinstance(value, (float, np.floating)):
+            dt, data = _dt_float64(), struct.pack("<d", float(value))
+        else:
+            raise NotImplementedError(f"attribute type {type(value)}")
+        nm = name.encode() + b"\0"
+        sp = bytes([1, 0, 0, 0]) + bytes(4)  # scalar dataspace
+        return (struct.pack("<BBHHH", 1, 0, len(nm), len(dt), len(sp)) + _pad8(nm) + _pad8(dt) + _pad8(sp) + data)
+
+    def _write_dataset(self, node) -> int:
+        arr = node["data"]
+        raw = arr.astype(arr.dtype.newbyteorder("<"), copy=False).tobytes()
+        data_addr = self._alloc(raw) if raw else _UNDEF
+        layout = bytes([3, 1]) + struct.pack("<QQ", data_addr, len(raw))
+        fill = bytes([2, 2, 2, 0])  # version 2: late allocation, never write fill, fill undefined
+        msgs = [(0x1, _dataspace(arr.shape)), (0x3, _dtype_message(arr.dtype)), (0x5, fill), (0x8, layout)]
+        msgs += [(0xC, self._attr_message(n, v)) for n, v in node["attrs"]]
+        return self._object_header(msgs)
+
+    def _write_group(self, node):
+        # children first (their object header addresses go into the symbol table)
+        entries = []
+        for name in sorted(node["children"], key=lambda s: s.encode()):
+            ch = node["children"][name]
+            if "data" in ch:
+                entries.append((name, self._write_dataset(ch), None))
+            else:
+                ohdr, bt, hp = self._write_group(ch)
+                entries.append((name, ohdr, (bt, hp)))
+        # local heap: "" at offset 0, then the names (8-byte padded)
+        heap_data = bytearray(8)
+        name_off = {}
+        for name, _, _ in entries:
+            name_off[name] = len(heap_data)
+            heap_data += _pad8(name.encode() + b"\0")
+        heap_data += bytes(8)  # a little free space, as libraries leave
+        seg = self._alloc(bytes(heap_data))
+        heap = self._alloc(b"HEAP" + bytes([0, 0, 0, 0]) + struct.pack("<QQQ", len(heap_data), _UNDEF, seg))
+        # symbol table nodes of up to 2 * leaf K entries
+        cap = 2 * _GROUP_LEAF_K
+        snods = []
+        for i in range(0, max(1, len(entries)), cap):
+            chunk = entries[i:i + cap]
+            body = b"SNOD" + bytes([1, 0]) + struct.pack("<H", len(chunk))
+            for name, addr, grp in chunk:
+                if grp is None:
+                    body += struct.pack("<QQII", name_off[name], addr, 0, 0) + bytes(16)
+                else:
+                    body += struct.pack("<QQII", name_off[name], addr, 1, 0) + struct.pack("<QQ", *grp)
+            body += bytes(40 * (cap - len(chunk)))
+            last = name_off[chunk[-1][0]] if chunk else 0
+            snods.append((self._alloc(body), last))
+        btree = self._btree(snods, 0)
+        msgs = [(0x11, struct.pack("<QQ", btree, heap))]
+        msgs += [(0xC, self._attr_message(n, v)) for n, v in node["attrs"]]
+        return self._object_header(msgs), btree, heap
+
+    def _btree(self, children, level) -> int:
+        """v1 group B-tree over (child address, key = heap offset of its largest
+        name) pairs; adds levels while a node would exceed 2K children."""
+        k2 = 2 * _GROUP_INTERNAL_K
+        if len(children) > k2:
+            parents = []
+            for i in range(0, len(children), k2):
+                grp = children[i:i + k2]
+                parents.append((self._btree_node(grp, level), grp[-1][1]))
+            return self._btree(parents, level + 1)
+        return self._btree_node(children, level)
+
+    def _btree_node(self, children, level) -> int:
+        k2 = 2 * _GROUP_INTERNAL_K
+        body = b"TREE" + bytes([0, level]) + struct.pack("<H", len(children)) + struct.pack("<QQ", _UNDEF, _UNDEF)
+        body += struct.pack("<Q", 0)  # key 0: the empty name
+        for addr, key in children:
+            body += struct.pack("<QQ", addr, key)
+        body += bytes(16 * (k2 - len(children)))  # the node is allocated at full size
+        return self._alloc(body)

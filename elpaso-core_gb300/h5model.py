@@ -20,6 +20,12 @@ analysisfrequencybasic.cpp:184-262``): ``/Solution/State/vecFemStep{k}``
 complex vectors with ``FreqStep{k}`` attributes, ``/Solution/Maps/mtxDofMap``
 (node id, dof enum) per global row.
 
+and writes both files elpasoC writes for this path: the solution file
+(``write_solution``, the layout above) and the system-matrix export of
+``-exportSysH5`` (``write_system_matrix``: ``/SystemMatrices/<type>`` with
+integer attributes ``numrow``, ``numcol``, 1-based CSR ``vecCsrIa``,
+``vecCsrJa`` and complex ``cmpCsrVal``; ``ESC/math/mathlibrary.cpp:53-86``).
+
 Interface elements, element loads and nodal moments are not read (a model
 that has them raises ``NotImplementedError``).
 """
@@ -125,3 +131,45 @@ def read_solution(path: str):
         v = state[f"vecFemStep{k}"].read()
         xs.append(v["real"] + 1j * v["imag"])
     return freqs, np.array(xs), f["Solution/Maps/mtxDofMap"].read().astype(np.int64)
+
+
+def dof_map(node_ids, global_rows) -> np.ndarray:
+    """(node id, dof enum) of every global row, as elpasoC's mtxDofMap:
+    nodes in id order, active DOFs in enum order (analysisfrequencybasic.cpp:248-256).
+    `global_rows` is the [nodes, known dofs] row table of Model.global_rows()."""
+    gr = np.asarray(global_rows)
+    node, dof = np.nonzero(gr >= 0)
+    out = np.empty((int(gr.max()) + 1, 2), np.int32)
+    out[gr[node, dof], 0] = np.asarray(node_ids)[node]
+    out[gr[node, dof], 1] = dof
+    return out
+
+
+def write_solution(path: str, freqs, xs, dofs) -> None:
+    """elpasoC's solution file: /Solution/State/vecFemStep{k} (complex
+    {real, imag}, k = 1..), string attributes FreqStep{k} on /Solution/State
+    (the frequency as std::to_string prints it), /Solution/Maps/mtxDofMap."""
+    w = h5lite.Writer(path)
+    for k, (f, x) in enumerate(zip(freqs, xs)):
+        w.dataset(f"/Solution/State/vecFemStep{k + 1}", np.asarray(x, np.complex128))
+        w.attr("/Solution/State", f"FreqStep{k + 1}", "%f" % float(f))
+    w.dataset("/Solution/Maps/mtxDofMap", np.asarray(dofs, np.int32))
+    w.close()
+
+
+def write_system_matrix(path: str, row_ptr, col_idx, values, ncols: int | None = None,
+                        system: str = "DynamicStiffness") -> None:
+    """The -exportSysH5 file of one assembled system: 0-based CSR in, 1-based
+    vecCsrIa / vecCsrJa out (MathLibrary::RetrieveRowVectorsFromMat with
+    offset 1), complex cmpCsrVal, numrow / numcol attributes."""
+    rp = np.asarray(row_ptr, np.int64)
+    n = len(rp) - 1
+    w = h5lite.Writer(path)
+    g = f"/SystemMatrices/{system}"
+    w.group(g)
+    w.attr(g, "numrow", n)
+    w.attr(g, "numcol", n if ncols is None else int(ncols))
+    w.dataset(g + "/vecCsrIa", (rp + 1).astype(np.int32))
+    w.dataset(g + "/vecCsrJa", (np.asarray(col_idx, np.int64) + 1).astype(np.int32))
+    w.dataset(g + "/cmpCsrVal", np.asarray(values, np.complex128))
+    w.close()

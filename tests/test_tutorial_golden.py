@@ -15,7 +15,8 @@ Checks:
 * the oracle's FP64 solve differs from the reference's by <= 1e-15 kappa_2;
 * on the GPU, both precisions converge to 1e-12 and differ from the
   reference's solution by at most the perturbation bound
-  kappa_2 (res_ours + res_ref) (+ 1e-13).
+  kappa_2 (res_ours + res_ref) (+ 1e-13), read back from the solution file
+  written in elpasoC's layout (h5model.write_solution).
 """
 import os
 
@@ -76,12 +77,20 @@ def test_oracle_solve_matches_reference(elp, oracle, tut):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["FP64_PLAIN", "MIXED"])
-def test_gpu_solve_matches_reference(elp, oracle, tut, precision):
+def test_gpu_solve_matches_reference(elp, oracle, tut, precision, tmp_path):
+    import importlib
+    h5model = importlib.import_module("elpaso_core_gb300.h5model")
     d = tutorial_desc(elp, tut)
     s = oracle.System(d)
     m = elp.Model(d).assemble().analyse()
     om = 2 * np.pi * tut["freqs"]
     x, info = m.solve(om, precision=getattr(elp, precision), tol=1e-12)
+    # through the solution file elpasoC writes (eGenOutput layout) and back
+    out = str(tmp_path / "eGenOutput_tutorial.hdf5")
+    h5model.write_solution(out, tut["freqs"], x, h5model.dof_map(d.node_ids, m.global_rows()))
+    f2, x, dm = h5model.read_solution(out)
+    np.testing.assert_array_equal(dm, tut["dof_map"])
+    np.testing.assert_allclose(f2, tut["freqs"], rtol=0, atol=1e-6)
     for k, (A, r_ref) in enumerate(_reference_residuals(s, tut)):
         xr = tut["solutions"][k]
         res = np.linalg.norm(s.f - A @ x[k]) / np.linalg.norm(s.f)
