@@ -1796,6 +1796,8 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
     const double2* src = f_dev ? f_dev + (size_t)s * n : reinterpret_cast<const double2*>(m.dev->rhs.p);
     ELP_CUDA(cudaMemcpyAsync(w.f.p + (size_t)s * n, src, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
   }
+  // the tensor-core timeout flag reports this batch only
+  ELP_CUDA(cudaMemsetAsync(w.tc_err.p, 0, sizeof(int), st));
   int iters = 0;
   float ms[3] = {0, 0, 0};
   if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 12, st, ms);
