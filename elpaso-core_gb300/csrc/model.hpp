@@ -98,7 +98,8 @@ struct Model {
   std::unique_ptr<DeviceModel> dev;
   std::unique_ptr<Symbolic> sym;
   std::unique_ptr<DeviceSymbolic> dsym;
-  std::unique_ptr<Workspace> ws[2];  // per precision
+  std::unique_ptr<Workspace> ws[2];    // per precision
+  std::unique_ptr<Workspace> ws_b[2];  // per precision: second lane of a batch solved in two halves
 
   Model();
   ~Model();

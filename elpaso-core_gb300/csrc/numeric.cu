@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 
 #include "numeric.cuh"
 #include "prof.cuh"
@@ -1217,8 +1218,8 @@ int64_t workspace_bytes(const Model& m, int precision, int slots) {
   return b;
 }
 
-int workspace_ensure(Model& m, int precision, int slots) {
-  std::unique_ptr<Workspace>& W = m.ws[precision];
+int workspace_ensure(Model& m, int precision, int slots, int lane) {
+  std::unique_ptr<Workspace>& W = lane ? m.ws_b[precision] : m.ws[precision];
   if (W && W->slots >= slots) return ELP_OK;
   W.reset(new Workspace());
   Workspace& w = *W;
@@ -1779,16 +1780,13 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
   return ELP_OK;
 }
 
-int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega, const double2* f_dev,
-                        double2* x_dev, elp_solve_info* info, double tol, cudaStream_t user_stream) {
-  if (n_omega <= 0) return ELP_OK;
-  if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
-  for (int s = 0; s < n_omega; ++s)
-    if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
-  int rc = workspace_ensure(m, precision, n_omega);
+// One batch on one workspace lane (0 or 1), on `stream` (its own when null).
+static int solve_lane(Model& m, int precision, int lane, const double* omegas, int n_omega, const double2* f_dev,
+                      double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream) {
+  int rc = workspace_ensure(m, precision, n_omega, lane);
   if (rc) return rc;
-  Workspace& w = *m.ws[precision];
-  cudaStream_t st = user_stream ? user_stream : w.stream;
+  Workspace& w = lane ? *m.ws_b[precision] : *m.ws[precision];
+  cudaStream_t st = stream ? stream : w.stream;
   const int64_t n = m.n;
   for (int s = 0; s < n_omega; ++s) make_coef(m, omegas[s], w.h_coef[s]);
   ELP_CUDA(cudaMemcpyAsync(w.coef.p, w.h_coef, sizeof(Coef) * n_omega, cudaMemcpyHostToDevice, st));
@@ -1836,6 +1834,69 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
     }
   }
   if (!ok) {
+    set_error("iterative refinement did not reach the requested relative residual");
+    return ELP_ERR_NOCONV;
+  }
+  return ELP_OK;
+}
+
+// Batches of kSplitMin or more frequencies are solved as two halves on two
+// workspace lanes at once (two host threads, two streams): the top of the
+// assembly tree is latency-bound (one CTA per front and frequency), so one
+// half's top levels overlap the other half's throughput-bound lower levels.
+// Every frequency slot is computed independently, so the results do not
+// depend on the split. Not split while kernel profiling is on.
+constexpr int kSplitMin = 16;
+
+int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega, const double2* f_dev,
+                        double2* x_dev, elp_solve_info* info, double tol, cudaStream_t user_stream) {
+  if (n_omega <= 0) return ELP_OK;
+  if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
+  for (int s = 0; s < n_omega; ++s)
+    if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
+  static const bool split_on = !(getenv("ELP_SPLIT") && getenv("ELP_SPLIT")[0] == '0');
+  if (!split_on || n_omega < kSplitMin || prof_on())
+    return solve_lane(m, precision, 0, omegas, n_omega, f_dev, x_dev, info, tol, user_stream);
+  const int64_t n = m.n;
+  const int h0 = (n_omega + 1) / 2, h1 = n_omega - h0;
+  int rc = workspace_ensure(m, precision, h0, 0);
+  if (!rc) rc = workspace_ensure(m, precision, h0, 1);
+  if (rc) return rc;
+  // both lanes start after the work already queued on the caller's stream
+  cudaEvent_t ev;
+  ELP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  ELP_CUDA(cudaEventRecord(ev, user_stream));
+  ELP_CUDA(cudaStreamWaitEvent(m.ws[precision]->stream, ev, 0));
+  ELP_CUDA(cudaStreamWaitEvent(m.ws_b[precision]->stream, ev, 0));
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int rc1 = ELP_OK;
+  std::string err1;
+  std::thread lane1([&] {
+    try {
+      cudaSetDevice(dev);
+      rc1 = solve_lane(m, precision, 1, omegas + h0, h1, f_dev ? f_dev + (size_t)h0 * n : nullptr,
+                       x_dev + (size_t)h0 * n, info ? info + h0 : nullptr, tol, nullptr);
+    } catch (const std::exception& e) {
+      rc1 = ELP_ERR_CUDA;
+      set_error(std::string("second lane: ") + e.what());
+    }
+    if (rc1) err1 = get_error();
+  });
+  int rc0 = ELP_OK;
+  try {
+    rc0 = solve_lane(m, precision, 0, omegas, h0, f_dev, x_dev, info, tol, nullptr);
+  } catch (...) {
+    lane1.join();
+    cudaEventDestroy(ev);
+    throw;
+  }
+  lane1.join();
+  cudaEventDestroy(ev);
+  // each lane synchronised its stream before returning: the results are complete
+  if (rc0 && rc0 != ELP_ERR_NOCONV) return rc0;
+  if (rc1 && rc1 != ELP_ERR_NOCONV) { set_error(err1); return rc1; }
+  if (rc0 || rc1) {
     set_error("iterative refinement did not reach the requested relative residual");
     return ELP_ERR_NOCONV;
   }

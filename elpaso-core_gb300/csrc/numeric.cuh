@@ -182,7 +182,7 @@ struct Workspace {
 };
 
 int device_upload_symbolic(Model& m);
-int workspace_ensure(Model& m, int precision, int slots);
+int workspace_ensure(Model& m, int precision, int slots, int lane = 0);
 int64_t workspace_bytes(const Model& m, int precision, int slots);
 int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega,
                         const double2* f_dev, double2* x_dev, elp_solve_info* info, double tol,

@@ -120,6 +120,7 @@ struct elp_server {
       ModelSlot& o = models[i];
       if (i == mi || o.busy || o.resident == 0 || !o.queue.empty()) continue;
       for (auto& w : o.h->m.ws) w.reset();
+      for (auto& w : o.h->m.ws_b) w.reset();
       resident -= o.resident;
       o.resident = 0;
     }
