@@ -1638,6 +1638,10 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
   const dim3 gv((unsigned)std::min<int64_t>((n + 255) / 256, 4096), S_used);
   const dim3 gr((unsigned)w.nparts, S_used);
   V* z = reinterpret_cast<V*>(w.z.p);
+  // dot products: few blocks per slot, so each thread sums several entries before
+  // the (FP64, costly) block reduction of every basis vector
+  const int nd = std::min(w.nparts, 64);
+  const dim3 gd((unsigned)nd, S_used);
   static const bool trace = getenv("ELP_TRACE") != nullptr;
   std::vector<double> fn(S_used), rel(S_used);
   auto residual = [&](int x_zero) -> int {
@@ -1694,14 +1698,14 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
       PROF_LAUNCH(KC_SPMV, st, k_spmv<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n,
                                                                  w.Zb.p + (int64_t)j * n, zst, w.wv.p, w.inner.p));
       const int nv = j + 1;
-      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p));
-      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd1.p, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gd, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, nd, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, nd, nv, w.hd1.p, w.inner.p));
       PROF_LAUNCH(KC_KRYLOV, st, k_gs<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.hd1.p, w.wv.p, n, w.inner.p));
-      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gr, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p));
-      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, nv, w.hd2.p, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gd, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, w.dpart.p, nd, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, nd, nv, w.hd2.p, w.inner.p));
       PROF_LAUNCH(KC_KRYLOV, st, k_gs<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.hd2.p, w.wv.p, n, w.inner.p));
-      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gr, 256, 0, st>>>(w.wv.p, n, 0, 1, w.wv.p, n, w.dpart.p, w.nparts, w.inner.p));
-      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, w.nparts, 1, w.hnd.p, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots<<<gd, 256, 0, st>>>(w.wv.p, n, 0, 1, w.wv.p, n, w.dpart.p, nd, w.inner.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_reduce<<<S_used, 32, 0, st>>>(w.dpart.p, nd, 1, w.hnd.p, w.inner.p));
       ELP_CUDA(cudaMemcpyAsync(w.h_h, w.hd1.p, sizeof(double2) * S_used * kMaxBasis, cudaMemcpyDeviceToHost, st));
       ELP_CUDA(cudaMemcpyAsync(w.h_h + S_used * kMaxBasis, w.hd2.p, sizeof(double2) * S_used * kMaxBasis,
                                cudaMemcpyDeviceToHost, st));
