@@ -126,6 +126,16 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+__device__ __forceinline__ void ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
   asm volatile(
@@ -174,6 +184,34 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(mbar)) : "memory");
 }
 }  // namespace tc
+
+// The update C -= D of a front's Schur complement written into its parent
+// instead (extend-add fused): cv[q] = C[i, jb + q] - D[i, jb + q] for one row
+// i of the border, q < Q; the parent entry of border (i, j) is
+// (pmap[i], pmap[j]). Loads of 8 parent entries are issued together.
+template <int Q>
+__device__ __forceinline__ void add_into_parent(const LevelArgs& L, float2* arena, int f, int s, int i, int jb,
+                                                int ncols, const float2* cv) {
+  const int P = L.fparent[f];
+  const int64_t mP = L.fp[P] + L.fb[P];
+  float2* PF = arena + s * L.arena_size + L.foff[P];
+  const int32_t* pm = L.pmap + L.map_off[f];
+  const int64_t pi = pm[i];
+#pragma unroll
+  for (int h = 0; h < Q; h += 8) {
+    float2 pv[8];
+    int64_t po[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (jb + h + t < ncols) {
+        po[t] = (int64_t)pm[jb + h + t] * mP + pi;
+        pv[t] = PF[po[t]];
+      }
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (jb + h + t < ncols) PF[po[t]] = make_float2(pv[t].x + cv[h + t].x, pv[t].y + cv[h + t].y);
+  }
+}
 
 // C -= A B on one front's sub-block, FP32 complex, tcgen05 3xTF32.
 template <int NB, int NT, bool TRANS>
@@ -379,19 +417,29 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
 #pragma unroll
         for (int part = 0; part < 2; ++part) {  // 16 columns at a time: loads first, then stores
           const int jb = j0 + half * 32 + part * 16;
-          if (!TRANS) {  // lanes along rows of C: coalesced
-            float re[16], im[16];
-            tc::ld16(tD + lane_base + half * 32 + part * 16, re);
-            tc::ld16(tD + lane_base + NT + half * 32 + part * 16, im);
-            if (ok && i < MR) {
-              float2* dst0 = F + (int64_t)(ca + jb) * m + ra + i;
-              float2 cv[16];
+          if (!TRANS) {  // lanes along rows of C: coalesced; 8 columns at a time
 #pragma unroll
-              for (int q = 0; q < 16; ++q)
-                if (jb + q < NC) cv[q] = dst0[(int64_t)q * m];
+            for (int e8 = 0; e8 < 16; e8 += 8) {
+              const int jb8 = jb + e8;
+              float re[8], im[8];
+              tc::ld8(tD + lane_base + half * 32 + part * 16 + e8, re);
+              tc::ld8(tD + lane_base + NT + half * 32 + part * 16 + e8, im);
+              if (ok && i < MR) {
+                float2* dst0 = F + (int64_t)(ca + jb8) * m + ra + i;
+                float2 cv[8];
 #pragma unroll
-              for (int q = 0; q < 16; ++q)
-                if (jb + q < NC) dst0[(int64_t)q * m] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+                for (int q = 0; q < 8; ++q)
+                  if (jb8 + q < NC) cv[q] = dst0[(int64_t)q * m];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) cv[q] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+                if (NT == 64 && mode == GM_SCHUR && L.fuse) {  // only the 64-wide tiles run GM_SCHUR
+                  add_into_parent<8>(L, arena, f, s, i, jb8, NC, cv);  // border (i, j) of the Schur complement
+                } else {
+#pragma unroll
+                  for (int q = 0; q < 8; ++q)
+                    if (jb8 + q < NC) dst0[(int64_t)q * m] = cv[q];
+                }
+              }
             }
           } else {
             // C^T: the MMA row i is a column of C, contiguous along j; the warp's 32 x 16 block
@@ -661,8 +709,14 @@ __global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __rest
         for (int q = 0; q < 16; ++q)
           if (jb + q < b) cv[q] = dst0[(int64_t)q * m];
 #pragma unroll
-        for (int q = 0; q < 16; ++q)
-          if (jb + q < b) dst0[(int64_t)q * m] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+        for (int q = 0; q < 16; ++q) cv[q] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+        if (L.fuse) {
+          add_into_parent<16>(L, arena, f, s, i, jb, b, cv);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 16; ++q)
+            if (jb + q < b) dst0[(int64_t)q * m] = cv[q];
+        }
       }
     }
   } else if (tid == 0) {

@@ -130,6 +130,10 @@ struct LevelArgs {
   const int64_t* foff;
   int64_t arena_size;
   int64_t n;
+  // Schur complement added straight into the parent (extend-add fused into the
+  // update; `list` then holds fronts with distinct parents)
+  const int32_t *fparent, *map_off, *pmap;
+  int fuse;
 };
 
 constexpr int kPanelSmemBytes = 200 * 1024;  // panel rows held in shared memory when they fit
@@ -1317,6 +1321,10 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   L.foff = D.f_off.p;
   L.arena_size = D.arena;
   L.n = n;
+  L.fparent = D.f_parent.p;
+  L.map_off = D.f_map_off.p;
+  L.pmap = D.parent_map.p;
+  L.fuse = 0;
   const R tiny = sizeof(R) == 8 ? (R)1e-10 : (R)1e-6;
   // FP32 fronts: Schur updates on the tensor cores (tcgen05, 3xTF32) unless ELP_TC=0
   static const bool use_tc = !(getenv("ELP_TC") && getenv("ELP_TC")[0] == '0');
@@ -1352,7 +1360,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     ELP_CUDA(e);
   }
   // mode: GM_COL / GM_ROW / GM_SCHUR; rows_c, cols_c: upper bounds of the C block over the level
-  auto gemm = [&](int mode, int k, int rows_c, int cols_c) {
+  auto gemm = [&](int mode, int k, int rows_c, int cols_c, const LevelArgs& L) {
     if (tc) {
       float2* fa = reinterpret_cast<float2*>(arena);
       if (mode == GM_SCHUR) {
@@ -1388,7 +1396,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     for (int k = 0; k < steps; ++k) {
       const int rows = LV.max_m - k * NB;       // rows k0..m-1 of the panel columns
       const int rest = LV.max_m - k * NB - 1;   // columns right of the panel (upper bound)
-      if (k > 0) gemm(GM_COL, k, rows, NB);     // panel columns from all previous panels
+      if (k > 0) gemm(GM_COL, k, rows, NB, L);  // panel columns from all previous panels
       dim3 g1(LV.count, S_used);
       {
         const int rows_max = LV.max_p - k * NB;
@@ -1406,33 +1414,51 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
         PROF_LAUNCH(KC_BORDER, st, k_border<R, NB><<<g2, 128, 0, st>>>(L, arena, k));
       }
       if (rest > 0) {
-        if (k > 0) gemm(GM_ROW, k, NB, rest);  // pivot rows right of the panel from all previous panels
+        if (k > 0) gemm(GM_ROW, k, NB, rest, L);  // pivot rows right of the panel from all previous panels
         dim3 g3(LV.count, S_used, (unsigned)std::min(65535, (rest + 127) / 128));
         g3.z = (unsigned)std::min(65535, (rest + urow_cols<R>() - 1) / urow_cols<R>());
         PROF_LAUNCH(KC_UROW, st, k_urow<R, NB><<<g3, 128, 0, st>>>(L, arena, k));
       }
     }
-    if (LV.max_b > 0) {  // Schur complement, depth p
+    if (LV.max_b > 0 && tc) {
+      // Schur complement C -= L21 U12 added straight into each parent front (the
+      // extend-add fused into the update's epilogue): one child slot per launch,
+      // so no two fronts of a launch share a parent (fixed summation order)
       // few, large fronts (the top of the tree): operands split into TF32 planes once,
       // then bulk-copied by the MMA kernel (k_schur_tc); below, the converter kernel wins
       // (128-wide tiles waste work on short borders and the pack pass does not pay off)
-      if (tc && use_pack && w.pack.p && (pack_all || packed_schur_level(LV))) {
-        float2* fa = reinterpret_cast<float2*>(arena);
-        uint32_t* pk = reinterpret_cast<uint32_t*>(w.pack.p);
+      const bool packed = use_pack && w.pack.p && (pack_all || packed_schur_level(LV));
+      float2* fa = reinterpret_cast<float2*>(arena);
+      uint32_t* pk = reinterpret_cast<uint32_t*>(w.pack.p);
+      if (packed) {
         dim3 gp(LV.count, S_used, (unsigned)LV.pack_blocks);
         PROF_LAUNCH(KC_GEMM_TC, st, k_pack_schur<NB><<<gp, 256, 0, st>>>(L, fa, pk, D.pack_base.p, LV.pack_bytes));
-        dim3 gs(LV.count, S_used, (unsigned)LV.schur_tiles);
-        PROF_LAUNCH(KC_GEMM_TC, st, k_schur_tc<NB><<<gs, 256, kSchurSmemBytes, st>>>(L, fa, pk, D.pack_base.p,
-                                                                                      LV.pack_bytes, w.tc_err.p));
-      } else {
-        gemm(GM_SCHUR, 0, LV.max_b, LV.max_b);
       }
+      LevelArgs Lc = L;
+      Lc.fuse = 1;
+      for (size_t k = 0; k < LV.ea_count.size(); ++k) {
+        if (!LV.ea_count[k]) continue;
+        Lc.list = D.ea_list.p + LV.ea_start[k];
+        Lc.count = LV.ea_count[k];
+        if (packed) {
+          dim3 gs(Lc.count, S_used, (unsigned)LV.schur_tiles);
+          PROF_LAUNCH(KC_GEMM_TC, st, k_schur_tc<NB><<<gs, 256, kSchurSmemBytes, st>>>(Lc, fa, pk, D.pack_base.p,
+                                                                                        LV.pack_bytes, w.tc_err.p));
+        } else {
+          gemm(GM_SCHUR, 0, LV.ea_max_b, LV.ea_max_b, Lc);
+        }
+      }
+    } else if (LV.max_b > 0) {
+      gemm(GM_SCHUR, 0, LV.max_b, LV.max_b, L);  // Schur complement, depth p
     }
-    for (size_t k = 0; k < LV.ea_count.size(); ++k) {
-      if (!LV.ea_count[k]) continue;
-      dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, (LV.ea_max_b + 3) / 4));  // 4 columns per pass
-      PROF_LAUNCH(KC_EXTEND_ADD, st, k_extend_add<R><<<g5, 256, 0, st>>>(D.ea_list.p + LV.ea_start[k], D.f_p.p, D.f_b.p, D.f_parent.p, D.f_map_off.p,
-                                          D.f_off.p, D.parent_map.p, arena, D.arena));
+    if (!tc) {  // extend-add of the children's Schur complements into their parents
+      for (size_t k = 0; k < LV.ea_count.size(); ++k) {
+        if (!LV.ea_count[k]) continue;
+        dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, (LV.ea_max_b + 3) / 4));  // 4 columns per pass
+        PROF_LAUNCH(KC_EXTEND_ADD, st, k_extend_add<R><<<g5, 256, 0, st>>>(D.ea_list.p + LV.ea_start[k], D.f_p.p, D.f_b.p,
+                                                                           D.f_parent.p, D.f_map_off.p, D.f_off.p,
+                                                                           D.parent_map.p, arena, D.arena));
+      }
     }
   }
   ELP_CUDA(cudaGetLastError());
