@@ -98,8 +98,8 @@ struct Model {
   std::unique_ptr<DeviceModel> dev;
   std::unique_ptr<Symbolic> sym;
   std::unique_ptr<DeviceSymbolic> dsym;
-  std::unique_ptr<Workspace> ws[2];    // per precision
-  std::unique_ptr<Workspace> ws_b[2];  // per precision: second lane of a batch solved in two halves
+  std::unique_ptr<Workspace> ws[2];      // per precision
+  std::unique_ptr<Workspace> ws_b[2][3];  // per precision: lanes 1..3 of a batch solved in parts at once
 
   Model();
   ~Model();

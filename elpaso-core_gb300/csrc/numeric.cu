@@ -1223,7 +1223,7 @@ int64_t workspace_bytes(const Model& m, int precision, int slots) {
 }
 
 int workspace_ensure(Model& m, int precision, int slots, int lane) {
-  std::unique_ptr<Workspace>& W = lane ? m.ws_b[precision] : m.ws[precision];
+  std::unique_ptr<Workspace>& W = lane ? m.ws_b[precision][lane - 1] : m.ws[precision];
   if (W && W->slots >= slots) return ELP_OK;
   W.reset(new Workspace());
   Workspace& w = *W;
@@ -1815,7 +1815,7 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
                       double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream) {
   int rc = workspace_ensure(m, precision, n_omega, lane);
   if (rc) return rc;
-  Workspace& w = lane ? *m.ws_b[precision] : *m.ws[precision];
+  Workspace& w = lane ? *m.ws_b[precision][lane - 1] : *m.ws[precision];
   cudaStream_t st = stream ? stream : w.stream;
   const int64_t n = m.n;
   for (int s = 0; s < n_omega; ++s) make_coef(m, omegas[s], w.h_coef[s]);
@@ -1870,12 +1870,13 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
   return ELP_OK;
 }
 
-// Batches of kSplitMin or more frequencies are solved as two halves on two
-// workspace lanes at once (two host threads, two streams): the top of the
-// assembly tree is latency-bound (one CTA per front and frequency), so one
-// half's top levels overlap the other half's throughput-bound lower levels.
+// Batches of kSplitMin or more frequencies are solved in parts on several
+// workspace lanes at once (one host thread and stream per lane): the top of
+// the assembly tree is latency-bound (one CTA per front and frequency), so
+// one part's top levels overlap another part's throughput-bound lower levels.
 // Every frequency slot is computed independently, so the results do not
-// depend on the split. Not split while kernel profiling is on.
+// depend on the split. Lanes: 2 (ELP_LANES = 1..4); not split while kernel
+// profiling is on.
 constexpr int kSplitMin = 16;
 
 int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega, const double2* f_dev,
@@ -1884,49 +1885,58 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
   if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
   for (int s = 0; s < n_omega; ++s)
     if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
-  static const bool split_on = !(getenv("ELP_SPLIT") && getenv("ELP_SPLIT")[0] == '0');
-  if (!split_on || n_omega < kSplitMin || prof_on())
+  static const int lanes_env = [] {
+    const char* e = getenv("ELP_LANES");
+    int v = e ? atoi(e) : 2;
+    return v < 1 ? 1 : v > 4 ? 4 : v;
+  }();
+  const int lanes = std::min(lanes_env, std::max(1, n_omega / (kSplitMin / 2)));
+  if (lanes < 2 || n_omega < kSplitMin || prof_on())
     return solve_lane(m, precision, 0, omegas, n_omega, f_dev, x_dev, info, tol, user_stream);
   const int64_t n = m.n;
-  const int h0 = (n_omega + 1) / 2, h1 = n_omega - h0;
-  int rc = workspace_ensure(m, precision, h0, 0);
-  if (!rc) rc = workspace_ensure(m, precision, h0, 1);
-  if (rc) return rc;
-  // both lanes start after the work already queued on the caller's stream
+  int first[5];
+  for (int l = 0; l <= lanes; ++l) first[l] = (int)((int64_t)n_omega * l / lanes);
+  const int part_max = first[1] - first[0] + 1;
+  for (int l = 0; l < lanes; ++l) {
+    int rc = workspace_ensure(m, precision, part_max, l);
+    if (rc) return rc;
+  }
+  // every lane starts after the work already queued on the caller's stream
   cudaEvent_t ev;
   ELP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   ELP_CUDA(cudaEventRecord(ev, user_stream));
-  ELP_CUDA(cudaStreamWaitEvent(m.ws[precision]->stream, ev, 0));
-  ELP_CUDA(cudaStreamWaitEvent(m.ws_b[precision]->stream, ev, 0));
+  for (int l = 0; l < lanes; ++l) {
+    Workspace& w = l ? *m.ws_b[precision][l - 1] : *m.ws[precision];
+    ELP_CUDA(cudaStreamWaitEvent(w.stream, ev, 0));
+  }
   int dev = 0;
   cudaGetDevice(&dev);
-  int rc1 = ELP_OK;
-  std::string err1;
-  std::thread lane1([&] {
+  int rcs[4] = {ELP_OK, ELP_OK, ELP_OK, ELP_OK};
+  std::string errs[4];
+  auto run = [&](int l) {
     try {
       cudaSetDevice(dev);
-      rc1 = solve_lane(m, precision, 1, omegas + h0, h1, f_dev ? f_dev + (size_t)h0 * n : nullptr,
-                       x_dev + (size_t)h0 * n, info ? info + h0 : nullptr, tol, nullptr);
+      const int a = first[l], c = first[l + 1] - first[l];
+      rcs[l] = solve_lane(m, precision, l, omegas + a, c, f_dev ? f_dev + (size_t)a * n : nullptr,
+                          x_dev + (size_t)a * n, info ? info + a : nullptr, tol, nullptr);
     } catch (const std::exception& e) {
-      rc1 = ELP_ERR_CUDA;
-      set_error(std::string("second lane: ") + e.what());
+      rcs[l] = ELP_ERR_CUDA;
+      set_error(std::string("solve lane: ") + e.what());
     }
-    if (rc1) err1 = get_error();
-  });
-  int rc0 = ELP_OK;
-  try {
-    rc0 = solve_lane(m, precision, 0, omegas, h0, f_dev, x_dev, info, tol, nullptr);
-  } catch (...) {
-    lane1.join();
-    cudaEventDestroy(ev);
-    throw;
-  }
-  lane1.join();
+    if (rcs[l]) errs[l] = get_error();
+  };
+  std::vector<std::thread> threads;
+  for (int l = 1; l < lanes; ++l) threads.emplace_back(run, l);
+  run(0);
+  for (auto& t : threads) t.join();
   cudaEventDestroy(ev);
   // each lane synchronised its stream before returning: the results are complete
-  if (rc0 && rc0 != ELP_ERR_NOCONV) return rc0;
-  if (rc1 && rc1 != ELP_ERR_NOCONV) { set_error(err1); return rc1; }
-  if (rc0 || rc1) {
+  bool noconv = false;
+  for (int l = 0; l < lanes; ++l) {
+    if (rcs[l] == ELP_ERR_NOCONV) noconv = true;
+    else if (rcs[l]) { set_error(errs[l]); return rcs[l]; }
+  }
+  if (noconv) {
     set_error("iterative refinement did not reach the requested relative residual");
     return ELP_ERR_NOCONV;
   }

@@ -120,7 +120,8 @@ struct elp_server {
       ModelSlot& o = models[i];
       if (i == mi || o.busy || o.resident == 0 || !o.queue.empty()) continue;
       for (auto& w : o.h->m.ws) w.reset();
-      for (auto& w : o.h->m.ws_b) w.reset();
+      for (auto& lw : o.h->m.ws_b)
+        for (auto& w : lw) w.reset();
       resident -= o.resident;
       o.resident = 0;
     }
