@@ -1875,8 +1875,9 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
 // the assembly tree is latency-bound (one CTA per front and frequency), so
 // one part's top levels overlap another part's throughput-bound lower levels.
 // Every frequency slot is computed independently, so the results do not
-// depend on the split. Lanes: 2 (ELP_LANES = 1..4); not split while kernel
-// profiling is on.
+// depend on the split. Lanes: 4, parts of >= 8 frequencies (ELP_LANES = 1..4;
+// 32 frequencies per step: 2 lanes 105.7, 3 lanes 107.3, 4 lanes 108.6
+// solves/s); not split while kernel profiling is on.
 constexpr int kSplitMin = 16;
 
 int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega, const double2* f_dev,
@@ -1887,7 +1888,7 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
     if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
   static const int lanes_env = [] {
     const char* e = getenv("ELP_LANES");
-    int v = e ? atoi(e) : 2;
+    int v = e ? atoi(e) : 4;
     return v < 1 ? 1 : v > 4 ? 4 : v;
   }();
   const int lanes = std::min(lanes_env, std::max(1, n_omega / (kSplitMin / 2)));
