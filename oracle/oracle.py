@@ -247,12 +247,41 @@ class System:
         import scipy.sparse as sp
         return sp.csr_matrix((self.values(omega), self.col_idx, self.row_ptr), shape=(self.n, self.n))
 
+    def lifted(self, omega, f=None):
+        """A(w) x = f with the Dirichlet columns moved to the right-hand side.
+
+        The boundary rows are identity rows (MatZeroRows with diagonal 1,
+        elpasoCore/source/analysis/analysis.cpp:426-441), so they fix
+        x_c = rhs_c; every other row i then gets rhs_i -= A_ic x_c and
+        A_ic = 0. Same solution in exact arithmetic, same pattern (the lifted
+        entries stay as explicit zeros). A direct solver on the unlifted
+        matrix pivots the identity rows against column entries of ~1e11 and
+        loses up to four digits on a clamped thin plate; on the lifted one
+        it sees the free block, whose conditioning is the physical one."""
+        A = self.matrix(omega)
+        rhs = np.array(self.f if f is None else f, np.complex128, copy=True)
+        if self.bc_rows:
+            bc = np.zeros(self.n, bool)
+            bc[self.bc_rows] = True
+            g = np.where(bc, rhs, 0)
+            rhs[~bc] -= (A @ g)[~bc]
+            rows = np.repeat(np.arange(self.n), np.diff(A.indptr))
+            A.data[bc[A.indices] & ~bc[rows]] = 0
+        return A, rhs
+
+    def free_block(self, omega):
+        """(A_ff, free rows): A(w) restricted to the rows and columns that
+        carry no Dirichlet condition."""
+        free = np.ones(self.n, bool)
+        free[self.bc_rows] = False
+        idx = np.nonzero(free)[0]
+        return self.matrix(omega)[idx][:, idx], idx
+
     def solve(self, omega, f=None):
+        """FP64 direct solve (SuperLU) of the lifted system."""
         import scipy.sparse.linalg as sla
-        A = self.matrix(omega).tocsc()
-        rhs = self.f if f is None else f
-        x = sla.splu(A).solve(rhs)
-        return x
+        A, rhs = self.lifted(omega, f)
+        return sla.splu(A.tocsc()).solve(rhs)
 
 
 def dof_nodes(system):

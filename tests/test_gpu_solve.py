@@ -1,11 +1,14 @@
 """Per-frequency solve on the GPU (plain FP64 and mixed FP32 fronts + FP64
 refinement) against the FP64 direct-solve oracle (SciPy SuperLU on the
-oracle's own CSR).
+oracle's own CSR, Dirichlet columns lifted).
 
 Bars: relative residual ||f - A x||_2 / ||f||_2 <= 1e-10, measured with the
-ORACLE's matrix; relative error vs the oracle's solution within what the
-residual allows, ||x - x_ref|| / ||x_ref|| <= 4 * kappa_1(A) * 1e-10 (kappa_1
-estimated with onenormest; thin-hex and near-resonance systems reach 1e7+)."""
+ORACLE's matrix; relative error vs the oracle's solution within what both
+residuals allow, in 1-norms ||x - x_ref|| / ||x_ref|| <= kappa_1(A_ff)
+(res_1 + res_ref_1) (the perturbation bound on the free block A_ff, the only
+part either solution can err in: the boundary rows fix x_c exactly; kappa_1
+estimated with onenormest, a lower bound, x 3; thin-hex and near-resonance
+systems reach 1e7)."""
 import numpy as np
 import pytest
 
@@ -30,9 +33,13 @@ def check(elp, oracle, d, f_list, prec):
         A = s.matrix(om)
         res = np.linalg.norm(s.f - A @ x[k]) / np.linalg.norm(s.f)
         xr = s.solve(om)
-        err = np.linalg.norm(x[k] - xr) / np.linalg.norm(xr)
+        n1 = np.linalg.norm(s.f, 1)
+        res1 = np.linalg.norm(s.f - A @ x[k], 1) / n1
+        res_ref1 = np.linalg.norm(s.f - A @ xr, 1) / n1
+        err = np.linalg.norm(x[k] - xr, 1) / np.linalg.norm(xr, 1)
         assert res <= RES_TOL, (k, res)
-        assert err <= max(1e-12, 4.0 * cond1(A) * RES_TOL), (k, err)
+        bound = 3.0 * cond1(s.free_block(om)[0]) * (res1 + res_ref1)
+        assert err <= max(1e-13, bound), (k, err, bound)
         if prec == 1:  # FP32 fronts are a good preconditioner: few GMRES steps
             assert infos[k]["iterations"] <= 24, (k, infos[k]["iterations"])
         assert infos[k]["converged"] == 1
