@@ -313,11 +313,19 @@ class Model:
         return a.value, b.value
 
     def solve(self, omegas, precision: int = FP64_PLAIN, f: np.ndarray | None = None, tol: float = 1e-10,
-              raise_on_noconv: bool = True):
-        """Solves A(w) u = f for each angular frequency; returns (x[n_omega, n], infos)."""
+              raise_on_noconv: bool = True, out: np.ndarray | None = None):
+        """Solves A(w) u = f for each angular frequency; returns (x[n_omega, n], infos).
+
+        f and out may be host buffers the caller owns (pinned ones copy at
+        full link speed); out must be C-contiguous complex128 [n_omega, n]."""
         om = np.ascontiguousarray(np.atleast_1d(omegas), dtype=np.float64)
         n = self.n
-        x = np.zeros((len(om), n), np.complex128)
+        if out is None:
+            x = np.zeros((len(om), n), np.complex128)
+        else:
+            if out.dtype != np.complex128 or out.shape != (len(om), n) or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous complex128 array of shape (n_omega, n)")
+            x = out
         infos = (SolveInfo * max(1, len(om)))()
         fp = None
         if f is not None:

@@ -212,12 +212,13 @@ int elp_solve_device(elp_model* h, const double* omegas, int n_omega, int precis
   if (!(tol > 0.0)) tol = 1e-10;
   Model& m = h->m;
   const int64_t n = m.n;
-  // batch size: as many frequencies as fit a quarter of free memory, <= kMaxSlots
+  // batch size: as many frequencies as fit half of the free memory (with the
+  // bytes this precision's workspaces already hold, which the batch reuses),
+  // <= kMaxSlots
   size_t freeb = 0, totb = 0;
   ELP_CUDA(cudaMemGetInfo(&freeb, &totb));
-  const size_t elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
-  const size_t per_slot = (size_t)m.dsym->arena * elem + (size_t)n * (3 * sizeof(double2) + 24 + elem) +
-                          (size_t)m.dsym->cb_total * elem;
+  freeb += (size_t)workspace_held(m, precision);
+  const size_t per_slot = (size_t)workspace_bytes(m, precision, 1);
   int slots = (int)std::min<size_t>((size_t)kMaxSlots, std::max<size_t>(1, (freeb / 2) / std::max<size_t>(1, per_slot)));
   if (m.ws[precision] && m.ws[precision]->slots > 0) slots = std::max(slots, std::min(m.ws[precision]->slots, kMaxSlots));
   slots = std::min(slots, std::max(1, n_omega));

@@ -1222,6 +1222,14 @@ int64_t workspace_bytes(const Model& m, int precision, int slots) {
   return b;
 }
 
+int64_t workspace_held(const Model& m, int precision) {
+  int64_t b = 0;
+  if (m.ws[precision]) b += workspace_bytes(m, precision, m.ws[precision]->slots);
+  for (const auto& w : m.ws_b[precision])
+    if (w) b += workspace_bytes(m, precision, w->slots);
+  return b;
+}
+
 int workspace_ensure(Model& m, int precision, int slots, int lane) {
   std::unique_ptr<Workspace>& W = lane ? m.ws_b[precision][lane - 1] : m.ws[precision];
   if (W && W->slots >= slots) return ELP_OK;
@@ -1881,7 +1889,8 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
 constexpr int kSplitMin = 16;
 
 int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega, const double2* f_dev,
-                        double2* x_dev, elp_solve_info* info, double tol, cudaStream_t user_stream) {
+                        double2* x_dev, elp_solve_info* info, double tol, cudaStream_t user_stream,
+                        int max_lanes) {
   if (n_omega <= 0) return ELP_OK;
   if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
   for (int s = 0; s < n_omega; ++s)
@@ -1891,7 +1900,7 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
     int v = e ? atoi(e) : 4;
     return v < 1 ? 1 : v > 4 ? 4 : v;
   }();
-  const int lanes = std::min(lanes_env, std::max(1, n_omega / (kSplitMin / 2)));
+  const int lanes = std::min({lanes_env, max_lanes, std::max(1, n_omega / (kSplitMin / 2))});
   if (lanes < 2 || n_omega < kSplitMin || prof_on())
     return solve_lane(m, precision, 0, omegas, n_omega, f_dev, x_dev, info, tol, user_stream);
   const int64_t n = m.n;

@@ -184,9 +184,15 @@ struct Workspace {
 int device_upload_symbolic(Model& m);
 int workspace_ensure(Model& m, int precision, int slots, int lane = 0);
 int64_t workspace_bytes(const Model& m, int precision, int slots);
+// Device bytes held by the model's workspaces of one precision (all lanes):
+// reusable by the next batch of that precision.
+int64_t workspace_held(const Model& m, int precision);
+// max_lanes: upper bound on the workspace lanes a batch is split over (1: one
+// lane; callers that overlap several batches themselves, like the serving
+// loop, pass 1).
 int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega,
                         const double2* f_dev, double2* x_dev, elp_solve_info* info, double tol,
-                        cudaStream_t user_stream);
+                        cudaStream_t user_stream, int max_lanes = 4);
 int numeric_system_values(Model& m, double omega, double2* out_dev);
 void make_coef(const Model& m, double w, Coef& c);
 

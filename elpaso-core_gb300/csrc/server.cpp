@@ -180,9 +180,11 @@ struct elp_server {
           if (xdev.alloc((size_t)n * cfg.omega_batch) != cudaSuccess) rc = ELP_ERR_NOMEM;
         }
         if (!rc) {
-          // every batch uses the full slot count so the workspace is shaped once
+          // every batch uses the full slot count so the workspace is shaped once;
+          // one lane: the loop already overlaps up to max_inflight batches, and
+          // lane workspaces per model would double the allocations it admits
           rc = numeric_solve_batch(m, cfg.precision, oms.data(), (int)oms.size(), nullptr, xdev.p, info.data(),
-                                   cfg.tol, st);
+                                   cfg.tol, st, 1);
           if (rc == ELP_ERR_NOCONV) rc = ELP_OK;  // reported per request through its residual
         }
         if (!rc || rc == ELP_ERR_NOCONV) {
