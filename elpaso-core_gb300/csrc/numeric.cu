@@ -171,8 +171,14 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
   __shared__ int red_i[8];
   __shared__ V prow[NB];
   __shared__ int s_piv, spiv[NB];
+  __shared__ int s_rows[2 * NB], s_src[2 * NB], s_n;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   if ((rows <= cap_rows) != SMEM) return;  // the other variant's front (uniform per CTA)
+  // perm holds the front's row position map: row r of the factorised pivot
+  // block is original row pv[r]; identity before the first panel, each panel
+  // applies its swap map to it (below)
+  if (step == 0)
+    for (int r = tid; r < p; r += blockDim.x) pv[r] = r;
   constexpr bool in_smem = SMEM;
   V* P;       // P[c * ld + r] = F[(k0 + c) * m + k0 + r]
   int64_t ld;
@@ -213,7 +219,6 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
       if (i0 < j || i0 >= rows) i0 = j;
       s_piv = i0;
       spiv[j] = k0 + i0;
-      pv[k0 + j] = k0 + i0;
     }
     __syncthreads();
     const int pr = s_piv;
@@ -269,9 +274,8 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
     // min |u_jj| stored as bits of 1/|u_jj| max
     atomicMax(stats + 4 * s + 2, (unsigned long long)__double_as_longlong(1.0 / (double)pmin));
     // swap map: panel rows sit at list position row - k0, rows below the panel are appended
-    int32_t* mp = swapmap + ((int64_t)blockIdx.x * gridDim.y + s) * swapmap_ints<NB>();
-    int32_t* mrows = mp + 1;
-    int32_t* msrc = mp + 1 + 2 * NB;
+    int* mrows = s_rows;
+    int* msrc = s_src;
     int n = w;
     bool any = false;
     for (int j = 0; j < w; ++j) { mrows[j] = k0 + j; msrc[j] = k0 + j; }
@@ -288,8 +292,20 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
       }
       const int t = msrc[j]; msrc[j] = msrc[b]; msrc[b] = t;
     }
-    mp[0] = any ? n : 0;
+    s_n = any ? n : 0;
   }
+  __syncthreads();
+  const int n = s_n;
+  int32_t* mp = swapmap + ((int64_t)blockIdx.x * gridDim.y + s) * swapmap_ints<NB>();
+  if (tid == 0) mp[0] = n;
+  int32_t moved = 0;
+  if (tid < n) {  // n <= 2 NB <= blockDim.x
+    mp[1 + tid] = s_rows[tid];
+    mp[1 + 2 * NB + tid] = s_src[tid];
+    moved = pv[s_src[tid]];
+  }
+  __syncthreads();  // every source entry of the position map is read before any is overwritten
+  if (tid < n) pv[s_rows[tid]] = moved;
 }
 
 // Row interchanges of one panel applied to every column outside it (LAPACK's
@@ -575,6 +591,27 @@ struct SolveArgs {
   const int* active;
 };
 
+// dst[k] = src[idx[k]] for k < count: every thread issues the index loads of
+// four entries, then their value loads, so the dependent pairs of loads
+// overlap instead of running one after another
+template <class V>
+__device__ __forceinline__ void gather_rows(V* dst, const V* __restrict__ src, const int32_t* __restrict__ idx,
+                                            int count) {
+  const int nt = blockDim.x;
+  for (int k0 = threadIdx.x; k0 < count; k0 += 4 * nt) {
+    int ix[4];
+    V v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ix[q] = k0 + q * nt < count ? idx[k0 + q * nt] : 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (k0 + q * nt < count) v[q] = src[ix[q]];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (k0 + q * nt < count) dst[k0 + q * nt] = v[q];
+  }
+}
+
 template <class R>
 __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                  const int32_t* __restrict__ perm, typename Vec2<R>::T* __restrict__ z,
@@ -591,24 +628,35 @@ __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec
   V* zs = z + s * S.n;
   V* cbs = cb + s * S.cb_total;
   const int tid = threadIdx.x;
-  for (int k = tid; k < m; k += blockDim.x) w[k] = k < p ? zs[I[k]] : cmk<V>(0.0, 0.0);
+  gather_rows(w, zs, I, p);
+  for (int k = p + tid; k < m; k += blockDim.x) w[k] = cmk<V>(0.0, 0.0);
   __syncthreads();
   for (int q = S.child_ptr[f]; q < S.child_ptr[f + 1]; ++q) {
     const int c = S.child_list[q];
     const int bc = S.fb[c];
     const int32_t* mp = S.pmap + S.map_off[c];
     const V* src = cbs + S.cb_off[c];
-    for (int i = tid; i < bc; i += blockDim.x) w[mp[i]] = cadd(w[mp[i]], src[i]);
+    const int nt = blockDim.x;
+    for (int i0 = tid; i0 < bc; i0 += 4 * nt) {  // four entries' loads in flight (targets are distinct)
+      int mi[4];
+      V sv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u * nt < bc) { mi[u] = mp[i0 + u * nt]; sv[u] = src[i0 + u * nt]; }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u * nt < bc) w[mi[u]] = cadd(w[mi[u]], sv[u]);
+    }
     __syncthreads();
   }
-  if (tid == 0) {
+  {  // row interchanges of the factorisation: pivot row j is original row pv[j]
+    V* w2 = w + m;
     const int32_t* pv = perm + s * S.n + S.piv_off[f];
-    for (int j = 0; j < p; ++j) {
-      int r = pv[j];
-      if (r != j) { V t = w[j]; w[j] = w[r]; w[r] = t; }
-    }
+    for (int j = tid; j < p; j += blockDim.x) w2[j] = w[pv[j]];
+    __syncthreads();
+    for (int j = tid; j < p; j += blockDim.x) w[j] = w2[j];
+    __syncthreads();
   }
-  __syncthreads();
   const int lane = tid & 31, wid = tid >> 5;
   // L11 solve on the pivot block only; the border rows (L21) are updated by
   // k_fwd_border across many CTAs
@@ -668,7 +716,7 @@ __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename 
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   const V* zs = z + s * S.n;
-  for (int k = threadIdx.x; k < p; k += blockDim.x) y[k] = zs[I[k]];
+  gather_rows(y, zs, I, p);
   __syncthreads();
   const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
   const int i = blockIdx.z * 32 + lane;
@@ -716,7 +764,7 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   const V* zs = z + s * S.n;
-  for (int k = threadIdx.x; k < b; k += blockDim.x) xb[k] = zs[I[p + k]];
+  gather_rows(xb, zs, I + p, b);
   __syncthreads();
   const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
   const int r = blockIdx.z * 32 + lane;
@@ -773,8 +821,10 @@ __global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Ve
     __syncthreads();
     if (wid == 0) {
       V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
+      // every lane inverts its own diagonal entry up front: no division on the sequential chain
+      const V dinv = lane < jw ? cinv(dblk[lane][lane]) : cmk<V>(0.0, 0.0);
       for (int jj = jw - 1; jj >= 0; --jj) {
-        if (lane == jj) val = cmul(val, cinv(dblk[jj][jj]));
+        if (lane == jj) val = cmul(val, dinv);
         V x;
         x.x = __shfl_sync(0xffffffffu, val.x, jj);
         x.y = __shfl_sync(0xffffffffu, val.y, jj);
@@ -1505,7 +1555,7 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     const auto& LV = D.levels[l];
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
-    size_t sm = (size_t)LV.max_m * sizeof(V);
+    size_t sm = (size_t)(LV.max_m + LV.max_p) * sizeof(V);  // front vector + permutation buffer
     PROF_LAUNCH(KC_FORWARD, st, k_forward<R><<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, w.perm.p, z, cb));
     if (LV.max_b > 0) {
       const unsigned chunks = (unsigned)((LV.max_b + 31) / 32);
@@ -1531,7 +1581,7 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
 template <class R>
 static int solve_smem(const Model& m) {
   using V = typename Vec2<R>::T;
-  const size_t smem_need = (size_t)m.dsym->max_front * sizeof(V);
+  const size_t smem_need = 2 * (size_t)m.dsym->max_front * sizeof(V);  // k_forward: front + permutation buffer
   if (smem_need > 227 * 1024) {
     set_error("front larger than the shared-memory solve buffer (max 227 KB)");
     return ELP_ERR_NOMEM;
