@@ -143,6 +143,24 @@ constexpr int kPanelSmemBytes = 200 * 1024;  // panel rows held in shared memory
 template <int NB>
 __host__ __device__ constexpr int swapmap_ints() { return 1 + 4 * NB; }
 
+// Block-strided copy t = tid, tid + nt, ... < count with U loads in flight per
+// thread: load(t) for U indices first, then store(t, value) for them, so the
+// copy costs count / (nt U) memory latencies instead of count / nt. valid(t)
+// masks entries that are neither loaded nor stored.
+template <int U, class Valid, class Load, class Store>
+__device__ __forceinline__ void staged_copy(int count, Valid valid, Load load, Store store) {
+  const int nt = blockDim.x;
+  for (int t0 = threadIdx.x; t0 < count; t0 += U * nt) {
+    decltype(load(0)) v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (t0 + u * nt < count && valid(t0 + u * nt)) v[u] = load(t0 + u * nt);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (t0 + u * nt < count && valid(t0 + u * nt)) store(t0 + u * nt, v[u]);
+  }
+}
+
 // Panel factorisation (columns k0..k0+w-1, fully summed rows k0..p-1) with
 // partial pivoting restricted to the fully summed rows and a static pivot
 // floor. SMEM = true handles the fronts whose panel rows fit in shared memory
@@ -185,10 +203,10 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
   if (in_smem) {
     P = reinterpret_cast<V*>(psm_raw);
     ld = rows;
-    for (int t = tid; t < rows * w; t += blockDim.x) {
-      const int c = t / rows, r = t - c * rows;
-      P[t] = F[(int64_t)(k0 + c) * m + k0 + r];
-    }
+    staged_copy<4>(
+        rows * w, [](int) { return true; },
+        [&](int t) { const int c = t / rows, r = t - c * rows; return F[(int64_t)(k0 + c) * m + k0 + r]; },
+        [&](int t, V v) { P[t] = v; });
     __syncthreads();
   } else {
     P = F + (int64_t)k0 * m + k0;
@@ -264,10 +282,9 @@ __global__ void __launch_bounds__(256) k_panel(LevelArgs L, typename Vec2<R>::T*
     __syncthreads();
   }
   if (in_smem)
-    for (int t = tid; t < rows * w; t += blockDim.x) {
-      const int c = t / rows, r = t - c * rows;
-      F[(int64_t)(k0 + c) * m + k0 + r] = P[t];
-    }
+    staged_copy<4>(
+        rows * w, [](int) { return true; }, [&](int t) { return P[t]; },
+        [&](int t, V v) { const int c = t / rows, r = t - c * rows; F[(int64_t)(k0 + c) * m + k0 + r] = v; });
   if (tid == 0) {
     if (nstatic) atomicAdd(stats + 4 * s + 0, (unsigned long long)nstatic);
     atomicMax(stats + 4 * s + 1, (unsigned long long)__double_as_longlong((double)pmax));
@@ -360,10 +377,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 1) k_border(LevelArg
   V* F = arena + s * L.arena_size + L.foff[f];
   __shared__ V U[NB][NB + 1];
   __shared__ V dinv[NB];
-  for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
-    int i = t % w, j = t / w;
-    if (i <= j) U[i][j] = F[(int64_t)(k0 + j) * m + k0 + i];
-  }
+  staged_copy<8>(
+      w * w, [&](int t) { return t % w <= t / w; }, [&](int t) { return F[(int64_t)(k0 + t / w) * m + k0 + t % w]; },
+      [&](int t, V v) { U[t % w][t / w] = v; });
   __syncthreads();
   for (int j = threadIdx.x; j < w; j += blockDim.x) dinv[j] = cinv(U[j][j]);
   __syncthreads();
@@ -408,15 +424,26 @@ __global__ void __launch_bounds__(128) k_urow(LevelArgs L, typename Vec2<R>::T* 
   V* F = arena + s * L.arena_size + L.foff[f];
   __shared__ V Lp[NB][NB + 1];
   __shared__ V tile[TC][NB + 1];  // [column][panel row]
-  for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
-    int i = t % w, j = t / w;
-    if (i > j) Lp[i][j] = F[(int64_t)(k0 + j) * m + k0 + i];
-  }
+  staged_copy<8>(
+      w * w, [&](int t) { return t % w > t / w; }, [&](int t) { return F[(int64_t)(k0 + t / w) * m + k0 + t % w]; },
+      [&](int t, V v) { Lp[t % w][t / w] = v; });
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int cb = k0 + w + blockIdx.z * TC; cb < m; cb += gridDim.z * TC) {
-    for (int cc = wid; cc < TC; cc += nw) {
-      const int c = cb + cc;
-      if (c < m && lane < w) tile[cc][lane] = F[(int64_t)c * m + k0 + lane];
+    {  // the warp's columns, 4 loads in flight per lane
+      constexpr int U = 4;
+      for (int cc0 = wid; cc0 < TC; cc0 += U * nw) {
+        V v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int cc = cc0 + u * nw, c = cb + cc;
+          if (cc < TC && c < m && lane < w) v[u] = F[(int64_t)c * m + k0 + lane];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int cc = cc0 + u * nw, c = cb + cc;
+          if (cc < TC && c < m && lane < w) tile[cc][lane] = v[u];
+        }
+      }
     }
     __syncthreads();
     if ((int)threadIdx.x < TC && cb + (int)threadIdx.x < m) {
@@ -663,10 +690,10 @@ __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec
   __shared__ V dblk[32][33];  // diagonal 32 x 32 block, staged so the warp solve never waits on DRAM
   for (int j0 = 0; j0 < p; j0 += 32) {
     const int jw = min(32, p - j0);
-    for (int t = tid; t < 32 * 32; t += blockDim.x) {
-      const int jj = t >> 5, ii = t & 31;
-      if (jj < jw && ii < jw) dblk[ii][jj] = F[(int64_t)(j0 + jj) * m + j0 + ii];
-    }
+    staged_copy<sizeof(R) == 4 ? 8 : 4>(
+        32 * 32, [&](int t) { return (t >> 5) < jw && (t & 31) < jw; },
+        [&](int t) { return F[(int64_t)(j0 + (t >> 5)) * m + j0 + (t & 31)]; },
+        [&](int t, V v) { dblk[t & 31][t >> 5] = v; });
     __syncthreads();
     if (wid == 0) {
       V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
@@ -814,10 +841,10 @@ __global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Ve
   for (int jend = p; jend > 0; jend -= 32) {
     const int j0 = max(0, jend - 32);
     const int jw = jend - j0;
-    for (int t = tid; t < 32 * 32; t += blockDim.x) {
-      const int jj = t >> 5, ii = t & 31;
-      if (jj < jw && ii < jw) dblk[ii][jj] = F[(int64_t)(j0 + jj) * m + j0 + ii];
-    }
+    staged_copy<sizeof(R) == 4 ? 8 : 4>(
+        32 * 32, [&](int t) { return (t >> 5) < jw && (t & 31) < jw; },
+        [&](int t) { return F[(int64_t)(j0 + (t >> 5)) * m + j0 + (t & 31)]; },
+        [&](int t, V v) { dblk[t & 31][t >> 5] = v; });
     __syncthreads();
     if (wid == 0) {
       V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
