@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -115,7 +116,14 @@ int elp_model_analyse(elp_model* h) {
   int rc;
   if (!m.sym) {  // host phase; kept when the device step below fails
     std::unique_ptr<Symbolic> s(new Symbolic());
-    rc = symbolic_analyse(m, *s, 128);
+    // leaves of the nested dissection: subsets of at most this many DOFs
+    // (ELP_LEAF, default 128)
+    static const int leaf = [] {
+      const char* e = getenv("ELP_LEAF");
+      const int v = e ? atoi(e) : 128;
+      return v < 8 ? 8 : v;
+    }();
+    rc = symbolic_analyse(m, *s, leaf);
     if (rc) return rc;
     m.sym = std::move(s);
   }

@@ -1274,6 +1274,15 @@ int device_upload_symbolic(Model& m) {
   return ELP_OK;
 }
 
+int pack_max_count() {
+  static const int v = [] {
+    const char* e = getenv("ELP_PACK_COUNT");
+    const int c = e ? atoi(e) : 8;
+    return c < 0 ? 0 : c;
+  }();
+  return v;
+}
+
 constexpr int kGmresRestart = 24;  // GMRES(24) of the mixed path
 
 // Device bytes of the workspace `workspace_ensure` (+ the GMRES buffers of the

@@ -140,7 +140,13 @@ struct DeviceSymbolic {
 
 // The packed-operand Schur update pays off for the few, large fronts at the
 // top of the tree; lower levels keep the converter kernel.
-inline bool packed_schur_level(const DeviceSymbolic::Level& L) { return L.count <= 8 && L.max_b >= 1024; }
+// Levels whose Schur update runs from packed operands (k_pack_schur + k_schur_tc):
+// few large fronts. pack_max_count(): fronts per level up to which a level with
+// borders of 1024+ rows is packed (ELP_PACK_COUNT, default 8).
+int pack_max_count();
+inline bool packed_schur_level(const DeviceSymbolic::Level& L) {
+  return L.count <= pack_max_count() && L.max_b >= 1024;
+}
 
 struct Workspace {
   int precision = 0;              // ELP_FP64_PLAIN / ELP_MIXED
