@@ -55,7 +55,9 @@ def library_path() -> str:
 # ---------------------------------------------------------------- ctypes mirror of the header
 class _Material(C.Structure):
     _fields_ = [("kind", C.c_int), ("E", C.c_double), ("nu", C.c_double), ("rho", C.c_double),
-                ("t", C.c_double), ("eta", C.c_double), ("visco_type", C.c_int), ("c", C.c_double)]
+                ("t", C.c_double), ("eta", C.c_double), ("visco_type", C.c_int), ("c", C.c_double),
+                ("n_E_table", C.c_int), ("E_table", C.POINTER(C.c_double)),
+                ("n_eta_table", C.c_int), ("eta_table", C.POINTER(C.c_double))]
 
 
 class _Block(C.Structure):
@@ -182,7 +184,8 @@ class ModelDesc:
     """
     node_ids: np.ndarray
     coords: np.ndarray
-    materials: list = field(default_factory=list)     # dicts: kind, E, nu, rho, t, eta, visco_type, c
+    materials: list = field(default_factory=list)     # dicts: kind, E, nu, rho, t, eta, visco_type, c,
+                                                      # optional E_table / eta_table: rows (Hz, value)
     blocks: list = field(default_factory=list)        # (type, material index, conn[ne, npe])
     interfaces: dict | None = None                    # ori[q], snodes[q,4], fnodes[q,4], fmat[q]
     fixed: dict | None = None                         # node[k], dof[k], value[k] complex
@@ -204,10 +207,19 @@ class _DescHolder:
         self.ids = np.ascontiguousarray(d.node_ids, dtype=np.int64)
         self.xyz = np.ascontiguousarray(d.coords, dtype=np.float64).reshape(-1)
         mats = (_Material * max(1, len(d.materials)))()
+        self.tables = []
         for i, m in enumerate(d.materials):
             mats[i] = _Material(int(m["kind"]), float(m.get("E", 0.0)), float(m.get("nu", 0.0)),
                                 float(m.get("rho", 0.0)), float(m.get("t", 0.0)), float(m.get("eta", 0.0)),
                                 int(m.get("visco_type", 1)), float(m.get("c", 0.0)))
+            for key in ("E_table", "eta_table"):
+                tab = m.get(key)
+                if tab is None or len(tab) == 0:
+                    continue
+                tab = np.ascontiguousarray(np.asarray(tab, dtype=np.float64).reshape(-1, 2))
+                self.tables.append(tab)
+                setattr(mats[i], "n_" + key, int(tab.shape[0]))
+                setattr(mats[i], key, tab.ctypes.data_as(C.POINTER(C.c_double)))
         self.mats = mats
         self.conns = []
         blocks = (_Block * max(1, len(d.blocks)))()

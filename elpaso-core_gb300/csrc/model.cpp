@@ -65,10 +65,43 @@ const int* element_dofs(int type) {
   return nullptr;
 }
 
+// Value of a (w, value) table at w: the first / last value outside the table,
+// linear interpolation between the two rows around w inside
+// (cMaterialStructureVisco::updateMaterial, materialstructurevisco.cpp:229-281).
+static double table_value(const std::vector<double>& om, const std::vector<double>& val, double w) {
+  const size_t n = om.size();
+  if (w <= om[0]) return val[0];
+  if (w >= om[n - 1]) return val[n - 1];
+  size_t k = 1;
+  while (!(om[k - 1] <= w && om[k] > w)) ++k;  // ascending table: exactly one interval holds w
+  return (val[k] - val[k - 1]) * (w - om[k - 1]) / (om[k] - om[k - 1]) + val[k - 1];
+}
+
 cplx group_coefficient(const StructGroup& g, double w) {
-  if (g.visco_type == 1) return cplx(1.0, g.eta);
-  if (g.visco_type == 2) return cplx(1.0, w * g.eta);
-  return cplx(1.0, 0.0);
+  const double scale = g.om_e.empty() ? 1.0 : table_value(g.om_e, g.val_e, w) / g.e_ref;
+  const double eta = g.om_eta.empty() ? g.eta : table_value(g.om_eta, g.val_eta, w);
+  if (g.visco_type == 1) return scale * cplx(1.0, eta);
+  if (g.visco_type == 2) return scale * cplx(1.0, w * eta);
+  return cplx(scale, 0.0);
+}
+
+// Copies a caller's (frequency [Hz], value) table into (w, value) vectors.
+static bool copy_table(int n, const double* tab, std::vector<double>& om, std::vector<double>& val,
+                       std::string& err, const char* what) {
+  om.clear();
+  val.clear();
+  if (n <= 0) return true;
+  if (!tab) { err = std::string(what) + " table pointer is null"; return false; }
+  for (int k = 0; k < n; ++k) {
+    const double f = tab[2 * k], v = tab[2 * k + 1];
+    if (!std::isfinite(f) || !std::isfinite(v) || (k > 0 && !(f > tab[2 * (k - 1)]))) {
+      err = std::string(what) + " table needs finite values at strictly increasing frequencies";
+      return false;
+    }
+    om.push_back(2.0 * M_PI * f);
+    val.push_back(v);
+  }
+  return true;
 }
 
 static bool is_structure_type(int t) { return t == ELP_BRICK8 || t == ELP_DSG4; }
@@ -82,6 +115,24 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
   m.coords.assign(d->coords, d->coords + 3 * d->n_nodes);
   if (d->n_materials < 0 || (d->n_materials > 0 && !d->materials)) { err = "bad materials"; return ELP_ERR_ARG; }
   m.materials.assign(d->materials, d->materials + d->n_materials);
+  // frequency tables: copied here, the caller's pointers are not kept
+  std::vector<StructGroup> tables(m.materials.size());
+  for (size_t i = 0; i < m.materials.size(); ++i) {
+    elp_material& mt = m.materials[i];
+    const bool any = mt.n_E_table > 0 || mt.n_eta_table > 0;
+    if (any && mt.kind != ELP_STR_LIN_VIS_ISO_DIR) { err = "frequency tables need a visco material"; return ELP_ERR_ARG; }
+    if (!copy_table(mt.n_E_table, mt.E_table, tables[i].om_e, tables[i].val_e, err, "E") ||
+        !copy_table(mt.n_eta_table, mt.eta_table, tables[i].om_eta, tables[i].val_eta, err, "eta"))
+      return ELP_ERR_ARG;
+    if (!tables[i].om_e.empty() && mt.E == 0.0) mt.E = tables[i].val_e[0];
+    tables[i].e_ref = mt.E;
+    if (!tables[i].om_e.empty() && !(mt.E != 0.0 && std::isfinite(mt.E))) {
+      err = "E table needs a nonzero reference modulus";
+      return ELP_ERR_ARG;
+    }
+    mt.n_E_table = mt.n_eta_table = 0;
+    mt.E_table = mt.eta_table = nullptr;
+  }
   for (auto& mt : m.materials) {
     if (mt.kind != ELP_STR_LIN_ELA_ISO_DIR && mt.kind != ELP_STR_LIN_VIS_ISO_DIR &&
         mt.kind != ELP_AF_LIN_UAF_ISO_DIR) { err = "unknown material kind"; return ELP_ERR_ARG; }
@@ -182,12 +233,15 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
     for (size_t i = 0; i < m.materials.size(); ++i) {
       const elp_material& mt = m.materials[i];
       if (mt.kind == ELP_AF_LIN_UAF_ISO_DIR) continue;
-      StructGroup g{mt.kind == ELP_STR_LIN_VIS_ISO_DIR ? mt.visco_type : 0,
-                    mt.kind == ELP_STR_LIN_VIS_ISO_DIR ? mt.eta : 0.0};
-      if (g.visco_type != 0 && g.eta == 0.0) g.visco_type = 0;
+      StructGroup g = tables[i];
+      g.visco_type = mt.kind == ELP_STR_LIN_VIS_ISO_DIR ? mt.visco_type : 0;
+      g.eta = mt.kind == ELP_STR_LIN_VIS_ISO_DIR ? mt.eta : 0.0;
+      if (g.visco_type != 0 && g.eta == 0.0 && !g.tabulated()) g.visco_type = 0;
       int found = -1;
-      for (size_t j = 0; j < m.groups.size(); ++j)
-        if (m.groups[j].visco_type == g.visco_type && m.groups[j].eta == g.eta) found = (int)j;
+      if (!g.tabulated())  // a tabulated material is a group of its own
+        for (size_t j = 0; j < m.groups.size(); ++j)
+          if (!m.groups[j].tabulated() && m.groups[j].visco_type == g.visco_type && m.groups[j].eta == g.eta)
+            found = (int)j;
       if (found < 0) { found = (int)m.groups.size(); m.groups.push_back(g); count.push_back(0); }
       m.material_group[i] = found;
     }
@@ -205,6 +259,10 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
       }
     }
     if (m.groups.empty()) m.groups.push_back(StructGroup{0, 0.0});
+    if (m.groups.size() > (size_t)kMaxStructGroups) {
+      err = "more than " + std::to_string(kMaxStructGroups) + " distinct structure loss-factor groups";
+      return ELP_ERR_ARG;
+    }
   }
 
   // ---- node -> incident elements (per block), CSR

@@ -34,10 +34,17 @@ constexpr uint8_t CLS_BC_COLUMN = 0x80;
 constexpr uint8_t CLS_MASK = 0x7f;
 
 // Loss-factor group of the structure stiffness: coefficient c_g(w).
+// Materials with frequency tables form groups of their own:
+// c_g(w) = E(w) / e_ref * (1 + i eta(w)) or (1 + i w eta(w)).
 struct StructGroup {
   int visco_type;  // 0 elastic, 1: 1 + i eta, 2: 1 + i w eta
   double eta;
+  double e_ref = 0.0;                 // modulus the stiffness was assembled with (tables only)
+  std::vector<double> om_e, val_e;    // E(w) table (w = 2 pi f), ascending
+  std::vector<double> om_eta, val_eta;
+  bool tabulated() const { return !om_e.empty() || !om_eta.empty(); }
 };
+constexpr int kMaxStructGroups = 8;  // groups a model may have (value arrays VK + 7 VKg)
 
 int nodes_per_element(int type);
 int dofs_per_node(int type);

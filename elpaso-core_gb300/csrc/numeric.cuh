@@ -9,7 +9,7 @@
 
 namespace elp {
 
-constexpr int kMaxGroups = 8;    // structure loss-factor groups supported per model
+constexpr int kMaxGroups = kMaxStructGroups;  // structure loss-factor groups supported per model
 constexpr int kMaxSlots = 64;    // frequencies factorised together
 
 // per-slot coefficients of the value arrays

@@ -9,11 +9,16 @@ path (``ESC/misc/parser/femparserhdf5.cpp:202-499``; group names from
   ``ElementType`` (DSG4 / Brick8 / Fluid8) and ``MaterialId``;
 * ``/Materials/*``: attributes ``Id``, ``MaterialType`` and the parameters as
   strings (``E``, ``nu``, ``rho``, ``t``, ``eta``, ``type``, ``c``;
-  ``ESC/misc/hdf5/rulesh5.h:112-141``);
+  ``ESC/misc/hdf5/rulesh5.h:112-141``); a visco material's ``E`` or ``eta``
+  that is not a number (``isnumber``, ``ESC/basics/misc.cpp:22-45``) names a
+  dataset of rows (frequency [Hz], value): the frequency table
+  (``materialstructurevisco.cpp:75-170, 643-690``);
 * ``/NodeConstraints/*``: structural constraints with flags ``u1..u3``,
   ``w1..w3`` and values ``valu*``/``valw*`` (reference DOF enum 0..5);
 * ``/NodeLoads/*``: ``point_force`` loads ``Fx, Fy, Fz`` at ``NodeId``;
-* ``/Analysis`` attributes ``start``, ``steps``, ``delta``: the frequency list.
+* ``/Analysis`` attributes ``start``, ``steps``, ``delta``: the frequency list,
+  unless a ``<input file>.frq`` list exists beside the file
+  (``generateFrequencies``, ``analysisfrequencybasic.cpp:36-72``).
 
 and the solution file elpasoC writes (``ESC/analysis/frequency/
 analysisfrequencybasic.cpp:184-262``): ``/Solution/State/vecFemStep{k}``
@@ -53,6 +58,53 @@ def _num(attrs, key, default=0.0):
     return float(v) if not isinstance(v, str) or v.strip() else default
 
 
+def _is_number(s: str) -> bool:
+    """The reference's isnumber (ESC/basics/misc.cpp:22-45): digits, at most one
+    '.', at most one 'e'/'E', a sign only first or right after 'e'/'E'."""
+    points = exps = 0
+    for i, ch in enumerate(s):
+        if ch in "+-" and (i == 0 or s[i - 1] in "eE"):
+            continue
+        if ch == ".":
+            points += 1
+        elif ch in "eE":
+            exps += 1
+        elif not ch.isdigit():
+            return False
+    return points <= 1 and exps <= 1
+
+
+def _num_or_table(f, attrs, key):
+    """(value, table): a number, or a dataset named by the attribute holding
+    rows (frequency [Hz], value) (cReaderH5::readDenseDoubleMatrix, first two
+    columns)."""
+    v = attrs.get(key, 0.0)
+    if isinstance(v, str):
+        v = v.strip()
+        if v and not _is_number(v):
+            t = np.asarray(f[v.lstrip("/")].read(), dtype=np.float64)
+            return 0.0, t.reshape(t.shape[0], -1)[:, :2].copy()
+        return (float(v) if v else 0.0), None
+    return float(v), None
+
+
+def frequency_list(input_path: str, start: float, delta: float, steps: int) -> np.ndarray:
+    """Frequencies [Hz] of a run (generateFrequencies,
+    analysisfrequencybasic.cpp:36-72): the numbers of ``<input>.frq`` (a trailing
+    ``.ak3`` of the input name removed first) if that file exists, else
+    start + delta * step for step < steps; sorted and unique either way (a
+    std::set). A token that is not a number ends the reference's read loop
+    without reaching end-of-file; here it raises ValueError."""
+    name = input_path[:-4] if input_path.endswith(".ak3") else input_path
+    frq = name + ".frq"
+    if os.path.exists(frq):
+        with open(frq) as fh:
+            vals = [float(tok) for tok in fh.read().split()]
+    else:
+        vals = [start + delta * k for k in range(int(steps))]
+    return np.unique(np.asarray(vals, dtype=np.float64))
+
+
 def read_model(path: str, model_desc_cls=None):
     """Reads an elpasoC model file. Returns (ModelDesc, frequencies in Hz)."""
     if model_desc_cls is None:
@@ -72,8 +124,15 @@ def read_model(path: str, model_desc_cls=None):
         if kind is None:
             raise NotImplementedError(f"material type {a['MaterialType']}")
         mat_index[int(a["Id"])] = len(mats)
-        mats.append(dict(kind=kind, E=_num(a, "E"), nu=_num(a, "nu"), rho=_num(a, "rho"), t=_num(a, "t"),
-                         eta=_num(a, "eta"), visco_type=int(_num(a, "type", 1.0)) or 1, c=_num(a, "c")))
+        E, E_table = _num_or_table(f, a, "E") if kind == 2 else (_num(a, "E"), None)
+        eta, eta_table = _num_or_table(f, a, "eta") if kind == 2 else (_num(a, "eta"), None)
+        mat = dict(kind=kind, E=E, nu=_num(a, "nu"), rho=_num(a, "rho"), t=_num(a, "t"),
+                   eta=eta, visco_type=int(_num(a, "type", 1.0)) or 1, c=_num(a, "c"))
+        if E_table is not None:
+            mat["E_table"] = E_table
+        if eta_table is not None:
+            mat["eta_table"] = eta_table
+        mats.append(mat)
 
     blocks = []
     for name in sorted(f["Elements"].keys(), key=lambda s: int("".join(c for c in s if c.isdigit()) or 0)):
@@ -110,7 +169,7 @@ def read_model(path: str, model_desc_cls=None):
             lf.append([float(a["Fx"]), float(a["Fy"]), float(a["Fz"])])
 
     an = f["Analysis"].attrs
-    freqs = float(an["start"]) + float(an["delta"]) * np.arange(int(an["steps"]))
+    freqs = frequency_list(path, float(an["start"]), float(an["delta"]), int(an["steps"]))
     desc = model_desc_cls(
         node_ids=ids, coords=coords, materials=mats, blocks=blocks,
         fixed=dict(node=np.array(fnode, np.int64), dof=np.array(fdof, np.int64), value=np.array(fval, complex)),

@@ -76,6 +76,17 @@ typedef struct {
   double eta;      /* loss factor (visco)                                     */
   int visco_type;  /* 1: E(1+i eta), 2: E(1+i w eta) (materialstructurevisco.cpp:284-285) */
   double c;        /* speed of sound (fluid)                                  */
+  /* Frequency-dependent E and eta of a visco material, as the reference reads
+   * them from a file or dataset of rows (frequency [Hz], value)
+   * (materialstructurevisco.cpp:75-170) and interpolates linearly in w, held
+   * constant outside the table (updateMaterial, :229-287). n = 0: the scalar
+   * E / eta above. With an E table, E above is the modulus the stiffness is
+   * assembled with (0: the table's first value); the per-w coefficient is
+   * E(w) / E. Rows in ascending frequency; the tables are copied. */
+  int n_E_table;
+  const double* E_table;   /* n_E_table x 2, row-major                        */
+  int n_eta_table;
+  const double* eta_table; /* n_eta_table x 2, row-major                      */
 } elp_material;
 
 typedef struct {

@@ -14,8 +14,11 @@ elpasoCore/source/ of the reference):
   RHS            analysis/analysis.cpp:171-279 (nodal forces, ADD)
   values         element matrices EM(w) of oracle/elp_oracle.c, inserted per
                  element, interfaces with -ori (analysisfrequencybasic.cpp:101-157)
-  solve          SciPy SuperLU, complex128 (stand-in for MUMPS, which is not
-                 available here) -- the FP64 direct-solve oracle
+  materials      E_vis(w), E and eta from frequency tables where given
+                 (material/.../viscoelastic/materialstructurevisco.cpp:229-287)
+  solve          SciPy SuperLU, complex128, on the system with the Dirichlet
+                 columns lifted to the right-hand side (stand-in for MUMPS,
+                 which is not available here) -- the FP64 direct-solve oracle
 
 The element restatement itself is pinned against the reference's own
 element code compiled from its sources (oracle/_ref, tests/golden/).
@@ -103,12 +106,34 @@ def interface_mindlin(xyz_fluid, transform=False):
     return Cm.view(np.complex128).reshape(12, 4)
 
 
+def table_value(table, omega):
+    """A frequency table at angular frequency omega, by the rule of
+    cMaterialStructureVisco::updateMaterial (materialstructurevisco.cpp:229-281):
+    rows (frequency [Hz], value) are read as (2 pi f, value)
+    (readEFromFile / readEtaFromFile, :75-170); at or below the first row the
+    first value, at or above the last row the last value, otherwise linear
+    interpolation between the rows k-1, k with w_{k-1} <= omega < w_k."""
+    t = np.asarray(table, dtype=np.float64).reshape(-1, 2)
+    om, v = 2.0 * np.pi * t[:, 0], t[:, 1]
+    if omega <= om[0]:
+        return v[0]
+    if omega >= om[-1]:
+        return v[-1]
+    for k in range(1, len(om)):
+        if om[k - 1] <= omega < om[k]:
+            return ((v[k] - v[k - 1]) * (omega - om[k - 1]) / (om[k] - om[k - 1])) + v[k - 1]
+    raise ValueError("frequency table not ascending")
+
+
 def e_vis(mat, omega):
-    """E_vis of materialstructurevisco.cpp:284-285, real E for the elastic kind."""
+    """E_vis of materialstructurevisco.cpp:284-285 (E and eta from their
+    frequency tables when the material has them), real E for the elastic kind."""
     if mat["kind"] == VIS:
+        E = table_value(mat["E_table"], omega) if len(mat.get("E_table", ())) else mat["E"]
+        eta = table_value(mat["eta_table"], omega) if len(mat.get("eta_table", ())) else mat["eta"]
         if int(mat.get("visco_type", 1)) == 2:
-            return mat["E"] * (1.0 + 1j * omega * mat["eta"])
-        return mat["E"] * (1.0 + 1j * mat["eta"])
+            return E * (1.0 + 1j * omega * eta)
+        return E * (1.0 + 1j * eta)
     return complex(mat["E"])
 
 

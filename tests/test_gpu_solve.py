@@ -87,3 +87,21 @@ def test_batch_result_equals_single(elp, meshes):
     for k, om in enumerate(oms):
         xs, _ = m.solve([om], precision=1)
         assert np.array_equal(xs[0], xb[k])
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("visco_type", [1, 2])
+def test_visco_frequency_tables(elp, meshes, oracle, prec, visco_type):
+    """E(f) and eta(f) tables (materialstructurevisco.cpp:229-287): the device
+    scales the assembled stiffness by E(w)/E_ref (1 + i eta(w)) per w; the
+    oracle's matrix takes E_vis(w) per element. Frequencies below, inside and
+    above the tables, where the FP64 floor eps || |A| |x| || / ||f|| of this
+    plate is at most 4e-11 (at 310-450 Hz it is 1e-10 to 5e-10: no FP64
+    solution, the oracle's included, reaches 1e-10 there)."""
+    import copy
+    d = copy.deepcopy(meshes.solid_plate(10, 10, 2))
+    d.materials[0].update(visco_type=visco_type,
+                          E_table=np.array([[50.0, 200e9], [150.0, 230e9], [300.0, 180e9]]),
+                          eta_table=np.array([[20.0, 0.01], [200.0, 0.05]]) / ([1.0, 1.0] if visco_type == 1 else
+                                                                              [1.0, 2 * np.pi * 100.0]))
+    check(elp, oracle, d, [10.0, 90.0, 175.0, 700.0], prec)
