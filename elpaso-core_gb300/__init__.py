@@ -78,13 +78,28 @@ class _Force(C.Structure):
     _fields_ = [("node", C.c_int32), ("f", C.c_double * 3)]
 
 
+class _Moment(C.Structure):
+    _fields_ = [("node", C.c_int32), ("m", C.c_double * 3)]
+
+
+class _FluidSource(C.Structure):
+    _fields_ = [("node", C.c_int32), ("p", C.c_double)]
+
+
+class _VnLoad(C.Structure):
+    _fields_ = [("block", C.c_int32), ("face", C.c_int32), ("element", C.c_int64), ("vn", C.c_double)]
+
+
 class _Desc(C.Structure):
     _fields_ = [("n_nodes", C.c_int64), ("node_ids", C.POINTER(C.c_int64)), ("coords", C.POINTER(C.c_double)),
                 ("n_materials", C.c_int), ("materials", C.POINTER(_Material)),
                 ("n_blocks", C.c_int), ("blocks", C.POINTER(_Block)),
                 ("n_interfaces", C.c_int64), ("interfaces", C.POINTER(_Interface)),
                 ("n_fixed", C.c_int64), ("fixed", C.POINTER(_Fixed)),
-                ("n_forces", C.c_int64), ("forces", C.POINTER(_Force))]
+                ("n_forces", C.c_int64), ("forces", C.POINTER(_Force)),
+                ("n_moments", C.c_int64), ("moments", C.POINTER(_Moment)),
+                ("n_fluid_sources", C.c_int64), ("fluid_sources", C.POINTER(_FluidSource)),
+                ("n_vn_loads", C.c_int64), ("vn_loads", C.POINTER(_VnLoad))]
 
 
 class _Info(C.Structure):
@@ -117,6 +132,7 @@ class RequestResult(C.Structure):
 EXPORTS = [
     "elp_model_create", "elp_model_assemble", "elp_model_analyse", "elp_model_get_info",
     "elp_model_pattern", "elp_model_global_rows", "elp_model_system_values", "elp_model_rhs",
+    "elp_model_rhs_omega",
     "elp_solve", "elp_model_destroy", "elp_last_error", "elp_solve_device", "elp_model_time_assembly",
     "elp_server_create", "elp_server_add_model", "elp_server_submit", "elp_server_wait",
     "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc",
@@ -147,6 +163,7 @@ def load_library(path: str | None = None):
     lib.elp_model_global_rows.argtypes = [P, P]
     lib.elp_model_system_values.argtypes = [P, C.c_double, P]
     lib.elp_model_rhs.argtypes = [P, P]
+    lib.elp_model_rhs_omega.argtypes = [P, C.c_double, P]
     lib.elp_solve.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_double]
     lib.elp_solve_device.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_double, P]
     lib.elp_model_time_assembly.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -190,6 +207,9 @@ class ModelDesc:
     interfaces: dict | None = None                    # ori[q], snodes[q,4], fnodes[q,4], fmat[q]
     fixed: dict | None = None                         # node[k], dof[k], value[k] complex
     forces: dict | None = None                        # node[k], f[k,3]
+    moments: dict | None = None                       # node[k], m[k,3] (on w1 w2 w3)
+    fluid_sources: dict | None = None                 # node[k], p[k] (F += 4 pi p on the fluid row)
+    vn_loads: dict | None = None                      # block[k], element[k], face[k] (1..6), vn[k]
     name: str = "model"
 
     @property
@@ -250,9 +270,27 @@ class _DescHolder:
             for j in range(3):
                 fo[k].f[j] = float(d.forces["f"][k][j])
         self.fo = fo
+        nm = 0 if d.moments is None else len(d.moments["node"])
+        mo = (_Moment * max(1, nm))()
+        for k in range(nm):
+            mo[k].node = int(d.moments["node"][k])
+            for j in range(3):
+                mo[k].m[j] = float(d.moments["m"][k][j])
+        self.mo = mo
+        ns = 0 if d.fluid_sources is None else len(d.fluid_sources["node"])
+        so = (_FluidSource * max(1, ns))()
+        for k in range(ns):
+            so[k] = _FluidSource(int(d.fluid_sources["node"][k]), float(d.fluid_sources["p"][k]))
+        self.so = so
+        nv = 0 if d.vn_loads is None else len(d.vn_loads["element"])
+        vl = (_VnLoad * max(1, nv))()
+        for k in range(nv):
+            vl[k] = _VnLoad(int(d.vn_loads["block"][k]), int(d.vn_loads["face"][k]), int(d.vn_loads["element"][k]),
+                            float(d.vn_loads["vn"][k]))
+        self.vl = vl
         self.desc = _Desc(len(self.ids), self.ids.ctypes.data_as(C.POINTER(C.c_int64)),
                           self.xyz.ctypes.data_as(C.POINTER(C.c_double)), len(d.materials), mats,
-                          len(d.blocks), blocks, nq, ifs, nf, fx, nl, fo)
+                          len(d.blocks), blocks, nq, ifs, nf, fx, nl, fo, nm, mo, ns, so, nv, vl)
 
 
 class Model:
@@ -314,9 +352,13 @@ class Model:
         _check(self.lib.elp_model_system_values(self.handle, float(omega), _ptr(out)))
         return out.view(np.complex128)
 
-    def rhs(self) -> np.ndarray:
+    def rhs(self, omega: float | None = None) -> np.ndarray:
+        """F without omega (the w-independent part), F(omega) with it."""
         out = np.zeros(2 * self.n, np.float64)
-        _check(self.lib.elp_model_rhs(self.handle, _ptr(out)))
+        if omega is None:
+            _check(self.lib.elp_model_rhs(self.handle, _ptr(out)))
+        else:
+            _check(self.lib.elp_model_rhs_omega(self.handle, float(omega), _ptr(out)))
         return out.view(np.complex128)
 
     def time_assembly(self, repeats: int = 3):

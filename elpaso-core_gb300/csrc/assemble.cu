@@ -545,6 +545,10 @@ int device_upload_model(Model& m) {
   std::vector<double> rhs(2 * m.n);
   for (int64_t i = 0; i < m.n; ++i) { rhs[2 * i] = m.rhs[i].real(); rhs[2 * i + 1] = m.rhs[i].imag(); }
   ELP_CUDA(D.rhs.upload(rhs));
+  if (m.has_vn) {
+    for (int64_t i = 0; i < m.n; ++i) { rhs[2 * i] = m.rhs_vn[i].real(); rhs[2 * i + 1] = m.rhs_vn[i].imag(); }
+    ELP_CUDA(D.rhs_vn.upload(rhs));
+  }
   ELP_CUDA(D.bc_rows.upload(m.bc_rows));
   // element lists per type
   std::vector<int32_t> bc, pc, fc;

@@ -186,6 +186,22 @@ int elp_model_rhs(const elp_model* h, double* f_out) {
   GUARD_END
 }
 
+int elp_model_rhs_omega(const elp_model* h, double omega, double* f_out) {
+  GUARD_BEGIN
+  if (!h || !f_out) { set_error("null argument"); return ELP_ERR_ARG; }
+  if (!(omega > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
+  const Model& m = h->m;
+  const double iw = 1.0 / omega;
+  for (int64_t i = 0; i < m.n; ++i) {
+    cplx v = m.rhs[i];
+    if (m.has_vn && m.rhs_vn[i] != 0.0) v += m.rhs_vn[i] * iw;
+    f_out[2 * i] = v.real();
+    f_out[2 * i + 1] = v.imag();
+  }
+  return ELP_OK;
+  GUARD_END
+}
+
 int elp_model_system_values(elp_model* h, double omega, double* values_out) {
   GUARD_BEGIN
   if (!h || !values_out) { set_error("null argument"); return ELP_ERR_ARG; }

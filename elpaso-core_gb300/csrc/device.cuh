@@ -66,6 +66,7 @@ struct DeviceModel {
   DevBuf<double> VK, VM;           // nnz each
   DevBuf<double> VKg;              // (G - 1) x nnz extra structure groups
   DevBuf<double> rhs;              // 2 n
+  DevBuf<double> rhs_vn;           // 2 n: G of F(w) = rhs + G / w (allocated when the model has such loads)
   DevBuf<int32_t> bc_rows;
   // element work lists
   DevBuf<int32_t> brick_conn, plate_conn, fluid_conn;   // 8 / 4 / 8 node indices

@@ -17,7 +17,10 @@
 //  - BC rows: nodes in id order, each BC of the node, DOFs 0..20 that are
 //    active and fixed (analysis.cpp:366-414); MatZeroRows(diag = 1) and
 //    F[row] = value (analysis.cpp:419-454);
-//  - nodal forces add F on active x1, x2, x3 rows (analysis.cpp:171-279).
+//  - nodal forces add F on active x1, x2, x3 rows (analysis.cpp:171-279),
+//    fluid point sources 4 pi p on the fluid row, nodal moments on w1..w3
+//    (analysis.cpp:243-265, 281-364); normal-velocity loads on Fluid8 faces
+//    form the 1/w part of F (elementfluid3d.cpp:241-309).
 #include "model.hpp"
 
 #include <algorithm>
@@ -106,6 +109,45 @@ static bool copy_table(int n, const double* tab, std::vector<double>& om, std::v
 
 static bool is_structure_type(int t) { return t == ELP_BRICK8 || t == ELP_DSG4; }
 
+// The four nodes of face f (0..5) of a hexahedron, cShapeHex8's surfaces with
+// outward normals (shapehex8.cpp:119-150).
+static void face_nodes_hex8(int f, const int32_t* en, int32_t* out) {
+  static const int kFace[6][4] = {{0, 1, 5, 4}, {2, 3, 7, 6}, {0, 3, 2, 1},
+                                  {1, 2, 6, 5}, {4, 5, 6, 7}, {0, 4, 7, 3}};
+  for (int k = 0; k < 4; ++k) out[k] = en[kFace[f][k]];
+}
+
+// int_face N_z dA of the bilinear face shape functions, 2 x 2 Gauss points,
+// surface Jacobian |a1 x a2| from the tangents a1 = dx/dxi, a2 = dx/deta
+// (evaluateSurfaceIntegral, elementfluid3d.cpp:169-233: the load is
+// sum_s C(z, s) vn with C(z, s) = int N_z N_s dA, and sum_s N_s = 1).
+// False if the Jacobian is not positive at a Gauss point.
+static bool face_shape_integrals(const Model& m, const int32_t* fn, double* nint) {
+  const double g = 1.0 / std::sqrt(3.0);
+  const double xi[4] = {-1.0, 1.0, 1.0, -1.0}, et[4] = {-1.0, -1.0, 1.0, 1.0};  // quad4 node corners
+  for (int z = 0; z < 4; ++z) nint[z] = 0.0;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      const double u = (a ? g : -g), v = (b ? g : -g);
+      double a1[3] = {0, 0, 0}, a2[3] = {0, 0, 0}, N[4];
+      for (int k = 0; k < 4; ++k) {
+        N[k] = 0.25 * (1.0 + xi[k] * u) * (1.0 + et[k] * v);
+        const double dxi = 0.25 * xi[k] * (1.0 + et[k] * v), det = 0.25 * et[k] * (1.0 + xi[k] * u);
+        for (int d3 = 0; d3 < 3; ++d3) {
+          a1[d3] += dxi * m.coords[3 * (size_t)fn[k] + d3];
+          a2[d3] += det * m.coords[3 * (size_t)fn[k] + d3];
+        }
+      }
+      const double s11 = a1[0] * a1[0] + a1[1] * a1[1] + a1[2] * a1[2];
+      const double s22 = a2[0] * a2[0] + a2[1] * a2[1] + a2[2] * a2[2];
+      const double s12 = a1[0] * a2[0] + a1[1] * a2[1] + a1[2] * a2[2];
+      const double jac = std::sqrt(s11 * s22 - s12 * s12);
+      if (!(jac > 0.0)) return false;
+      for (int z = 0; z < 4; ++z) nint[z] += N[z] * jac;  // Gauss weights 1
+    }
+  return true;
+}
+
 int build_model(const elp_model_desc* d, Model& m, std::string& err) {
   if (!d) { err = "null model description"; return ELP_ERR_ARG; }
   if (d->n_nodes <= 0 || !d->coords || !d->node_ids) { err = "model has no nodes"; return ELP_ERR_ARG; }
@@ -180,6 +222,30 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
     m.forces.assign(d->forces, d->forces + d->n_forces);
     for (auto& f : m.forces)
       if (f.node < 0 || f.node >= d->n_nodes) { err = "force node out of range"; return ELP_ERR_ARG; }
+  }
+  if (d->n_moments > 0) {
+    if (!d->moments) { err = "bad moments"; return ELP_ERR_ARG; }
+    m.moments.assign(d->moments, d->moments + d->n_moments);
+    for (auto& f : m.moments)
+      if (f.node < 0 || f.node >= d->n_nodes) { err = "moment node out of range"; return ELP_ERR_ARG; }
+  }
+  if (d->n_fluid_sources > 0) {
+    if (!d->fluid_sources) { err = "bad fluid sources"; return ELP_ERR_ARG; }
+    m.fluid_sources.assign(d->fluid_sources, d->fluid_sources + d->n_fluid_sources);
+    for (auto& f : m.fluid_sources)
+      if (f.node < 0 || f.node >= d->n_nodes) { err = "fluid source node out of range"; return ELP_ERR_ARG; }
+  }
+  if (d->n_vn_loads > 0) {
+    if (!d->vn_loads) { err = "bad normal-velocity loads"; return ELP_ERR_ARG; }
+    m.vn_loads.assign(d->vn_loads, d->vn_loads + d->n_vn_loads);
+    for (auto& l : m.vn_loads) {
+      if (l.block < 0 || l.block >= (int)m.blocks.size() || m.blocks[l.block].type != ELP_FLUID8 ||
+          l.element < 0 || l.element >= m.blocks[l.block].n_elements || l.face < 1 || l.face > 6 ||
+          !std::isfinite(l.vn)) {
+        err = "normal-velocity load needs a Fluid8 element, a face 1..6 and a finite value";
+        return ELP_ERR_ARG;
+      }
+    }
   }
 
   const int64_t N = m.n_nodes;
@@ -402,7 +468,44 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
           if (g >= 0) m.rhs[g] += cplx(m.forces[fi].f[d3], 0.0);
         }
     }
-    for (size_t i = 0; i < m.bc_rows.size(); ++i) m.rhs[m.bc_rows[i]] = m.bc_values[i];
+    // nodal moments on the active rotations w1 w2 w3 (analysis.cpp:281-364),
+    // fluid point sources 4 pi p on the fluid row (analysis.cpp:243-265)
+    std::vector<std::vector<int32_t>> node_moments(N), node_sources(N);
+    for (size_t i = 0; i < m.moments.size(); ++i) node_moments[m.moments[i].node].push_back((int32_t)i);
+    for (size_t i = 0; i < m.fluid_sources.size(); ++i) node_sources[m.fluid_sources[i].node].push_back((int32_t)i);
+    for (int64_t r = 0; r < N; ++r) {
+      const int32_t v = m.order[r];
+      for (int32_t si : node_sources[v]) {
+        const int32_t g = grow(v, ELP_DOF_FLUID);
+        if (g >= 0) m.rhs[g] += cplx(4.0 * M_PI * m.fluid_sources[si].p, 0.0);
+      }
+    }
+    for (int64_t r = 0; r < N; ++r) {
+      const int32_t v = m.order[r];
+      for (int32_t mi : node_moments[v])
+        for (int d3 = 0; d3 < 3; ++d3) {
+          const int32_t g = grow(v, ELP_DOF_W1 + d3);
+          if (g >= 0) m.rhs[g] += cplx(m.moments[mi].m[d3], 0.0);
+        }
+    }
+    // normal-velocity loads: G of F(w) = rhs + G / w
+    m.rhs_vn.assign(n, cplx(0.0, 0.0));
+    for (const auto& l : m.vn_loads) {
+      const int32_t* en = &m.blocks[l.block].conn[(size_t)l.element * 8];
+      int32_t fn[4];
+      face_nodes_hex8(l.face - 1, en, fn);
+      double nint[4];
+      if (!face_shape_integrals(m, fn, nint)) { err = "normal-velocity load on a degenerate face"; return ELP_ERR_ARG; }
+      for (int z = 0; z < 4; ++z) {
+        const int32_t g = grow(fn[z], ELP_DOF_FLUID);
+        if (g >= 0) m.rhs_vn[g] += cplx(0.0, -l.vn * nint[z]);
+      }
+      m.has_vn = true;
+    }
+    for (size_t i = 0; i < m.bc_rows.size(); ++i) {
+      m.rhs[m.bc_rows[i]] = m.bc_values[i];
+      m.rhs_vn[m.bc_rows[i]] = 0.0;
+    }
   }
   return ELP_OK;
 }

@@ -73,6 +73,9 @@ struct Model {
   std::vector<elp_interface_quad> interfaces;
   std::vector<elp_fixed_dof> fixed;
   std::vector<elp_nodal_force> forces;
+  std::vector<elp_nodal_moment> moments;
+  std::vector<elp_fluid_source> fluid_sources;
+  std::vector<elp_vn_load> vn_loads;
 
   // ---- numbering (analysis.cpp:475-520)
   std::vector<int32_t> order;        // node indices by ascending id
@@ -92,7 +95,9 @@ struct Model {
   std::vector<int32_t> bc_rows;
   std::vector<cplx> bc_values;
   std::vector<uint8_t> is_bc_row;    // n
-  std::vector<cplx> rhs;             // n
+  std::vector<cplx> rhs;             // n: w-independent part
+  std::vector<cplx> rhs_vn;          // n: G of F(w) = rhs + G / w (normal-velocity loads), 0 on BC rows
+  bool has_vn = false;
 
   // ---- structure loss-factor groups
   std::vector<StructGroup> groups;   // groups[0] -> VK, groups[g>0] -> VKg[g-1]

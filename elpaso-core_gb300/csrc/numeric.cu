@@ -75,6 +75,18 @@ template <class V> __device__ __forceinline__ V cinv(V a) {
 
 // ------------------------------------------------------------- combine
 
+// F_s += G / w_s: the normal-velocity loads of each slot's right-hand side
+__global__ void k_add_vn(const double2* __restrict__ g, const Coef* __restrict__ coef, int64_t n,
+                         double2* __restrict__ f) {
+  const int s = blockIdx.y;
+  const double iw = coef[s].inv_w;
+  double2* fs = f + s * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = g[i];
+    if (v.x != 0.0 || v.y != 0.0) fs[i] = make_double2(fs[i].x + v.x * iw, fs[i].y + v.y * iw);
+  }
+}
+
 __global__ void k_dscale(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ diag,
                          int64_t n, double* __restrict__ dscale) {
   const int s = blockIdx.y;
@@ -1173,6 +1185,7 @@ Workspace::~Workspace() {
 
 void make_coef(const Model& m, double w, Coef& c) {
   memset(&c, 0, sizeof(c));
+  c.inv_w = 1.0 / w;
   cplx c0 = group_coefficient(m.groups[0], w);
   c.a[CLS_STRUCT] = make_double2(c0.real(), c0.imag());
   c.b[CLS_STRUCT] = -w * w;
@@ -1917,6 +1930,11 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
   for (int s = 0; s < n_omega; ++s) {
     const double2* src = f_dev ? f_dev + (size_t)s * n : reinterpret_cast<const double2*>(m.dev->rhs.p);
     ELP_CUDA(cudaMemcpyAsync(w.f.p + (size_t)s * n, src, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+  }
+  if (!f_dev && m.has_vn) {  // the model's F(w) = F + G / w
+    const dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 1024), n_omega);
+    PROF_LAUNCH(KC_RHS, st, k_add_vn<<<g, 256, 0, st>>>(reinterpret_cast<const double2*>(m.dev->rhs_vn.p), w.coef.p, n,
+                                                        w.f.p));
   }
   // the tensor-core timeout flag reports this batch only
   ELP_CUDA(cudaMemsetAsync(w.tc_err.p, 0, sizeof(int), st));

@@ -17,6 +17,7 @@ struct Coef {
   double2 a[3];                  // CLS_STRUCT, CLS_FLUID, CLS_COUPLE coefficient of VK
   double b[3];                   // coefficient of VM
   double2 g[kMaxGroups];         // coefficient of VKg[g - 1] (g >= 1) on structure entries
+  double inv_w;                  // 1 / w: weight of the normal-velocity loads in F(w)
 };
 
 // the w-independent value arrays of a model and the per-w combine

@@ -15,7 +15,10 @@ path (``ESC/misc/parser/femparserhdf5.cpp:202-499``; group names from
   (``materialstructurevisco.cpp:75-170, 643-690``);
 * ``/NodeConstraints/*``: structural constraints with flags ``u1..u3``,
   ``w1..w3`` and values ``valu*``/``valw*`` (reference DOF enum 0..5);
-* ``/NodeLoads/*``: ``point_force`` loads ``Fx, Fy, Fz`` at ``NodeId``;
+* ``/NodeLoads/*``: ``point_force`` loads ``Fx, Fy, Fz`` and ``fluid`` point
+  sources ``P`` at ``NodeId``; ``/NodeMoments/*``: ``point_moment`` loads
+  ``Mx, My, Mz``; ``/ElemLoads/*``: ``vn`` loads (``vn``, ``Face``,
+  ``ElementId``) on Fluid8 faces;
 * ``/Analysis`` attributes ``start``, ``steps``, ``delta``: the frequency list,
   unless a ``<input file>.frq`` list exists beside the file
   (``generateFrequencies``, ``analysisfrequencybasic.cpp:36-72``).
@@ -31,8 +34,8 @@ and writes both files elpasoC writes for this path: the solution file
 integer attributes ``numrow``, ``numcol``, 1-based CSR ``vecCsrIa``,
 ``vecCsrJa`` and complex ``cmpCsrVal``; ``ESC/math/mathlibrary.cpp:53-86``).
 
-Interface elements, element loads and nodal moments are not read (a model
-that has them raises ``NotImplementedError``).
+Interface elements are not read (a model that has them raises
+``NotImplementedError``; coupled models are described in code).
 """
 from __future__ import annotations
 
@@ -135,6 +138,7 @@ def read_model(path: str, model_desc_cls=None):
         mats.append(mat)
 
     blocks = []
+    element_at = {}  # element id -> (block, index in the block)
     for name in sorted(f["Elements"].keys(), key=lambda s: int("".join(c for c in s if c.isdigit()) or 0)):
         ds = f["Elements"][name]
         typ = _ELEMENT_TYPES.get(ds.attrs["ElementType"])
@@ -142,6 +146,8 @@ def read_model(path: str, model_desc_cls=None):
             raise NotImplementedError(f"element type {ds.attrs['ElementType']}")
         rows = ds.read().astype(np.int64)
         conn = np.vectorize(index.__getitem__, otypes=[np.int64])(rows[:, 1:])
+        for e, eid in enumerate(rows[:, 0]):
+            element_at[int(eid)] = (len(blocks), e)
         blocks.append((typ, mat_index[int(ds.attrs["MaterialId"])], conn.astype(np.int32)))
 
     for grp in ("InterfaceElements", "NCInterfaceElements"):
@@ -159,14 +165,37 @@ def read_model(path: str, model_desc_cls=None):
                     fnode.append(index[int(a["NodeId"])])
                     fdof.append(dof)
                     fval.append(complex(float(a.get("val" + key, 0.0))))
-    lnode, lf = [], []
-    if "NodeLoads" in f:
+    lnode, lf, snode, sp = [], [], [], []
+    if "NodeLoads" in f:  # cNodalForceFactory (nodalforcefactory.cpp:36-55)
         for name in sorted(f["NodeLoads"].keys()):
             a = f["NodeLoads"][name].attrs
-            if a.get("LoadType") != "point_force":
+            if a.get("LoadType") == "point_force":
+                lnode.append(index[int(a["NodeId"])])
+                lf.append([float(a["Fx"]), float(a["Fy"]), float(a["Fz"])])
+            elif a.get("LoadType") == "fluid":
+                snode.append(index[int(a["NodeId"])])
+                sp.append(float(a["P"]))
+            else:
                 raise NotImplementedError(f"load type {a.get('LoadType')}")
-            lnode.append(index[int(a["NodeId"])])
-            lf.append([float(a["Fx"]), float(a["Fy"]), float(a["Fz"])])
+    mnode, mm = [], []
+    if "NodeMoments" in f:  # cNodalMomentFactory: point_moment (nodalmomentfactory.cpp:40)
+        for name in sorted(f["NodeMoments"].keys()):
+            a = f["NodeMoments"][name].attrs
+            if a.get("LoadType") != "point_moment":
+                raise NotImplementedError(f"moment type {a.get('LoadType')}")
+            mnode.append(index[int(a["NodeId"])])
+            mm.append([float(a["Mx"]), float(a["My"]), float(a["Mz"])])
+    vb, ve, vf, vv = [], [], [], []
+    if "ElemLoads" in f:  # cElementLoadFactory: vn (elementloadfactory.cpp:34-46)
+        for name in sorted(f["ElemLoads"].keys()):
+            a = f["ElemLoads"][name].attrs
+            if a.get("LoadType") != "vn":
+                raise NotImplementedError(f"element load type {a.get('LoadType')}")
+            b, e = element_at[int(a["ElementId"])]
+            vb.append(b)
+            ve.append(e)
+            vf.append(int(a["Face"]))
+            vv.append(float(a["vn"]))
 
     an = f["Analysis"].attrs
     freqs = frequency_list(path, float(an["start"]), float(an["delta"]), int(an["steps"]))
@@ -174,6 +203,10 @@ def read_model(path: str, model_desc_cls=None):
         node_ids=ids, coords=coords, materials=mats, blocks=blocks,
         fixed=dict(node=np.array(fnode, np.int64), dof=np.array(fdof, np.int64), value=np.array(fval, complex)),
         forces=dict(node=np.array(lnode, np.int64), f=np.array(lf).reshape(-1, 3)),
+        moments=dict(node=np.array(mnode, np.int64), m=np.array(mm).reshape(-1, 3)),
+        fluid_sources=dict(node=np.array(snode, np.int64), p=np.array(sp, float)),
+        vn_loads=dict(block=np.array(vb, np.int64), element=np.array(ve, np.int64), face=np.array(vf, np.int64),
+                      vn=np.array(vv, float)),
         name=os.path.splitext(os.path.basename(path))[0])
     return desc, freqs
 

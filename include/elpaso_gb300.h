@@ -64,6 +64,7 @@ extern "C" {
 #define ELP_DOF_X3 2
 #define ELP_DOF_W1 3
 #define ELP_DOF_W2 4
+#define ELP_DOF_W3 5
 #define ELP_DOF_FLUID 16
 #define ELP_NUM_KNOWN_DOFS 21
 
@@ -115,6 +116,29 @@ typedef struct {
 } elp_nodal_force;
 
 typedef struct {
+  int32_t node;           /* node index                                          */
+  double m[3];            /* Mx My Mz on the active rows of w1 w2 w3
+                             (applyNodalMoments, analysis.cpp:281-364)           */
+} elp_nodal_moment;
+
+typedef struct {
+  int32_t node;           /* node index                                          */
+  double p;               /* fluid point source: F[fluid row] += 4 pi p
+                             (applyNodalForces, analysis.cpp:243-265)            */
+} elp_fluid_source;
+
+/* Normal-velocity load on a face of a Fluid8 element (cElementLoadVn,
+ * elementfluid3d.cpp:241-309): F += -(i vn / w) int_face N dA at the face's
+ * four nodes. face 1..6 selects cShapeHex8's surfaces[face - 1]
+ * (shapehex8.cpp:119-150), as the input's Face attribute does. */
+typedef struct {
+  int32_t block;          /* index into blocks (an ELP_FLUID8 block)            */
+  int32_t face;           /* 1..6                                               */
+  int64_t element;        /* element index within the block                     */
+  double vn;              /* normal velocity                                    */
+} elp_vn_load;
+
+typedef struct {
   int64_t n_nodes;
   const int64_t* node_ids;  /* reference node ids; numbering follows ascending id */
   const double* coords;     /* 3 x n_nodes                                        */
@@ -128,6 +152,12 @@ typedef struct {
   const elp_fixed_dof* fixed;
   int64_t n_forces;
   const elp_nodal_force* forces;
+  int64_t n_moments;
+  const elp_nodal_moment* moments;
+  int64_t n_fluid_sources;
+  const elp_fluid_source* fluid_sources;
+  int64_t n_vn_loads;
+  const elp_vn_load* vn_loads;
 } elp_model_desc;
 
 typedef struct elp_model elp_model;
@@ -191,11 +221,16 @@ int elp_model_global_rows(const elp_model* m, int32_t* rows_out /* n_nodes x 21 
  * combine, copied to the host. */
 int elp_model_system_values(elp_model* m, double omega, double* values_out);
 
-/* Right-hand side F after nodal loads and BC values, complex interleaved. */
+/* Right-hand side F after nodal loads and BC values, complex interleaved:
+ * the w-independent part (normal-velocity loads excluded). */
 int elp_model_rhs(const elp_model* m, double* f_out);
 
+/* Right-hand side at angular frequency omega: F + (1/omega) G, G the
+ * normal-velocity loads (zero on Dirichlet rows), complex interleaved. */
+int elp_model_rhs_omega(const elp_model* m, double omega, double* f_out);
+
 /* Solve A(w_k) u_k = f for n_omega angular frequencies. f == NULL uses the
- * model's own right-hand side. x_out: n_omega x n complex interleaved.
+ * model's own right-hand side at each w_k (elp_model_rhs_omega). x_out: n_omega x n complex interleaved.
  * info: n_omega entries (may be NULL). tol: target relative residual
  * (<= 0 selects 1e-10). */
 int elp_solve(elp_model* m, const double* omegas, int n_omega, int precision,

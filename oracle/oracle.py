@@ -11,7 +11,9 @@ elpasoCore/source/ of the reference):
                  negative rows dropped by PETSc, explicit zeros kept,
                  diagonal inserted by preallocateMatrix (analysis.cpp:791)
   BC rows        analysis/analysis.cpp:366-454 (MatZeroRows diag = 1, F[row] = value)
-  RHS            analysis/analysis.cpp:171-279 (nodal forces, ADD)
+  RHS            analysis/analysis.cpp:171-364 (nodal forces, fluid point
+                 sources, nodal moments, ADD); normal-velocity face loads of
+                 Fluid8 elements as the 1/w part (elementfluid3d.cpp:241-309)
   values         element matrices EM(w) of oracle/elp_oracle.c, inserted per
                  element, interfaces with -ori (analysisfrequencybasic.cpp:101-157)
   materials      E_vis(w), E and eta from frequency tables where given
@@ -137,6 +139,32 @@ def e_vis(mat, omega):
     return complex(mat["E"])
 
 
+# faces of a hexahedron as cShapeHex8::getIndicesOfFaceNodes numbers them
+# (shape/shapehex8.cpp:119-150); an input face f is surfaces[f - 1]
+HEX8_FACES = ((0, 1, 5, 4), (2, 3, 7, 6), (0, 3, 2, 1), (1, 2, 6, 5), (4, 5, 6, 7), (0, 4, 7, 3))
+
+
+def face_integrals(xyz):
+    """int N_z dA over a 4-node face (rows: the face's nodes in order), the
+    row sums of C(z, s) = int N_z N_s dA of evaluateSurfaceIntegral
+    (element/fluid/elementfluid3d.cpp:169-233): bilinear N on
+    [-1, 1]^2 with nodes at (-1,-1), (1,-1), (1,1), (-1,1), 2 x 2 Gauss points
+    (weight 1), surface Jacobian sqrt(|a1|^2 |a2|^2 - (a1.a2)^2)."""
+    xyz = np.asarray(xyz, np.float64)
+    cx = np.array([-1.0, 1.0, 1.0, -1.0])
+    cy = np.array([-1.0, -1.0, 1.0, 1.0])
+    out = np.zeros(4)
+    g = 1.0 / np.sqrt(3.0)
+    for u in (-g, g):
+        for v in (-g, g):
+            N = 0.25 * (1 + cx * u) * (1 + cy * v)
+            a1 = (0.25 * cx * (1 + cy * v)) @ xyz
+            a2 = (0.25 * cy * (1 + cx * u)) @ xyz
+            jac = np.sqrt(a1 @ a1 * (a2 @ a2) - (a1 @ a2) ** 2)
+            out += N * jac
+    return out
+
+
 # ------------------------------------------------------------------ host flow
 class System:
     """Numbering, pattern, BC rows and RHS of a model description."""
@@ -205,9 +233,37 @@ class System:
                 for dd in range(3):
                     if rows[v, dd] >= 0:
                         f[rows[v, dd]] += d.forces["f"][k][dd]
+        # fluid point sources: F += 4 pi p on the fluid row (analysis.cpp:243-265)
+        if getattr(d, "fluid_sources", None) is not None:
+            for k in range(len(d.fluid_sources["node"])):
+                v = int(d.fluid_sources["node"][k])
+                if rows[v, 16] >= 0:
+                    f[rows[v, 16]] += 4.0 * np.pi * d.fluid_sources["p"][k]
+        # nodal moments on the active w1 w2 w3 (analysis.cpp:281-364)
+        if getattr(d, "moments", None) is not None:
+            for k in range(len(d.moments["node"])):
+                v = int(d.moments["node"][k])
+                for dd in range(3):
+                    if rows[v, 3 + dd] >= 0:
+                        f[rows[v, 3 + dd]] += d.moments["m"][k][dd]
+        # normal-velocity loads: the 1/w part G of F(w) = f + G / w
+        g = np.zeros(r, np.complex128)
+        if getattr(d, "vn_loads", None) is not None:
+            for k in range(len(d.vn_loads["element"])):
+                conn = np.asarray(d.blocks[int(d.vn_loads["block"][k])][2])[int(d.vn_loads["element"][k])]
+                face = conn[list(HEX8_FACES[int(d.vn_loads["face"][k]) - 1])]
+                for z, nz in enumerate(face_integrals(d.coords[face])):
+                    if rows[face[z], 16] >= 0:
+                        g[rows[face[z], 16]] += -1j * d.vn_loads["vn"][k] * nz
         for rr, val in zip(self.bc_rows, self.bc_vals):
             f[rr] = val
+            g[rr] = 0.0
         self.f = f
+        self.f_vn = g
+
+    def rhs(self, omega):
+        """F(w) = f + G / w (G: normal-velocity loads, zero on BC rows)."""
+        return self.f + self.f_vn / omega
 
     def values(self, omega):
         """A(w) on the pattern after BC rows (complex128, nnz)."""
@@ -284,7 +340,7 @@ class System:
         loses up to four digits on a clamped thin plate; on the lifted one
         it sees the free block, whose conditioning is the physical one."""
         A = self.matrix(omega)
-        rhs = np.array(self.f if f is None else f, np.complex128, copy=True)
+        rhs = np.array(self.rhs(omega) if f is None else f, np.complex128, copy=True)
         if self.bc_rows:
             bc = np.zeros(self.n, bool)
             bc[self.bc_rows] = True
