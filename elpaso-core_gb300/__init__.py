@@ -132,7 +132,7 @@ class RequestResult(C.Structure):
 EXPORTS = [
     "elp_model_create", "elp_model_assemble", "elp_model_analyse", "elp_model_get_info",
     "elp_model_pattern", "elp_model_global_rows", "elp_model_system_values", "elp_model_rhs",
-    "elp_model_rhs_omega",
+    "elp_model_rhs_omega", "elp_cell_stresses",
     "elp_solve", "elp_model_destroy", "elp_last_error", "elp_solve_device", "elp_model_time_assembly",
     "elp_server_create", "elp_server_add_model", "elp_server_submit", "elp_server_wait",
     "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc",
@@ -164,6 +164,7 @@ def load_library(path: str | None = None):
     lib.elp_model_system_values.argtypes = [P, C.c_double, P]
     lib.elp_model_rhs.argtypes = [P, P]
     lib.elp_model_rhs_omega.argtypes = [P, C.c_double, P]
+    lib.elp_cell_stresses.argtypes = [P, C.c_double, P, P, P]
     lib.elp_solve.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_double]
     lib.elp_solve_device.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_double, P]
     lib.elp_model_time_assembly.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -360,6 +361,18 @@ class Model:
         else:
             _check(self.lib.elp_model_rhs_omega(self.handle, float(omega), _ptr(out)))
         return out.view(np.complex128)
+
+    def cell_stresses(self, omega: float, x: np.ndarray):
+        """(sigma, sigma_lower): [n_elements, 9] complex per element of the
+        solution x at omega (elements in descriptor order)."""
+        ne = int(sum(len(b[2]) for b in self.desc.blocks))
+        xs = np.ascontiguousarray(x, dtype=np.complex128)
+        if xs.shape != (self.n,):
+            raise ValueError("x must hold n complex values")
+        up = np.zeros((ne, 9), np.complex128)
+        lo = np.zeros((ne, 9), np.complex128)
+        _check(self.lib.elp_cell_stresses(self.handle, float(omega), _ptr(xs), _ptr(up), _ptr(lo)))
+        return up, lo
 
     def time_assembly(self, repeats: int = 3):
         a, b = C.c_double(), C.c_double()

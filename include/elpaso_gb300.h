@@ -236,6 +236,18 @@ int elp_model_rhs_omega(const elp_model* m, double omega, double* f_out);
 int elp_solve(elp_model* m, const double* omegas, int n_omega, int precision,
               const double* f_or_null, double* x_out, elp_solve_info* info, double tol);
 
+/* Cell stresses of a solution x (n complex interleaved, e.g. one frequency of
+ * elp_solve's output) at angular frequency omega, as the reference computes
+ * them after a solve (cAnalysis::computeStressesCells, analysis.cpp:869-905):
+ * 9 complex slots per element, elements in descriptor order (blocks, then
+ * elements; the reference orders them by ascending element id, Id0n).
+ * Brick8: sigma at the element centre, slots 0..5
+ * (elementstructurebrick.cpp:48-159); DSG4: the Mindlin plate stresses of the
+ * upper surface in sigma, of the lower surface in sigma_lower, slots 0, 1, 3
+ * (elementstructuremindlin.cpp:51-175); other slots and Fluid8 elements 0.
+ * sigma_lower may be NULL. */
+int elp_cell_stresses(const elp_model* m, double omega, const double* x, double* sigma, double* sigma_lower);
+
 int elp_model_destroy(elp_model* m);
 
 /* Text of the last error on the calling thread. */

@@ -16,6 +16,7 @@ elpasoCore/source/ of the reference):
                  Fluid8 elements as the 1/w part (elementfluid3d.cpp:241-309)
   values         element matrices EM(w) of oracle/elp_oracle.c, inserted per
                  element, interfaces with -ori (analysisfrequencybasic.cpp:101-157)
+  stresses       cell stresses after the solve (analysis.cpp:869-905)
   materials      E_vis(w), E and eta from frequency tables where given
                  (material/.../viscoelastic/materialstructurevisco.cpp:229-287)
   solve          SciPy SuperLU, complex128, on the system with the Dirichlet
@@ -363,6 +364,77 @@ class System:
         import scipy.sparse.linalg as sla
         A, rhs = self.lifted(omega, f)
         return sla.splu(A.tocsc()).solve(rhs)
+
+
+def material_c6(E, nu):
+    """The 3D constitutive matrix of cMaterialStructureVisco::setupC
+    (materialstructurevisco.cpp:349-372), from the C restatement."""
+    C6 = np.zeros(72); Cb = np.zeros(18); Cs = np.zeros(8)
+    lib().orc_material(_d(complex(E).real), _d(complex(E).imag), _d(nu), _d(1.0), _p(C6), _p(Cb), _p(Cs))
+    return C6.view(np.complex128).reshape(6, 6)
+
+
+def _centre_shape_derivatives(nn):
+    """dN/dxi (rows: xi, eta[, zeta]) of the hex8 / quad4 shape functions at the
+    element centre, nodes ordered as cShapeHex8 / cShapeQuad4."""
+    sx = np.array([-1, 1, 1, -1, -1, 1, 1, -1], float)
+    sy = np.array([-1, -1, 1, 1, -1, -1, 1, 1], float)
+    sz = np.array([-1, -1, -1, -1, 1, 1, 1, 1], float)
+    if nn == 8:
+        return np.stack([sx, sy, sz]) / 8.0
+    return np.stack([sx[:4], sy[:4]]) / 4.0
+
+
+def cell_stresses(system, omega, x):
+    """computeStressesCells of every structure element (elements in the
+    description's block order): 9 slots per element, (upper, lower).
+    Brick8 (elementstructurebrick.cpp:48-159): Bm (6 x 24) at the centre,
+    stress = C(w) Bm u. DSG4 (elementstructuremindlin.cpp:51-175): per node
+    (w2, w1, w2), Bm rows (Nx, 0, 0), (0, Ny, 0), (0, 0, Ny), strains scaled
+    to the upper (t/2, -t/2, t) and lower (-t/2, t/2, -t) surface,
+    stress = Cm(w) strain into slots 0, 1, 3 (setupCm,
+    materialstructurevisco.cpp:331-345)."""
+    d, rows = system.d, system.rows
+    x = np.asarray(x)
+    val = lambda v, k: x[rows[v, k]] if rows[v, k] >= 0 else 0.0  # noqa: E731
+    up, lo = [], []
+    for typ, mi, conn in d.blocks:
+        mat = d.materials[mi]
+        for e in np.asarray(conn):
+            s1 = np.zeros(9, complex); s2 = np.zeros(9, complex)
+            if typ == BRICK8:
+                dN = _centre_shape_derivatives(8)
+                J = dN @ d.coords[e]
+                G = np.linalg.inv(J) @ dN  # rows: d/dx, d/dy, d/dz per node
+                Bm = np.zeros((6, 24))
+                for k in range(8):
+                    Nx, Ny, Nz = G[:, k]
+                    Bm[0, 3 * k] = Nx; Bm[1, 3 * k + 1] = Ny; Bm[2, 3 * k + 2] = Nz
+                    Bm[3, 3 * k] = Ny; Bm[3, 3 * k + 1] = Nx
+                    Bm[4, 3 * k + 1] = Nz; Bm[4, 3 * k + 2] = Ny
+                    Bm[5, 3 * k] = Nz; Bm[5, 3 * k + 2] = Nx
+                u = np.array([val(v, k) for v in e for k in (0, 1, 2)], complex)
+                s1[:6] = material_c6(e_vis(mat, omega), mat["nu"]) @ (Bm @ u)
+            elif typ == DSG4:
+                dN = _centre_shape_derivatives(4)
+                J = dN @ d.coords[e][:, :2]
+                G = np.linalg.inv(J) @ dN
+                Bm = np.zeros((3, 12))
+                for k in range(4):
+                    Bm[0, 3 * k] = G[0, k]; Bm[1, 3 * k + 1] = G[1, k]; Bm[2, 3 * k + 2] = G[1, k]
+                loc = [val(v, k) for v in e for k in (2, 3, 4)]  # x3, w1, w2
+                rel = np.array([loc[3 * k + j] for k in range(4) for j in (2, 1, 2)], complex)
+                eps = Bm @ rel
+                t, nu = mat["t"], mat["nu"]
+                f = e_vis(mat, omega) / (1.0 - nu * nu)
+                Cm = f * np.array([[1.0, nu, 0.0], [nu, 1.0, 0.0], [0.0, 0.0, 0.5 * (1.0 - nu)]])
+                a = Cm @ (np.array([0.5 * t, -0.5 * t, t]) * eps)
+                b = Cm @ (np.array([-0.5 * t, 0.5 * t, -t]) * eps)
+                s1[[0, 1, 3]] = a
+                s2[[0, 1, 3]] = b
+            up.append(s1)
+            lo.append(s2)
+    return np.array(up), np.array(lo)
 
 
 def dof_nodes(system):
