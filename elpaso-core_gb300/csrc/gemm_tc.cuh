@@ -506,26 +506,31 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
 // shared-memory layout the MMAs read (K-major, no swizzle, 16-deep chunks):
 //   A block (tile row tr, chunk c): L21 rows 128 tr.., 4 planes re_hi, re_lo,
 //     im_hi, im_lo of 128 x 16 words (32 KB);
-//   B block (tile col tc, chunk c): U12 columns 128 tc.., 4 planes of 256 x 16
-//     words: W1 = [B_re ; B_im] hi, lo and W2 = [-B_im ; B_re] hi, lo (64 KB).
+//   B block (tile col tc, chunk c): U12 columns 128 tc.., the 2 planes hi, lo
+//     of W = [B_re ; B_im], 256 x 16 words each (32 KB).
 // k_schur_tc then needs no converter threads: one thread issues two 1D bulk
 // copies (cp.async.bulk, completing on an mbarrier with a byte count) per
-// chunk into a two-stage ring, one thread issues the MMAs, all eight warps
-// run the epilogue. A 128 x 128 complex tile is
-//   [D_re | D_im] += A_re W1 + A_im W2    (6 MMAs of N = 256 per K = 8 step,
-// 3xTF32: hi*hi + hi*lo + lo*hi), accumulated in 256 TMEM columns.
+// chunk into a three-stage ring, one thread issues the MMAs, all eight warps
+// run the epilogue. A 128 x 128 complex tile, per K = 8 step (3xTF32:
+// hi*hi + hi*lo + lo*hi), accumulated in 256 TMEM columns:
+//   [D_re | D_im] += A_re W          (N = 256)
+//    D_re         -= A_im B_im        (N = 128, negate-A, B_im = rows 128.. of W)
+//    D_im         += A_im B_re        (N = 128)
+// 9 MMAs with the work of 6 of N = 256, and half the B bytes of a layout that
+// also stores [-B_im ; B_re].
 constexpr int kSchurTile = 128;                  // complex rows and columns of a tile
 constexpr int64_t kSchurABlock = 4 * 128 * kTcKC * 4;
-constexpr int64_t kSchurBBlock = 4 * 256 * kTcKC * 4;
+constexpr int64_t kSchurBBlock = 2 * 256 * kTcKC * 4;
 constexpr uint32_t kSchurCols = 256;
+constexpr int kSchurStages = 3;
 
 struct SchurStage {
   uint32_t a[4][128 * kTcKC];
-  uint32_t b[4][256 * kTcKC];
+  uint32_t b[2][256 * kTcKC];
 };
 struct SchurSmem {
-  SchurStage st[2];
-  uint64_t full[2], empty[2];
+  SchurStage st[kSchurStages];
+  uint64_t full[kSchurStages], empty[kSchurStages];
   uint32_t tmem_base;
 };
 constexpr int kSchurSmemBytes = (int)((sizeof(SchurSmem) + 1023) / 1024 * 1024);
@@ -596,14 +601,10 @@ __global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* _
       tc::split_tf32(v.x, rh, rl);
       tc::split_tf32(v.y, ih, il);
       const int w_re = tc_word(jj, kk), w_im = tc_word(128 + jj, kk);
-      P[0 * PL + w_re] = rh;  // W1 = [B_re ; B_im]
+      P[0 * PL + w_re] = rh;  // W = [B_re ; B_im]
       P[1 * PL + w_re] = rl;
       P[0 * PL + w_im] = ih;
       P[1 * PL + w_im] = il;
-      P[2 * PL + w_re] = ih ^ 0x80000000u;  // W2 = [-B_im ; B_re] (negation is exact)
-      P[3 * PL + w_re] = il ^ 0x80000000u;
-      P[2 * PL + w_im] = rh;
-      P[3 * PL + w_im] = rl;
     }
   }
 }
@@ -635,7 +636,7 @@ __global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __rest
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < kSchurStages; ++q) {
       tc::mbar_init(&sm.full[q], 1);
       tc::mbar_init(&sm.empty[q], 1);
     }
@@ -647,11 +648,13 @@ __global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __rest
   const uint32_t tmem = sm.tmem_base;
   bool ok = true;
   int issued = 0;  // chunks whose copies the producer issued (thread 0)
+  // chunk c uses stage c % kSchurStages; its use n = c / kSchurStages of that
+  // stage completes mbarrier phase n & 1
   if (tid == 0) {
     // ------------------------------------------------ producer
     for (int c = 0; c < nch; ++c) {
-      const int st = c & 1;
-      if (c >= 2 && ok) ok = tc::mbar_wait(&sm.empty[st], ((c >> 1) + 1) & 1);  // MMAs of chunk c - 2 done
+      const int st = c % kSchurStages, use = c / kSchurStages;
+      if (c >= kSchurStages && ok) ok = tc::mbar_wait(&sm.empty[st], (use + 1) & 1);  // MMAs of c - stages done
       tc::mbar_expect_tx(&sm.full[st], (uint32_t)(kSchurABlock + kSchurBBlock));
       tc::bulk_g2s(&sm.st[st].a[0][0], Ab + (int64_t)c * kSchurABlock, (uint32_t)kSchurABlock, &sm.full[st]);
       tc::bulk_g2s(&sm.st[st].b[0][0], Bb + (int64_t)c * kSchurBBlock, (uint32_t)kSchurBBlock, &sm.full[st]);
@@ -659,36 +662,43 @@ __global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __rest
     }
   } else if (tid == 32) {
     // ------------------------------------------------ MMA issue
-    constexpr uint32_t idesc = tc::idesc_tf32(128, 256, false);
+    constexpr uint32_t id_w = tc::idesc_tf32(128, 256, false);
+    constexpr uint32_t id_p = tc::idesc_tf32(128, 128, false), id_n = tc::idesc_tf32(128, 128, true);
     constexpr uint32_t LBO = 128, SBO = (kTcKC / 4) * 128;
+    constexpr uint32_t half_off = (128 / 8) * SBO;  // bytes from the B_re rows of W to its B_im rows
     for (int c = 0; c < nch; ++c) {
-      const int st = c & 1;
-      if (ok) ok = tc::mbar_wait(&sm.full[st], (c >> 1) & 1);
+      const int st = c % kSchurStages;
+      if (ok) ok = tc::mbar_wait(&sm.full[st], (c / kSchurStages) & 1);
       tc::fence_after();
-      uint32_t a[4], w[4];
+      uint32_t a[4], w[2];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        a[q] = tc::smem_u32(sm.st[st].a[q]);
-        w[q] = tc::smem_u32(sm.st[st].b[q]);
-      }
+      for (int q = 0; q < 4; ++q) a[q] = tc::smem_u32(sm.st[st].a[q]);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) w[q] = tc::smem_u32(sm.st[st].b[q]);
 #pragma unroll
       for (int ks = 0; ks < kTcKC / 8; ++ks) {
         const uint32_t o = ks * 2 * 128;  // two core matrices per K = 8 step
         auto d = [&](uint32_t x) { return tc::smem_desc(x + o, LBO, SBO); };
         const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
-        tc::mma_tf32_ss(tmem, d(a[0]), d(w[0]), idesc, acc0);  // A_re_hi W1_hi
-        tc::mma_tf32_ss(tmem, d(a[0]), d(w[1]), idesc, 1u);    // A_re_hi W1_lo
-        tc::mma_tf32_ss(tmem, d(a[1]), d(w[0]), idesc, 1u);    // A_re_lo W1_hi
-        tc::mma_tf32_ss(tmem, d(a[2]), d(w[2]), idesc, 1u);    // A_im_hi W2_hi
-        tc::mma_tf32_ss(tmem, d(a[2]), d(w[3]), idesc, 1u);    // A_im_hi W2_lo
-        tc::mma_tf32_ss(tmem, d(a[3]), d(w[2]), idesc, 1u);    // A_im_lo W2_hi
+        // [D_re | D_im] += A_re [B_re | B_im]
+        tc::mma_tf32_ss(tmem, d(a[0]), d(w[0]), id_w, acc0);  // A_re_hi W_hi
+        tc::mma_tf32_ss(tmem, d(a[0]), d(w[1]), id_w, 1u);    // A_re_hi W_lo
+        tc::mma_tf32_ss(tmem, d(a[1]), d(w[0]), id_w, 1u);    // A_re_lo W_hi
+        // D_re -= A_im B_im
+        tc::mma_tf32_ss(tmem, d(a[2]), d(w[0] + half_off), id_n, 1u);
+        tc::mma_tf32_ss(tmem, d(a[2]), d(w[1] + half_off), id_n, 1u);
+        tc::mma_tf32_ss(tmem, d(a[3]), d(w[0] + half_off), id_n, 1u);
+        // D_im += A_im B_re
+        tc::mma_tf32_ss(tmem + 128, d(a[2]), d(w[0]), id_p, 1u);
+        tc::mma_tf32_ss(tmem + 128, d(a[2]), d(w[1]), id_p, 1u);
+        tc::mma_tf32_ss(tmem + 128, d(a[3]), d(w[0]), id_p, 1u);
       }
       tc::commit(&sm.empty[st]);
     }
   }
   // every warp: the accumulator is complete when the last chunk's commit has arrived
   const int gl = nch - 1;
-  if (lane == 0 && ok) ok = tc::mbar_wait(&sm.empty[gl & 1], (gl >> 1) & 1);
+  if (lane == 0 && ok) ok = tc::mbar_wait(&sm.empty[gl % kSchurStages], (gl / kSchurStages) & 1);
   __syncwarp();
   tc::fence_after();
   ok = __syncthreads_and(ok);
@@ -723,9 +733,9 @@ __global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __rest
     // a wait ran out: copies or MMAs of the last chunks may still be in flight;
     // wait (bounded) for their barriers before the shared memory and TMEM go away
     atomicExch(err, 1);
-    for (int c = (issued > 2 ? issued - 2 : 0); c < issued; ++c) {
-      tc::mbar_wait(&sm.full[c & 1], (c >> 1) & 1);
-      tc::mbar_wait(&sm.empty[c & 1], (c >> 1) & 1);
+    for (int c = (issued > kSchurStages ? issued - kSchurStages : 0); c < issued; ++c) {
+      tc::mbar_wait(&sm.full[c % kSchurStages], (c / kSchurStages) & 1);
+      tc::mbar_wait(&sm.empty[c % kSchurStages], (c / kSchurStages) & 1);
     }
   }
   tc::fence_before();
