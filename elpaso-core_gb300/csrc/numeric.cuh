@@ -142,11 +142,13 @@ struct DeviceSymbolic {
 // The packed-operand Schur update pays off for the few, large fronts at the
 // top of the tree; lower levels keep the converter kernel.
 // Levels whose Schur update runs from packed operands (k_pack_schur + k_schur_tc):
-// few large fronts. pack_max_count(): fronts per level up to which a level with
-// borders of 1024+ rows is packed (ELP_PACK_COUNT, default 8).
+// few large fronts. pack_max_count(): fronts per level up to which a level is
+// packed (ELP_PACK_COUNT, default 36); pack_min_border(): the largest border
+// of the level must reach this many rows (ELP_PACK_MINB, default 1024).
 int pack_max_count();
+int pack_min_border();
 inline bool packed_schur_level(const DeviceSymbolic::Level& L) {
-  return L.count <= pack_max_count() && L.max_b >= 1024;
+  return L.count <= pack_max_count() && L.max_b >= pack_min_border();
 }
 
 struct Workspace {
