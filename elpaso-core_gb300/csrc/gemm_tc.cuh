@@ -531,6 +531,7 @@ struct SchurStage {
 struct SchurSmem {
   SchurStage st[kSchurStages];
   uint64_t full[kSchurStages], empty[kSchurStages];
+  uint64_t acc_full[2], acc_empty[2];
   uint32_t tmem_base;
 };
 constexpr int kSchurSmemBytes = (int)((sizeof(SchurSmem) + 1023) / 1024 * 1024);
@@ -609,12 +610,26 @@ __global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* _
   }
 }
 
-// C -= L21 U12 for one 128 x 128 complex tile of one front and frequency.
+// C -= L21 U12 over the 128 x 128 complex tiles of one front and frequency:
+// CTA blockIdx.z takes tiles z, z + gridDim.z, ... (one CTA per SM: 197 KB of
+// shared memory). Warp 0 lane 0 copies the operand chunks into the
+// three-stage ring, warp 1 lane 0 issues the MMAs, warps 2..9 run the
+// epilogue (warp w reads TMEM lane quarter w % 4, column half (w - 2) / 4).
+// Two accumulators (TMEM columns 0..255 and 256..511) let the epilogue of one
+// tile run while the MMAs of the next fill the other:
+//   full[st] / empty[st]  - operand stage loaded (bytes) / read by the MMAs (commit);
+//   acc_full[a]           - the MMAs of a tile are complete (commit);
+//   acc_empty[a]          - the 8 epilogue warps have read accumulator a.
+// Every wait is bounded; after a timeout a role stops, the CTA sets the error
+// flag and waits (bounded) for its copies and MMAs in flight before the TMEM
+// is released.
+constexpr int kSchurThreads = 320;
+
 template <int NB>
-__global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __restrict__ arena,
-                                                     const uint32_t* __restrict__ pack,
-                                                     const int64_t* __restrict__ pack_base, int64_t slot_bytes,
-                                                     int* __restrict__ err) {
+__global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, float2* __restrict__ arena,
+                                                               const uint32_t* __restrict__ pack,
+                                                               const int64_t* __restrict__ pack_base,
+                                                               int64_t slot_bytes, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char schur_smem_raw[];
   SchurSmem& sm = *reinterpret_cast<SchurSmem*>(schur_smem_raw);
   const int f = L.list[blockIdx.x];
@@ -622,16 +637,17 @@ __global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __rest
   const int p = L.fp[f], b = L.fb[f], m = p + b;
   if (p == 0 || b == 0) return;
   const int tiles = (b + kSchurTile - 1) / kSchurTile, nch = (p + kTcKC - 1) / kTcKC;
-  if ((int)blockIdx.z >= tiles * tiles) return;  // uniform per CTA, before any TMEM allocation
-  const int tr = blockIdx.z % tiles, tcol = blockIdx.z / tiles;
+  const int ntile = tiles * tiles;
+  if ((int)blockIdx.z >= ntile) return;  // uniform per CTA, before any TMEM allocation
+  const int nmine = (ntile - 1 - (int)blockIdx.z) / (int)gridDim.z + 1;
   const char* base = reinterpret_cast<const char*>(pack) + s * slot_bytes + pack_base[f];
-  const char* Ab = base + (int64_t)(tr * nch) * kSchurABlock;
-  const char* Bb = base + (int64_t)tiles * nch * kSchurABlock + (int64_t)(tcol * nch) * kSchurBBlock;
+  const char* Abase = base;
+  const char* Bbase = base + (int64_t)tiles * nch * kSchurABlock;
   float2* F = arena + s * L.arena_size + L.foff[f];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc::smem_u32(&sm.tmem_base)),
-                 "r"(kSchurCols)
+                 "r"(2 * kSchurCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -640,6 +656,10 @@ __global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __rest
       tc::mbar_init(&sm.full[q], 1);
       tc::mbar_init(&sm.empty[q], 1);
     }
+    for (int q = 0; q < 2; ++q) {
+      tc::mbar_init(&sm.acc_full[q], 1);
+      tc::mbar_init(&sm.acc_empty[q], 8);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_before();
@@ -647,102 +667,138 @@ __global__ void __launch_bounds__(256, 1) k_schur_tc(LevelArgs L, float2* __rest
   tc::fence_after();
   const uint32_t tmem = sm.tmem_base;
   bool ok = true;
-  int issued = 0;  // chunks whose copies the producer issued (thread 0)
-  // chunk c uses stage c % kSchurStages; its use n = c / kSchurStages of that
-  // stage completes mbarrier phase n & 1
-  if (tid == 0) {
+  // chunk g (counted over all this CTA's tiles) uses stage g % kSchurStages, and
+  // its use g / kSchurStages of the stage completes mbarrier phase (g / kSchurStages) & 1;
+  // tile j uses accumulator j & 1, whose use j / 2 completes phase (j / 2) & 1
+  int issued = 0, mma_chunks = 0, mma_tiles = 0;
+  if (warp == 0 && lane == 0) {
     // ------------------------------------------------ producer
-    for (int c = 0; c < nch; ++c) {
-      const int st = c % kSchurStages, use = c / kSchurStages;
-      if (c >= kSchurStages && ok) ok = tc::mbar_wait(&sm.empty[st], (use + 1) & 1);  // MMAs of c - stages done
-      tc::mbar_expect_tx(&sm.full[st], (uint32_t)(kSchurABlock + kSchurBBlock));
-      tc::bulk_g2s(&sm.st[st].a[0][0], Ab + (int64_t)c * kSchurABlock, (uint32_t)kSchurABlock, &sm.full[st]);
-      tc::bulk_g2s(&sm.st[st].b[0][0], Bb + (int64_t)c * kSchurBBlock, (uint32_t)kSchurBBlock, &sm.full[st]);
-      issued = c + 1;
+    int g = 0;
+    for (int j = 0; j < nmine && ok; ++j) {
+      const int t = (int)blockIdx.z + j * (int)gridDim.z;
+      const int tr = t % tiles, tcol = t / tiles;
+      const char* Ab = Abase + (int64_t)(tr * nch) * kSchurABlock;
+      const char* Bb = Bbase + (int64_t)(tcol * nch) * kSchurBBlock;
+      for (int c = 0; c < nch; ++c, ++g) {
+        const int st = g % kSchurStages;
+        if (g >= kSchurStages && ok) ok = tc::mbar_wait(&sm.empty[st], ((g / kSchurStages) + 1) & 1);
+        if (!ok) break;
+        tc::mbar_expect_tx(&sm.full[st], (uint32_t)(kSchurABlock + kSchurBBlock));
+        tc::bulk_g2s(&sm.st[st].a[0][0], Ab + (int64_t)c * kSchurABlock, (uint32_t)kSchurABlock, &sm.full[st]);
+        tc::bulk_g2s(&sm.st[st].b[0][0], Bb + (int64_t)c * kSchurBBlock, (uint32_t)kSchurBBlock, &sm.full[st]);
+        issued = g + 1;
+      }
     }
-  } else if (tid == 32) {
+  } else if (warp == 1 && lane == 0) {
     // ------------------------------------------------ MMA issue
     constexpr uint32_t id_w = tc::idesc_tf32(128, 256, false);
     constexpr uint32_t id_p = tc::idesc_tf32(128, 128, false), id_n = tc::idesc_tf32(128, 128, true);
     constexpr uint32_t LBO = 128, SBO = (kTcKC / 4) * 128;
     constexpr uint32_t half_off = (128 / 8) * SBO;  // bytes from the B_re rows of W to its B_im rows
-    for (int c = 0; c < nch; ++c) {
-      const int st = c % kSchurStages;
-      if (ok) ok = tc::mbar_wait(&sm.full[st], (c / kSchurStages) & 1);
+    int g = 0;
+    for (int j = 0; j < nmine && ok; ++j) {
+      const int acc = j & 1;
+      const uint32_t D = tmem + (uint32_t)acc * kSchurCols;
+      if (j >= 2) ok = tc::mbar_wait(&sm.acc_empty[acc], ((j / 2) + 1) & 1);  // epilogue of tile j - 2 read it
       tc::fence_after();
-      uint32_t a[4], w[2];
+      for (int c = 0; c < nch && ok; ++c, ++g) {
+        const int st = g % kSchurStages;
+        ok = tc::mbar_wait(&sm.full[st], (g / kSchurStages) & 1);
+        if (!ok) break;
+        tc::fence_after();
+        uint32_t a[4], w[2];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) a[q] = tc::smem_u32(sm.st[st].a[q]);
+        for (int q = 0; q < 4; ++q) a[q] = tc::smem_u32(sm.st[st].a[q]);
 #pragma unroll
-      for (int q = 0; q < 2; ++q) w[q] = tc::smem_u32(sm.st[st].b[q]);
+        for (int q = 0; q < 2; ++q) w[q] = tc::smem_u32(sm.st[st].b[q]);
 #pragma unroll
-      for (int ks = 0; ks < kTcKC / 8; ++ks) {
-        const uint32_t o = ks * 2 * 128;  // two core matrices per K = 8 step
-        auto d = [&](uint32_t x) { return tc::smem_desc(x + o, LBO, SBO); };
-        const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
-        // [D_re | D_im] += A_re [B_re | B_im]
-        tc::mma_tf32_ss(tmem, d(a[0]), d(w[0]), id_w, acc0);  // A_re_hi W_hi
-        tc::mma_tf32_ss(tmem, d(a[0]), d(w[1]), id_w, 1u);    // A_re_hi W_lo
-        tc::mma_tf32_ss(tmem, d(a[1]), d(w[0]), id_w, 1u);    // A_re_lo W_hi
-        // D_re -= A_im B_im
-        tc::mma_tf32_ss(tmem, d(a[2]), d(w[0] + half_off), id_n, 1u);
-        tc::mma_tf32_ss(tmem, d(a[2]), d(w[1] + half_off), id_n, 1u);
-        tc::mma_tf32_ss(tmem, d(a[3]), d(w[0] + half_off), id_n, 1u);
-        // D_im += A_im B_re
-        tc::mma_tf32_ss(tmem + 128, d(a[2]), d(w[0]), id_p, 1u);
-        tc::mma_tf32_ss(tmem + 128, d(a[2]), d(w[1]), id_p, 1u);
-        tc::mma_tf32_ss(tmem + 128, d(a[3]), d(w[0]), id_p, 1u);
+        for (int ks = 0; ks < kTcKC / 8; ++ks) {
+          const uint32_t o = ks * 2 * 128;  // two core matrices per K = 8 step
+          auto d = [&](uint32_t x) { return tc::smem_desc(x + o, LBO, SBO); };
+          const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
+          // [D_re | D_im] += A_re [B_re | B_im]
+          tc::mma_tf32_ss(D, d(a[0]), d(w[0]), id_w, acc0);  // A_re_hi W_hi
+          tc::mma_tf32_ss(D, d(a[0]), d(w[1]), id_w, 1u);    // A_re_hi W_lo
+          tc::mma_tf32_ss(D, d(a[1]), d(w[0]), id_w, 1u);    // A_re_lo W_hi
+          // D_re -= A_im B_im
+          tc::mma_tf32_ss(D, d(a[2]), d(w[0] + half_off), id_n, 1u);
+          tc::mma_tf32_ss(D, d(a[2]), d(w[1] + half_off), id_n, 1u);
+          tc::mma_tf32_ss(D, d(a[3]), d(w[0] + half_off), id_n, 1u);
+          // D_im += A_im B_re
+          tc::mma_tf32_ss(D + 128, d(a[2]), d(w[0]), id_p, 1u);
+          tc::mma_tf32_ss(D + 128, d(a[2]), d(w[1]), id_p, 1u);
+          tc::mma_tf32_ss(D + 128, d(a[3]), d(w[0]), id_p, 1u);
+        }
+        tc::commit(&sm.empty[st]);
+        mma_chunks = g + 1;
       }
-      tc::commit(&sm.empty[st]);
+      if (!ok) break;
+      tc::commit(&sm.acc_full[acc]);
+      mma_tiles = j + 1;
     }
-  }
-  // every warp: the accumulator is complete when the last chunk's commit has arrived
-  const int gl = nch - 1;
-  if (lane == 0 && ok) ok = tc::mbar_wait(&sm.empty[gl % kSchurStages], (gl / kSchurStages) & 1);
-  __syncwarp();
-  tc::fence_after();
-  ok = __syncthreads_and(ok);
-  if (ok) {
-    const int lg = warp & 3, half = warp >> 2;  // TMEM lane quarter, 64-column half of the tile
+  } else if (warp >= 2) {
+    // ------------------------------------------------ epilogue
+    const int lg = warp & 3, half = (warp - 2) >> 2;  // TMEM lane quarter, 64-column half of the tile
     const uint32_t lane_base = (uint32_t)(32 * lg) << 16;
-    const int i = tr * kSchurTile + 32 * lg + lane;  // row of C (within the border block)
+    for (int j = 0; j < nmine; ++j) {
+      const int acc = j & 1;
+      const int t = (int)blockIdx.z + j * (int)gridDim.z;
+      const int tr = t % tiles, tcol = t / tiles;
+      if (lane == 0 && ok) ok = tc::mbar_wait(&sm.acc_full[acc], (j / 2) & 1);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      tc::fence_after();
+      const uint32_t D = tmem + lane_base + (uint32_t)acc * kSchurCols;
+      const int i = tr * kSchurTile + 32 * lg + lane;  // row of C (within the border block)
 #pragma unroll
-    for (int part = 0; part < 4; ++part) {  // 16 complex columns at a time: loads first, then stores
-      const int jb = tcol * kSchurTile + half * 64 + part * 16;
-      float re[16], im[16];
-      tc::ld16(tmem + lane_base + half * 64 + part * 16, re);
-      tc::ld16(tmem + lane_base + 128 + half * 64 + part * 16, im);
-      if (i < b) {
-        float2* dst0 = F + (int64_t)(p + jb) * m + p + i;
-        float2 cv[16];
-#pragma unroll
-        for (int q = 0; q < 16; ++q)
-          if (jb + q < b) cv[q] = dst0[(int64_t)q * m];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) cv[q] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
-        if (L.fuse) {
-          add_into_parent<16>(L, arena, f, s, i, jb, b, cv);
-        } else {
+      for (int part = 0; part < 4; ++part) {  // 16 complex columns at a time: loads first, then stores
+        const int jb = tcol * kSchurTile + half * 64 + part * 16;
+        float re[16], im[16];
+        tc::ld16(D + half * 64 + part * 16, re);
+        tc::ld16(D + 128 + half * 64 + part * 16, im);
+        if (i < b) {
+          float2* dst0 = F + (int64_t)(p + jb) * m + p + i;
+          float2 cv[16];
 #pragma unroll
           for (int q = 0; q < 16; ++q)
-            if (jb + q < b) dst0[(int64_t)q * m] = cv[q];
+            if (jb + q < b) cv[q] = dst0[(int64_t)q * m];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) cv[q] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
+          if (L.fuse) {
+            add_into_parent<16>(L, arena, f, s, i, jb, b, cv);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+              if (jb + q < b) dst0[(int64_t)q * m] = cv[q];
+          }
         }
       }
+      // this warp has read accumulator acc (ld16 waits for its loads)
+      tc::fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&sm.acc_empty[acc]);
     }
-  } else if (tid == 0) {
-    // a wait ran out: copies or MMAs of the last chunks may still be in flight;
+  }
+  const bool any_fail = __syncthreads_or(!ok);
+  if (any_fail) {
+    // a wait ran out: copies and MMAs of the last chunks may still be in flight;
     // wait (bounded) for their barriers before the shared memory and TMEM go away
-    atomicExch(err, 1);
-    for (int c = (issued > kSchurStages ? issued - kSchurStages : 0); c < issued; ++c) {
-      tc::mbar_wait(&sm.full[c % kSchurStages], (c / kSchurStages) & 1);
-      tc::mbar_wait(&sm.empty[c % kSchurStages], (c / kSchurStages) & 1);
+    if (tid == 0) {
+      atomicExch(err, 1);
+      for (int g = (issued > kSchurStages ? issued - kSchurStages : 0); g < issued; ++g)
+        tc::mbar_wait(&sm.full[g % kSchurStages], (g / kSchurStages) & 1);
+    } else if (tid == 32) {
+      for (int g = (mma_chunks > kSchurStages ? mma_chunks - kSchurStages : 0); g < mma_chunks; ++g)
+        tc::mbar_wait(&sm.empty[g % kSchurStages], (g / kSchurStages) & 1);
+      for (int j = (mma_tiles > 2 ? mma_tiles - 2 : 0); j < mma_tiles; ++j)
+        tc::mbar_wait(&sm.acc_full[j & 1], (j / 2) & 1);
     }
   }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kSchurCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kSchurCols) : "memory");
   }
 }
 

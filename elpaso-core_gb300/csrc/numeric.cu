@@ -1290,6 +1290,17 @@ int device_upload_symbolic(Model& m) {
 // Fronts per level / border rows that select packed Schur levels. Measured
 // (32 frequencies per step, coupled 85k-DOF sweep): up to 8 / 12 / 20 / 36
 // fronts 115.1 / 116.2 / 116.8 / 116.9 solves/s.
+// streaming multiprocessors of the current device (read once)
+static int num_sms() {
+  static const int v = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
+  return v;
+}
+
 int pack_max_count() {
   static const int v = [] {
     const char* e = getenv("ELP_PACK_COUNT");
@@ -1560,9 +1571,13 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
         Lc.list = D.ea_list.p + LV.ea_start[k];
         Lc.count = LV.ea_count[k];
         if (packed) {
-          dim3 gs(Lc.count, S_used, (unsigned)LV.schur_tiles);
-          PROF_LAUNCH(KC_GEMM_TC, st, k_schur_tc<NB><<<gs, 256, kSchurSmemBytes, st>>>(Lc, fa, pk, D.pack_base.p,
-                                                                                        LV.pack_bytes, w.tc_err.p));
+          // persistent CTAs (one per SM): about two waves over the launch, the
+          // tiles of a front and slot split over gridDim.z of them
+          const int64_t pairs = (int64_t)Lc.count * S_used;
+          const int64_t gz = std::min<int64_t>(LV.schur_tiles, std::max<int64_t>(1, (2 * num_sms() + pairs - 1) / pairs));
+          dim3 gs(Lc.count, S_used, (unsigned)gz);
+          PROF_LAUNCH(KC_GEMM_TC, st, k_schur_tc<NB><<<gs, kSchurThreads, kSchurSmemBytes, st>>>(
+                                          Lc, fa, pk, D.pack_base.p, LV.pack_bytes, w.tc_err.p));
         } else {
           gemm(GM_SCHUR, 0, LV.ea_max_b, LV.ea_max_b, Lc);
         }
