@@ -1287,9 +1287,6 @@ int device_upload_symbolic(Model& m) {
   return ELP_OK;
 }
 
-// Fronts per level / border rows that select packed Schur levels. Measured
-// (32 frequencies per step, coupled 85k-DOF sweep): up to 8 / 12 / 20 / 36
-// fronts 115.1 / 116.2 / 116.8 / 116.9 solves/s.
 // streaming multiprocessors of the current device (read once)
 static int num_sms() {
   static const int v = [] {
@@ -1301,10 +1298,13 @@ static int num_sms() {
   return v;
 }
 
+// Fronts per level / border rows that select packed Schur levels. Measured
+// with the persistent packed kernel (32 frequencies per step, coupled 85k-DOF
+// sweep): (36, 1024) 120.7, (80, 512) 121.1, (150, 300) 121.6 solves/s.
 int pack_max_count() {
   static const int v = [] {
     const char* e = getenv("ELP_PACK_COUNT");
-    const int c = e ? atoi(e) : 36;
+    const int c = e ? atoi(e) : 150;
     return c < 0 ? 0 : c;
   }();
   return v;
@@ -1313,7 +1313,7 @@ int pack_max_count() {
 int pack_min_border() {
   static const int v = [] {
     const char* e = getenv("ELP_PACK_MINB");
-    const int c = e ? atoi(e) : 1024;
+    const int c = e ? atoi(e) : 300;
     return c < 0 ? 0 : c;
   }();
   return v;

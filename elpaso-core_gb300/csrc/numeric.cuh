@@ -139,12 +139,11 @@ struct DeviceSymbolic {
   int64_t pack_max = 0;           // largest pack_bytes of a level that uses the packed Schur update
 };
 
-// The packed-operand Schur update pays off for the few, large fronts at the
-// top of the tree; lower levels keep the converter kernel.
-// Levels whose Schur update runs from packed operands (k_pack_schur + k_schur_tc):
-// few large fronts. pack_max_count(): fronts per level up to which a level is
-// packed (ELP_PACK_COUNT, default 36); pack_min_border(): the largest border
-// of the level must reach this many rows (ELP_PACK_MINB, default 1024).
+// Levels whose Schur update runs from packed operands (k_pack_schur + k_schur_tc);
+// the others keep the converter kernel. pack_max_count(): fronts per level up
+// to which a level is packed (ELP_PACK_COUNT, default 150); pack_min_border():
+// the largest border of the level must reach this many rows (ELP_PACK_MINB,
+// default 300).
 int pack_max_count();
 int pack_min_border();
 inline bool packed_schur_level(const DeviceSymbolic::Level& L) {
