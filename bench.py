@@ -409,9 +409,10 @@ def run_ours(args):
         ach = flops / (top[1]["ms"] / 1e3) / 1e12
         roof = {"kernel": top[0], "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "traffic": None,
-                "traffic_ref": "ncu, profiles/k_gemm_tc_schur_plate_cavity_60x40x30.md: 254 MB DRAM for the "
-                               "level-9 Schur launch of 63.4 GFLOP (2 frequencies); per step the class is "
-                               "many launches of every tree level, so no single per-launch figure applies",
+                "traffic_ref": "ncu, profiles/k_schur_tc_plate_cavity_60x40x30.md: 227 MB DRAM for the "
+                               "level-9 packed Schur launch of 31.7 GFLOP (2 frequencies, one front); per "
+                               "step the class is many launches of every tree level, so no single per-launch "
+                               "figure applies",
                 "note": f"algorithmic = Schur-update flops of one factorisation x {S} frequencies; "
                         f"peak = dense bf16 ({src})"}
     else:
