@@ -558,7 +558,10 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 }  // namespace tc
 
 // Packs L21 and U12 of every front of a level and every frequency slot.
-// Grid: (fronts, slots, blocks); a CTA of 256 threads writes one block.
+// Grid: (fronts, slots, blocks); a CTA of 256 threads writes one block. A
+// thread takes one row and 4 consecutive k (one 16-byte row of a core matrix
+// per plane): 4 loads, then one 16-byte store per plane, so a warp writes
+// whole 128-byte lines.
 template <int NB>
 __global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* __restrict__ arena,
                                                     uint32_t* __restrict__ pack, const int64_t* __restrict__ pack_base,
@@ -573,39 +576,50 @@ __global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* _
   if (blk >= 2 * nA) return;
   const float2* F = arena + s * L.arena_size + L.foff[f];
   char* base = reinterpret_cast<char*>(pack) + s * slot_bytes + pack_base[f];
+  // word of (row, k) within a plane, k = 4 kq + (0..3) stored contiguously
+  auto row16 = [](int row, int kq) { return ((row >> 3) * (kTcKC >> 2) + kq) * 32 + (row & 7) * 4; };
   if (blk < nA) {
     const int tr = blk / nch, c = blk % nch;
     uint32_t* P = reinterpret_cast<uint32_t*>(base + (int64_t)blk * kSchurABlock);
-    for (int t = threadIdx.x; t < 128 * kTcKC; t += blockDim.x) {
-      const int ii = t % 128, kk = t / 128;  // lanes along the rows of L21: coalesced
-      const int i = tr * 128 + ii, k = c * kTcKC + kk;
-      const float2 v = (i < b && k < p) ? F[(int64_t)k * m + p + i] : make_float2(0.f, 0.f);
-      const int wd = tc_word(ii, kk);
-      uint32_t h, l;
-      tc::split_tf32(v.x, h, l);
-      P[0 * 128 * kTcKC + wd] = h;
-      P[1 * 128 * kTcKC + wd] = l;
-      tc::split_tf32(v.y, h, l);
-      P[2 * 128 * kTcKC + wd] = h;
-      P[3 * 128 * kTcKC + wd] = l;
+    constexpr int PL = 128 * kTcKC;  // words per plane
+    for (int t = threadIdx.x; t < 128 * (kTcKC / 4); t += blockDim.x) {
+      const int ii = t % 128, kq = t / 128;  // lanes along the rows of L21: coalesced loads
+      const int i = tr * 128 + ii, k0 = c * kTcKC + 4 * kq;
+      float2 v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = (i < b && k0 + q < p) ? F[(int64_t)(k0 + q) * m + p + i] : make_float2(0.f, 0.f);
+      uint4 rh, rl, ih, il;
+      tc::split_tf32(v[0].x, rh.x, rl.x); tc::split_tf32(v[1].x, rh.y, rl.y);
+      tc::split_tf32(v[2].x, rh.z, rl.z); tc::split_tf32(v[3].x, rh.w, rl.w);
+      tc::split_tf32(v[0].y, ih.x, il.x); tc::split_tf32(v[1].y, ih.y, il.y);
+      tc::split_tf32(v[2].y, ih.z, il.z); tc::split_tf32(v[3].y, ih.w, il.w);
+      const int wd = row16(ii, kq);
+      *reinterpret_cast<uint4*>(&P[0 * PL + wd]) = rh;
+      *reinterpret_cast<uint4*>(&P[1 * PL + wd]) = rl;
+      *reinterpret_cast<uint4*>(&P[2 * PL + wd]) = ih;
+      *reinterpret_cast<uint4*>(&P[3 * PL + wd]) = il;
     }
   } else {
     blk -= nA;
     const int tcol = blk / nch, c = blk % nch;
     uint32_t* P = reinterpret_cast<uint32_t*>(base + (int64_t)nA * kSchurABlock + (int64_t)blk * kSchurBBlock);
     constexpr int PL = 256 * kTcKC;  // words per plane
-    for (int t = threadIdx.x; t < 128 * kTcKC; t += blockDim.x) {
-      const int kk = t % kTcKC, jj = t / kTcKC;  // lanes along k: contiguous in a U12 column
-      const int j = tcol * 128 + jj, k = c * kTcKC + kk;
-      const float2 v = (j < b && k < p) ? F[(int64_t)(p + j) * m + k] : make_float2(0.f, 0.f);
-      uint32_t rh, rl, ih, il;
-      tc::split_tf32(v.x, rh, rl);
-      tc::split_tf32(v.y, ih, il);
-      const int w_re = tc_word(jj, kk), w_im = tc_word(128 + jj, kk);
-      P[0 * PL + w_re] = rh;  // W = [B_re ; B_im]
-      P[1 * PL + w_re] = rl;
-      P[0 * PL + w_im] = ih;
-      P[1 * PL + w_im] = il;
+    for (int t = threadIdx.x; t < 128 * (kTcKC / 4); t += blockDim.x) {
+      const int kq = t % (kTcKC / 4), jj = t / (kTcKC / 4);  // 4 lanes cover 16 k of a U12 column: coalesced
+      const int j = tcol * 128 + jj, k0 = c * kTcKC + 4 * kq;
+      float2 v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = (j < b && k0 + q < p) ? F[(int64_t)(p + j) * m + k0 + q] : make_float2(0.f, 0.f);
+      uint4 rh, rl, ih, il;
+      tc::split_tf32(v[0].x, rh.x, rl.x); tc::split_tf32(v[1].x, rh.y, rl.y);
+      tc::split_tf32(v[2].x, rh.z, rl.z); tc::split_tf32(v[3].x, rh.w, rl.w);
+      tc::split_tf32(v[0].y, ih.x, il.x); tc::split_tf32(v[1].y, ih.y, il.y);
+      tc::split_tf32(v[2].y, ih.z, il.z); tc::split_tf32(v[3].y, ih.w, il.w);
+      const int w_re = row16(jj, kq), w_im = row16(128 + jj, kq);  // W = [B_re ; B_im]
+      *reinterpret_cast<uint4*>(&P[0 * PL + w_re]) = rh;
+      *reinterpret_cast<uint4*>(&P[1 * PL + w_re]) = rl;
+      *reinterpret_cast<uint4*>(&P[0 * PL + w_im]) = ih;
+      *reinterpret_cast<uint4*>(&P[1 * PL + w_im]) = il;
     }
   }
 }
