@@ -1300,11 +1300,12 @@ static int num_sms() {
 
 // Fronts per level / border rows that select packed Schur levels. Measured
 // with the persistent packed kernel (32 frequencies per step, coupled 85k-DOF
-// sweep): (36, 1024) 120.7, (80, 512) 121.1, (150, 300) 121.6 solves/s.
+// sweep): (36, 1024) 120.7, (80, 512) 121.1, (150, 300) 121.6 solves/s; with
+// the vectorised pack pass (150, 300) 122.1, (300, 300) 123.2, (600, 200) 122.2.
 int pack_max_count() {
   static const int v = [] {
     const char* e = getenv("ELP_PACK_COUNT");
-    const int c = e ? atoi(e) : 150;
+    const int c = e ? atoi(e) : 300;
     return c < 0 ? 0 : c;
   }();
   return v;

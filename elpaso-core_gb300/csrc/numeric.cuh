@@ -141,7 +141,7 @@ struct DeviceSymbolic {
 
 // Levels whose Schur update runs from packed operands (k_pack_schur + k_schur_tc);
 // the others keep the converter kernel. pack_max_count(): fronts per level up
-// to which a level is packed (ELP_PACK_COUNT, default 150); pack_min_border():
+// to which a level is packed (ELP_PACK_COUNT, default 300); pack_min_border():
 // the largest border of the level must reach this many rows (ELP_PACK_MINB,
 // default 300).
 int pack_max_count();
