@@ -7,7 +7,7 @@ air cavity (depth 0.3 m), 2,400 InterfaceMindlin quads, unit force at a
 seeded plate node, f = 1..500 Hz (n = 85,034 DOFs). Synthetic, seeded
 (no public dataset exists for this path).
 
-A step solves one batch of `--batch` (default 32) frequencies of the sweep
+A step solves one batch of `--batch` (default 48) frequencies of the sweep
 through the mixed path (FP32 fronts + FP64 refinement to ||f - A u|| / ||f|| <= 1e-10);
 the plain FP64 path is timed beside it. `value` is whole-job solves/s with
 inputs resident in HBM; `e2e` is the same metric through elp_solve with host
@@ -494,7 +494,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plate_cavity")
-    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--batch", type=int, default=48)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-assembly", action="store_true")
