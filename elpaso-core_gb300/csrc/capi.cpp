@@ -258,6 +258,12 @@ int elp_solve_device(elp_model* h, const double* omegas, int n_omega, int precis
   int slots = (int)std::min<size_t>((size_t)kMaxSlots, std::max<size_t>(1, (freeb / 2) / std::max<size_t>(1, per_slot)));
   if (m.ws[precision] && m.ws[precision]->slots > 0) slots = std::max(slots, std::min(m.ws[precision]->slots, kMaxSlots));
   slots = std::min(slots, std::max(1, n_omega));
+  // equal chunks when the batch must be split (48 over 46 slots: 2 x 24, not
+  // 46 + 2, whose small remainder would cost nearly a whole factorisation pass)
+  if (n_omega > slots) {
+    const int chunks = (n_omega + slots - 1) / slots;
+    slots = (n_omega + chunks - 1) / chunks;
+  }
   int worst = ELP_OK;
   for (int s0 = 0; s0 < n_omega; s0 += slots) {
     int cnt = std::min(slots, n_omega - s0);
