@@ -132,7 +132,7 @@ class RequestResult(C.Structure):
 EXPORTS = [
     "elp_model_create", "elp_model_assemble", "elp_model_analyse", "elp_model_get_info",
     "elp_model_pattern", "elp_model_global_rows", "elp_model_system_values", "elp_model_rhs",
-    "elp_model_rhs_omega", "elp_cell_stresses",
+    "elp_model_rhs_omega", "elp_cell_stresses", "elp_node_stresses",
     "elp_solve", "elp_model_destroy", "elp_last_error", "elp_solve_device", "elp_model_time_assembly",
     "elp_server_create", "elp_server_add_model", "elp_server_submit", "elp_server_wait",
     "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc",
@@ -165,6 +165,7 @@ def load_library(path: str | None = None):
     lib.elp_model_rhs.argtypes = [P, P]
     lib.elp_model_rhs_omega.argtypes = [P, C.c_double, P]
     lib.elp_cell_stresses.argtypes = [P, C.c_double, P, P, P]
+    lib.elp_node_stresses.argtypes = [P, C.c_double, P, P]
     lib.elp_solve.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_double]
     lib.elp_solve_device.argtypes = [P, P, C.c_int, C.c_int, P, P, P, C.c_double, P]
     lib.elp_model_time_assembly.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -373,6 +374,16 @@ class Model:
         lo = np.zeros((ne, 9), np.complex128)
         _check(self.lib.elp_cell_stresses(self.handle, float(omega), _ptr(xs), _ptr(up), _ptr(lo)))
         return up, lo
+
+    def node_stresses(self, omega: float, x: np.ndarray) -> np.ndarray:
+        """[n_nodes, 9] complex nodal stresses of the solution x at omega,
+        nodes in ascending id."""
+        xs = np.ascontiguousarray(x, dtype=np.complex128)
+        if xs.shape != (self.n,):
+            raise ValueError("x must hold n complex values")
+        out = np.zeros((self.desc.n_nodes, 9), np.complex128)
+        _check(self.lib.elp_node_stresses(self.handle, float(omega), _ptr(xs), _ptr(out)))
+        return out
 
     def time_assembly(self, repeats: int = 3):
         a, b = C.c_double(), C.c_double()

@@ -198,6 +198,17 @@ int elp_cell_stresses(const elp_model* h, double omega, const double* x, double*
   GUARD_END
 }
 
+int elp_node_stresses(const elp_model* h, double omega, const double* x, double* sigma_nodes) {
+  GUARD_BEGIN
+  if (!h || !x || !sigma_nodes) { set_error("null argument"); return ELP_ERR_ARG; }
+  if (!(omega > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
+  std::string err;
+  const int rc = node_stresses(h->m, omega, reinterpret_cast<const cplx*>(x), reinterpret_cast<cplx*>(sigma_nodes), err);
+  if (rc) set_error(err);
+  return rc;
+  GUARD_END
+}
+
 int elp_model_rhs_omega(const elp_model* h, double omega, double* f_out) {
   GUARD_BEGIN
   if (!h || !f_out) { set_error("null argument"); return ELP_ERR_ARG; }

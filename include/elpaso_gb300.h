@@ -248,6 +248,14 @@ int elp_solve(elp_model* m, const double* omegas, int n_omega, int precision,
  * sigma_lower may be NULL. */
 int elp_cell_stresses(const elp_model* m, double omega, const double* x, double* sigma, double* sigma_lower);
 
+/* Nodal stresses of a solution x at omega (cAnalysis::computeStressesNodes,
+ * analysis.cpp:907-935): 9 complex slots per node, nodes in ascending id
+ * (GlobalSeqId). Brick8 adds its centre stress divided by the number of
+ * elements at the node to slots 0..5 (elementstructurebrick.cpp:161-270);
+ * Fluid8 adds grad p at each corner to slots 6..8, unaveraged
+ * (elementfluid3d.cpp:380-557); DSG4 adds nothing (not implemented there). */
+int elp_node_stresses(const elp_model* m, double omega, const double* x, double* sigma_nodes);
+
 int elp_model_destroy(elp_model* m);
 
 /* Text of the last error on the calling thread. */

@@ -437,6 +437,43 @@ def cell_stresses(system, omega, x):
     return np.array(up), np.array(lo)
 
 
+def node_stresses(system, omega, x):
+    """computeStressesNodes (analysis.cpp:907-935): 9 slots per node, nodes in
+    ascending id (GlobalSeqId, analysis.cpp:516). Brick8: centre stress / the
+    number of mesh elements at the node (countElementsPerNode, :455-469) added
+    to slots 0..5 (elementstructurebrick.cpp:161-270). Fluid8: grad p at each
+    corner, J^-1 dN/dxi p evaluated at that corner, added to slots 6..8
+    without averaging (elementfluid3d.cpp:380-557). Plates: nothing."""
+    d, rows = system.d, system.rows
+    x = np.asarray(x)
+    N = len(d.node_ids)
+    seq = np.empty(N, np.int64)
+    seq[np.argsort(np.asarray(d.node_ids), kind="stable")] = np.arange(N)
+    count = np.zeros(N)
+    for _, _, conn in d.blocks:
+        np.add.at(count, np.asarray(conn).ravel(), 1.0)
+    centre, _ = cell_stresses(system, omega, x)
+    out = np.zeros((N, 9), complex)
+    s = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
+                  [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], float)
+    idx = 0
+    for typ, _, conn in d.blocks:
+        for e in np.asarray(conn):
+            if typ == BRICK8:
+                for v in e:
+                    out[seq[v], :6] += centre[idx, :6] * (1.0 / count[v])
+            elif typ == FLUID8:
+                pv = np.array([x[rows[v, 16]] if rows[v, 16] >= 0 else 0.0 for v in e], complex)
+                for k, v in enumerate(e):
+                    g = 1.0 + s * s[k]  # (1 + s_f xi_k) per direction
+                    dN = 0.125 * np.stack([s[:, 0] * g[:, 1] * g[:, 2], s[:, 1] * g[:, 0] * g[:, 2],
+                                           s[:, 2] * g[:, 0] * g[:, 1]])
+                    J = dN @ d.coords[e]
+                    out[seq[v], 6:] += np.linalg.inv(J) @ dN @ pv
+            idx += 1
+    return out
+
+
 def dof_nodes(system):
     """Node index of every dof (global row) of an oracle System."""
     out = np.empty(system.n, np.int64)

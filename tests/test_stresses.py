@@ -1,8 +1,9 @@
-"""Cell stresses after a solve (cAnalysis::computeStressesCells,
-analysis.cpp:869-905; Brick8 elementstructurebrick.cpp:48-159, Mindlin/DSG4
-elementstructuremindlin.cpp:51-175), computed by the library
-(`elp_cell_stresses`) against the oracle's restatement and against closed
-forms. The stresses are linear in the solution, so arbitrary vectors stand
+"""Cell and nodal stresses after a solve (cAnalysis::computeStressesCells /
+computeStressesNodes, analysis.cpp:869-935; Brick8
+elementstructurebrick.cpp:48-270, Mindlin/DSG4 elementstructuremindlin.cpp:51-175,
+Fluid8 grad p elementfluid3d.cpp:380-557), computed by the library
+(`elp_cell_stresses`, `elp_node_stresses`) against the oracle's restatement
+and against closed forms. The stresses are linear in the solution, so arbitrary vectors stand
 in for solutions (no GPU needed)."""
 import copy
 
@@ -71,3 +72,39 @@ def test_cell_stresses_match_oracle(elp, meshes, oracle, model):
     scale = max(np.abs(ou).max(), 1e-300)
     np.testing.assert_allclose(up, ou, rtol=0, atol=1e-13 * scale)
     np.testing.assert_allclose(lo, ol, rtol=0, atol=1e-13 * scale)
+
+
+@pytest.mark.parametrize("model", ["cube", "plate_cavity"])
+def test_node_stresses_match_oracle(elp, meshes, oracle, model):
+    d = meshes.solid_cube(4) if model == "cube" else meshes.plate_cavity(6, 4, 3, 0.6, 0.4, 0.3)
+    m = elp.Model(d)
+    s = oracle.System(d)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(m.n) + 1j * rng.standard_normal(m.n)
+    om = 2 * np.pi * 77.0
+    got, ref = m.node_stresses(om, x), oracle.node_stresses(s, om, x)
+    scale = np.abs(ref).max()
+    assert scale > 0
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13 * scale)
+
+
+def test_node_pressure_gradient_closed_form(elp, meshes):
+    """A linear pressure field has the exact gradient g at every corner; the
+    nodal slots sum it over the node's Fluid8 elements."""
+    d = meshes.plate_cavity(6, 4, 3, 0.6, 0.4, 0.3)
+    m = elp.Model(d)
+    rows = m.global_rows()
+    g = np.array([3.0, -2.0, 0.5])
+    x = np.zeros(m.n, complex)
+    for v in range(d.n_nodes):
+        if rows[v, 16] >= 0:
+            x[rows[v, 16]] = (1 + 2j) * (d.coords[v] @ g)
+    out = m.node_stresses(2 * np.pi * 10.0, x)
+    fluid = [b for b in d.blocks if b[0] == 3][0][2]
+    nfl = np.bincount(np.asarray(fluid).ravel(), minlength=d.n_nodes)
+    seq = np.empty(d.n_nodes, np.int64)
+    seq[np.argsort(d.node_ids, kind="stable")] = np.arange(d.n_nodes)
+    expect = np.zeros((d.n_nodes, 3), complex)
+    expect[seq] = nfl[:, None] * (1 + 2j) * g[None, :]
+    np.testing.assert_allclose(out[:, 6:], expect, rtol=0, atol=1e-11 * np.abs(expect).max())
+
