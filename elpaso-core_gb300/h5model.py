@@ -34,8 +34,9 @@ and writes both files elpasoC writes for this path: the solution file
 integer attributes ``numrow``, ``numcol``, 1-based CSR ``vecCsrIa``,
 ``vecCsrJa`` and complex ``cmpCsrVal``; ``ESC/math/mathlibrary.cpp:53-86``).
 
-Interface elements are not read (a model that has them raises
-``NotImplementedError``; coupled models are described in code).
+``/InterfaceElements`` of type ``InterfaceMindlin`` are read
+(``read_interfaces``); non-conforming interface elements raise
+``NotImplementedError``.
 """
 from __future__ import annotations
 
@@ -108,6 +109,35 @@ def frequency_list(input_path: str, start: float, delta: float, steps: int) -> n
     return np.unique(np.asarray(vals, dtype=np.float64))
 
 
+def read_interfaces(f, index, mat_index):
+    """``/InterfaceElements`` (cFemParserHDF5::getInterfaceElementsData,
+    femparserhdf5.cpp:527-552; cElementInterfaceFactory::parseSingleInterfaceElement,
+    elementinterfacefactory.cpp:62-97): per dataset, attribute ``type``
+    (``InterfaceMindlin``), ``matF``, and integer rows (element id, ori,
+    structure node ids..., fluid node ids...). Returns the ModelDesc
+    ``interfaces`` dict, or None without interface elements. ``index`` maps
+    node ids to indices, ``mat_index`` material ids to material indices."""
+    if "InterfaceElements" not in f or not int(f["InterfaceElements"].attrs.get("N", 0)):
+        return None
+    ori, snodes, fnodes, fmat = [], [], [], []
+    for name in sorted(f["InterfaceElements"].keys()):
+        ds = f["InterfaceElements"][name]
+        a = ds.attrs
+        if a.get("type") != "InterfaceMindlin":
+            raise NotImplementedError(f"interface type {a.get('type')}")
+        nnod = int(a.get("NfluidNodes", 4))
+        if nnod != 4 or int(a.get("NstructNodes", 4)) != 4:
+            raise NotImplementedError("interface elements with other than 4 + 4 nodes")
+        rows = np.asarray(ds.read()).astype(np.int64).reshape(-1, 2 + 2 * nnod)
+        for r in rows:
+            ori.append(float(r[1]))
+            snodes.append([index[int(v)] for v in r[2:2 + nnod]])
+            fnodes.append([index[int(v)] for v in r[2 + nnod:2 + 2 * nnod]])
+            fmat.append(mat_index[int(a["matF"])])
+    return dict(ori=np.array(ori), snodes=np.array(snodes, np.int64), fnodes=np.array(fnodes, np.int64),
+                fmat=np.array(fmat, np.int64))
+
+
 def read_model(path: str, model_desc_cls=None):
     """Reads an elpasoC model file. Returns (ModelDesc, frequencies in Hz)."""
     if model_desc_cls is None:
@@ -150,9 +180,9 @@ def read_model(path: str, model_desc_cls=None):
             element_at[int(eid)] = (len(blocks), e)
         blocks.append((typ, mat_index[int(ds.attrs["MaterialId"])], conn.astype(np.int32)))
 
-    for grp in ("InterfaceElements", "NCInterfaceElements"):
-        if grp in f and int(f[grp].attrs.get("N", 0)):
-            raise NotImplementedError(f"{grp} are not read")
+    interfaces = read_interfaces(f, index, mat_index)
+    if "NCInterfaceElements" in f and int(f["NCInterfaceElements"].attrs.get("N", 0)):
+        raise NotImplementedError("NCInterfaceElements are not read")
 
     fnode, fdof, fval = [], [], []
     if "NodeConstraints" in f:
@@ -200,7 +230,7 @@ def read_model(path: str, model_desc_cls=None):
     an = f["Analysis"].attrs
     freqs = frequency_list(path, float(an["start"]), float(an["delta"]), int(an["steps"]))
     desc = model_desc_cls(
-        node_ids=ids, coords=coords, materials=mats, blocks=blocks,
+        node_ids=ids, coords=coords, materials=mats, blocks=blocks, interfaces=interfaces,
         fixed=dict(node=np.array(fnode, np.int64), dof=np.array(fdof, np.int64), value=np.array(fval, complex)),
         forces=dict(node=np.array(lnode, np.int64), f=np.array(lf).reshape(-1, 3)),
         moments=dict(node=np.array(mnode, np.int64), m=np.array(mm).reshape(-1, 3)),

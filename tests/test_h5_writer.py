@@ -56,3 +56,27 @@ def test_dof_map_matches_reference_tutorial(elp, h5model):
     d = tutorial_desc(elp, g)
     dm = h5model.dof_map(d.node_ids, elp.Model(d).global_rows())
     np.testing.assert_array_equal(dm, g["dof_map"])
+
+
+def test_interface_elements_are_read(h5model, tmp_path):
+    """/InterfaceElements rows (element id, ori, 4 structure node ids, 4 fluid
+    node ids) with type InterfaceMindlin and matF (femparserhdf5.cpp:527-552,
+    elementinterfacefactory.cpp:62-97) become the ModelDesc interfaces."""
+    h5 = h5model.h5lite
+    path = str(tmp_path / "iface.hdf5")
+    rows = np.array([[7, 1, 11, 12, 13, 14, 21, 22, 23, 24],
+                     [8, -1, 12, 15, 16, 13, 22, 25, 26, 23]], np.int32)
+    w = h5.Writer(path)
+    w.group("InterfaceElements")
+    w.attr("InterfaceElements", "N", 1)
+    w.dataset("InterfaceElements/mtxFemInterfaceElementGroup1", rows)
+    for k, v in (("type", "InterfaceMindlin"), ("matF", 3), ("mats", 1), ("NfluidNodes", 4), ("NstructNodes", 4)):
+        w.attr("InterfaceElements/mtxFemInterfaceElementGroup1", k, v)
+    w.close()
+    ids = [11, 12, 13, 14, 15, 16, 21, 22, 23, 24, 25, 26]
+    index = {v: i for i, v in enumerate(ids)}
+    q = h5model.read_interfaces(h5.File(path), index, {3: 1, 1: 0})
+    np.testing.assert_array_equal(q["ori"], [1.0, -1.0])
+    np.testing.assert_array_equal(q["snodes"], [[0, 1, 2, 3], [1, 4, 5, 2]])
+    np.testing.assert_array_equal(q["fnodes"], [[6, 7, 8, 9], [7, 10, 11, 8]])
+    np.testing.assert_array_equal(q["fmat"], [1, 1])
