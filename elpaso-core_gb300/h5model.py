@@ -14,7 +14,8 @@ path (``ESC/misc/parser/femparserhdf5.cpp:202-499``; group names from
   dataset of rows (frequency [Hz], value): the frequency table
   (``materialstructurevisco.cpp:75-170, 643-690``);
 * ``/NodeConstraints/*``: structural constraints with flags ``u1..u3``,
-  ``w1..w3`` and values ``valu*``/``valw*`` (reference DOF enum 0..5);
+  ``w1..w3`` and values ``valu*``/``valw*`` (reference DOF enum 0..5), and
+  ``acoustic`` ones fixing the fluid dof (enum 16) at ``p``;
 * ``/NodeLoads/*``: ``point_force`` loads ``Fx, Fy, Fz`` and ``fluid`` point
   sources ``P`` at ``NodeId``; ``/NodeMoments/*``: ``point_moment`` loads
   ``Mx, My, Mz``; ``/ElemLoads/*``: ``vn`` loads (``vn``, ``Face``,
@@ -188,13 +189,19 @@ def read_model(path: str, model_desc_cls=None):
     if "NodeConstraints" in f:
         for name in sorted(f["NodeConstraints"].keys()):
             a = f["NodeConstraints"][name].attrs
-            if a.get("ConstraintType") != "structure":
-                raise NotImplementedError(f"constraint type {a.get('ConstraintType')}")
-            for key, dof in _CONSTRAINT_DOFS:
-                if int(a.get(key, 0)):
-                    fnode.append(index[int(a["NodeId"])])
-                    fdof.append(dof)
-                    fval.append(complex(float(a.get("val" + key, 0.0))))
+            kind = a.get("ConstraintType")
+            if kind == "structure":
+                for key, dof in _CONSTRAINT_DOFS:
+                    if int(a.get(key, 0)):
+                        fnode.append(index[int(a["NodeId"])])
+                        fdof.append(dof)
+                        fval.append(complex(float(a.get("val" + key, 0.0))))
+            elif kind == "acoustic":  # fixed pressure p on the fluid dof (boundaryconditionfluid.cpp:36-57)
+                fnode.append(index[int(a["NodeId"])])
+                fdof.append(16)
+                fval.append(complex(float(a.get("p", 0.0))))
+            else:
+                raise NotImplementedError(f"constraint type {kind}")
     lnode, lf, snode, sp = [], [], [], []
     if "NodeLoads" in f:  # cNodalForceFactory (nodalforcefactory.cpp:36-55)
         for name in sorted(f["NodeLoads"].keys()):
