@@ -24,7 +24,8 @@ attribute storage, variable-length types) raises ``NotImplementedError``.
 ``Writer`` produces files in the same subset (superblock 0, v1 object
 headers, symbol-table groups with full-size v1 B-tree nodes of K = 16 and
 symbol nodes of K = 4 -- up to 8,192 links per group --, contiguous datasets
-of float64 / int32 / int64 / complex128 stored as the compound {real, imag},
+of float64 / int32 / int64 / complex128 stored as the compound {real, imag}
+/ structured arrays of those (compounds, e.g. elpasoC's node table),
 scalar int64 / float64 / fixed-length string attributes). The image this was
 built in has no HDF5 library, so files are checked by a round trip through
 ``File`` only.
@@ -368,7 +369,19 @@ def _dt_complex() -> bytes:
     return out
 
 
+def _dt_struct(dt: np.dtype) -> bytes:
+    # class 6 (compound), version 1, one member per field of a structured dtype
+    out = bytes([0x16, len(dt.names) & 0xFF, len(dt.names) >> 8, 0]) + struct.pack("<I", dt.itemsize)
+    for name in dt.names:
+        sub, off = dt.fields[name][:2]
+        out += _pad8(name.encode() + b"\0") + struct.pack("<I", off) + bytes(4) + bytes(4) + bytes(4) + bytes(16)
+        out += _dtype_message(sub)
+    return out
+
+
 def _dtype_message(dt: np.dtype) -> bytes:
+    if dt.names is not None:
+        return _dt_struct(dt)
     if dt == np.float64:
         return _dt_float64()
     if dt == np.complex128:
@@ -416,7 +429,11 @@ class Writer:
         parts = [p for p in path.split("/") if p]
         parent = self._group("/".join(parts[:-1]))
         arr = np.ascontiguousarray(data)
-        if arr.dtype not in (np.float64, np.complex128, np.int32, np.int64):
+        plain = (np.float64, np.complex128, np.int32, np.int64)
+        if arr.dtype.names is not None:  # compound of plain members (e.g. the node table)
+            if any(arr.dtype.fields[n][0] not in plain for n in arr.dtype.names):
+                raise NotImplementedError(f"compound member type in {arr.dtype}")
+        elif arr.dtype not in plain:
             raise NotImplementedError(f"dataset type {arr.dtype}")
         parent["children"][parts[-1]] = {"data": arr, "attrs": []}
         return self
