@@ -29,7 +29,9 @@ analysisfrequencybasic.cpp:184-262``): ``/Solution/State/vecFemStep{k}``
 complex vectors with ``FreqStep{k}`` attributes, ``/Solution/Maps/mtxDofMap``
 (node id, dof enum) per global row.
 
-and writes both files elpasoC writes for this path: the solution file
+and writes elpasoC model files (``write_model``: a ModelDesc in the layout
+above, so the reference can run the package's synthetic configurations) and
+both files elpasoC writes for this path: the solution file
 (``write_solution``, the layout above) and the system-matrix export of
 ``-exportSysH5`` (``write_system_matrix``: ``/SystemMatrices/<type>`` with
 integer attributes ``numrow``, ``numcol``, 1-based CSR ``vecCsrIa``,
@@ -246,6 +248,116 @@ def read_model(path: str, model_desc_cls=None):
                       vn=np.array(vv, float)),
         name=os.path.splitext(os.path.basename(path))[0])
     return desc, freqs
+
+
+def write_model(path: str, d, start: float = 1.0, delta: float = 1.0, steps: int = 1, node_order=None):
+    """Writes a ModelDesc as an elpasoC model file (the layout read_model and
+    the reference's cFemParserHDF5 read; group and attribute names of
+    ESC/misc/hdf5/rulesh5.h:31-332), so the reference can run the same model.
+    Material i gets Id i + 10, element ids run from 100 over the blocks,
+    interface elements from 9000; E / eta tables go to root datasets named by
+    the material's attributes. node_order permutes the rows of the node table
+    (the reference sorts nodes by id)."""
+    w = h5lite.Writer(path)
+    n = d.n_nodes
+    ids = np.asarray(d.node_ids, np.int64)
+    nodes = np.zeros(n, dtype=[("Ids", np.int64), ("xCoords", np.float64), ("yCoords", np.float64),
+                                 ("zCoords", np.float64)])
+    perm = np.arange(n) if node_order is None else np.asarray(node_order)
+    nodes["Ids"] = ids[perm]
+    for k, c in enumerate(("xCoords", "yCoords", "zCoords")):
+        nodes[c] = np.asarray(d.coords)[perm, k]
+    w.dataset("Nodes/mtxFemNodes", nodes)
+    kinds = {v: k for k, v in _MATERIAL_KINDS.items()}
+    for i, m in enumerate(d.materials):
+        g = f"Materials/material{i + 1}"
+        w.group(g)
+        w.attr(g, "Id", i + 10)
+        w.attr(g, "MaterialType", kinds[int(m["kind"])])
+        for key in ("E", "nu", "rho", "t", "eta", "c"):
+            tab = m.get(key + "_table")
+            if tab is not None and len(tab):
+                w.dataset(f"{key}_table_{i}", np.asarray(tab, float).reshape(-1, 2))
+                w.attr(g, key, f"{key}_table_{i}")
+            else:
+                w.attr(g, key, repr(float(m.get(key, 0.0))))
+        w.attr(g, "type", str(int(m.get("visco_type", 1))))
+    eid = 100
+    names = {v: k for k, v in _ELEMENT_TYPES.items()}
+    starts = [eid]
+    for b, (typ, mi, conn) in enumerate(d.blocks):
+        conn = np.asarray(conn)
+        rows = np.column_stack([np.arange(eid, eid + len(conn)), ids[conn]]).astype(np.int64)
+        eid += len(conn)
+        starts.append(eid)
+        ds = f"Elements/mtxFemElemGroup{b + 1}"
+        w.dataset(ds, rows)
+        w.attr(ds, "ElementType", names[int(typ)])
+        w.attr(ds, "MaterialId", int(mi) + 10)
+    q = d.interfaces
+    if q is not None and len(q["ori"]):
+        fmat = np.asarray(q.get("fmat", np.zeros(len(q["ori"]), np.int64)))
+        w.group("InterfaceElements")
+        groups = sorted(set(int(v) for v in fmat))
+        w.attr("InterfaceElements", "N", len(groups))
+        for gi, fm in enumerate(groups):
+            sel = np.nonzero(fmat == fm)[0]
+            rows = np.column_stack([sel + 9000, np.rint(np.asarray(q["ori"])[sel]).astype(np.int64),
+                                    ids[np.asarray(q["snodes"])[sel]], ids[np.asarray(q["fnodes"])[sel]]])
+            ds = f"InterfaceElements/mtxFemInterfaceElements{gi + 1}"
+            w.dataset(ds, rows.astype(np.int64))
+            for k, v in (("type", "InterfaceMindlin"), ("matF", fm + 10), ("mats", 10), ("NfluidNodes", 4),
+                         ("NstructNodes", 4)):
+                w.attr(ds, k, v)
+    dof_keys = ("u1", "u2", "u3", "w1", "w2", "w3")
+    if d.fixed is not None:
+        vals = d.fixed.get("value", np.zeros(len(d.fixed["node"]), complex))
+        for k, (node, dof, val) in enumerate(zip(d.fixed["node"], d.fixed["dof"], vals)):
+            g = f"NodeConstraints/nodeConstraint{k}"
+            w.dataset(g, np.zeros(1))
+            w.attr(g, "NodeId", int(ids[node]))
+            w.attr(g, "Id", k + 1)
+            if int(dof) == 16:
+                w.attr(g, "ConstraintType", "acoustic")
+                w.attr(g, "p", float(complex(val).real))
+            else:
+                w.attr(g, "ConstraintType", "structure")
+                w.attr(g, dof_keys[int(dof)], 1)
+                w.attr(g, "val" + dof_keys[int(dof)], float(complex(val).real))
+    k = 0
+    for node, f in zip(*(() if d.forces is None else (d.forces["node"], d.forces["f"]))):
+        g = f"NodeLoads/load{k}"
+        k += 1
+        w.dataset(g, np.zeros(1))
+        for key, v in (("LoadType", "point_force"), ("Id", k), ("NodeId", int(ids[node])), ("Fx", float(f[0])),
+                       ("Fy", float(f[1])), ("Fz", float(f[2]))):
+            w.attr(g, key, v)
+    src = getattr(d, "fluid_sources", None)
+    for node, p in zip(*(() if src is None else (src["node"], src["p"]))):
+        g = f"NodeLoads/load{k}"
+        k += 1
+        w.dataset(g, np.zeros(1))
+        for key, v in (("LoadType", "fluid"), ("Id", k), ("NodeId", int(ids[node])), ("P", float(p))):
+            w.attr(g, key, v)
+    mom = getattr(d, "moments", None)
+    for j, (node, mm) in enumerate(zip(*(() if mom is None else (mom["node"], mom["m"])))):
+        g = f"NodeMoments/moment{j}"
+        w.dataset(g, np.zeros(1))
+        for key, v in (("LoadType", "point_moment"), ("Id", j + 1), ("NodeId", int(ids[node])), ("Mx", float(mm[0])),
+                       ("My", float(mm[1])), ("Mz", float(mm[2]))):
+            w.attr(g, key, v)
+    vl = getattr(d, "vn_loads", None)
+    for j in range(0 if vl is None else len(vl["vn"])):
+        g = f"ElemLoads/eload{j}"
+        w.dataset(g, np.zeros(1))
+        e = starts[int(vl["block"][j])] + int(vl["element"][j])
+        for key, v in (("LoadType", "vn"), ("Id", j + 1), ("ElementId", e), ("Face", int(vl["face"][j])),
+                       ("vn", float(vl["vn"][j]))):
+            w.attr(g, key, v)
+    w.group("Analysis")
+    for key, v in (("start", repr(float(start))), ("delta", repr(float(delta))), ("steps", str(int(steps)))):
+        w.attr("Analysis", key, v)
+    w.close()
 
 
 def read_solution(path: str):
