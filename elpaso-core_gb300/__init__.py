@@ -90,6 +90,10 @@ class _VnLoad(C.Structure):
     _fields_ = [("block", C.c_int32), ("face", C.c_int32), ("element", C.c_int64), ("vn", C.c_double)]
 
 
+class _FaceTraction(C.Structure):
+    _fields_ = [("block", C.c_int32), ("face", C.c_int32), ("element", C.c_int64), ("t", C.c_double * 6)]
+
+
 class _Desc(C.Structure):
     _fields_ = [("n_nodes", C.c_int64), ("node_ids", C.POINTER(C.c_int64)), ("coords", C.POINTER(C.c_double)),
                 ("n_materials", C.c_int), ("materials", C.POINTER(_Material)),
@@ -99,7 +103,8 @@ class _Desc(C.Structure):
                 ("n_forces", C.c_int64), ("forces", C.POINTER(_Force)),
                 ("n_moments", C.c_int64), ("moments", C.POINTER(_Moment)),
                 ("n_fluid_sources", C.c_int64), ("fluid_sources", C.POINTER(_FluidSource)),
-                ("n_vn_loads", C.c_int64), ("vn_loads", C.POINTER(_VnLoad))]
+                ("n_vn_loads", C.c_int64), ("vn_loads", C.POINTER(_VnLoad)),
+                ("n_face_tractions", C.c_int64), ("face_tractions", C.POINTER(_FaceTraction))]
 
 
 class _Info(C.Structure):
@@ -212,6 +217,7 @@ class ModelDesc:
     moments: dict | None = None                       # node[k], m[k,3] (on w1 w2 w3)
     fluid_sources: dict | None = None                 # node[k], p[k] (F += 4 pi p on the fluid row)
     vn_loads: dict | None = None                      # block[k], element[k], face[k] (1..6), vn[k]
+    face_tractions: dict | None = None                # Brick8: block[k], element[k], face[k] (1..6), t[k,3] complex
     name: str = "model"
 
     @property
@@ -290,9 +296,19 @@ class _DescHolder:
             vl[k] = _VnLoad(int(d.vn_loads["block"][k]), int(d.vn_loads["face"][k]), int(d.vn_loads["element"][k]),
                             float(d.vn_loads["vn"][k]))
         self.vl = vl
+        nt = 0 if d.face_tractions is None else len(d.face_tractions["element"])
+        tr = (_FaceTraction * max(1, nt))()
+        for k in range(nt):
+            tr[k].block = int(d.face_tractions["block"][k])
+            tr[k].face = int(d.face_tractions["face"][k])
+            tr[k].element = int(d.face_tractions["element"][k])
+            for j in range(3):
+                t = complex(d.face_tractions["t"][k][j])
+                tr[k].t[2 * j], tr[k].t[2 * j + 1] = t.real, t.imag
+        self.tr = tr
         self.desc = _Desc(len(self.ids), self.ids.ctypes.data_as(C.POINTER(C.c_int64)),
                           self.xyz.ctypes.data_as(C.POINTER(C.c_double)), len(d.materials), mats,
-                          len(d.blocks), blocks, nq, ifs, nf, fx, nl, fo, nm, mo, ns, so, nv, vl)
+                          len(d.blocks), blocks, nq, ifs, nf, fx, nl, fo, nm, mo, ns, so, nv, vl, nt, tr)
 
 
 class Model:

@@ -20,7 +20,9 @@
 //  - nodal forces add F on active x1, x2, x3 rows (analysis.cpp:171-279),
 //    fluid point sources 4 pi p on the fluid row, nodal moments on w1..w3
 //    (analysis.cpp:243-265, 281-364); normal-velocity loads on Fluid8 faces
-//    form the 1/w part of F (elementfluid3d.cpp:241-309).
+//    form the 1/w part of F (elementfluid3d.cpp:241-309); constant tractions
+//    on Brick8 faces add to F before the nodal loads
+//    (elementstructurebrick.cpp:556-662).
 #include "model.hpp"
 
 #include <algorithm>
@@ -247,6 +249,19 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
       }
     }
   }
+  if (d->n_face_tractions > 0) {
+    if (!d->face_tractions) { err = "bad face tractions"; return ELP_ERR_ARG; }
+    m.face_tractions.assign(d->face_tractions, d->face_tractions + d->n_face_tractions);
+    for (auto& l : m.face_tractions) {
+      bool finite = true;
+      for (double t : l.t) finite = finite && std::isfinite(t);
+      if (l.block < 0 || l.block >= (int)m.blocks.size() || m.blocks[l.block].type != ELP_BRICK8 ||
+          l.element < 0 || l.element >= m.blocks[l.block].n_elements || l.face < 1 || l.face > 6 || !finite) {
+        err = "face traction needs a Brick8 element, a face 1..6 and finite values";
+        return ELP_ERR_ARG;
+      }
+    }
+  }
 
   const int64_t N = m.n_nodes;
   // ---- node order by ascending id, duplicate ids rejected
@@ -457,6 +472,21 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
   // ---- right-hand side: nodal forces (ADD) then BC values (set)
   m.rhs.assign(n, cplx(0.0, 0.0));
   {
+    // element load vectors first (assembleGlobalTensors adds them before the
+    // nodal loads): Brick8 face tractions, t_d int_face N_z dA on u_d of each
+    // face node (sum_s C(z, s) t_d with sum_s N_s = 1)
+    for (const auto& l : m.face_tractions) {
+      const int32_t* en = &m.blocks[l.block].conn[(size_t)l.element * 8];
+      int32_t fn[4];
+      face_nodes_hex8(l.face - 1, en, fn);
+      double nint[4];
+      if (!face_shape_integrals(m, fn, nint)) { err = "face traction on a degenerate face"; return ELP_ERR_ARG; }
+      for (int z = 0; z < 4; ++z)
+        for (int d3 = 0; d3 < 3; ++d3) {
+          const int32_t g = grow(fn[z], d3);
+          if (g >= 0) m.rhs[g] += cplx(l.t[2 * d3], l.t[2 * d3 + 1]) * nint[z];
+        }
+    }
     // forces are applied per node in id order (analysis.cpp:187-276)
     std::vector<std::vector<int32_t>> node_forces(N);
     for (size_t i = 0; i < m.forces.size(); ++i) node_forces[m.forces[i].node].push_back((int32_t)i);

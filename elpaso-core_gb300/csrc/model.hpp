@@ -76,6 +76,7 @@ struct Model {
   std::vector<elp_nodal_moment> moments;
   std::vector<elp_fluid_source> fluid_sources;
   std::vector<elp_vn_load> vn_loads;
+  std::vector<elp_face_traction> face_tractions;
 
   // ---- numbering (analysis.cpp:475-520)
   std::vector<int32_t> order;        // node indices by ascending id

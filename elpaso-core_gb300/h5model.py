@@ -257,7 +257,10 @@ def write_model(path: str, d, start: float = 1.0, delta: float = 1.0, steps: int
     Material i gets Id i + 10, element ids run from 100 over the blocks,
     interface elements from 9000; E / eta tables go to root datasets named by
     the material's attributes. node_order permutes the rows of the node table
-    (the reference sorts nodes by id)."""
+    (the reference sorts nodes by id). Brick8 face tractions have no entry in
+    that format (its element-load factory makes vn loads only) and are refused."""
+    if getattr(d, "face_tractions", None) is not None and len(d.face_tractions["element"]):
+        raise ValueError("an elpasoC model file cannot hold Brick8 face tractions")
     w = h5lite.Writer(path)
     n = d.n_nodes
     ids = np.asarray(d.node_ids, np.int64)

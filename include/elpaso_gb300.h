@@ -138,6 +138,20 @@ typedef struct {
   double vn;              /* normal velocity                                    */
 } elp_vn_load;
 
+/* Constant traction on a face of a Brick8 element (cElementLoadStructureConst,
+ * elementloadstructureconst.cpp; cElementStructureBrick::assembleLoadVector and
+ * evaluateSurfaceIntegral, elementstructurebrick.cpp:556-662): the u1 u2 u3
+ * rows of the face's four nodes get sum_s C(z, s) t_d with
+ * C(z, s) = int_face N_z N_s dA, the same traction t at every face node.
+ * The reference reads three amplitudes and one phase: t_d = amp_d e^(i phase).
+ * face 1..6 as for elp_vn_load. The load does not depend on w. */
+typedef struct {
+  int32_t block;          /* index into blocks (an ELP_BRICK8 block)            */
+  int32_t face;           /* 1..6                                               */
+  int64_t element;        /* element index within the block                     */
+  double t[6];            /* (re, im) of t1, t2, t3                             */
+} elp_face_traction;
+
 typedef struct {
   int64_t n_nodes;
   const int64_t* node_ids;  /* reference node ids; numbering follows ascending id */
@@ -158,6 +172,8 @@ typedef struct {
   const elp_fluid_source* fluid_sources;
   int64_t n_vn_loads;
   const elp_vn_load* vn_loads;
+  int64_t n_face_tractions;
+  const elp_face_traction* face_tractions;
 } elp_model_desc;
 
 typedef struct elp_model elp_model;

@@ -13,7 +13,9 @@ elpasoCore/source/ of the reference):
   BC rows        analysis/analysis.cpp:366-454 (MatZeroRows diag = 1, F[row] = value)
   RHS            analysis/analysis.cpp:171-364 (nodal forces, fluid point
                  sources, nodal moments, ADD); normal-velocity face loads of
-                 Fluid8 elements as the 1/w part (elementfluid3d.cpp:241-309)
+                 Fluid8 elements as the 1/w part (elementfluid3d.cpp:241-309);
+                 constant Brick8 face tractions, C t with the face matrix C
+                 (elementstructurebrick.cpp:556-662), before the nodal loads
   values         element matrices EM(w) of oracle/elp_oracle.c, inserted per
                  element, interfaces with -ori (analysisfrequencybasic.cpp:101-157)
   stresses       cell stresses after the solve (analysis.cpp:869-905)
@@ -166,6 +168,25 @@ def face_integrals(xyz):
     return out
 
 
+def face_matrix(xyz):
+    """C(z, s) = int N_z N_s dA over a 4-node face, evaluateSurfaceIntegral of
+    the Brick8 element (element/structure/linear/brick/elementstructurebrick.cpp:597-662;
+    the same quadrature as face_integrals, whose results are the row sums)."""
+    xyz = np.asarray(xyz, np.float64)
+    cx = np.array([-1.0, 1.0, 1.0, -1.0])
+    cy = np.array([-1.0, -1.0, 1.0, 1.0])
+    C = np.zeros((4, 4))
+    g = 1.0 / np.sqrt(3.0)
+    for u in (-g, g):
+        for v in (-g, g):
+            N = 0.25 * (1 + cx * u) * (1 + cy * v)
+            a1 = (0.25 * cx * (1 + cy * v)) @ xyz
+            a2 = (0.25 * cy * (1 + cx * u)) @ xyz
+            jac = np.sqrt(a1 @ a1 * (a2 @ a2) - (a1 @ a2) ** 2)
+            C += np.outer(N, N) * jac
+    return C
+
+
 # ------------------------------------------------------------------ host flow
 class System:
     """Numbering, pattern, BC rows and RHS of a model description."""
@@ -228,6 +249,21 @@ class System:
                         self.bc_rows.append(int(rows[v, dof]))
                         self.bc_vals.append(complex(d.fixed["value"][k]) if "value" in d.fixed else 0j)
         f = np.zeros(r, np.complex128)
+        # element load vectors come first (assembleGlobalTensors, then the nodal
+        # loads): a constant traction t on a Brick8 face adds
+        # LV[3 z + d] = sum_s C(z, s) t_d (elementstructurebrick.cpp:556-595)
+        if getattr(d, "face_tractions", None) is not None:
+            ft = d.face_tractions
+            for k in range(len(ft["element"])):
+                conn = np.asarray(d.blocks[int(ft["block"][k])][2])[int(ft["element"][k])]
+                face = conn[list(HEX8_FACES[int(ft["face"][k]) - 1])]
+                C = face_matrix(d.coords[face])
+                t = np.asarray(ft["t"][k], np.complex128)
+                lv = C @ np.tile(t, (4, 1))  # F[3 s + d] = t_d at every face node
+                for z in range(4):
+                    for dd in range(3):
+                        if rows[face[z], dd] >= 0:
+                            f[rows[face[z], dd]] += lv[z, dd]
         if d.forces is not None:
             for k in range(len(d.forces["node"])):
                 v = int(d.forces["node"][k])

@@ -123,3 +123,12 @@ def test_moments_sources_and_normal_velocity_loads(elp, meshes, oracle, prec):
     d.fluid_sources["p"] = d.fluid_sources["p"] * 3e-4
     d.vn_loads["vn"] = d.vn_loads["vn"] * 3e-3
     check(elp, oracle, d, [2.0, 61.0, 233.0, 499.0], prec)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_brick_face_tractions(elp, meshes, oracle, prec):
+    """Clamped 20 x 20 x 2 Brick8 plate (the system of the 100 Hz test above)
+    with complex constant tractions on 40 random faces besides the centre
+    force: the right-hand side built at model creation reaches the solve."""
+    from test_loads import traction_brick
+    check(elp, oracle, traction_brick(meshes, nx=20, ny=20, count=40), [100.0], prec)

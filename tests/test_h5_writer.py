@@ -130,3 +130,12 @@ def test_model_file_round_trip(elp, meshes, h5model, tmp_path):
     m1, m2 = elp.Model(d), elp.Model(r)
     np.testing.assert_array_equal(m1.pattern()[1], m2.pattern()[1])
     np.testing.assert_allclose(m2.rhs(2 * np.pi * 20.0), m1.rhs(2 * np.pi * 20.0), rtol=0, atol=1e-15)
+
+
+def test_model_file_refuses_face_tractions(meshes, h5model, tmp_path):
+    """elpasoC's model file has no structure element loads: writing a model
+    with Brick8 face tractions fails instead of dropping them."""
+    from test_loads import traction_brick
+    with pytest.raises(ValueError):
+        h5model.write_model(str(tmp_path / "t.hdf5"), traction_brick(meshes))
+    assert not (tmp_path / "t.hdf5").exists()
