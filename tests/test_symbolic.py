@@ -1,0 +1,107 @@
+"""Host symbolic phase (nested dissection + multifrontal fronts, the part of
+`elp_model_analyse` that replaces MUMPS's analysis behind
+initializeSolverObjects, analysis.cpp:1071-1226) on edge-case models. It runs
+on the host before the device step, so these run without a GPU: analyse
+either succeeds (GPU present) or fails with the no-device status, and the
+front statistics are there in both cases.
+
+Invariants: one element is one dense front (m^2 entries, sum over the
+pivots of 8 r (r + 1) = 8 (m - 1) m (m + 1) / 3 real flops of a complex LU);
+two identical disconnected bodies give exactly twice the fronts, entries and
+flops; nodes without elements add no DOFs; the analysis is deterministic."""
+import copy
+
+import numpy as np
+import pytest
+
+
+def analysed(elp, d):
+    m = elp.Model(d)
+    try:
+        m.analyse()
+    except elp.ElpasoError as e:
+        assert e.code == 2, e  # no device: the host phase ran
+    return m, m.info()
+
+
+def lu_flops(m):
+    return 8.0 * (m - 1) * m * (m + 1) / 3.0
+
+
+def test_one_element_is_one_dense_front(elp, meshes):
+    for d, nd in ((meshes.solid_cube(1, perturb=0.0, n_materials=1), 24), (meshes.plate(2, 2, 0.1, 0.1, 0.002), 27)):
+        m, i = analysed(elp, d)
+        assert m.n == nd
+        assert (i["n_fronts"], i["n_levels"], i["max_front"]) == (1, 1, nd)
+        assert i["factor_entries"] == nd * nd
+        assert i["factor_flops"] == lu_flops(nd)
+        assert i["gemm_flops"] == 0.0  # a single panel sweep has no trailing rows
+
+
+def two_bodies(a, shift=3.0):
+    d = copy.deepcopy(a)
+    n0 = len(a.node_ids)
+    d.node_ids = np.concatenate([a.node_ids, a.node_ids + 10 ** 6])
+    d.coords = np.vstack([a.coords, a.coords + [shift, 0.0, 0.0]])
+    d.blocks = [(t, mat, np.vstack([c, c + n0])) for t, mat, c in a.blocks]
+    d.fixed = {k: np.concatenate([a.fixed[k], a.fixed[k] + (n0 if k == "node" else 0)]) for k in ("node", "dof")}
+    d.fixed["value"] = np.concatenate([a.fixed["value"], a.fixed["value"]])
+    return d
+
+
+@pytest.mark.parametrize("n", [2, 5])
+def test_disconnected_bodies_double_everything(elp, meshes, n):
+    a = meshes.solid_cube(n, perturb=0.0, n_materials=1)
+    _, i1 = analysed(elp, a)
+    m2, i2 = analysed(elp, two_bodies(a))
+    assert m2.n == 2 * i1["n_dofs"]
+    assert i2["n_fronts"] == 2 * i1["n_fronts"]
+    assert i2["factor_entries"] == 2 * i1["factor_entries"]
+    assert i2["factor_flops"] == pytest.approx(2 * i1["factor_flops"], rel=1e-15)
+    assert i2["max_front"] == i1["max_front"]
+
+
+def test_nodes_without_elements_add_nothing(elp, meshes):
+    a = meshes.solid_cube(3, perturb=0.0, n_materials=1)
+    d = copy.deepcopy(a)
+    d.node_ids = np.concatenate([a.node_ids, [10 ** 7, 10 ** 7 + 1]])
+    d.coords = np.vstack([a.coords, [[5.0, 5.0, 5.0], [6.0, 6.0, 6.0]]])
+    _, i1 = analysed(elp, a)
+    m, i2 = analysed(elp, d)
+    assert not (m.global_rows()[-2:] >= 0).any()
+    for k in ("n_dofs", "nnz", "n_fronts", "factor_entries", "factor_flops", "max_front"):
+        assert i1[k] == i2[k], k
+
+
+def test_every_dof_fixed_and_no_elements(elp, meshes):
+    d = copy.deepcopy(meshes.solid_cube(2, perturb=0.0, n_materials=1))
+    N = len(d.node_ids)
+    d.fixed = dict(node=np.repeat(np.arange(N), 3), dof=np.tile([0, 1, 2], N), value=np.ones(3 * N, complex))
+    d.forces = None
+    m, i = analysed(elp, d)  # identity rows everywhere: still one valid front tree
+    assert i["n_fronts"] >= 1 and i["factor_entries"] >= i["nnz"]
+    np.testing.assert_array_equal(m.rhs(), np.ones(m.n))
+    d.blocks, d.fixed = [], None
+    with pytest.raises(elp.ElpasoError) as e:
+        elp.Model(d)
+    assert e.value.code == 1
+
+
+@pytest.mark.parametrize("make", ["plate_cavity", "thin_strip", "fluid_only"])
+def test_front_statistics_are_consistent_and_deterministic(elp, meshes, make):
+    if make == "plate_cavity":
+        d = meshes.plate_cavity(10, 8, 6, 0.6, 0.4, 0.3)
+    elif make == "thin_strip":
+        d = meshes.solid_plate(40, 1, 1, 4.0, 0.1, 0.1)
+    else:
+        d = copy.deepcopy(meshes.plate_cavity(6, 4, 4, 0.3, 0.2, 0.2))
+        d.blocks = [b for b in d.blocks if b[0] == 3]
+        d.interfaces, d.fixed, d.forces = None, None, None
+    _, i = analysed(elp, d)
+    n = i["n_dofs"]
+    assert 1 <= i["max_front"] <= n
+    assert i["factor_entries"] >= i["nnz"]  # every stored entry lives in some front
+    assert 0 < i["factor_flops"] <= lu_flops(n)  # never worse than dense
+    assert i["n_levels"] >= (2 if i["n_fronts"] > 1 else 1)
+    _, again = analysed(elp, d)
+    assert again == i
