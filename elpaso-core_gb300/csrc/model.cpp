@@ -339,7 +339,7 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
         }
       }
     }
-    if (m.groups.empty()) m.groups.push_back(StructGroup{0, 0.0});
+    if (m.groups.empty()) m.groups.push_back(StructGroup());  // elastic, eta 0
     if (m.groups.size() > (size_t)kMaxStructGroups) {
       err = "more than " + std::to_string(kMaxStructGroups) + " distinct structure loss-factor groups";
       return ELP_ERR_ARG;

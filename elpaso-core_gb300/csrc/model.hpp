@@ -37,8 +37,8 @@ constexpr uint8_t CLS_MASK = 0x7f;
 // Materials with frequency tables form groups of their own:
 // c_g(w) = E(w) / e_ref * (1 + i eta(w)) or (1 + i w eta(w)).
 struct StructGroup {
-  int visco_type;  // 0 elastic, 1: 1 + i eta, 2: 1 + i w eta
-  double eta;
+  int visco_type = 0;  // 0 elastic, 1: 1 + i eta, 2: 1 + i w eta
+  double eta = 0.0;
   double e_ref = 0.0;                 // modulus the stiffness was assembled with (tables only)
   std::vector<double> om_e, val_e;    // E(w) table (w = 2 pi f), ascending
   std::vector<double> om_eta, val_eta;
