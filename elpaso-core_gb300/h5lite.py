@@ -15,8 +15,10 @@ HDF5 File Format Specification (version 2.0 document, sections II-IV):
   (0x8, versions 1-3, contiguous/compact), attribute (0xC), continuation
   (0x10), symbol table (0x11);
 * datatypes: fixed-point, floating-point, fixed- and variable-length strings
-  (the latter in global heap collections, ``GCOL``) and compounds of those
-  (the elpasoC complex type is the compound ``{real, imag}``).
+  (the latter in global heap collections, ``GCOL``), enumerations (read as
+  their base integer type, the members in the dtype's metadata; booleans
+  are the ``{FALSE, TRUE}`` enum of a byte) and compounds of those (the
+  elpasoC complex type is the compound ``{real, imag}``).
 
 Anything else (chunked or filtered storage, v2 object headers, dense
 attribute storage, variable-length types) raises ``NotImplementedError``.
@@ -255,6 +257,19 @@ class File(Group):
                 offsets.append(off)
             dt = np.dtype({"names": names, "formats": formats, "offsets": offsets, "itemsize": size})
             return dt, q - p
+        if cls == 8:  # enumeration (booleans are the {FALSE, TRUE} enum of an 8-bit integer)
+            nmem = bits & 0xFFFF
+            base, used = self._datatype(d, q)
+            q += used
+            names = []
+            for _ in range(nmem):
+                e = d.index(b"\0", q)
+                names.append(d[q:e].decode())
+                q = q + ((e - q) // 8 + 1) * 8 if ver < 3 else e + 1
+            values = np.frombuffer(d, base, nmem, q)
+            q += nmem * base.itemsize
+            members = {nm: int(v) for nm, v in zip(names, values)}
+            return np.dtype(base, metadata={"enum": members}), q - p
         raise NotImplementedError(f"datatype class {cls}")
 
     def _attribute(self, d: bytes):

@@ -1,0 +1,126 @@
+"""The HDF5 reader against the reference's own HDF5 unit tests.
+
+elpasoCore/test/misc/hdf5/testInputHDF5.h and testReaderHDF5.h read the
+fixtures under elpasoCore/test/resources/unitHDF5/ (TestContainer.hdf5,
+plate.hdf5, plate1_structBC.hdf5; names in test/resources/properties/
+testproperties.h:30-82) and assert counts, ids, coordinates, attribute values
+and matrix entries; misc/parser/testFemParserHDF5.h:89-208 asserts what the
+parser makes of plate.hdf5 and plate1_structBC.hdf5. The same known answers
+are asserted here on what h5lite / h5model read from the same files, which
+are read in place (the reference tree is only present where it was
+unpacked; elsewhere these tests skip). plate1_structBC.hdf5 and
+plate2_interface_and_fluid.hdf5 store their boolean constraint and output
+flags as HDF5 enumerations, which the reader must decode."""
+import os
+
+import numpy as np
+import pytest
+
+from __graft_entry__ import REFERENCE
+
+UNIT = os.path.join(os.environ.get("ELPASO_REFERENCE", REFERENCE), "elpasoCore", "test", "resources", "unitHDF5")
+
+pytestmark = pytest.mark.skipif(not os.path.isdir(UNIT), reason="reference test resources not present")
+
+
+@pytest.fixture(scope="module")
+def h5lite(elp):
+    import importlib
+    return importlib.import_module("elpaso_core_gb300.h5lite")
+
+
+def _open(h5lite, name):
+    return h5lite.File(os.path.join(UNIT, name))
+
+
+def test_container_vectors_and_matrices(h5lite):
+    f = _open(h5lite, "TestContainer.hdf5")
+    np.testing.assert_array_equal(f["Vector/IntegerVector"].read().ravel(), [1, 2, 3, 7])  # testReaderHDF5.h:69-79
+    ns = f["Vector/IntegerVector_Attribute"].attrs["NS"]  # testInputHDF5.h:80-94
+    assert len(ns) == 9 and list(ns[:4]) == [76, 75, 90, 89]
+    dm = f["Matrices/DoubleMatrix"].read()  # testInputHDF5.h:96-112
+    assert dm.shape == (2, 2)
+    np.testing.assert_array_equal(dm.ravel(), [10, 0.01, 100, 0.001])
+    im = f["Matrices/IntegerMatrix"].read()  # testReaderHDF5.h:114-130
+    assert im.shape == (8, 20)
+    assert list(im.ravel()[[0, 1, 2, 20]]) == [81, -1, 126, 82]
+    np.testing.assert_array_equal(f["Vector/DoubleVector64"].read(), [4.5, 0.0001, 500.01, 4.2e-4])
+
+
+def test_container_compounds(h5lite):
+    f = _open(h5lite, "TestContainer.hdf5")
+    v = f["Compound/vecFemStep1"].read()  # testInputHDF5.h:151-162
+    assert v.shape == (918,)
+    assert (v["real"][3], v["imag"][3]) == (2.0054695597675435e-7, 0.0)
+    k = f["Compound/mtxStiffnessRom"].read().ravel()  # testInputHDF5.h:270-283
+    assert k.size == 2025
+    assert k["real"][0] == pytest.approx(36621.04312976473, abs=1e-4) and k["imag"][0] == 0
+    assert k["real"][1] == pytest.approx(-1937.9915546127222, abs=1e-4)
+    nodes = f["Compound/mtxFemNodes"].read()  # testReaderHDF5.h:137-151
+    assert nodes.shape == (55,)
+    assert list(nodes["Ids"][:4]) == [1, 2, 7, 9]
+    assert (nodes["xCoords"][0], nodes["yCoords"][0], nodes["zCoords"][0]) == (0.5, 0.2, 0.0)
+    assert len(list(f["Compound"].keys())) == 3  # testReaderHDF5.h:300-303
+
+
+def test_plate_file_entities(h5lite):
+    f = _open(h5lite, "plate.hdf5")
+    np.testing.assert_array_equal(f["Nodesets/vecNodeset1"].read().ravel(), [1])  # testInputHDF5.h:71-79
+    nodes = f["Nodes/mtxFemNodes"].read()  # testInputHDF5.h:131-149
+    assert nodes.shape == (6,)
+    assert list(nodes["Ids"][:4]) == [1, 2, 4, 5]
+    assert (nodes["xCoords"][0], nodes["yCoords"][0], nodes["zCoords"][0]) == (0.8, 0.4, 0.0)
+    a = f["Analysis"].attrs  # testInputHDF5.h:165-188, 214-222
+    assert (int(a["steps"]), float(a["start"]), a["type"]) == (1, 10.0, "frequency-basic")
+    assert f["Materials/material1"].attrs["MaterialType"] == "STR_LIN_ELA_ISO_DIR"  # :226-234
+    assert len(list(f["ElemLoads"].keys())) == 0  # :250-257
+    assert sorted(f["NodeLoads"].keys())[0] == "mtxFemNodeLoad1_1"  # :259-267
+
+
+def test_structure_constraint_file_enumerations(h5lite):
+    """plate1_structBC.hdf5: four constrained nodes (testFemParserHDF5.h:
+    200-208), valu3 = 0 on the first (testInputHDF5.h:190-198), no valp
+    (read as 0 by the reference, :200-210), MaterialId 1 of the element group
+    (:238-246); the u1..w3 flags are HDF5 enumerations (FALSE / TRUE)."""
+    f = _open(h5lite, "plate1_structBC.hdf5")
+    bcs = [f["NodeConstraints"][k].attrs for k in sorted(f["NodeConstraints"].keys())]
+    assert len(bcs) == 4 and len({int(b["NodeId"]) for b in bcs}) == 4
+    first = f["NodeConstraints/nodeConstraint1_1"].attrs
+    assert float(first["valu3"]) == 0.0 and "valp" not in first
+    assert [int(first[k]) for k in ("u1", "u2", "u3", "w1", "w2", "w3")] == [0, 0, 1, 0, 0, 0]
+    assert int(f["Elements/mtxFemElemGroup1"].attrs["MaterialId"]) == 1
+
+
+def test_interface_and_fluid_file_reads(h5lite):
+    """plate2_interface_and_fluid.hdf5 (the parser's interface/fluid fixture,
+    testproperties.h:39-40): two structure blocks, a fluid block, 16
+    InterfaceMindlin elements in two datasets, the output flags as enums."""
+    f = _open(h5lite, "plate2_interface_and_fluid.hdf5")
+    assert int(f["InterfaceElements"].attrs["N"]) == 16
+    ie = [f["InterfaceElements"][k] for k in sorted(f["InterfaceElements"].keys())]
+    assert sum(d.read().shape[0] for d in ie) == 16
+    assert all(d.attrs["type"] == "InterfaceMindlin" for d in ie)
+    assert int(f["Analysis"].attrs["hdf5"]) == 1 and int(f["Analysis"].attrs["vtk"]) == 0
+    assert f["Materials/material2"].attrs["MaterialType"] == "AF_LIN_UAF_ISO_DIR"
+    assert f["Nodes/mtxFemNodes"].read().shape == (810,)
+
+
+def test_plate_file_through_the_model_reader(elp, oracle):
+    """What the parser tests assert of plate.hdf5 (testFemParserHDF5.h:89-190):
+    analysis start 10, delta 10, one step; 6 nodes with ids 1..6 (100 is not
+    one); 2 elements of material 1 with rho 2700; one nodal force. The model
+    built from it matches the oracle."""
+    import importlib
+    h5model = importlib.import_module("elpaso_core_gb300.h5model")
+    d, freqs = h5model.read_model(os.path.join(UNIT, "plate.hdf5"))
+    np.testing.assert_array_equal(freqs, [10.0])
+    assert sorted(d.node_ids) == [1, 2, 3, 4, 5, 6] and 100 not in d.node_ids
+    assert d.n_elements() == 2 and [b[1] for b in d.blocks] == [0]
+    assert len(d.materials) == 1 and d.materials[0]["rho"] == 2700.0
+    assert len(d.forces["node"]) == 1
+    m = elp.Model(d)
+    s = oracle.System(d)
+    assert m.n == 18  # DSG4: x3 w1 w2 per node
+    np.testing.assert_array_equal(m.pattern()[1], s.col_idx)
+    np.testing.assert_array_equal(m.rhs(), s.f)
+    assert m.rhs().sum() == 1.0  # Fz of the point force; DSG4 nodes have no x1 / x2

@@ -139,3 +139,23 @@ def test_model_file_refuses_face_tractions(meshes, h5model, tmp_path):
     with pytest.raises(ValueError):
         h5model.write_model(str(tmp_path / "t.hdf5"), traction_brick(meshes))
     assert not (tmp_path / "t.hdf5").exists()
+
+
+@pytest.mark.parametrize("version", [1, 3])
+def test_enumeration_datatype_message(elp, version):
+    """An HDF5 enumeration datatype message (class 8) as the File Format
+    Specification lays it out: the 8-byte header (member count in the class
+    bits, element size), the base type message, the member names (NUL
+    terminated, padded to 8 bytes before version 3), then the member values.
+    The {FALSE, TRUE} enum over a signed byte is how booleans are stored."""
+    import importlib
+    import struct
+    h5lite = importlib.import_module("elpaso_core_gb300.h5lite")
+    base = bytes([0x10, 0x08, 0, 0]) + struct.pack("<I", 1) + struct.pack("<HH", 0, 8)
+    pad = (lambda s: s + b"\0" * (8 - len(s) % 8)) if version < 3 else (lambda s: s + b"\0")
+    names = pad(b"FALSE") + pad(b"TRUE")
+    msg = bytes([(version << 4) | 8, 2, 0, 0]) + struct.pack("<I", 1) + base + names + bytes([0, 1])
+    reader = h5lite.File.__new__(h5lite.File)
+    dt, used = reader._datatype(msg + b"\xff" * 5, 0)
+    assert used == len(msg)
+    assert dt == np.dtype("i1") and dt.metadata["enum"] == {"FALSE": 0, "TRUE": 1}
