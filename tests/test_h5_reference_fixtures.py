@@ -5,7 +5,9 @@ fixtures under elpasoCore/test/resources/unitHDF5/ (TestContainer.hdf5,
 plate.hdf5, plate1_structBC.hdf5; names in test/resources/properties/
 testproperties.h:30-82) and assert counts, ids, coordinates, attribute values
 and matrix entries; misc/parser/testFemParserHDF5.h:89-208 asserts what the
-parser makes of plate.hdf5 and plate1_structBC.hdf5. The same known answers
+parser makes of plate.hdf5 and plate1_structBC.hdf5; the material and
+boundary-condition tests (test/material/..., test/bc/...) assert material
+values and a fluid constraint of their 2-element files. The same known answers
 are asserted here on what h5lite / h5model read from the same files, which
 are read in place (the reference tree is only present where it was
 unpacked; elsewhere these tests skip). plate1_structBC.hdf5 and
@@ -124,3 +126,55 @@ def test_plate_file_through_the_model_reader(elp, oracle):
     np.testing.assert_array_equal(m.pattern()[1], s.col_idx)
     np.testing.assert_array_equal(m.rhs(), s.f)
     assert m.rhs().sum() == 1.0  # Fz of the point force; DSG4 nodes have no x1 / x2
+
+
+MAT = "material/structure/isotrop/linear/"
+
+
+def _model(name):
+    import importlib
+    h5model = importlib.import_module("elpaso_core_gb300.h5model")
+    return h5model.read_model(os.path.join(UNIT, name))
+
+
+def test_structure_material_fixtures(elp, oracle):
+    """testmaterialstructurevisco.h: E 7e10, eta 0.001, nu 0.3, type 1, t
+    0.003, rho 2700 (:104-142, 233-238, 420-425) and E_vis = 7e10 + 7e7 i at
+    w = 1 (:92-99, exact); the frequency-dependent file names its E and eta
+    tables /Parameters/material1_E and /Parameters/material1_eta
+    (:196-216), whose first rows (clamped below 10 Hz) give the same E_vis."""
+    d, _ = _model(MAT + "elastic/plate_dsg4_2elem_STR_LIN_ELA_ISO_DIR.hdf5")
+    m = d.materials[0]
+    assert (m["kind"], m["E"], m["nu"], m["rho"], m["t"]) == (elp.STR_LIN_ELA_ISO_DIR, 7e10, 0.3, 2700.0, 0.003)
+    d, _ = _model(MAT + "viscoelastic/plate_dsg4_2elem_STR_LIN_VIS_ISO_DIR.hdf5")
+    m = d.materials[0]
+    assert (m["kind"], m["E"], m["eta"], m["nu"], m["visco_type"], m["t"], m["rho"]) == \
+        (elp.STR_LIN_VIS_ISO_DIR, 7e10, 0.001, 0.3, 1, 0.003, 2700.0)
+    assert oracle.e_vis(m, 1.0) == 7e10 + 7e7j
+    import importlib
+    h5lite = importlib.import_module("elpaso_core_gb300.h5lite")
+    path = MAT + "viscoelastic/plate_dsg4_2elemf_STR_LIN_VIS_ISO_DIR.hdf5"
+    attrs = h5lite.File(os.path.join(UNIT, path))["Materials/material1"].attrs
+    assert (attrs["E"], attrs["eta"]) == ("/Parameters/material1_E", "/Parameters/material1_eta")
+    d, _ = _model(path)
+    m = d.materials[0]
+    np.testing.assert_array_equal(m["E_table"][0], [10.0, 7e10])
+    np.testing.assert_array_equal(m["eta_table"][0], [10.0, 0.001])
+    assert oracle.e_vis(m, 1.0) == 7e10 + 7e7j
+    elp.Model(d)  # the tables pass the library's checks
+
+
+def test_fluid_material_and_constraint_fixtures(elp):
+    """testmaterialfluidideal.h:93-110: c 343, rho 1.21; testboundary
+    conditionfluid.h:84-156: constraint 17 fixes only the fluid DOF (enum 16)
+    of its node, prescribed value 1."""
+    d, _ = _model("material/fluid/linear/elastic/acousticmedium_fluid8_2elem_AF_LIN_UAF_ISO_DIR.hdf5")
+    m = d.materials[0]
+    assert (m["kind"], m["c"], m["rho"]) == (elp.AF_LIN_UAF_ISO_DIR, 343.0, 1.21)
+    d, _ = _model("bc/acousticmedium_fluid8_2elem_AF_LIN_UAF_ISO_DIR.hdf5")
+    assert list(d.fixed["dof"]) == [16] and list(d.fixed["value"]) == [1.0]
+    node = int(d.fixed["node"][0])
+    model = elp.Model(d)
+    f = model.rhs()
+    row = model.global_rows()[node, 16]
+    assert f[row] == 1.0 and np.count_nonzero(f) == 1
