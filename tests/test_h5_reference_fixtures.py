@@ -178,3 +178,16 @@ def test_fluid_material_and_constraint_fixtures(elp):
     f = model.rhs()
     row = model.global_rows()[node, 16]
     assert f[row] == 1.0 and np.count_nonzero(f) == 1
+
+
+@pytest.mark.parametrize("name, etype", [
+    ("plate1_structBC.hdf5", "PlShell9"),
+    ("plate2_interface_and_fluid.hdf5", "PlShell9"),
+    ("bc/plate_shell4_uwbc.hdf5", "PlShell4"),
+    (MAT + "elastic/beam_4elem.hdf5", "BeamBernoulli"),
+])
+def test_other_element_families_are_refused_by_name(name, etype):
+    """Element families outside this path (shells, beams, Fluid27) are not
+    silently dropped: read_model names the first one it meets."""
+    with pytest.raises(NotImplementedError, match=etype):
+        _model(name)
