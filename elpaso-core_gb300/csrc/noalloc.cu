@@ -1,10 +1,11 @@
 // Allocation-free residual check: r = f - A(w) x and ||r||_2 / ||f||_2 for
 // up to ELP_NOALLOC_MAX_OMEGA frequencies, without any device allocation.
 //
-// Some callers cannot call cudaMalloc while they run: a host that captures
-// its per-frequency loop into a CUDA graph, a process whose device memory is
-// owned by a pool or budget it cannot grow, or an embedding that forbids
-// allocation after start-up. They still need the FP64 residual check that
+// Some callers cannot call cudaMalloc while they run: a process whose device
+// memory is owned by another framework's pool or a fixed budget that it
+// cannot grow, an embedding (a plugin inside a larger solver, a real-time
+// host) that forbids allocation after start-up, or a loop that must not pay
+// the implicit device-wide synchronisation a cudaMalloc/cudaFree can cause. They still need the FP64 residual check that
 // the solve path performs (numeric.cu k_residual / k_norms), whose reduction
 // partials and coefficient table normally live in a workspace allocated by
 // the library. This variant keeps that scratch in one file-scope device

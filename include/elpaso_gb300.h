@@ -293,9 +293,10 @@ int elp_model_time_assembly(elp_model* m, int repeats, double* ms_per_assembly,
 /* ---- allocation-free residual check ------------------------------------ */
 
 /* No counterpart in the reference: it exists for callers that cannot
- * allocate device memory while they run (a host loop captured into a CUDA
- * graph, a device-memory pool or budget that cannot grow, an embedding that
- * forbids allocation after start-up). Computes r = f - A(w_k) x_k and
+ * allocate device memory while they run (device memory owned by another
+ * framework's pool or a fixed budget that cannot grow, an embedding that
+ * forbids allocation after start-up, a loop that must not pay the implicit
+ * synchronisation of cudaMalloc / cudaFree). Computes r = f - A(w_k) x_k and
  * ||r||_2 / ||f||_2 for n_omega <= ELP_NOALLOC_MAX_OMEGA frequencies of an
  * assembled model; f_dev, x_dev, r_dev are the caller's device buffers
  * (n_omega x n complex interleaved), rel_residual_out is host memory

@@ -1,8 +1,9 @@
 """Allocation-free residual check, elp_residual_noalloc.
 
-Callers that cannot allocate device memory while they run (a host loop
-captured into a CUDA graph, a device-memory pool that cannot grow) check
-their solutions with this entry point. Here it must agree with the residual
+Callers that cannot allocate device memory while they run (device memory
+owned by another framework's pool or a fixed budget, an embedding that
+forbids allocation after start-up) check their solutions with this entry
+point. Here it must agree with the residual
 that the solve path itself reports (elp_solve_device, info.rel_residual) for
 the same solutions, on two calls in a row, its residual vector must match
 its own norm, and it must reject more frequencies than its fixed scratch
