@@ -388,54 +388,113 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
   }
 
   // ---- per-row column lists (parallel over nodes)
-  std::vector<std::vector<int32_t>> rowcols(n);
-  const int64_t nnodes = N;
-#pragma omp parallel for schedule(dynamic, 256)
-  for (int64_t v = 0; v < nnodes; ++v) {
-    std::vector<int32_t> cols;
-    for (int k = 0; k < ELP_NUM_KNOWN_DOFS; ++k) {
-      int32_t r = grow((int32_t)v, k);
-      if (r < 0) continue;
-      cols.clear();
-      for (int64_t p = ne_ptr[v]; p < ne_ptr[v + 1]; ++p) {
-        const Block& blk = m.blocks[ne_list[p].block];
-        const int* dofs = element_dofs(blk.type);
-        int ndn = dofs_per_node(blk.type), npe = nodes_per_element(blk.type);
-        bool has = false;
-        for (int q = 0; q < ndn; ++q) has |= (dofs[q] == k);
-        if (!has) continue;
-        const int32_t* en = &blk.conn[(size_t)ne_list[p].elem * npe];
-        for (int a = 0; a < npe; ++a)
-          for (int q = 0; q < ndn; ++q) {
-            int32_t c = grow(en[a], dofs[q]);
-            if (c >= 0) cols.push_back(c);
-          }
-      }
-      cols.push_back(r);  // diagonal always present
-      auto it = extra_slot.find(r);
-      if (it != extra_slot.end()) cols.insert(cols.end(), extra[it->second].begin(), extra[it->second].end());
-      std::sort(cols.begin(), cols.end());
-      cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-      rowcols[r] = cols;
+  // Row (v, k) holds every DOF of every node of each element at v whose
+  // family carries DOF k, the diagonal, and the row's interface columns.
+  // Which of v's elements count depends on k only through the families that
+  // carry k, so the DOFs of v with the same families share one column set.
+  // The set is built from v's neighbour nodes taken in node order, each
+  // with the DOFs its selected elements give it in enum order: rows are
+  // numbered node by node and DOF by DOF in that order, so the set comes
+  // out sorted and unique with no per-row sort. Pass 1 counts the row
+  // lengths, pass 2 writes the columns straight into col_idx.
+  std::vector<int32_t> node_rank(N);
+  for (int64_t i = 0; i < N; ++i) node_rank[m.order[i]] = (int32_t)i;
+  uint32_t fam_of_dof[ELP_NUM_KNOWN_DOFS] = {0};  // bit (1 << type) per family carrying the DOF
+  uint32_t dofs_of_type[8] = {0};                 // DOF bits carried by each family
+  for (int t : {ELP_BRICK8, ELP_DSG4, ELP_FLUID8}) {
+    const int* dofs = element_dofs(t);
+    for (int q = 0; q < dofs_per_node(t); ++q) {
+      fam_of_dof[dofs[q]] |= 1u << t;
+      dofs_of_type[t] |= 1u << dofs[q];
     }
   }
+  for (auto& e : extra) {
+    std::sort(e.begin(), e.end());
+    e.erase(std::unique(e.begin(), e.end()), e.end());
+  }
   m.row_ptr.assign(n + 1, 0);
-  int64_t nnz = 0;
-  for (int64_t r = 0; r < n; ++r) {
-    nnz += (int64_t)rowcols[r].size();
-    if (nnz >= ((int64_t)1 << 31) - 1) { err = "nnz exceeds int32 CSR range"; return ELP_ERR_ARG; }
-    m.row_ptr[r + 1] = (int32_t)nnz;
-  }
-  m.nnz = nnz;
-  m.col_idx.resize(nnz);
   m.diag_idx.resize(n);
-#pragma omp parallel for schedule(static)
-  for (int64_t r = 0; r < n; ++r) {
-    std::copy(rowcols[r].begin(), rowcols[r].end(), m.col_idx.begin() + m.row_ptr[r]);
-    auto it = std::lower_bound(rowcols[r].begin(), rowcols[r].end(), (int32_t)r);
-    m.diag_idx[r] = m.row_ptr[r] + (int32_t)(it - rowcols[r].begin());
-    std::vector<int32_t>().swap(rowcols[r]);
+  // columns of row r = base (sorted, unique) + r + the row's interface columns
+  auto row_columns = [&](int32_t r, const std::vector<int32_t>& base, std::vector<int32_t>& out) {
+    out.clear();
+    auto it = extra_slot.find(r);
+    const int32_t one[1] = {r};
+    if (it == extra_slot.end()) {
+      if (std::binary_search(base.begin(), base.end(), r)) { out = base; return; }
+      std::set_union(base.begin(), base.end(), one, one + 1, std::back_inserter(out));
+      return;
+    }
+    std::vector<int32_t> tmp;
+    std::set_union(base.begin(), base.end(), one, one + 1, std::back_inserter(tmp));
+    const std::vector<int32_t>& ex = extra[it->second];
+    std::set_union(tmp.begin(), tmp.end(), ex.begin(), ex.end(), std::back_inserter(out));
+  };
+  const int64_t nnodes = N;
+  for (int pass = 0; pass < 2; ++pass) {
+#pragma omp parallel
+    {
+      std::vector<std::pair<int32_t, uint32_t>> nbr;  // (node rank, DOF bits)
+      // one slot per distinct family set among a node's DOFs (at most one per DOF)
+      std::vector<int32_t> base[ELP_NUM_KNOWN_DOFS], cols;
+      uint32_t base_fam[ELP_NUM_KNOWN_DOFS];
+#pragma omp for schedule(dynamic, 256)
+      for (int64_t v = 0; v < nnodes; ++v) {
+        int nb = 0;
+        for (int k = 0; k < ELP_NUM_KNOWN_DOFS; ++k) {
+          const int32_t r = grow((int32_t)v, k);
+          if (r < 0) continue;
+          const uint32_t fam = fam_of_dof[k];
+          int b = 0;
+          while (b < nb && base_fam[b] != fam) ++b;
+          if (b == nb) {  // first DOF of v with this family set: build its columns
+            ++nb;
+            base_fam[b] = fam;
+            nbr.clear();
+            for (int64_t p = ne_ptr[v]; p < ne_ptr[v + 1]; ++p) {
+              const Block& blk = m.blocks[ne_list[p].block];
+              if (!(fam & (1u << blk.type))) continue;
+              const int npe = nodes_per_element(blk.type);
+              const int32_t* en = &blk.conn[(size_t)ne_list[p].elem * npe];
+              for (int a = 0; a < npe; ++a) nbr.emplace_back(node_rank[en[a]], dofs_of_type[blk.type]);
+            }
+            std::sort(nbr.begin(), nbr.end());
+            std::vector<int32_t>& B = base[b];
+            B.clear();
+            for (size_t i = 0; i < nbr.size();) {
+              uint32_t bits = 0;
+              size_t j = i;
+              for (; j < nbr.size() && nbr[j].first == nbr[i].first; ++j) bits |= nbr[j].second;
+              const int32_t a = m.order[nbr[i].first];
+              for (int q = 0; q < ELP_NUM_KNOWN_DOFS; ++q)
+                if (bits & (1u << q)) {
+                  const int32_t c = grow(a, q);
+                  if (c >= 0) B.push_back(c);
+                }
+              i = j;
+            }
+          }
+          row_columns(r, base[b], cols);
+          if (pass == 0) {
+            m.row_ptr[r + 1] = (int32_t)cols.size();
+          } else {
+            std::copy(cols.begin(), cols.end(), m.col_idx.begin() + m.row_ptr[r]);
+            m.diag_idx[r] = m.row_ptr[r] + (int32_t)(std::lower_bound(cols.begin(), cols.end(), r) - cols.begin());
+          }
+        }
+      }
+    }
+    if (pass == 0) {
+      int64_t nnz = 0;
+      for (int64_t r = 0; r < n; ++r) {
+        nnz += m.row_ptr[r + 1];
+        if (nnz >= ((int64_t)1 << 31) - 1) { err = "nnz exceeds int32 CSR range"; return ELP_ERR_ARG; }
+        m.row_ptr[r + 1] = (int32_t)nnz;
+      }
+      m.nnz = nnz;
+      m.col_idx.resize(nnz);
+    }
   }
+  const int64_t nnz = m.nnz;
 
   // ---- BC rows in reference order (analysis.cpp:376-413)
   std::vector<std::vector<int32_t>> node_bcs(N);

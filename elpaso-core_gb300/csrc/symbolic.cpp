@@ -294,45 +294,42 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
   for (int t = 0; t < T; ++t)
     if (S.fronts[t].parent < 0 && S.fronts[t].b != 0) { set_error("root front with a border"); return ELP_ERR_ARG; }
 
-  // ---- per-entry arena offsets (bucket entries by owner front)
+  // ---- per-entry arena offsets
+  // Entry (r, c) belongs to the front F that eliminates min(pos r, pos c);
+  // that DOF is one of F's pivots, whose positions are consecutive, so its
+  // local index is its position minus F's first. The other DOF is a later
+  // pivot of F or in F's border; the border runs in ascending elimination
+  // position (its nodes are sorted by rank and all come after F's pivots),
+  // so its local index is a binary search there. Rows are independent.
   const int64_t nnz = m.nnz;
-  std::vector<int32_t> owner(nnz);
-  std::vector<int64_t> cnt(T + 1, 0);
   std::vector<int32_t> front_of_pos(n);
   for (int t = 0; t < T; ++t)
     for (int k = 0; k < S.fronts[t].p; ++k) front_of_pos[S.fronts[t].piv_off + k] = t;
-  for (int64_t r = 0; r < n; ++r)
-    for (int32_t q = m.row_ptr[r]; q < m.row_ptr[r + 1]; ++q) {
-      int32_t c = m.col_idx[q];
-      int32_t pmin = std::min(dof_pos[r], dof_pos[c]);
-      owner[q] = front_of_pos[pmin];
-      cnt[owner[q] + 1]++;
-    }
-  for (int t = 0; t < T; ++t) cnt[t + 1] += cnt[t];
-  std::vector<int64_t> bucket(nnz), rowof(nnz);
-  {
-    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
-    for (int64_t r = 0; r < n; ++r)
-      for (int32_t q = m.row_ptr[r]; q < m.row_ptr[r + 1]; ++q) {
-        int64_t at = fill[owner[q]]++;
-        bucket[at] = q;
-        rowof[at] = r;
-      }
-  }
+  std::vector<int32_t> list_pos(S.front_dofs.size());
+  for (size_t k = 0; k < S.front_dofs.size(); ++k) list_pos[k] = dof_pos[S.front_dofs[k]];
   S.entry_off.assign(nnz, -1);
-  for (int t = 0; t < T; ++t) {
-    const FrontInfo& F = S.fronts[t];
-    const int mm = F.p + F.b;
-    for (int k = 0; k < mm; ++k) loc[S.front_dofs[F.idx_off + k]] = k;
-    for (int64_t at = cnt[t]; at < cnt[t + 1]; ++at) {
-      int64_t q = bucket[at];
-      int32_t r = (int32_t)rowof[at], c = m.col_idx[q];
-      int32_t lr = loc[r], lc = loc[c];
-      if (lr < 0 || lc < 0) { set_error("entry outside its owner front"); return ELP_ERR_ARG; }
-      S.entry_off[q] = F.off + (int64_t)lc * mm + lr;
+  int outside = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : outside)
+  for (int64_t r = 0; r < n; ++r) {
+    const int32_t pr = dof_pos[r];
+    for (int32_t q = m.row_ptr[r]; q < m.row_ptr[r + 1]; ++q) {
+      const int32_t pc = dof_pos[m.col_idx[q]];
+      const int32_t first = std::min(pr, pc), later = std::max(pr, pc);
+      const FrontInfo& F = S.fronts[front_of_pos[first]];
+      int32_t loc_later = later - F.piv_off;
+      if (loc_later >= F.p) {
+        const int32_t* lo = list_pos.data() + F.idx_off + F.p;
+        const int32_t* hi = lo + F.b;
+        const int32_t* it = std::lower_bound(lo, hi, later);
+        if (it == hi || *it != later) { outside = 1; continue; }
+        loc_later = F.p + (int32_t)(it - lo);
+      }
+      const int32_t loc_first = first - F.piv_off;
+      const int32_t lr = pr == first ? loc_first : loc_later, lc = pr == first ? loc_later : loc_first;
+      S.entry_off[q] = F.off + (int64_t)lc * (F.p + F.b) + lr;
     }
-    for (int k = 0; k < mm; ++k) loc[S.front_dofs[F.idx_off + k]] = -1;
   }
+  if (outside) { set_error("entry outside its owner front"); return ELP_ERR_ARG; }
 
   // ---- levels
   int L = 0;
