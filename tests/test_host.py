@@ -96,3 +96,32 @@ def test_malformed_models_are_rejected(elp, meshes):
     d.materials[0]["kind"] = 3  # fluid material on a plate block
     with pytest.raises(elp.ElpasoError):
         elp.Model(d)
+
+
+def test_pattern_of_nodes_shared_by_element_families_matches_oracle(elp, meshes, oracle):
+    """A Brick8 cube whose top face also carries DSG4 plate elements on the
+    same nodes: those nodes hold x1 x2 (Brick8 only), x3 (both families) and
+    w1 w2 (DSG4 only), so their rows see different element sets (the
+    reference's getDofs()-driven pattern, analysis.cpp:815-823). Every row
+    must still equal the oracle's."""
+    d = meshes.cube(4)
+    conn = d.blocks[0][2]
+    top = conn[:, 4:8]
+    zmax = d.coords[:, 2].max()
+    on_top = np.all(np.abs(d.coords[top][:, :, 2] - zmax) < 1e-9, axis=1)
+    d.materials.append(dict(kind=meshes.STR_LIN_VIS_ISO_DIR, E=70e9, nu=0.33, rho=2700.0, t=0.002, eta=0.05,
+                            visco_type=1))
+    d.blocks.append((meshes.DSG4, 1, np.ascontiguousarray(top[on_top])))
+    m = elp.Model(d)
+    s = oracle.System(d)
+    assert np.array_equal(m.global_rows(), s.rows)
+    rp, ci = m.pattern()
+    assert np.array_equal(rp, s.row_ptr)
+    assert np.array_equal(ci, s.col_idx)
+    rows = m.global_rows()
+    shared = np.unique(top[on_top])
+    lens = np.diff(rp)
+    x1, x3, w1 = rows[shared, 0], rows[shared, 2], rows[shared, 4]
+    assert np.all(w1 >= 0)
+    # x1 sees only the bricks, w1 only the plates, x3 both
+    assert np.all(lens[x3] > lens[x1]) and np.all(lens[x3] > lens[w1])
