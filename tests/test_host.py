@@ -121,7 +121,7 @@ def test_pattern_of_nodes_shared_by_element_families_matches_oracle(elp, meshes,
     rows = m.global_rows()
     shared = np.unique(top[on_top])
     lens = np.diff(rp)
-    x1, x3, w1 = rows[shared, 0], rows[shared, 2], rows[shared, 4]
+    x1, x3, w1 = rows[shared, 0], rows[shared, 2], rows[shared, 3]
     assert np.all(w1 >= 0)
     # x1 sees only the bricks, w1 only the plates, x3 both
     assert np.all(lens[x3] > lens[x1]) and np.all(lens[x3] > lens[w1])
