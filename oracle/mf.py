@@ -7,7 +7,10 @@ restating the published algorithm of the reference's solver, MUMPS
 a fill-reducing nested-dissection order, an assembly tree of dense fronts,
 partial pivoting within each front's fully summed block, and Schur
 complements extend-added into the parent. Dense work goes to LAPACK/BLAS
-(SciPy), which uses every host thread.
+(SciPy). Like MUMPS, it uses tree parallelism: the fronts of one tree level
+are independent, so a level with many (small) fronts is spread over a pool
+of host threads, each calling single-threaded BLAS, while the few large
+fronts near the root get multithreaded BLAS.
 
 It is written independently of the product's symbolic phase. The ordering
 is a geometric nested dissection on node coordinates (median cut along the
@@ -15,9 +18,61 @@ longest box axis, separator = the side boundary of the smaller cost).
 """
 from __future__ import annotations
 
+import contextlib
+import ctypes
+import os
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
 import scipy.linalg as sla
 import scipy.sparse as sp
+
+_THREADS = os.cpu_count() or 1
+_SET_NAMES = ("openblas_set_num_threads", "openblas_set_num_threads64_", "scipy_openblas_set_num_threads",
+              "scipy_openblas_set_num_threads64_")
+_blas_setters = None
+
+
+def _blas_libs():
+    """(set, get) pairs of every OpenBLAS loaded in this process (numpy and
+    SciPy may each carry their own); empty where none is found."""
+    global _blas_setters
+    if _blas_setters is None:
+        found, seen = [], set()
+        try:
+            paths = {ln.split()[-1] for ln in open("/proc/self/maps") if "blas" in ln.lower() and ".so" in ln}
+        except OSError:
+            paths = set()
+        for path in sorted(paths):
+            try:
+                lib = ctypes.CDLL(path)
+            except OSError:
+                continue
+            for name in _SET_NAMES:
+                get = name.replace("set_num", "get_num")
+                if hasattr(lib, name) and hasattr(lib, get):
+                    fs, fg = getattr(lib, name), getattr(lib, get)
+                    key = ctypes.cast(fs, ctypes.c_void_p).value
+                    if key not in seen:
+                        seen.add(key)
+                        fs.argtypes, fs.restype, fg.restype = [ctypes.c_int], None, ctypes.c_int
+                        found.append((fs, fg))
+        _blas_setters = found
+    return _blas_setters
+
+
+@contextlib.contextmanager
+def _blas_threads(n):
+    """Run the block with n BLAS threads, then restore the previous counts."""
+    libs = _blas_libs()
+    old = [g() for _, g in libs]
+    for s, _ in libs:
+        s(n)
+    try:
+        yield
+    finally:
+        for (s, _), k in zip(libs, old):
+            s(k)
 
 
 def _node_graph(indptr, indices, dof_node, n_nodes):
@@ -105,9 +160,12 @@ class Multifrontal:
             rank[nodes] = np.arange(r, r + len(nodes))
             r += len(nodes)
         parent = np.full(T, -1, np.int64)
+        level = np.zeros(T, np.int64)  # 0 at the leaves, 1 + the highest child above them
         for t, (_, kids) in enumerate(out):
             for c in kids:
                 parent[c] = t
+                level[t] = max(level[t], level[c] + 1)
+        self.levels = [np.nonzero(level == L)[0].tolist() for L in range(int(level.max()) + 1 if T else 0)]
         borders = []
         for t, (nodes, kids) in enumerate(out):
             cand = set()
@@ -147,39 +205,48 @@ class Multifrontal:
         self.indptr, self.indices = indptr, indices
 
     def factor(self, A):
-        """A: scipy CSR (complex128) on the analysed pattern."""
+        """A: scipy CSR (complex128) on the analysed pattern. Levels run in
+        order (children before parents); a level of at least 4 fronts is
+        spread over the thread pool with single-threaded BLAS."""
         A = A.tocsr()
         assert np.array_equal(A.indptr, self.indptr) and np.array_equal(A.indices, self.indices)
         data = A.data
-        F_all = []
-        cb = {}
-        for t, (piv, bor, kids) in enumerate(self.fronts):
-            p, m = len(piv), len(piv) + len(bor)
-            q, lr, lc, kid_maps = self.assembly[t]
-            F = np.zeros((m, m), np.complex128)
-            F[lr, lc] = data[q]
-            for c, loc in zip(kids, kid_maps):
-                S = cb.pop(c)
-                F[np.ix_(loc, loc)] += S
-            lu, perm = sla.lu_factor(F[:p, :p], check_finite=False)
-            F12 = F[:p, p:]
-            for k, pk in enumerate(perm):  # LAPACK row interchanges on F12
-                if pk != k:
-                    F12[[k, pk]] = F12[[pk, k]]
-            U12 = sla.solve_triangular(lu, F12, lower=True, unit_diagonal=True, check_finite=False)
-            L21 = sla.solve_triangular(lu, F[p:, :p].T, trans="T", lower=False, check_finite=False).T
-            if m > p:
-                cb[t] = F[p:, p:] - L21 @ U12
-            F_all.append((lu, perm, L21, U12))
-        self.F = F_all
+        self.F = [None] * len(self.fronts)
+        self._cb = {}
+        with ThreadPoolExecutor(max_workers=_THREADS) as pool:
+            for group in self.levels:
+                if len(group) >= 4 and _THREADS > 1:
+                    with _blas_threads(1):
+                        list(pool.map(lambda t: self._factor_front(t, data), group))
+                else:
+                    for t in group:
+                        self._factor_front(t, data)
+        del self._cb
+
+    def _factor_front(self, t, data):
+        piv, bor, kids = self.fronts[t]
+        p, m = len(piv), len(piv) + len(bor)
+        q, lr, lc, kid_maps = self.assembly[t]
+        F = np.zeros((m, m), np.complex128)
+        F[lr, lc] = data[q]
+        for c, loc in zip(kids, kid_maps):
+            F[np.ix_(loc, loc)] += self._cb.pop(c)
+        lu, perm = sla.lu_factor(F[:p, :p], check_finite=False)
+        pv = list(range(p))  # LAPACK's row interchanges, in order, as one permutation
+        for k, pk in enumerate(perm.tolist()):
+            if pk != k:
+                pv[k], pv[pk] = pv[pk], pv[k]
+        pv = np.asarray(pv, np.int64)
+        U12 = sla.solve_triangular(lu, F[:p, p:][pv], lower=True, unit_diagonal=True, check_finite=False)
+        L21 = sla.solve_triangular(lu, F[p:, :p].T, trans="T", lower=False, check_finite=False).T
+        if m > p:
+            self._cb[t] = F[p:, p:] - L21 @ U12
+        self.F[t] = (lu, pv, L21, U12)
 
     def solve(self, b):
         y = np.array(b, np.complex128, copy=True)
         for (piv, bor, _), (lu, perm, L21, U12) in zip(self.fronts, self.F):
-            yp = y[piv]
-            for k, pk in enumerate(perm):
-                if pk != k:
-                    yp[[k, pk]] = yp[[pk, k]]
+            yp = y[piv][perm]
             yp = sla.solve_triangular(lu, yp, lower=True, unit_diagonal=True, check_finite=False)
             y[piv] = yp
             if len(bor):
