@@ -207,15 +207,17 @@ class Multifrontal:
     def factor(self, A):
         """A: scipy CSR (complex128) on the analysed pattern. Levels run in
         order (children before parents); a level of at least 4 fronts is
-        spread over the thread pool with single-threaded BLAS."""
+        spread over the thread pool with single-threaded BLAS (only where
+        this process's BLAS thread count can be set; else all run in order)."""
         A = A.tocsr()
         assert np.array_equal(A.indptr, self.indptr) and np.array_equal(A.indices, self.indices)
         data = A.data
         self.F = [None] * len(self.fronts)
         self._cb = {}
+        parallel = _THREADS > 1 and bool(_blas_libs())
         with ThreadPoolExecutor(max_workers=_THREADS) as pool:
             for group in self.levels:
-                if len(group) >= 4 and _THREADS > 1:
+                if parallel and len(group) >= 4:
                     with _blas_threads(1):
                         list(pool.map(lambda t: self._factor_front(t, data), group))
                 else:
