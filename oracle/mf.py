@@ -8,9 +8,10 @@ a fill-reducing nested-dissection order, an assembly tree of dense fronts,
 partial pivoting within each front's fully summed block, and Schur
 complements extend-added into the parent. Dense work goes to LAPACK/BLAS
 (SciPy). Like MUMPS, it uses tree parallelism: the fronts of one tree level
-are independent, so a level with many (small) fronts is spread over a pool
-of host threads, each calling single-threaded BLAS, while the few large
-fronts near the root get multithreaded BLAS.
+are independent, so the fronts of a level are spread over a pool of host
+threads that share the BLAS threads: single-threaded BLAS for the many small
+fronts near the leaves, multithreaded BLAS for the few large ones near the
+root.
 
 It is written independently of the product's symbolic phase. The ordering
 is a geometric nested dissection on node coordinates (median cut along the
@@ -206,9 +207,10 @@ class Multifrontal:
 
     def factor(self, A):
         """A: scipy CSR (complex128) on the analysed pattern. Levels run in
-        order (children before parents); a level of at least 4 fronts is
-        spread over the thread pool with single-threaded BLAS (only where
-        this process's BLAS thread count can be set; else all run in order)."""
+        order (children before parents); the fronts of a level of k >= 2
+        fronts are spread over the thread pool, each with 1/k of the BLAS
+        threads (only where this process's BLAS thread count can be set;
+        else all run in order)."""
         A = A.tocsr()
         assert np.array_equal(A.indptr, self.indptr) and np.array_equal(A.indices, self.indices)
         data = A.data
@@ -217,8 +219,8 @@ class Multifrontal:
         parallel = _THREADS > 1 and bool(_blas_libs())
         with ThreadPoolExecutor(max_workers=_THREADS) as pool:
             for group in self.levels:
-                if parallel and len(group) >= 4:
-                    with _blas_threads(1):
+                if parallel and len(group) >= 2:
+                    with _blas_threads(max(1, _THREADS // len(group))):
                         list(pool.map(lambda t: self._factor_front(t, data), group))
                 else:
                     for t in group:
