@@ -309,26 +309,27 @@ class System:
         buf = {}
 
         def pack(typ):
-            xyz, mat, rr = [], [], []
+            # per element, in block order: node coordinates, material row,
+            # global rows (node-major, then the family's DOFs)
+            xyz, mat, rr = [np.zeros(0)], [np.zeros(0)], [np.zeros(0, np.int32)]
+            ne = 0
             for btyp, mi, conn in d.blocks:
                 if btyp != typ:
                     continue
+                conn = np.asarray(conn)
                 m = d.materials[mi]
-                for e in np.asarray(conn):
-                    xyz.append(d.coords[e].reshape(-1))
-                    if typ == FLUID8:
-                        mat.append([m["c"], m["rho"]])
-                    else:
-                        E = e_vis(m, omega)
-                        mm = [E.real, E.imag, m["nu"], m["rho"]]
-                        if typ == DSG4:
-                            mm.append(m["t"])
-                        mat.append(mm)
-                    rr.append([rows[v, k] for v in e for k in ELEM_DOFS[typ]])
-            w = {BRICK8: 4, DSG4: 5, FLUID8: 2}[typ]
-            a = (np.ascontiguousarray(np.asarray(xyz, np.float64).reshape(-1)),
-                 np.ascontiguousarray(np.asarray(mat, np.float64).reshape(-1, w).reshape(-1)),
-                 np.ascontiguousarray(np.asarray(rr, np.int32).reshape(-1)), len(xyz))
+                if typ == FLUID8:
+                    mm = [m["c"], m["rho"]]
+                else:
+                    E = e_vis(m, omega)
+                    mm = [E.real, E.imag, m["nu"], m["rho"]] + ([m["t"]] if typ == DSG4 else [])
+                xyz.append(d.coords[conn].reshape(-1))
+                mat.append(np.tile(np.asarray(mm, np.float64), len(conn)))
+                rr.append(rows[conn][:, :, ELEM_DOFS[typ]].reshape(-1))
+                ne += len(conn)
+            a = (np.ascontiguousarray(np.concatenate(xyz), np.float64),
+                 np.ascontiguousarray(np.concatenate(mat), np.float64),
+                 np.ascontiguousarray(np.concatenate(rr), np.int32), ne)
             buf[typ] = a
             return a
         b, p, fl = pack(BRICK8), pack(DSG4), pack(FLUID8)
