@@ -111,7 +111,7 @@ class _Info(C.Structure):
     _fields_ = [("n_dofs", C.c_int64), ("nnz", C.c_int64), ("n_elements", C.c_int64), ("n_fronts", C.c_int64),
                 ("factor_entries", C.c_int64), ("factor_flops", C.c_double), ("n_levels", C.c_int),
                 ("max_front", C.c_int), ("n_struct_groups", C.c_int), ("gemm_flops", C.c_double),
-                ("factor_bytes", C.c_double)]
+                ("factor_bytes", C.c_double), ("n_nonpositive_jacobians", C.c_int64), ("factor_stored", C.c_int64)]
 
 
 class SolveInfo(C.Structure):
@@ -140,7 +140,8 @@ EXPORTS = [
     "elp_model_rhs_omega", "elp_cell_stresses", "elp_node_stresses",
     "elp_solve", "elp_model_destroy", "elp_last_error", "elp_solve_device", "elp_model_time_assembly",
     "elp_server_create", "elp_server_add_model", "elp_server_submit", "elp_server_wait",
-    "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc",
+    "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc", "elp_fault_inject",
+    "elp_front_update_test",
 ]
 KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
                   "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc", "spmv", "fwd_border",
@@ -181,6 +182,8 @@ def load_library(path: str | None = None):
     lib.elp_server_wait.argtypes = [P, C.POINTER(RequestResult), C.c_double]
     lib.elp_server_destroy.argtypes = [P]
     lib.elp_residual_noalloc.argtypes = [P, P, C.c_int, P, P, P, P, P]
+    lib.elp_fault_inject.argtypes = [C.c_int, C.c_int]
+    lib.elp_front_update_test.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P, P]
     lib.elp_profile.argtypes = [C.c_int]
     lib.elp_profile_read.argtypes = [P, P, P, C.POINTER(C.c_int)]
     if path is None:

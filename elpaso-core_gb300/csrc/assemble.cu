@@ -703,6 +703,9 @@ int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms) {
   D.assembly_ms = ms;
   int flags[4];
   ELP_CUDA(cudaMemcpy(flags, D.flags.p, sizeof(flags), cudaMemcpyDeviceToHost));
+  // Brick8 / Fluid8: the reference reports det J <= 0 and goes on
+  // (elementfem.cpp:183-188, its throw commented out); DSG4: it throws (:97-100)
+  D.bad_jacobians_3d = flags[0];
   if (flags[1] > 0) {
     set_error("detJac <= 0 in a DSG4 element: check orientation of the elements");
     return ELP_ERR_GEOMETRY;

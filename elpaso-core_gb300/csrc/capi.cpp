@@ -19,6 +19,23 @@ using namespace elp;
 namespace elp {
 Model::Model() = default;
 Model::~Model() = default;
+
+int model_symbolic_host(Model& m) {
+  if (m.sym) return ELP_OK;
+  fault_host_alloc_point();
+  std::unique_ptr<Symbolic> s(new Symbolic());
+  // leaves of the nested dissection: subsets of at most this many DOFs
+  // (ELP_LEAF, default 128)
+  static const int leaf = [] {
+    const char* e = getenv("ELP_LEAF");
+    const int v = e ? atoi(e) : 128;
+    return v < 8 ? 8 : v;
+  }();
+  int rc = symbolic_analyse(m, *s, leaf);
+  if (rc) return rc;
+  m.sym = std::move(s);
+  return ELP_OK;
+}
 }  // namespace elp
 
 #define GUARD_BEGIN try {
@@ -80,7 +97,10 @@ int elp_model_assemble(elp_model* h) {
   Model& m = h->m;
   if (!m.dev) {
     rc = device_upload_model(m);
-    if (rc) return rc;
+    if (rc) {
+      m.dev.reset();  // partly uploaded: the next call starts over
+      return rc;
+    }
   }
   float ms = 0.f;
   rc = device_assemble(m, 0, &ms);
@@ -113,20 +133,8 @@ int elp_model_analyse(elp_model* h) {
   if (!h) { set_error("null model"); return ELP_ERR_ARG; }
   Model& m = h->m;
   if (m.analysed) return ELP_OK;
-  int rc;
-  if (!m.sym) {  // host phase; kept when the device step below fails
-    std::unique_ptr<Symbolic> s(new Symbolic());
-    // leaves of the nested dissection: subsets of at most this many DOFs
-    // (ELP_LEAF, default 128)
-    static const int leaf = [] {
-      const char* e = getenv("ELP_LEAF");
-      const int v = e ? atoi(e) : 128;
-      return v < 8 ? 8 : v;
-    }();
-    rc = symbolic_analyse(m, *s, leaf);
-    if (rc) return rc;
-    m.sym = std::move(s);
-  }
+  int rc = model_symbolic_host(m);  // kept when the device step below fails
+  if (rc) return rc;
   rc = check_cuda_device();
   if (rc) return rc;
   rc = device_upload_symbolic(m);
@@ -153,7 +161,11 @@ int elp_model_get_info(const elp_model* h, elp_model_info* info) {
     info->factor_bytes = m.sym->factor_bytes;
     info->n_levels = m.sym->n_levels;
     info->max_front = m.sym->max_front;
+    int64_t stored = 0;
+    for (const FrontInfo& F : m.sym->fronts) stored += (int64_t)F.p * F.p + 2 * (int64_t)F.p * F.b;
+    info->factor_stored = stored;
   }
+  if (m.dev) info->n_nonpositive_jacobians = m.dev->bad_jacobians_3d;
   return ELP_OK;
   GUARD_END
 }
@@ -282,10 +294,11 @@ int elp_solve_device(elp_model* h, const double* omegas, int n_omega, int precis
                              f_dev ? reinterpret_cast<const double2*>(f_dev) + (size_t)s0 * n : nullptr,
                              reinterpret_cast<double2*>(x_dev) + (size_t)s0 * n, info ? info + s0 : nullptr, tol,
                              (cudaStream_t)stream);
-    if (rc == ELP_ERR_NOCONV) worst = rc;
-    else if (rc) return rc;
+    if (rc == ELP_ERR_SINGULAR || (rc == ELP_ERR_NOCONV && worst != ELP_ERR_SINGULAR)) worst = rc;
+    else if (rc && rc != ELP_ERR_NOCONV) return rc;
   }
-  if (worst) set_error("iterative refinement did not reach the requested relative residual");
+  if (worst == ELP_ERR_NOCONV) set_error("iterative refinement did not reach the requested relative residual");
+  if (worst == ELP_ERR_SINGULAR) set_error("zero pivot at one or more frequencies: singular system");
   return worst;
   GUARD_END
 }
@@ -307,9 +320,18 @@ int elp_solve(elp_model* h, const double* omegas, int n_omega, int precision, co
   ELP_CUDA(xd.alloc((size_t)n * n_omega));
   rc = elp_solve_device(h, omegas, n_omega, precision, f_or_null ? reinterpret_cast<double*>(fd.p) : nullptr,
                         reinterpret_cast<double*>(xd.p), info, tol, nullptr);
-  if (rc && rc != ELP_ERR_NOCONV) return rc;
+  if (rc && rc != ELP_ERR_NOCONV && rc != ELP_ERR_SINGULAR) return rc;
   ELP_CUDA(cudaMemcpy(x_out, xd.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToHost));
   return rc;
+  GUARD_END
+}
+
+int elp_front_update_test(int kernel, int p, int b, int step, int slots, float* fronts, int parent_m,
+                          const int32_t* pmap, float* parents) {
+  GUARD_BEGIN
+  int rc = check_cuda_device();
+  if (rc) return rc;
+  return front_update_test(kernel, p, b, step, slots, fronts, parent_m, pmap, parents);
   GUARD_END
 }
 

@@ -10,14 +10,21 @@
 
 namespace elp {
 
+// An allocation failure maps to ELP_ERR_NOMEM (and clears the runtime's
+// last error); every other runtime error to ELP_ERR_CUDA.
 #define ELP_CUDA(call)                                                            \
   do {                                                                            \
     cudaError_t e_ = (call);                                                      \
     if (e_ != cudaSuccess) {                                                      \
       set_error(std::string("CUDA: ") + cudaGetErrorString(e_) + " at " __FILE__); \
+      if (e_ == cudaErrorMemoryAllocation) {                                      \
+        cudaGetLastError();                                                       \
+        return ELP_ERR_NOMEM;                                                     \
+      }                                                                           \
       return ELP_ERR_CUDA;                                                        \
     }                                                                             \
   } while (0)
+
 
 // Per-element material constants for the assembly kernel (real E: the
 // loss factor is a per-w coefficient of the group's stiffness array).
@@ -46,9 +53,15 @@ struct DevBuf {
   }
   cudaError_t alloc(size_t count) {
     release();
-    n = count;
     if (count == 0) return cudaSuccess;
-    return cudaMalloc((void**)&p, count * sizeof(T));
+    if (fault_device_alloc()) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    return cudaSuccess;
   }
   cudaError_t upload(const T* h, size_t count) {
     cudaError_t e = alloc(count);
@@ -77,6 +90,7 @@ struct DeviceModel {
   DevBuf<double> iface_scale;      // per quad: -ori
   DevBuf<int32_t> iface_geom;      // per quad: 4 fluid node indices (geometry)
   DevBuf<int> flags;               // [0] 3D non-positive detJ count, [1] 2D count
+  int64_t bad_jacobians_3d = 0;    // flags[0] of the last assembly
   int64_t n_brick = 0, n_plate = 0, n_fluid = 0, n_iface = 0;
   double assembly_ms = 0.0;
 };

@@ -108,9 +108,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
 }
 
 // waits for the phase with an iteration bound; returns false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, uint32_t limit = 1u << 24) {
   const uint32_t a = smem_u32(mbar);
-  for (uint32_t it = 0; it < (1u << 24); ++it) {
+  for (uint32_t it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -636,14 +636,17 @@ __global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* _
 //   acc_empty[a]          - the 8 epilogue warps have read accumulator a.
 // Every wait is bounded; after a timeout a role stops, the CTA sets the error
 // flag and waits (bounded) for its copies and MMAs in flight before the TMEM
-// is released.
+// is released. fault != 0 (a host-side test switch, elp_fault_inject) makes
+// the producer issue nothing and bounds every wait at 2^14 polls: the MMA
+// and epilogue waits then run out with no copy or MMA in flight.
 constexpr int kSchurThreads = 320;
 
 template <int NB>
 __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, float2* __restrict__ arena,
                                                                const uint32_t* __restrict__ pack,
                                                                const int64_t* __restrict__ pack_base,
-                                                               int64_t slot_bytes, int* __restrict__ err) {
+                                                               int64_t slot_bytes, int* __restrict__ err,
+                                                               int fault) {
   extern __shared__ __align__(1024) unsigned char schur_smem_raw[];
   SchurSmem& sm = *reinterpret_cast<SchurSmem*>(schur_smem_raw);
   const int f = L.list[blockIdx.x];
@@ -681,6 +684,7 @@ __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, floa
   tc::fence_after();
   const uint32_t tmem = sm.tmem_base;
   bool ok = true;
+  const uint32_t lim = fault ? (1u << 14) : (1u << 24);  // poll bound of every wait
   // chunk g (counted over all this CTA's tiles) uses stage g % kSchurStages, and
   // its use g / kSchurStages of the stage completes mbarrier phase (g / kSchurStages) & 1;
   // tile j uses accumulator j & 1, whose use j / 2 completes phase (j / 2) & 1
@@ -688,14 +692,14 @@ __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, floa
   if (warp == 0 && lane == 0) {
     // ------------------------------------------------ producer
     int g = 0;
-    for (int j = 0; j < nmine && ok; ++j) {
+    for (int j = 0; j < nmine && ok && !fault; ++j) {
       const int t = (int)blockIdx.z + j * (int)gridDim.z;
       const int tr = t % tiles, tcol = t / tiles;
       const char* Ab = Abase + (int64_t)(tr * nch) * kSchurABlock;
       const char* Bb = Bbase + (int64_t)(tcol * nch) * kSchurBBlock;
       for (int c = 0; c < nch; ++c, ++g) {
         const int st = g % kSchurStages;
-        if (g >= kSchurStages && ok) ok = tc::mbar_wait(&sm.empty[st], ((g / kSchurStages) + 1) & 1);
+        if (g >= kSchurStages && ok) ok = tc::mbar_wait(&sm.empty[st], ((g / kSchurStages) + 1) & 1, lim);
         if (!ok) break;
         tc::mbar_expect_tx(&sm.full[st], (uint32_t)(kSchurABlock + kSchurBBlock));
         tc::bulk_g2s(&sm.st[st].a[0][0], Ab + (int64_t)c * kSchurABlock, (uint32_t)kSchurABlock, &sm.full[st]);
@@ -713,11 +717,11 @@ __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, floa
     for (int j = 0; j < nmine && ok; ++j) {
       const int acc = j & 1;
       const uint32_t D = tmem + (uint32_t)acc * kSchurCols;
-      if (j >= 2) ok = tc::mbar_wait(&sm.acc_empty[acc], ((j / 2) + 1) & 1);  // epilogue of tile j - 2 read it
+      if (j >= 2) ok = tc::mbar_wait(&sm.acc_empty[acc], ((j / 2) + 1) & 1, lim);  // epilogue of tile j - 2 read it
       tc::fence_after();
       for (int c = 0; c < nch && ok; ++c, ++g) {
         const int st = g % kSchurStages;
-        ok = tc::mbar_wait(&sm.full[st], (g / kSchurStages) & 1);
+        ok = tc::mbar_wait(&sm.full[st], (g / kSchurStages) & 1, lim);
         if (!ok) break;
         tc::fence_after();
         uint32_t a[4], w[2];
@@ -758,7 +762,7 @@ __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, floa
       const int acc = j & 1;
       const int t = (int)blockIdx.z + j * (int)gridDim.z;
       const int tr = t % tiles, tcol = t / tiles;
-      if (lane == 0 && ok) ok = tc::mbar_wait(&sm.acc_full[acc], (j / 2) & 1);
+      if (lane == 0 && ok) ok = tc::mbar_wait(&sm.acc_full[acc], (j / 2) & 1, lim);
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
       tc::fence_after();
@@ -800,12 +804,12 @@ __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, floa
     if (tid == 0) {
       atomicExch(err, 1);
       for (int g = (issued > kSchurStages ? issued - kSchurStages : 0); g < issued; ++g)
-        tc::mbar_wait(&sm.full[g % kSchurStages], (g / kSchurStages) & 1);
+        tc::mbar_wait(&sm.full[g % kSchurStages], (g / kSchurStages) & 1, lim);
     } else if (tid == 32) {
       for (int g = (mma_chunks > kSchurStages ? mma_chunks - kSchurStages : 0); g < mma_chunks; ++g)
-        tc::mbar_wait(&sm.empty[g % kSchurStages], (g / kSchurStages) & 1);
+        tc::mbar_wait(&sm.empty[g % kSchurStages], (g / kSchurStages) & 1, lim);
       for (int j = (mma_tiles > 2 ? mma_tiles - 2 : 0); j < mma_tiles; ++j)
-        tc::mbar_wait(&sm.acc_full[j & 1], (j / 2) & 1);
+        tc::mbar_wait(&sm.acc_full[j & 1], (j / 2) & 1, lim);
     }
   }
   tc::fence_before();

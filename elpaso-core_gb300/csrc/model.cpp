@@ -151,6 +151,7 @@ static bool face_shape_integrals(const Model& m, const int32_t* fn, double* nint
 }
 
 int build_model(const elp_model_desc* d, Model& m, std::string& err) {
+  fault_host_alloc_point();
   if (!d) { err = "null model description"; return ELP_ERR_ARG; }
   if (d->n_nodes <= 0 || !d->coords || !d->node_ids) { err = "model has no nodes"; return ELP_ERR_ARG; }
   if (d->n_nodes >= (int64_t)1 << 30) { err = "too many nodes"; return ELP_ERR_ARG; }

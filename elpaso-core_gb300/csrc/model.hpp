@@ -134,6 +134,12 @@ int node_stresses(const Model& m, double w, const cplx* x, cplx* out, std::strin
 void set_error(const std::string& s);
 const std::string& get_error();
 
+// Host-side fault injection (fault.cpp, elp_fault_inject): each returns true
+// (or throws std::bad_alloc) exactly once, when its countdown runs out.
+bool fault_device_alloc();
+void fault_host_alloc_point();
+bool fault_tc_wait();
+
 }  // namespace elp
 
 // the opaque handle of the C ABI

@@ -17,7 +17,10 @@
 //    GPU (different streams or threads at the same time) race on it;
 //  - the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (a host-side name is not a device address); make
-//    that first call before any stream capture.
+//    that first call before any stream capture;
+//  - it needs an assembled model only (the symbolic phase is not used);
+//  - its launches are not counted or timed by elp_profile.
+// A call with profiling on still allocates nothing.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -25,7 +28,6 @@
 
 #include "device.cuh"
 #include "numeric.cuh"
-#include "prof.cuh"
 
 namespace elp {
 namespace {
@@ -163,14 +165,15 @@ extern "C" int elp_residual_noalloc(elp_model* h, const double* omegas, int n_om
   const int64_t n = m.n;
   const int nparts = (int)std::min<int64_t>(kNoAllocParts, std::max<int64_t>(1, (n + 255) / 256));
   CombineArgs A = combine_args(m);
-  PROF_LAUNCH(KC_RESIDUAL, st,
-              k_noalloc_residual<<<dim3(nparts, n_omega), 256, 0, st>>>(
-                  A, sc, m.dev->row_ptr.p, m.dev->col_idx.p, n, reinterpret_cast<const double2*>(x_dev),
-                  reinterpret_cast<const double2*>(f_dev), reinterpret_cast<double2*>(r_dev)));
-  PROF_LAUNCH(KC_NORMS, st, k_noalloc_norms<<<n_omega, 256, 0, st>>>(sc, nparts));
+  // launched outside the library's launch profiler: its event pairs are
+  // created on demand and resolved across every stream, which would break
+  // both the no-allocation promise and the independence from other streams
+  k_noalloc_residual<<<dim3(nparts, n_omega), 256, 0, st>>>(
+      A, sc, m.dev->row_ptr.p, m.dev->col_idx.p, n, reinterpret_cast<const double2*>(x_dev),
+      reinterpret_cast<const double2*>(f_dev), reinterpret_cast<double2*>(r_dev));
+  k_noalloc_norms<<<n_omega, 256, 0, st>>>(sc, nparts);
   ELP_CUDA(cudaGetLastError());
   ELP_CUDA(cudaMemcpyAsync(rel_residual_out, sc->rel, sizeof(double) * n_omega, cudaMemcpyDeviceToHost, st));
   ELP_CUDA(cudaStreamSynchronize(st));
-  prof_resolve();
   return ELP_OK;
 }

@@ -1173,14 +1173,14 @@ Workspace::~Workspace() {
   if (h_norms) cudaFreeHost(h_norms);
   if (h_active) cudaFreeHost(h_active);
   if (h_stats) cudaFreeHost(h_stats);
+  if (h_flag) cudaFreeHost(h_flag);
   if (h_h) cudaFreeHost(h_h);
   if (h_y) cudaFreeHost(h_y);
   if (h_scal) cudaFreeHost(h_scal);
   if (h_inner) cudaFreeHost(h_inner);
-  if (stream) {
-    for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
-    cudaStreamDestroy(stream);
-  }
+  for (int i = 0; i < 8; ++i)
+    if (ev[i]) cudaEventDestroy(ev[i]);
+  if (stream) cudaStreamDestroy(stream);
 }
 
 void make_coef(const Model& m, double w, Coef& c) {
@@ -1260,7 +1260,6 @@ int device_upload_symbolic(Model& m) {
   // packed Schur operands (mixed path): per front with p, b > 0, tiles x chunks
   // blocks of A (L21, kSchurABlock bytes) then of B (U12, kSchurBBlock bytes)
   std::vector<int64_t> pbase(T, 0);
-  D.pack_max = 0;
   for (int l = 0; l < S.n_levels; ++l) {
     auto& L = D.levels[l];
     int64_t off = 0;
@@ -1274,9 +1273,8 @@ int device_upload_symbolic(Model& m) {
       }
     }
     L.pack_bytes = off;
-    static const bool pack_all_levels = getenv("ELP_TC_PACK") && std::string(getenv("ELP_TC_PACK")) == "all";
-    if (pack_all_levels || packed_schur_level(L)) D.pack_max = std::max(D.pack_max, off);
   }
+  D.pack_max = workspace_plan(S).pack_max;
   ELP_CUDA(D.pack_base.upload(pbase));
   ELP_CUDA(D.level_list.upload(ll));
   ELP_CUDA(D.ea_list.upload(ea));
@@ -1322,17 +1320,40 @@ int pack_min_border() {
 
 constexpr int kGmresRestart = 24;  // GMRES(24) of the mixed path
 
+WorkspacePlan workspace_plan(const Symbolic& S) {
+  WorkspacePlan P;
+  P.arena = S.arena;
+  P.cb_total = S.cb_total;
+  static const bool pack_all_levels = getenv("ELP_TC_PACK") && std::string(getenv("ELP_TC_PACK")) == "all";
+  for (int l = 0; l < S.n_levels; ++l) {
+    DeviceSymbolic::Level L;
+    L.count = (int)S.level_fronts[l].size();
+    int64_t off = 0;
+    for (int t : S.level_fronts[l]) {
+      const FrontInfo& F = S.fronts[t];
+      L.max_b = std::max(L.max_b, F.b);
+      if (F.p > 0 && F.b > 0) {
+        const int64_t tiles = (F.b + kSchurTile - 1) / kSchurTile, nch = (F.p + kTcKC - 1) / kTcKC;
+        off += tiles * nch * (kSchurABlock + kSchurBBlock);
+      }
+    }
+    P.max_count = std::max<int64_t>(P.max_count, L.count);
+    if (pack_all_levels || packed_schur_level(L)) P.pack_max = std::max(P.pack_max, off);
+  }
+  return P;
+}
+
 // Device bytes of the workspace `workspace_ensure` (+ the GMRES buffers of the
 // mixed path) allocates for `slots` frequencies; the serving loop admits
-// models against this figure, so it mirrors those allocations.
+// models against this figure, so it mirrors those allocations. Needs only the
+// host symbolic phase (no device allocation has to happen first).
 int64_t workspace_bytes(const Model& m, int precision, int slots) {
-  if (!m.dsym) return 0;
-  const DeviceSymbolic& D = *m.dsym;
+  if (!m.sym) return 0;
+  const WorkspacePlan D = workspace_plan(*m.sym);
   const int64_t n = m.n, S = slots;
   const int64_t elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
   const int64_t nparts = std::min<int64_t>(1024, (n + 255) / 256);
-  int64_t max_count = 1;
-  for (const auto& LV : D.levels) max_count = std::max<int64_t>(max_count, LV.count);
+  const int64_t max_count = D.max_count;
   int64_t b = S * (D.arena + std::max<int64_t>(1, D.cb_total) + 2 * n) * elem;  // arena, cb, z, tb
   b += S * n * (4 + 8 + 3 * 16);                                               // perm, dscale, x, r, f
   b += S * (int64_t)(sizeof(Coef) + 16 + nparts * 16 + 4 + 32) + 4;            // coef, norms, partials, flags
@@ -1353,11 +1374,21 @@ int64_t workspace_held(const Model& m, int precision) {
   return b;
 }
 
+static int workspace_alloc(Model& m, Workspace& w, int precision, int slots);
+
 int workspace_ensure(Model& m, int precision, int slots, int lane) {
   std::unique_ptr<Workspace>& W = lane ? m.ws_b[precision][lane - 1] : m.ws[precision];
   if (W && W->slots >= slots) return ELP_OK;
-  W.reset(new Workspace());
-  Workspace& w = *W;
+  W.reset();  // the old workspace goes before the new one is made
+  // built aside and kept only when every allocation succeeded
+  std::unique_ptr<Workspace> fresh(new Workspace());
+  int rc = workspace_alloc(m, *fresh, precision, slots);
+  if (rc) return rc;
+  W = std::move(fresh);
+  return ELP_OK;
+}
+
+static int workspace_alloc(Model& m, Workspace& w, int precision, int slots) {
   w.precision = precision;
   w.slots = slots;
   w.elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
@@ -1365,7 +1396,6 @@ int workspace_ensure(Model& m, int precision, int slots, int lane) {
   const int64_t n = m.n;
   cudaError_t e = w.arena.alloc((size_t)slots * D.arena * w.elem);
   if (e != cudaSuccess) {
-    W.reset();
     cudaGetLastError();
     set_error("front arena does not fit in device memory");
     return ELP_ERR_NOMEM;
@@ -1396,6 +1426,7 @@ int workspace_ensure(Model& m, int precision, int slots, int lane) {
   ELP_CUDA(cudaMallocHost((void**)&w.h_norms, sizeof(double) * 2 * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_active, sizeof(int) * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_stats, sizeof(unsigned long long) * 4 * slots));
+  ELP_CUDA(cudaMallocHost((void**)&w.h_flag, sizeof(int)));
   ELP_CUDA(cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking));
   for (int i = 0; i < 8; ++i) ELP_CUDA(cudaEventCreate(&w.ev[i]));
   return ELP_OK;
@@ -1421,6 +1452,26 @@ int numeric_system_values(Model& m, double omega, double2* out_dev) {
   PROF_LAUNCH(KC_VALUES, 0, k_values<<<1024, 256>>>(A, c.p, out_dev));
   ELP_CUDA(cudaGetLastError());
   ELP_CUDA(cudaDeviceSynchronize());
+  return ELP_OK;
+}
+
+// dynamic shared-memory limits of the tensor-core kernels (once per process)
+static int tc_kernel_attributes() {
+  constexpr int NB = 32;
+  static std::once_flag once;
+  static cudaError_t e = cudaSuccess;
+  std::call_once(once, [] {
+    cudaError_t a = cudaFuncSetAttribute(k_gemm_tc<NB, 32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kTcSmemBytes);
+    cudaError_t b = cudaFuncSetAttribute(k_gemm_tc<NB, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kTcSmemBytes);
+    cudaError_t c = cudaFuncSetAttribute(k_gemm_tc<NB, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kTcSmemBytes);
+    cudaError_t d = cudaFuncSetAttribute(k_schur_tc<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kSchurSmemBytes);
+    e = a != cudaSuccess ? a : b != cudaSuccess ? b : c != cudaSuccess ? c : d;
+  });
+  ELP_CUDA(e);
   return ELP_OK;
 }
 
@@ -1466,20 +1517,8 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   static const bool pack_all = pack_env && std::string(pack_env) == "all";
   const bool tc = std::is_same<R, float>::value && use_tc;
   if (tc) {
-    static std::once_flag once;
-    static cudaError_t e = cudaSuccess;
-    std::call_once(once, [] {
-      cudaError_t a = cudaFuncSetAttribute(k_gemm_tc<NB, 32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           kTcSmemBytes);
-      cudaError_t b = cudaFuncSetAttribute(k_gemm_tc<NB, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           kTcSmemBytes);
-      cudaError_t c = cudaFuncSetAttribute(k_gemm_tc<NB, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           kTcSmemBytes);
-      cudaError_t d = cudaFuncSetAttribute(k_schur_tc<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           kSchurSmemBytes);
-      e = a != cudaSuccess ? a : b != cudaSuccess ? b : c != cudaSuccess ? c : d;
-    });
-    ELP_CUDA(e);
+    int rc = tc_kernel_attributes();
+    if (rc) return rc;
   }
   const int panel_cap = kPanelSmemBytes / (NB * (int)sizeof(V));  // panel rows held in shared memory
   {
@@ -1577,8 +1616,9 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
           const int64_t pairs = (int64_t)Lc.count * S_used;
           const int64_t gz = std::min<int64_t>(LV.schur_tiles, std::max<int64_t>(1, (2 * num_sms() + pairs - 1) / pairs));
           dim3 gs(Lc.count, S_used, (unsigned)gz);
+          const int fault = fault_tc_wait() ? 1 : 0;  // host-side test switch (elp_fault_inject)
           PROF_LAUNCH(KC_GEMM_TC, st, k_schur_tc<NB><<<gs, kSchurThreads, kSchurSmemBytes, st>>>(
-                                          Lc, fa, pk, D.pack_base.p, LV.pack_bytes, w.tc_err.p));
+                                          Lc, fa, pk, D.pack_base.p, LV.pack_bytes, w.tc_err.p, fault));
         } else {
           gemm(GM_SCHUR, 0, LV.ea_max_b, LV.ea_max_b, Lc);
         }
@@ -1753,8 +1793,8 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
 }
 
 static int gmres_alloc(Workspace& w, int64_t n, int S, int rst) {
-  if (w.rst == rst && w.Vb.p) return ELP_OK;
-  w.rst = rst;
+  if (w.rst == rst) return ELP_OK;
+  w.rst = 0;  // set once every buffer below exists, so a failed call is retried in full
   ELP_CUDA(w.Vb.alloc((size_t)S * (rst + 1) * n));
   ELP_CUDA(w.Zb.alloc((size_t)S * rst * n));
   ELP_CUDA(w.wv.alloc((size_t)S * n));
@@ -1769,6 +1809,7 @@ static int gmres_alloc(Workspace& w, int64_t n, int S, int rst) {
   if (!w.h_y) ELP_CUDA(cudaMallocHost((void**)&w.h_y, sizeof(double2) * S * kMaxBasis));
   if (!w.h_scal) ELP_CUDA(cudaMallocHost((void**)&w.h_scal, sizeof(double) * S));
   if (!w.h_inner) ELP_CUDA(cudaMallocHost((void**)&w.h_inner, sizeof(int) * S));
+  w.rst = rst;
   return ELP_OK;
 }
 
@@ -1822,8 +1863,15 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
     PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, src, sstride, w.dscale.p, n, z, mask));
     return solve_sweep<R>(m, w, S_used, st, mask);
   };
+  // a tensor-core wait that ran out left the factors incomplete: stop before
+  // the Krylov cycles (the flag is read back with the first residual's sync)
+  ELP_CUDA(cudaMemcpyAsync(w.h_flag, w.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   rc = residual(1);  // x = 0
   if (rc) return rc;
+  if (*w.h_flag) {
+    set_error("a tensor-core Schur update gave up waiting for its MMAs");
+    return ELP_ERR_CUDA;
+  }
   std::vector<std::vector<cd>> H(S_used, std::vector<cd>((RST + 1) * RST));
   std::vector<std::vector<cd>> g(S_used, std::vector<cd>(RST + 1)), sn(S_used, std::vector<cd>(RST));
   std::vector<std::vector<double>> cs(S_used, std::vector<double>(RST));
@@ -1971,7 +2019,7 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
   if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 12, st, ms);
   else rc = run_batch<double>(m, w, n_omega, tol, 8, st, &iters, ms);
   if (rc) return rc;
-  ELP_CUDA(cudaMemcpyAsync(x_dev, w.x.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToDevice, st));
+  if (x_dev) ELP_CUDA(cudaMemcpyAsync(x_dev, w.x.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToDevice, st));
   ELP_CUDA(cudaMemcpyAsync(w.h_stats, w.stats.p, sizeof(unsigned long long) * 4 * n_omega, cudaMemcpyDeviceToHost, st));
   int tcerr = 0;
   ELP_CUDA(cudaMemcpyAsync(&tcerr, w.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1981,11 +2029,15 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
     set_error("a tensor-core Schur update gave up waiting for its MMAs");
     return ELP_ERR_CUDA;
   }
-  bool ok = true;
+  bool ok = true, singular = false;
   for (int s = 0; s < n_omega; ++s) {
     double fn = w.h_norms[2 * s + 1];
     double rel = fn > 0 ? std::sqrt(w.h_norms[2 * s] / fn) : std::sqrt(w.h_norms[2 * s]);
-    if (!(rel <= tol)) ok = false;
+    if (!(rel <= tol)) {
+      ok = false;
+      // a zero pivot the static-pivot floor stood in for, and the refinement could not recover
+      if (w.h_stats[4 * s + 0] > 0) singular = true;
+    }
     if (info) {
       elp_solve_info& I = info[s];
       I.rel_residual = rel;
@@ -2003,11 +2055,46 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
       I.ms_combine = 0.0;
     }
   }
+  if (singular) {
+    set_error("zero pivot: the static-pivot floor replaced it and the refinement did not converge "
+              "(singular system at this frequency)");
+    return ELP_ERR_SINGULAR;
+  }
   if (!ok) {
     set_error("iterative refinement did not reach the requested relative residual");
     return ELP_ERR_NOCONV;
   }
   return ELP_OK;
+}
+
+int numeric_solve_lane(Model& m, int precision, int lane, const double* omegas, int n_omega, const double2* f_dev,
+                       double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream) {
+  if (n_omega <= 0) return ELP_OK;
+  if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
+  if (lane < 0 || lane > 3) { set_error("workspace lane out of range"); return ELP_ERR_ARG; }
+  for (int s = 0; s < n_omega; ++s)
+    if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
+  return solve_lane(m, precision, lane, omegas, n_omega, f_dev, x_dev, info, tol, stream);
+}
+
+const double2* lane_solution(const Model& m, int precision, int lane) {
+  const std::unique_ptr<Workspace>& W = lane ? m.ws_b[precision][lane - 1] : m.ws[precision];
+  return W ? W->x.p : nullptr;
+}
+
+int64_t model_array_bytes(const Model& m) {
+  const int64_t groups = std::max<int64_t>(1, (int64_t)m.groups.size());
+  // row_ptr, col_idx, cls, diag, VK, VM, VKg, rhs (+ vn), bc rows, coordinates, element lists
+  int64_t b = m.nnz * (4 + 1 + 8 + 8 + 8 * (groups - 1)) + (m.n + 1) * 4 + m.n * (4 + 16 + (m.has_vn ? 16 : 0));
+  b += (int64_t)m.bc_rows.size() * 4 + m.n_nodes * (24 + 3 * 4);
+  for (const Block& B : m.blocks) b += (int64_t)B.conn.size() * 4 + B.n_elements * 2;
+  b += (int64_t)m.interfaces.size() * (16 * 4 + 8 + 4 * 4);
+  if (m.sym) {  // symbolic maps: per-entry arena offsets, front lists, extend-add maps
+    const Symbolic& S = *m.sym;
+    b += (int64_t)S.entry_off.size() * 8 + (int64_t)S.front_dofs.size() * 4 + (int64_t)S.parent_map.size() * 4;
+    b += (int64_t)S.fronts.size() * (8 * 4 + 8 + 8 + 4 * 4);
+  }
+  return b;
 }
 
 // Batches of kSplitMin or more frequencies are solved in parts on several
@@ -2073,14 +2160,116 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
   for (auto& t : threads) t.join();
   cudaEventDestroy(ev);
   // each lane synchronised its stream before returning: the results are complete
-  bool noconv = false;
+  // solutions and infos of every lane are complete; a frequency that did not
+  // reach the tolerance (ELP_ERR_NOCONV, or ELP_ERR_SINGULAR with static
+  // pivots) is reported with the results, any other error first
+  int soft = ELP_OK;
   for (int l = 0; l < lanes; ++l) {
-    if (rcs[l] == ELP_ERR_NOCONV) noconv = true;
-    else if (rcs[l]) { set_error(errs[l]); return rcs[l]; }
+    if (rcs[l] == ELP_ERR_NOCONV || rcs[l] == ELP_ERR_SINGULAR) {
+      if (soft != ELP_ERR_SINGULAR) { soft = rcs[l]; set_error(errs[l]); }
+    } else if (rcs[l]) {
+      set_error(errs[l]);
+      return rcs[l];
+    }
   }
-  if (noconv) {
-    set_error("iterative refinement did not reach the requested relative residual");
-    return ELP_ERR_NOCONV;
+  return soft;
+}
+
+
+// One front update of the mixed path on caller-given fronts (elp_front_update_test).
+int front_update_test(int kernel, int p, int b, int step, int slots, float* fronts, int parent_m,
+                      const int32_t* pmap, float* parents) {
+  constexpr int NB = 32;
+  if (kernel < 0 || kernel > 3 || p < 1 || b < 0 || slots < 1 || slots > kMaxSlots || !fronts || step < 0) {
+    set_error("bad front update test arguments");
+    return ELP_ERR_ARG;
+  }
+  const bool fused = parents != nullptr;
+  if (kernel == 3 && !fused) { set_error("the packed Schur update adds into a parent front"); return ELP_ERR_ARG; }
+  if (fused) {
+    if (kernel < 2 || !pmap || parent_m < b || b < 1) { set_error("bad parent arguments"); return ELP_ERR_ARG; }
+    std::vector<char> seen(parent_m, 0);
+    for (int i = 0; i < b; ++i) {
+      if (pmap[i] < 0 || pmap[i] >= parent_m || seen[pmap[i]]) { set_error("pmap must be injective into the parent"); return ELP_ERR_ARG; }
+      seen[pmap[i]] = 1;
+    }
+  }
+  if (kernel < 2 && step * NB >= p) { set_error("step beyond the pivots"); return ELP_ERR_ARG; }
+  int rc = tc_kernel_attributes();
+  if (rc) return rc;
+  const int64_t m = p + b, mP = fused ? parent_m : 0;
+  const int64_t per_slot = m * m + mP * mP;  // complex entries: front, then parent
+  DevBuf<float2> arena;
+  ELP_CUDA(arena.alloc((size_t)slots * per_slot));
+  for (int s = 0; s < slots; ++s) {
+    ELP_CUDA(cudaMemcpy(arena.p + s * per_slot, fronts + 2 * s * m * m, sizeof(float2) * m * m, cudaMemcpyHostToDevice));
+    if (fused)
+      ELP_CUDA(cudaMemcpy(arena.p + s * per_slot + m * m, parents + 2 * s * mP * mP, sizeof(float2) * mP * mP,
+                          cudaMemcpyHostToDevice));
+  }
+  const int32_t h_list[1] = {0}, h_fp[2] = {p, (int32_t)mP}, h_fb[2] = {b, 0}, h_par[2] = {fused ? 1 : -1, -1};
+  const int32_t h_zero[2] = {0, 0};
+  const int64_t h_off[2] = {0, m * m};
+  DevBuf<int32_t> list, fp, fb, par, zero, dmap;
+  DevBuf<int64_t> foff, pbase;
+  DevBuf<int> err;
+  ELP_CUDA(list.upload(h_list, 1));
+  ELP_CUDA(fp.upload(h_fp, 2));
+  ELP_CUDA(fb.upload(h_fb, 2));
+  ELP_CUDA(par.upload(h_par, 2));
+  ELP_CUDA(zero.upload(h_zero, 2));
+  ELP_CUDA(foff.upload(h_off, 2));
+  if (fused) ELP_CUDA(dmap.upload(pmap, b));
+  ELP_CUDA(err.alloc(1));
+  ELP_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+  LevelArgs L;
+  L.list = list.p;
+  L.count = 1;
+  L.fp = fp.p;
+  L.fb = fb.p;
+  L.piv_off = zero.p;
+  L.foff = foff.p;
+  L.arena_size = per_slot;
+  L.n = m;
+  L.fparent = par.p;
+  L.map_off = zero.p;
+  L.pmap = fused ? dmap.p : zero.p;
+  L.fuse = fused ? 1 : 0;
+  cudaStream_t st = 0;
+  if (kernel == 0) {
+    dim3 g(1, slots, (unsigned)((m - step * NB + 127) / 128));
+    k_gemm_tc<NB, 32, false><<<g, kTcThreads, kTcSmemBytes, st>>>(L, arena.p, step, GM_COL, err.p);
+  } else if (kernel == 1) {
+    dim3 g(1, slots, (unsigned)std::max<int64_t>(1, (m - step * NB - NB + 127) / 128));
+    k_gemm_tc<NB, 32, true><<<g, kTcThreads, kTcSmemBytes, st>>>(L, arena.p, step, GM_ROW, err.p);
+  } else if (kernel == 2) {
+    dim3 g(1, slots, (unsigned)(((b + 127) / 128) * ((b + 63) / 64)));
+    if (b > 0) k_gemm_tc<NB, 64, false><<<g, kTcThreads, kTcSmemBytes, st>>>(L, arena.p, 0, GM_SCHUR, err.p);
+  } else {
+    const int64_t tiles = (b + kSchurTile - 1) / kSchurTile, nch = (p + kTcKC - 1) / kTcKC;
+    const int64_t pack_bytes = tiles * nch * (kSchurABlock + kSchurBBlock);
+    const int64_t h_pb[1] = {0};
+    ELP_CUDA(pbase.upload(h_pb, 1));
+    DevBuf<char> pack;
+    ELP_CUDA(pack.alloc((size_t)slots * pack_bytes));
+    uint32_t* pk = reinterpret_cast<uint32_t*>(pack.p);
+    k_pack_schur<NB><<<dim3(1, slots, (unsigned)(2 * tiles * nch)), 256, 0, st>>>(L, arena.p, pk, pbase.p, pack_bytes);
+    const int64_t gz = std::min<int64_t>(tiles * tiles, std::max<int64_t>(1, (2 * num_sms() + slots - 1) / slots));
+    k_schur_tc<NB><<<dim3(1, slots, (unsigned)gz), kSchurThreads, kSchurSmemBytes, st>>>(L, arena.p, pk, pbase.p,
+                                                                                         pack_bytes, err.p, 0);
+    ELP_CUDA(cudaGetLastError());
+    ELP_CUDA(cudaDeviceSynchronize());
+  }
+  ELP_CUDA(cudaGetLastError());
+  ELP_CUDA(cudaDeviceSynchronize());
+  int h_err = 0;
+  ELP_CUDA(cudaMemcpy(&h_err, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h_err) { set_error("a tensor-core wait ran out"); return ELP_ERR_CUDA; }
+  for (int s = 0; s < slots; ++s) {
+    ELP_CUDA(cudaMemcpy(fronts + 2 * s * m * m, arena.p + s * per_slot, sizeof(float2) * m * m, cudaMemcpyDeviceToHost));
+    if (fused)
+      ELP_CUDA(cudaMemcpy(parents + 2 * s * mP * mP, arena.p + s * per_slot + m * m, sizeof(float2) * mP * mP,
+                          cudaMemcpyDeviceToHost));
   }
   return ELP_OK;
 }

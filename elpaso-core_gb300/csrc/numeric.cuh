@@ -173,8 +173,9 @@ struct Workspace {
   double* h_norms = nullptr;
   int* h_active = nullptr;
   unsigned long long* h_stats = nullptr;
+  int* h_flag = nullptr;          // pinned: tc_err read back after the factorisation
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[8];
+  cudaEvent_t ev[8] = {};
   int nparts = 0;
   // GMRES: basis (slots x (rst + 1) x n), work vectors, Hessenberg columns
   int rst = 0;
@@ -189,9 +190,30 @@ struct Workspace {
   ~Workspace();
 };
 
+// Sizes a workspace depends on, from the host symbolic phase alone.
+struct WorkspacePlan {
+  int64_t arena = 0, cb_total = 0, max_count = 1, pack_max = 0;
+};
+WorkspacePlan workspace_plan(const Symbolic& S);
+
 int device_upload_symbolic(Model& m);
 int workspace_ensure(Model& m, int precision, int slots, int lane = 0);
 int64_t workspace_bytes(const Model& m, int precision, int slots);
+// Device bytes of a model's resident arrays (pattern, value arrays, per-row
+// data, element lists, symbolic maps), from host data alone.
+int64_t model_array_bytes(const Model& m);
+// Host part of the symbolic phase (ordering, tree, maps); no device work.
+int model_symbolic_host(Model& m);
+// One batch on workspace lane `lane` (0..3) of the model, on `stream` (the
+// lane's own when null). Distinct lanes of one model may run on different
+// host threads at the same time.
+int numeric_solve_lane(Model& m, int precision, int lane, const double* omegas, int n_omega, const double2* f_dev,
+                       double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream);
+// The FP64 solution vectors of a lane's last batch (slot s at + s * n).
+const double2* lane_solution(const Model& m, int precision, int lane);
+// One front update kernel on caller-given FP32 complex fronts (elp_front_update_test).
+int front_update_test(int kernel, int p, int b, int step, int slots, float* fronts, int parent_m,
+                      const int32_t* pmap, float* parents);
 // Device bytes held by the model's workspaces of one precision (all lanes):
 // reusable by the next batch of that precision.
 int64_t workspace_held(const Model& m, int precision);

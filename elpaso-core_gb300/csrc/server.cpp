@@ -3,22 +3,30 @@
 //
 // The reference runs one model per process and one frequency at a time
 // (analysisfrequencybasic.cpp:101-242). Here a server keeps models resident
-// (assembled value arrays + symbolic factorisation + per-model front
-// workspace) and runs frequency work items:
+// (assembled value arrays + symbolic factorisation + front workspaces) and
+// runs frequency work items:
 //  - requests are split into frequencies; the frequencies waiting on one
 //    model are packed into batches of up to `omega_batch` slots in arrival
 //    order, so a request that arrives while another runs on the same model
 //    joins the next batch (continuous batching, not a request queue);
 //  - `max_inflight` worker threads, each with its own CUDA stream, run
-//    batches of DIFFERENT models at the same time, so their work overlaps
-//    on the device; a model is held by at most one worker at a time;
-//  - a model's device memory (arrays + front workspace) is admitted against
-//    `hbm_budget_bytes`; idle models' workspaces are released to admit
-//    others, and a model that cannot fit alone fails its requests with
+//    batches at the same time, so their work overlaps on the device; a
+//    model has up to kLanesPerModel workspace lanes, so while one worker
+//    runs a long batch of a model, a second worker can start the model's
+//    newer requests on another lane instead of waiting behind it;
+//  - device memory is admitted against `hbm_budget_bytes` BEFORE it is
+//    allocated: a model's resident arrays once (sized from the host model,
+//    before assembly), and each lane's front workspace per batch (sized from
+//    the host symbolic phase); a batch takes as many frequencies as the
+//    budget leaves room for, idle models' workspaces are released to make
+//    room, a batch that finds no room while other batches run waits for
+//    them, and a model that cannot fit alone fails its requests with
 //    ELP_ERR_NOMEM;
+//  - model slots have stable addresses (models may be added while batches
+//    run);
 //  - every slot of a batch is computed by the same kernels independently of
 //    its neighbours (fixed summation orders, no atomics on values), so a
-//    result does not depend on the batch it landed in.
+//    result does not depend on the batch or lane it landed in.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,7 +34,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
-#include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -41,6 +49,7 @@ using namespace elp;
 namespace {
 
 using Clock = std::chrono::steady_clock;
+constexpr int kLanesPerModel = 2;
 
 struct Request {
   int64_t id = 0;
@@ -56,19 +65,15 @@ struct Request {
 
 struct ModelSlot {
   elp_model* h = nullptr;
-  bool busy = false;
   bool ready = false;            // assembled + analysed
-  int64_t resident = 0;          // bytes charged against the budget
+  bool preparing = false;        // a worker is assembling / analysing it
+  bool failed = false;           // its arrays do not fit the budget: requests fail with NOMEM
+  int lanes_busy = 0;            // bit l: a worker runs a batch on workspace lane l
+  int64_t array_bytes = 0;       // charged once, when the model is first prepared
+  int64_t ws_bytes[kLanesPerModel] = {0, 0};  // charged per lane workspace
+  int ws_slots[kLanesPerModel] = {0, 0};      // frequencies the lane's workspace holds
   std::deque<int64_t> queue;     // requests with unscheduled frequencies
 };
-
-// device bytes of a resident model: value arrays (VK, VM, per-group VK,
-// col_idx, class, arena offsets) + per-row data + its solve workspace
-int64_t model_bytes(const Model& m, int precision, int slots) {
-  const int64_t groups = std::max<int64_t>(1, (int64_t)m.groups.size());
-  int64_t b = m.nnz * (8 + 8 + 8 * (groups - 1) + 4 + 1 + 8) + m.n * 64;
-  return b + workspace_bytes(m, precision, slots);
-}
 
 }  // namespace
 
@@ -76,12 +81,13 @@ struct elp_server {
   elp_server_config cfg;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::vector<ModelSlot> models;
+  std::vector<std::unique_ptr<ModelSlot>> models;
   std::unordered_map<int64_t, Request> reqs;
   std::deque<elp_request_result> done;
   std::vector<std::thread> workers;
   int64_t next_id = 1;
-  int64_t resident = 0;
+  int64_t resident = 0;          // bytes charged against the budget
+  int running = 0;               // batches on the device
   bool stop = false;
   int device = 0;
 
@@ -97,37 +103,134 @@ struct elp_server {
     cv_done.notify_all();
   }
 
-  // picks the idle model whose oldest waiting request arrived first
-  int pick_model() {
+  // fails every unscheduled frequency of model `mi` with `status`
+  void fail_queue(int mi, int status) {
+    ModelSlot& s = *models[mi];
+    while (!s.queue.empty()) {
+      auto it = reqs.find(s.queue.front());
+      s.queue.pop_front();
+      if (it == reqs.end()) continue;
+      Request& r = it->second;
+      r.status = status;
+      r.done += (int)r.omegas.size() - r.next;
+      r.next = (int)r.omegas.size();
+      if (r.done == (int)r.omegas.size()) finish_request(r);
+    }
+  }
+
+  // the model whose oldest waiting request arrived first, with a free lane;
+  // a model being prepared is left to the worker preparing it
+  int pick_model(int& lane) {
     int best = -1;
     Clock::time_point t0 = Clock::time_point::max();
     for (int i = 0; i < (int)models.size(); ++i) {
-      ModelSlot& s = models[i];
-      if (s.busy || s.queue.empty()) continue;
+      ModelSlot& s = *models[i];
+      if (s.queue.empty() || s.preparing) continue;
+      if (!s.ready && s.lanes_busy) continue;
+      int l = 0;
+      while (l < kLanesPerModel && (s.lanes_busy >> l & 1)) ++l;
+      if (l == kLanesPerModel) continue;
       const Request& r = reqs.at(s.queue.front());
-      if (r.arrival < t0) { t0 = r.arrival; best = i; }
+      if (r.arrival < t0) { t0 = r.arrival; best = i; lane = l; }
     }
     return best;
   }
 
-  // makes room for `need` bytes by releasing idle models' workspaces
-  bool admit(int mi, int64_t need) {
-    ModelSlot& s = models[mi];
-    if (s.resident >= need) return true;
-    int64_t extra = need - s.resident;
-    if (extra > cfg.hbm_budget_bytes) return false;
-    for (int i = 0; i < (int)models.size() && resident + extra > cfg.hbm_budget_bytes; ++i) {
-      ModelSlot& o = models[i];
-      if (i == mi || o.busy || o.resident == 0 || !o.queue.empty()) continue;
-      for (auto& w : o.h->m.ws) w.reset();
-      for (auto& lw : o.h->m.ws_b)
-        for (auto& w : lw) w.reset();
-      resident -= o.resident;
-      o.resident = 0;
+  // releases idle models' workspaces (no lane busy, nothing queued) until
+  // `need` more bytes fit; returns whether they do
+  bool make_room(int64_t need, int keep) {
+    for (int i = 0; i < (int)models.size() && resident + need > cfg.hbm_budget_bytes; ++i) {
+      ModelSlot& o = *models[i];
+      if (i == keep || o.lanes_busy || !o.queue.empty()) continue;
+      for (int l = 0; l < kLanesPerModel; ++l) {
+        if (!o.ws_bytes[l]) continue;
+        std::unique_ptr<Workspace>& W = l ? o.h->m.ws_b[cfg.precision][l - 1] : o.h->m.ws[cfg.precision];
+        W.reset();
+        resident -= o.ws_bytes[l];
+        o.ws_bytes[l] = 0;
+        o.ws_slots[l] = 0;
+      }
     }
-    if (resident + extra > cfg.hbm_budget_bytes) return false;
-    resident += extra;
-    s.resident = need;
+    return resident + need <= cfg.hbm_budget_bytes;
+  }
+
+  // frequencies a batch of model `mi` on `lane` may take (<= want), with the
+  // lane's workspace charged for them; 0 when no room is left now
+  int admit_batch(int mi, int lane, int want) {
+    ModelSlot& s = *models[mi];
+    const Model& m = s.h->m;
+    if (s.ws_slots[lane] >= want) return want;  // the lane's workspace already holds them
+    for (int S = want; S >= 1; S = S > 4 ? S / 2 : S - 1) {
+      if (S <= s.ws_slots[lane]) return S;
+      const int64_t bytes = workspace_bytes(m, cfg.precision, S);
+      const int64_t extra = bytes - s.ws_bytes[lane];  // the old workspace is freed before the new one is made
+      if (make_room(extra, mi)) {
+        resident += extra;
+        s.ws_bytes[lane] = bytes;
+        s.ws_slots[lane] = S;
+        return S;
+      }
+    }
+    return 0;
+  }
+
+  // host symbolic phase, admission of the resident arrays, then assembly and
+  // device upload; false when the model failed
+  bool prepare(std::unique_lock<std::mutex>& lk, int mi) {
+    ModelSlot& s = *models[mi];
+    elp_model* h = s.h;
+    s.preparing = true;
+    lk.unlock();
+    int rc;
+    try {
+      rc = model_symbolic_host(h->m);
+    } catch (const std::bad_alloc&) {
+      set_error("host allocation failed");
+      rc = ELP_ERR_NOMEM;
+    } catch (const std::exception& e) {
+      set_error(std::string("exception: ") + e.what());
+      rc = ELP_ERR_ARG;
+    }
+    lk.lock();
+    if (!rc) {
+      const int64_t arrays = model_array_bytes(h->m);
+      const int64_t one = workspace_bytes(h->m, cfg.precision, 1);
+      if (arrays + one > cfg.hbm_budget_bytes || !make_room(arrays, mi)) {
+        rc = ELP_ERR_NOMEM;
+      } else {
+        resident += arrays;
+        s.array_bytes = arrays;
+      }
+    }
+    if (!rc) {
+      // workspaces the model made before it was registered: the server keeps
+      // (and charges) the lanes it uses at its precision and releases the rest
+      Model& m = h->m;
+      for (int prec = 0; prec < 2; ++prec)
+        for (int l = 0; l < 4; ++l) {
+          std::unique_ptr<Workspace>& W = l ? m.ws_b[prec][l - 1] : m.ws[prec];
+          if (!W) continue;
+          if (prec != cfg.precision || l >= kLanesPerModel) { W.reset(); continue; }
+          s.ws_slots[l] = W->slots;
+          s.ws_bytes[l] = workspace_bytes(m, prec, W->slots);
+          resident += s.ws_bytes[l];
+        }
+    }
+    if (!rc) {
+      lk.unlock();
+      if (!h->m.assembled) rc = elp_model_assemble(h);
+      if (!rc) rc = elp_model_analyse(h);
+      lk.lock();
+    }
+    s.preparing = false;
+    if (rc) {
+      if (rc != ELP_ERR_NOMEM)
+        fprintf(stderr, "[elp server] model %d could not be prepared (%d): %s\n", mi, rc, get_error().c_str());
+      s.failed = true;
+      fail_queue(mi, rc);
+      return false;
+    }
+    s.ready = true;
     return true;
   }
 
@@ -135,67 +238,85 @@ struct elp_server {
     cudaSetDevice(device);
     cudaStream_t st;
     cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-    DevBuf<double2> xdev;
-    std::vector<double2> xh;
+    std::unique_lock<std::mutex> lk(mu);
     for (;;) {
-      std::unique_lock<std::mutex> lk(mu);
-      int mi = -1;
-      cv_work.wait(lk, [&] { return stop || (mi = pick_model()) >= 0; });
+      int mi = -1, lane = 0;
+      cv_work.wait(lk, [&] { return stop || (mi = pick_model(lane)) >= 0; });
       if (stop) break;
-      ModelSlot& s = models[mi];
-      s.busy = true;
-      // build the batch: frequencies of waiting requests in arrival order
+      ModelSlot& s = *models[mi];
+      if (s.failed) { fail_queue(mi, ELP_ERR_NOMEM); continue; }
+      if (!s.ready) {
+        if (!prepare(lk, mi)) { cv_work.notify_all(); continue; }
+        if (s.queue.empty() || (s.lanes_busy >> lane & 1)) { cv_work.notify_all(); continue; }
+      }
+      // batch size: waiting frequencies, capped by omega_batch and by the budget
+      int waiting = 0;
+      for (int64_t rid : s.queue) {
+        const Request& r = reqs.at(rid);
+        waiting += (int)r.omegas.size() - r.next;
+        if (waiting >= cfg.omega_batch) break;
+      }
+      const int S = admit_batch(mi, lane, std::min(waiting, cfg.omega_batch));
+      if (S == 0) {
+        if (running == 0) {  // nothing will free memory: the model cannot run at all
+          set_error("model does not fit the HBM budget");
+          fail_queue(mi, ELP_ERR_NOMEM);
+          cv_work.notify_all();
+        } else {
+          cv_work.wait(lk);  // a running batch frees memory when it ends
+        }
+        continue;
+      }
+      s.lanes_busy |= 1 << lane;
+      ++running;
       struct Item { int64_t rid; int k; double w; };
       std::vector<Item> items;
-      while (!s.queue.empty() && (int)items.size() < cfg.omega_batch) {
+      while (!s.queue.empty() && (int)items.size() < S) {
         Request& r = reqs.at(s.queue.front());
-        while (r.next < (int)r.omegas.size() && (int)items.size() < cfg.omega_batch) {
+        while (r.next < (int)r.omegas.size() && (int)items.size() < S) {
           items.push_back({r.id, r.next, r.omegas[r.next]});
           r.next++;
         }
         if (r.next >= (int)r.omegas.size()) s.queue.pop_front();
       }
       Model& m = s.h->m;
-      bool ready = s.ready;
       lk.unlock();
 
-      int rc = ELP_OK;
-      if (!ready) {
-        rc = elp_model_assemble(s.h);
-        if (!rc) rc = elp_model_analyse(s.h);
-      }
-      if (!rc) {
-        lk.lock();
-        s.ready = true;
-        bool ok = admit(mi, model_bytes(m, cfg.precision, cfg.omega_batch));
-        lk.unlock();
-        if (!ok) { rc = ELP_ERR_NOMEM; set_error("model does not fit the HBM budget"); }
-      }
       std::vector<elp_solve_info> info(items.size());
       const int64_t n = m.n;
-      if (!rc) {
-        std::vector<double> oms(items.size());
-        for (size_t i = 0; i < items.size(); ++i) oms[i] = items[i].w;
-        if (xdev.n < (size_t)n * items.size()) {
-          if (xdev.alloc((size_t)n * cfg.omega_batch) != cudaSuccess) rc = ELP_ERR_NOMEM;
-        }
-        if (!rc) {
-          // every batch uses the full slot count so the workspace is shaped once;
-          // one lane: the loop already overlaps up to max_inflight batches, and
-          // lane workspaces per model would double the allocations it admits
-          rc = numeric_solve_batch(m, cfg.precision, oms.data(), (int)oms.size(), nullptr, xdev.p, info.data(),
-                                   cfg.tol, st, 1);
-          if (rc == ELP_ERR_NOCONV) rc = ELP_OK;  // reported per request through its residual
-        }
-        if (!rc || rc == ELP_ERR_NOCONV) {
-          xh.resize((size_t)n * items.size());
-          if (cudaMemcpyAsync(xh.data(), xdev.p, sizeof(double2) * xh.size(), cudaMemcpyDeviceToHost, st) !=
-                  cudaSuccess ||
-              cudaStreamSynchronize(st) != cudaSuccess)
-            rc = ELP_ERR_CUDA;
-        }
+      std::vector<double> oms(items.size());
+      for (size_t i = 0; i < items.size(); ++i) oms[i] = items[i].w;
+      int rc;
+      try {
+        rc = numeric_solve_lane(m, cfg.precision, lane, oms.data(), (int)oms.size(), nullptr, nullptr, info.data(),
+                                cfg.tol, st);
+      } catch (const std::bad_alloc&) {
+        set_error("host allocation failed");
+        rc = ELP_ERR_NOMEM;
+      } catch (const std::exception& e) {
+        set_error(std::string("exception: ") + e.what());
+        rc = ELP_ERR_CUDA;
       }
-      if (rc && rc != ELP_ERR_NOMEM)  // the per-thread error text does not reach the caller's thread
+      // a frequency short of the tolerance is reported per request (status and residual)
+      if (rc == ELP_ERR_NOCONV || rc == ELP_ERR_SINGULAR) rc = ELP_OK;
+      if (!rc) {
+        // solutions straight from the lane's workspace into the requests' buffers
+        const double2* xw = lane_solution(m, cfg.precision, lane);
+        std::vector<double*> dst(items.size(), nullptr);
+        {
+          std::lock_guard<std::mutex> g(mu);
+          for (size_t i = 0; i < items.size(); ++i) {
+            auto it = reqs.find(items[i].rid);
+            if (it != reqs.end()) dst[i] = it->second.x_out + (size_t)items[i].k * 2 * n;
+          }
+        }
+        for (size_t i = 0; i < items.size() && !rc; ++i)
+          if (dst[i] && cudaMemcpyAsync(dst[i], xw + i * n, sizeof(double2) * n, cudaMemcpyDeviceToHost, st) !=
+                            cudaSuccess)
+            rc = ELP_ERR_CUDA;
+        if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = ELP_ERR_CUDA;
+      }
+      if (rc)  // the per-thread error text does not reach the caller's thread
         fprintf(stderr, "[elp server] batch of %zu frequencies on model %d failed (%d): %s\n", items.size(), mi, rc,
                 get_error().c_str());
       lk.lock();
@@ -205,17 +326,18 @@ struct elp_server {
         Request& r = it->second;
         if (rc) r.status = rc;
         else {
-          memcpy(r.x_out + (size_t)items[i].k * 2 * n, xh.data() + i * n, sizeof(double2) * n);
           r.max_res = std::max(r.max_res, info[i].rel_residual);
-          if (!(info[i].rel_residual <= cfg.tol)) r.status = ELP_ERR_NOCONV;
+          if (!(info[i].rel_residual <= cfg.tol) && r.status != ELP_ERR_SINGULAR)
+            r.status = info[i].static_pivots > 0 ? ELP_ERR_SINGULAR : ELP_ERR_NOCONV;
         }
         r.done++;
         if (r.done == (int)r.omegas.size()) finish_request(r);
       }
-      s.busy = false;
-      lk.unlock();
+      s.lanes_busy &= ~(1 << lane);
+      --running;
       cv_work.notify_all();
     }
+    lk.unlock();
     cudaStreamDestroy(st);
   }
 };
@@ -249,11 +371,10 @@ int elp_server_add_model(elp_server* s, elp_model* m, int* model_id) {
   if (!s || !m || !model_id) { set_error("null argument"); return ELP_ERR_ARG; }
   std::lock_guard<std::mutex> lk(s->mu);
   for (auto& ms : s->models)
-    if (ms.h == m) { set_error("model already registered"); return ELP_ERR_ARG; }
-  ModelSlot ms;
-  ms.h = m;
-  ms.ready = m->m.assembled && m->m.analysed;
-  s->models.push_back(ms);
+    if (ms->h == m) { set_error("model already registered"); return ELP_ERR_ARG; }
+  std::unique_ptr<ModelSlot> ms(new ModelSlot());
+  ms->h = m;  // prepared (and charged) by the first worker that picks it up
+  s->models.push_back(std::move(ms));
   *model_id = (int)s->models.size() - 1;
   return ELP_OK;
 }
@@ -272,7 +393,7 @@ int elp_server_submit(elp_server* s, int model_id, const double* omegas, int n_o
   r.x_out = x_out;
   r.arrival = Clock::now();
   s->reqs[r.id] = r;
-  s->models[model_id].queue.push_back(r.id);
+  s->models[model_id]->queue.push_back(r.id);
   if (request_id) *request_id = r.id;
   s->cv_work.notify_one();
   return ELP_OK;

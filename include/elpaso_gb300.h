@@ -190,6 +190,14 @@ typedef struct {
   int n_struct_groups;      /* distinct loss-factor groups of structure K     */
   double gemm_flops;        /* real flops of the Schur (trailing) updates of one factorisation */
   double factor_bytes;      /* bytes of the factors read by one forward+backward sweep, FP32 fronts */
+  int64_t n_nonpositive_jacobians; /* Brick8 / Fluid8 Gauss points with det J <= 0 in the last
+                               assembly: the reference prints a message for each and goes on
+                               (cElementFEM::setupJacobian3D, element/elementfem.cpp:183-188),
+                               so they are counted, not an error; a DSG4 element with
+                               det J <= 0 fails the assembly with ELP_ERR_GEOMETRY as the
+                               reference throws (setupJacobian2D, elementfem.cpp:97-100) */
+  int64_t factor_stored;    /* complex entries of the factors kept per frequency (L and U:
+                               p^2 + 2 p b per front)                                        */
 } elp_model_info;
 
 /* precision of the numeric factorisation */
@@ -305,10 +313,58 @@ int elp_model_time_assembly(elp_model* m, int repeats, double* ms_per_assembly,
  * keeps until the process exits. Larger n_omega is rejected with
  * ELP_ERR_ARG. All calls share that array: calls that overlap on the GPU
  * race on it. The first call on a device looks up the array's device
- * address; make it before any stream capture. */
+ * address; make it before any stream capture. The model must be assembled;
+ * the symbolic phase is not needed. Its launches are not counted or timed
+ * by elp_profile, so it allocates nothing with profiling on either. */
 #define ELP_NOALLOC_MAX_OMEGA 64
 int elp_residual_noalloc(elp_model* m, const double* omegas, int n_omega, const double* f_dev,
                          const double* x_dev, double* r_dev, double* rel_residual_out, void* stream);
+
+/* ---- fault injection for failure-path tests ---------------------------- */
+
+/* No counterpart in the reference. Arms one host-side fault, made on the host
+ * so that no test has to fault the GPU: it fires on the `countdown`-th
+ * matching event after the call (1: the next one), once.
+ *   ELP_FAULT_DEVICE_ALLOC: a device allocation of the library reports an
+ *     allocation failure without calling the allocator (the call in progress
+ *     returns ELP_ERR_NOMEM and leaves the model usable);
+ *   ELP_FAULT_HOST_ALLOC: a host allocation point of model creation or of
+ *     the host symbolic phase throws std::bad_alloc (ELP_ERR_NOMEM);
+ *   ELP_FAULT_TC_WAIT: a packed tensor-core Schur launch runs with its
+ *     producer issuing no copy and every wait bounded at 2^14 polls, so its
+ *     MMA and epilogue waits run out with no copy or MMA in flight; the
+ *     kernel sets its error flag and returns, and the solve returns
+ *     ELP_ERR_CUDA;
+ *   ELP_FAULT_NONE disarms all. */
+#define ELP_FAULT_NONE 0
+#define ELP_FAULT_DEVICE_ALLOC 1
+#define ELP_FAULT_HOST_ALLOC 2
+#define ELP_FAULT_TC_WAIT 3
+int elp_fault_inject(int kind, int countdown);
+
+/* ---- kernel test hook --------------------------------------------------- */
+
+/* No counterpart in the reference. Runs ONE front update of the mixed path's
+ * factorisation on caller-given FP32 complex fronts, so that its tensor-core
+ * arithmetic can be checked against a plain FP64 product. fronts: `slots`
+ * fronts one after another, each m x m column-major (m = p + b), complex
+ * interleaved floats, updated in place; k0 = 32 step:
+ *   ELP_KERNEL_GEMM_COL:   F[k0:m, k0:k0+32] -= F[k0:m, 0:k0] F[0:k0, k0:k0+32]
+ *   ELP_KERNEL_GEMM_ROW:   F[k0:k0+32, k0+32:m] -= F[k0:k0+32, 0:k0] F[0:k0, k0+32:m]
+ *   ELP_KERNEL_GEMM_SCHUR: S = F[p:m, p:m] - F[p:m, 0:p] F[0:p, p:m]; written
+ *     into F, or with `parents` (slots x parent_m^2 complex, same layout) added
+ *     into parent[pmap[i], pmap[j]] instead (the extend-add fused into the
+ *     update), F left as it was;
+ *   ELP_KERNEL_PACKED_SCHUR: S added into the parents through the packed
+ *     operands (split once into TF32 planes, bulk-copied by the MMA kernel).
+ * pmap: b distinct parent positions. Returns ELP_ERR_ARG for inconsistent
+ * sizes. */
+#define ELP_KERNEL_GEMM_COL 0
+#define ELP_KERNEL_GEMM_ROW 1
+#define ELP_KERNEL_GEMM_SCHUR 2
+#define ELP_KERNEL_PACKED_SCHUR 3
+int elp_front_update_test(int kernel, int p, int b, int step, int slots, float* fronts, int parent_m,
+                          const int32_t* pmap, float* parents);
 
 /* ---- launch counting and per-kernel device timing ---------------------- */
 
@@ -331,11 +387,14 @@ int elp_profile_read(double* ms /* [ELP_PROFILE_CLASSES] */, int64_t* launches, 
 typedef struct elp_server elp_server;
 
 typedef struct {
-  int64_t hbm_budget_bytes;  /* admission limit for resident models + work    */
-  int max_inflight;          /* slots: frequency work items on the device     */
+  int64_t hbm_budget_bytes;  /* admission limit for resident models + work:
+                                every model's resident arrays and each
+                                workspace lane, charged before allocation    */
+  int max_inflight;          /* worker threads: batches on the device at once */
   int precision;             /* ELP_FP64_PLAIN / ELP_MIXED                    */
   double tol;                /* relative residual target                      */
-  int omega_batch;           /* frequencies factorised together per launch    */
+  int omega_batch;           /* most frequencies factorised together; a batch
+                                takes fewer when the budget has less room     */
 } elp_server_config;
 
 typedef struct {
@@ -347,7 +406,14 @@ typedef struct {
 } elp_request_result;
 
 int elp_server_create(const elp_server_config* cfg, elp_server** out);
-/* Registers a model (assembled + analysed on first use); returns its slot id. */
+/* Registers a model; returns its slot id. The first worker that picks up
+ * one of its requests charges the model's resident arrays against the budget
+ * (sized on the host, before any device allocation), then assembles and
+ * analyses it if needed; a model whose arrays plus a one-frequency workspace
+ * exceed the budget fails its requests with ELP_ERR_NOMEM. Models may be
+ * added while batches run. Once registered, the model belongs to the server
+ * until the server is destroyed: the caller must not use the handle, and
+ * the server releases workspaces the model made before. */
 int elp_server_add_model(elp_server* s, elp_model* m, int* model_id);
 /* Queues a sweep request. x_out (n_omega x n complex) must stay valid until
  * the result is returned by elp_server_wait. */

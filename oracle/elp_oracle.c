@@ -353,9 +353,12 @@ static int64_t find(const orc_system* s, int32_t r, int32_t c) {
   return -1;
 }
 
-static int add_block(const orc_system* s, double* v, const int32_t* rows, int n, const double* EM) {
+/* keep (may be NULL): rows whose entries are assembled; the others are
+ * skipped (their pattern rows may then be empty) */
+static int add_block(const orc_system* s, const uint8_t* keep, double* v, const int32_t* rows, int n,
+                     const double* EM) {
   for (int i = 0; i < n; ++i) {
-    if (rows[i] < 0) continue;
+    if (rows[i] < 0 || (keep && !keep[rows[i]])) continue;
     for (int j = 0; j < n; ++j) {
       if (rows[j] < 0) continue;
       int64_t q = find(s, rows[i], rows[j]);
@@ -367,7 +370,7 @@ static int add_block(const orc_system* s, double* v, const int32_t* rows, int n,
   return 0;
 }
 
-int orc_assemble(const orc_system* s, double omega, double* v) {
+static int assemble_rows(const orc_system* s, const uint8_t* keep, double omega, double* v) {
   int64_t nnz = s->row_ptr[s->n];
   memset(v, 0, sizeof(double) * 2 * nnz);
   double EM[2 * 576];
@@ -375,17 +378,17 @@ int orc_assemble(const orc_system* s, double omega, double* v) {
   for (int64_t e = 0; e < s->n_brick; ++e) {
     const double* mt = s->brick_mat + 4 * e;
     orc_brick8(s->brick_xyz + 24 * e, mt[0], mt[1], mt[2], mt[3], omega, 0, 0, EM);
-    if ((rc = add_block(s, v, s->brick_rows + 24 * e, 24, EM))) return rc;
+    if ((rc = add_block(s, keep, v, s->brick_rows + 24 * e, 24, EM))) return rc;
   }
   for (int64_t e = 0; e < s->n_plate; ++e) {
     const double* mt = s->plate_mat + 5 * e;
     if (orc_dsg4(s->plate_xyz + 12 * e, mt[0], mt[1], mt[2], mt[3], mt[4], omega, 0, 0, EM)) return 2;
-    if ((rc = add_block(s, v, s->plate_rows + 12 * e, 12, EM))) return rc;
+    if ((rc = add_block(s, keep, v, s->plate_rows + 12 * e, 12, EM))) return rc;
   }
   for (int64_t e = 0; e < s->n_fluid; ++e) {
     const double* mt = s->fluid_mat + 2 * e;
     orc_fluid8(s->fluid_xyz + 24 * e, mt[0], mt[1], omega, 0, 0, EM);
-    if ((rc = add_block(s, v, s->fluid_rows + 8 * e, 8, EM))) return rc;
+    if ((rc = add_block(s, keep, v, s->fluid_rows + 8 * e, 8, EM))) return rc;
   }
   for (int64_t q = 0; q < s->n_iface; ++q) {
     double C[2 * 48];
@@ -397,10 +400,16 @@ int orc_assemble(const orc_system* s, double omega, double* v) {
       for (int c = 0; c < 4; ++c) {
         if (R[12 + c] < 0) continue;
         double val = C[2 * (z * 4 + c)] * f;
-        int64_t q1 = find(s, R[z], R[12 + c]), q2 = find(s, R[12 + c], R[z]);
-        if (q1 < 0 || q2 < 0) return 3;
-        v[2 * q1] += val;
-        v[2 * q2] += val;
+        if (!keep || keep[R[z]]) {
+          int64_t q1 = find(s, R[z], R[12 + c]);
+          if (q1 < 0) return 3;
+          v[2 * q1] += val;
+        }
+        if (!keep || keep[R[12 + c]]) {
+          int64_t q2 = find(s, R[12 + c], R[z]);
+          if (q2 < 0) return 3;
+          v[2 * q2] += val;
+        }
       }
     }
   }
@@ -412,6 +421,12 @@ int orc_assemble(const orc_system* s, double omega, double* v) {
     }
   }
   return 0;
+}
+
+int orc_assemble(const orc_system* s, double omega, double* v) { return assemble_rows(s, NULL, omega, v); }
+
+int orc_assemble_rows(const orc_system* s, const uint8_t* keep, double omega, double* v) {
+  return assemble_rows(s, keep, omega, v);
 }
 
 /* Constitutive matrices with complex E as the visco material builds them

@@ -48,6 +48,10 @@ typedef struct {
 } orc_system;
 
 int orc_assemble(const orc_system* s, double omega, double* values /* 2*nnz */);
+/* The same for the rows with keep[r] != 0 only (the pattern may leave the
+ * other rows empty; the elements passed are those touching kept rows):
+ * A(w) on a sample of rows of a model too large for the full pattern. */
+int orc_assemble_rows(const orc_system* s, const uint8_t* keep, double omega, double* values);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,7 @@ from __future__ import annotations
 import contextlib
 import ctypes
 import os
+import threading
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
@@ -60,6 +61,12 @@ def _blas_libs():
                         found.append((fs, fg))
         _blas_setters = found
     return _blas_setters
+
+
+# BLAS thread counts are process-wide: factorisations that change them run
+# one at a time (values would not change, but interleaved set / restore pairs
+# could leave BLAS oversubscribed or at one thread)
+_FACTOR_LOCK = threading.Lock()
 
 
 @contextlib.contextmanager
@@ -210,14 +217,15 @@ class Multifrontal:
         order (children before parents); the fronts of a level of k >= 2
         fronts are spread over the thread pool, each with 1/k of the BLAS
         threads (only where this process's BLAS thread count can be set;
-        else all run in order)."""
+        else all run in order). Calls from several Python threads run one
+        after another (the BLAS thread count is process-wide)."""
         A = A.tocsr()
         assert np.array_equal(A.indptr, self.indptr) and np.array_equal(A.indices, self.indices)
         data = A.data
         self.F = [None] * len(self.fronts)
         self._cb = {}
         parallel = _THREADS > 1 and bool(_blas_libs())
-        with ThreadPoolExecutor(max_workers=_THREADS) as pool:
+        with _FACTOR_LOCK, ThreadPoolExecutor(max_workers=_THREADS) as pool:
             for group in self.levels:
                 if parallel and len(group) >= 2:
                     with _blas_threads(max(1, _THREADS // len(group))):
@@ -246,6 +254,30 @@ class Multifrontal:
         if m > p:
             self._cb[t] = F[p:, p:] - L21 @ U12
         self.F[t] = (lu, pv, L21, U12)
+
+    def solve_h(self, c):
+        """Solves A^H y = c with the factors of A (for condition estimates).
+        A^-1 = B F with the forward sweep F = G_T..G_1 (G_t: the front's row
+        interchanges, then L11^-1 and the L21 update) and the backward sweep
+        B = B_1..B_T (B_t: U11^-1 after the U12 update); so A^-H = F^H B^H:
+        the adjoint backward steps in elimination order, then the adjoint
+        forward steps in reverse order, each ending with the interchanges
+        scattered back."""
+        y = np.array(c, np.complex128, copy=True)
+        for (piv, bor, _), (lu, perm, L21, U12) in zip(self.fronts, self.F):
+            yp = sla.solve_triangular(lu, y[piv], trans="C", lower=False, check_finite=False)
+            y[piv] = yp
+            if len(bor):
+                y[bor] -= U12.conj().T @ yp
+        for (piv, bor, _), (lu, perm, L21, U12) in zip(reversed(self.fronts), reversed(self.F)):
+            t = y[piv]
+            if len(bor):
+                t = t - L21.conj().T @ y[bor]
+            t = sla.solve_triangular(lu, t, trans="C", lower=True, unit_diagonal=True, check_finite=False)
+            out = np.empty_like(t)
+            out[perm] = t
+            y[piv] = out
+        return y
 
     def solve(self, b):
         y = np.array(b, np.complex128, copy=True)

@@ -58,7 +58,7 @@ def lib():
         if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "elp_oracle.c")):
             build_oracle()
         _lib = C.CDLL(LIB)
-        for f in ("orc_brick8", "orc_dsg4", "orc_fluid8", "orc_interface_mindlin", "orc_assemble"):
+        for f in ("orc_brick8", "orc_dsg4", "orc_fluid8", "orc_interface_mindlin", "orc_assemble", "orc_assemble_rows"):
             getattr(_lib, f).restype = C.c_int
     return _lib
 
@@ -304,63 +304,8 @@ class System:
 
     def values(self, omega):
         """A(w) on the pattern after BC rows (complex128, nnz)."""
-        d = self.d
-        rows = self.rows
-        buf = {}
-
-        def pack(typ):
-            # per element, in block order: node coordinates, material row,
-            # global rows (node-major, then the family's DOFs)
-            xyz, mat, rr = [np.zeros(0)], [np.zeros(0)], [np.zeros(0, np.int32)]
-            ne = 0
-            for btyp, mi, conn in d.blocks:
-                if btyp != typ:
-                    continue
-                conn = np.asarray(conn)
-                m = d.materials[mi]
-                if typ == FLUID8:
-                    mm = [m["c"], m["rho"]]
-                else:
-                    E = e_vis(m, omega)
-                    mm = [E.real, E.imag, m["nu"], m["rho"]] + ([m["t"]] if typ == DSG4 else [])
-                xyz.append(d.coords[conn].reshape(-1))
-                mat.append(np.tile(np.asarray(mm, np.float64), len(conn)))
-                rr.append(rows[conn][:, :, ELEM_DOFS[typ]].reshape(-1))
-                ne += len(conn)
-            a = (np.ascontiguousarray(np.concatenate(xyz), np.float64),
-                 np.ascontiguousarray(np.concatenate(mat), np.float64),
-                 np.ascontiguousarray(np.concatenate(rr), np.int32), ne)
-            buf[typ] = a
-            return a
-        b, p, fl = pack(BRICK8), pack(DSG4), pack(FLUID8)
-        nq = len(self.iface_rows)
-        if nq:
-            ixyz = np.ascontiguousarray(np.concatenate(
-                [d.coords[np.asarray(d.interfaces["fnodes"][q])].reshape(-1) for q in range(nq)]))
-            iori = np.ascontiguousarray(np.asarray(d.interfaces["ori"], np.float64))
-            irows = np.ascontiguousarray(np.asarray(self.iface_rows, np.int32).reshape(-1))
-            itr = np.ascontiguousarray(np.asarray(
-                [1 if rows[d.interfaces["snodes"][q][0], 0] >= 0 else 0 for q in range(nq)], np.int32))
-        else:
-            ixyz = np.zeros(1); iori = np.zeros(1); irows = np.zeros(16, np.int32); itr = np.zeros(1, np.int32)
-        bc = np.ascontiguousarray(np.asarray(self.bc_rows, np.int32)) if self.bc_rows else np.zeros(1, np.int32)
-
-        class S(C.Structure):
-            _fields_ = [("n", C.c_int64), ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p),
-                        ("n_brick", C.c_int64), ("n_plate", C.c_int64), ("n_fluid", C.c_int64), ("n_iface", C.c_int64),
-                        ("brick_xyz", C.c_void_p), ("brick_mat", C.c_void_p), ("brick_rows", C.c_void_p),
-                        ("plate_xyz", C.c_void_p), ("plate_mat", C.c_void_p), ("plate_rows", C.c_void_p),
-                        ("fluid_xyz", C.c_void_p), ("fluid_mat", C.c_void_p), ("fluid_rows", C.c_void_p),
-                        ("iface_xyz", C.c_void_p), ("iface_ori", C.c_void_p), ("iface_rows", C.c_void_p),
-                        ("iface_transform", C.c_void_p), ("n_bc", C.c_int64), ("bc_rows", C.c_void_p)]
-        s = S(self.n, _p(self.row_ptr), _p(self.col_idx), b[3], p[3], fl[3], nq,
-              _p(b[0]), _p(b[1]), _p(b[2]), _p(p[0]), _p(p[1]), _p(p[2]), _p(fl[0]), _p(fl[1]), _p(fl[2]),
-              _p(ixyz), _p(iori), _p(irows), _p(itr), len(self.bc_rows), _p(bc))
-        out = np.zeros(2 * len(self.col_idx))
-        rc = lib().orc_assemble(C.byref(s), _d(omega), _p(out))
-        if rc:
-            raise RuntimeError(f"oracle assembly failed ({rc})")
-        return out.view(np.complex128)
+        return _assemble(self.d, self.rows, self.n, self.row_ptr, self.col_idx, self.d, self.iface_rows,
+                         self.bc_rows, omega, None)
 
     def matrix(self, omega):
         import scipy.sparse as sp
@@ -519,7 +464,189 @@ def dof_nodes(system):
     return out
 
 
+def _assemble(d, rows, n, row_ptr, col_idx, elements, iface_rows, bc_rows, omega, keep):
+    """The oracle's C insertion loop (orc_assemble; orc_assemble_rows with a
+    row mask `keep`) over the element blocks of `elements` (d itself or a
+    ModelSubset of it) and the interface quads of d, on the pattern
+    (row_ptr, col_idx)."""
+    def pack(typ):
+        # per element, in block order: node coordinates, material row,
+        # global rows (node-major, then the family's DOFs)
+        xyz, mat, rr = [np.zeros(0)], [np.zeros(0)], [np.zeros(0, np.int32)]
+        ne = 0
+        for btyp, mi, conn in elements.blocks:
+            if btyp != typ:
+                continue
+            conn = np.asarray(conn)
+            m = d.materials[mi]
+            if typ == FLUID8:
+                mm = [m["c"], m["rho"]]
+            else:
+                E = e_vis(m, omega)
+                mm = [E.real, E.imag, m["nu"], m["rho"]] + ([m["t"]] if typ == DSG4 else [])
+            xyz.append(d.coords[conn].reshape(-1))
+            mat.append(np.tile(np.asarray(mm, np.float64), len(conn)))
+            rr.append(rows[conn][:, :, ELEM_DOFS[typ]].reshape(-1))
+            ne += len(conn)
+        return (np.ascontiguousarray(np.concatenate(xyz), np.float64),
+                np.ascontiguousarray(np.concatenate(mat), np.float64),
+                np.ascontiguousarray(np.concatenate(rr), np.int32), ne)
+    b, p, fl = pack(BRICK8), pack(DSG4), pack(FLUID8)
+    nq = len(iface_rows)
+    if nq:
+        ixyz = np.ascontiguousarray(np.concatenate(
+            [d.coords[np.asarray(d.interfaces["fnodes"][q])].reshape(-1) for q in range(nq)]))
+        iori = np.ascontiguousarray(np.asarray(d.interfaces["ori"], np.float64))
+        irows = np.ascontiguousarray(np.asarray(iface_rows, np.int32).reshape(-1))
+        itr = np.ascontiguousarray(np.asarray(
+            [1 if rows[d.interfaces["snodes"][q][0], 0] >= 0 else 0 for q in range(nq)], np.int32))
+    else:
+        ixyz = np.zeros(1); iori = np.zeros(1); irows = np.zeros(16, np.int32); itr = np.zeros(1, np.int32)
+    bc = np.ascontiguousarray(np.asarray(bc_rows, np.int32)) if len(bc_rows) else np.zeros(1, np.int32)
+    row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+    col_idx = np.ascontiguousarray(col_idx, np.int32)
+
+    class S(C.Structure):
+        _fields_ = [("n", C.c_int64), ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p),
+                    ("n_brick", C.c_int64), ("n_plate", C.c_int64), ("n_fluid", C.c_int64), ("n_iface", C.c_int64),
+                    ("brick_xyz", C.c_void_p), ("brick_mat", C.c_void_p), ("brick_rows", C.c_void_p),
+                    ("plate_xyz", C.c_void_p), ("plate_mat", C.c_void_p), ("plate_rows", C.c_void_p),
+                    ("fluid_xyz", C.c_void_p), ("fluid_mat", C.c_void_p), ("fluid_rows", C.c_void_p),
+                    ("iface_xyz", C.c_void_p), ("iface_ori", C.c_void_p), ("iface_rows", C.c_void_p),
+                    ("iface_transform", C.c_void_p), ("n_bc", C.c_int64), ("bc_rows", C.c_void_p)]
+    s = S(n, _p(row_ptr), _p(col_idx), b[3], p[3], fl[3], nq,
+          _p(b[0]), _p(b[1]), _p(b[2]), _p(p[0]), _p(p[1]), _p(p[2]), _p(fl[0]), _p(fl[1]), _p(fl[2]),
+          _p(ixyz), _p(iori), _p(irows), _p(itr), len(bc_rows), _p(bc))
+    out = np.zeros(2 * len(col_idx))
+    if keep is None:
+        rc = lib().orc_assemble(C.byref(s), _d(omega), _p(out))
+    else:
+        keep = np.ascontiguousarray(keep, np.uint8)
+        rc = lib().orc_assemble_rows(C.byref(s), _p(keep), _d(omega), _p(out))
+    if rc:
+        raise RuntimeError(f"oracle assembly failed ({rc})")
+    return out.view(np.complex128)
+
+
+def numbering(d):
+    """Global rows (N x 21, -1 inactive) and n: the numbering rule of
+    activateDofsAtNodes (elpasoCore/source/analysis/analysis.cpp:475-520) --
+    nodes in ascending id, per node the active DOFs in enum order -- written
+    with array operations for models too large for System's loop."""
+    N = len(d.node_ids)
+    active = np.zeros((N, 21), bool)
+    for typ, _, conn in d.blocks:
+        conn = np.asarray(conn)
+        if len(conn):
+            active[np.ix_(np.unique(conn.reshape(-1)), ELEM_DOFS[typ])] = True
+    order = np.argsort(np.asarray(d.node_ids), kind="stable")
+    act = active[order].reshape(-1)
+    num = np.cumsum(act) - 1
+    rows = -np.ones(N * 21, np.int64)
+    rows[act] = num[act]
+    out = -np.ones((N, 21), np.int64)
+    out[order] = rows.reshape(N, 21)
+    return out, int(act.sum())
+
+
+def _incident(conn, n_nodes):
+    """CSR of node -> elements of one block."""
+    conn = np.asarray(conn)
+    ne, k = conn.shape
+    nodes = conn.reshape(-1)
+    elems = np.repeat(np.arange(ne), k)
+    order = np.argsort(nodes, kind="stable")
+    ptr = np.zeros(n_nodes + 1, np.int64)
+    np.add.at(ptr, nodes + 1, 1)
+    return np.cumsum(ptr), elems[order]
+
+
+def sample_rows(d, sample, omega):
+    """A(w) on a sample of global rows of a model too large for the full
+    pattern (the 100^3 Brick8 cube: 245M nonzeros). For every sampled row i
+    of node v: its pattern is the union of the element blocks of the
+    elements at v (node-major DOFs of their nodes, inactive -1 dropped, the
+    diagonal always in), as getLocalSparsityPattern builds it
+    (analysis.cpp:806-867, insertElementMatrix :1238-1246); its values are
+    the element matrices of exactly those elements added by the oracle's C
+    restatement (orc_assemble_rows), then the Dirichlet rows. Returns
+    (sample sorted, row_ptr over the sample, col_idx, values)."""
+    if d.interfaces is not None and len(d.interfaces["ori"]):
+        raise ValueError("row samples cover element blocks only (no interface quads)")
+    rows, n = numbering(d)
+    N = len(d.node_ids)
+    sample = np.unique(np.asarray(sample, np.int64))
+    node_of = np.empty(n, np.int64)
+    r, _ = np.nonzero(rows >= 0)
+    node_of[rows[rows >= 0]] = r
+    keep = np.zeros(n, np.uint8)
+    keep[sample] = 1
+    snodes = np.unique(node_of[sample])
+    # elements at the sampled nodes, per block
+    picks = []
+    cols = [[] for _ in range(len(sample))]
+    pos = {int(x): k for k, x in enumerate(sample)}
+    for bi, (typ, mi, conn) in enumerate(d.blocks):
+        conn = np.asarray(conn)
+        ptr, el = _incident(conn, N)
+        es = np.unique(np.concatenate([el[ptr[v]:ptr[v + 1]] for v in snodes] or [np.zeros(0, np.int64)]))
+        picks.append(es)
+        for e in es:
+            g = rows[conn[e]][:, ELEM_DOFS[typ]].reshape(-1)
+            g = g[g >= 0]
+            for i in g:
+                k = pos.get(int(i))
+                if k is not None:
+                    cols[k].append(g)
+    row_ptr = np.zeros(n + 1, np.int64)
+    col_list = []
+    for k, i in enumerate(sample):
+        c = np.unique(np.concatenate(cols[k] + [np.array([i])]))
+        col_list.append(c)
+        row_ptr[i + 1] = len(c)
+    row_ptr = np.cumsum(row_ptr).astype(np.int32)
+    col_idx = np.ascontiguousarray(np.concatenate(col_list).astype(np.int32))
+    sub = ModelSubset(d, picks)
+    bc_rows = []
+    if d.fixed is not None:
+        for v, dof in zip(np.asarray(d.fixed["node"]), np.asarray(d.fixed["dof"])):
+            if rows[v, dof] >= 0 and keep[rows[v, dof]]:
+                bc_rows.append(int(rows[v, dof]))
+    vals = _assemble(d, rows, n, row_ptr, col_idx, sub, [], bc_rows, omega, keep)
+    cp = np.concatenate([[0], np.cumsum([len(c) for c in col_list])]).astype(np.int64)
+    return sample, cp, col_idx, vals[np.concatenate([np.arange(row_ptr[i], row_ptr[i + 1]) for i in sample])]
+
+
+class ModelSubset:
+    """The elements `picks[b]` of each block b of a model description."""
+
+    def __init__(self, d, picks):
+        self.blocks = [(typ, mi, np.asarray(conn)[picks[b]]) for b, (typ, mi, conn) in enumerate(d.blocks)]
+
+
 def multifrontal(system, leaf=96):
     """CPU multifrontal LU (oracle/mf.py) analysed on the system's pattern."""
     from oracle.mf import Multifrontal
     return Multifrontal(system.row_ptr, system.col_idx, dof_nodes(system), system.d.coords, leaf=leaf)
+
+
+def free_block_cond1(system, omega, mf):
+    """kappa_1(A_ff) of the free block, estimated with Hager / Higham's
+    1-norm estimator (scipy onenormest; a lower bound, usually exact) from
+    the factors `mf` of the LIFTED matrix (mf.factor(system.lifted(w)[0])
+    done by the caller). The lifted matrix is the free block A_ff plus
+    identity rows and columns for the Dirichlet dofs, so A_ff^-1 v is the
+    free part of A_lifted^-1 applied to v with zero Dirichlet entries."""
+    import scipy.sparse.linalg as sla
+    Aff, idx = system.free_block(omega)
+    n = system.n
+
+    def embed(v):
+        z = np.zeros(n, np.complex128)
+        z[idx] = v
+        return z
+
+    inv = sla.LinearOperator((len(idx), len(idx)), dtype=complex,
+                             matvec=lambda v: mf.solve(embed(np.ravel(v)))[idx],
+                             rmatvec=lambda v: mf.solve_h(embed(np.ravel(v)))[idx])
+    return sla.onenormest(Aff) * sla.onenormest(inv)

@@ -67,7 +67,7 @@ def cases(rng):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("ELPASO_REFERENCE", "/root/reference"))
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={args.ref}"], check=True)
     lib = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libelpref.so"))

@@ -47,7 +47,7 @@ class _Desc:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("ELPASO_REFERENCE", "/root/reference"))
     ap.add_argument("--out", default=os.path.join(HERE, "tutorial_plate_dsg4.npz"))
     args = ap.parse_args()
     h5model = _load("h5model")

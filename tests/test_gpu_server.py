@@ -87,3 +87,53 @@ def test_wait_times_out_without_work(elp):
         srv.wait(50.0)
     assert e.value.code == 8
     srv.close()
+
+
+def test_models_added_while_batches_run(elp, meshes, oracle):
+    """Model slots keep their addresses: models registered while other
+    models' batches run (the slot table grows under the running workers)
+    are served, and every result meets the residual target."""
+    first = elp.Model(meshes.plate_cavity(12, 8, 6, 0.6, 0.4, 0.3))
+    srv = elp.Server(hbm_budget_bytes=16 << 30, max_inflight=2, precision=1, tol=1e-10, omega_batch=8)
+    a = srv.add_model(first)
+    xa = np.zeros((8, first.n), np.complex128)
+    ra = srv.submit(a, 2 * np.pi * np.linspace(20.0, 480.0, 8), xa)
+    later, outs = [], {}
+    for k in range(12):  # registered while model a's batch is in flight
+        d = meshes.plate(6 + k, 5 + k, 0.3, 0.2, 0.002)
+        m = elp.Model(d)
+        mid = srv.add_model(m)
+        later.append((mid, m, d))
+        x = np.zeros((2, m.n), np.complex128)
+        outs[srv.submit(mid, 2 * np.pi * np.array([33.0, 210.0]), x)] = (x, d)
+    got = {}
+    for _ in range(1 + len(later)):
+        r = srv.wait(120000.0)
+        got[r["request_id"]] = r
+    assert all(r["status"] == 0 and r["max_rel_residual"] <= 1e-10 for r in got.values()), got
+    for rid, (x, d) in list(outs.items())[:3]:
+        s = oracle.System(d)
+        A = s.matrix(2 * np.pi * 210.0)
+        assert np.linalg.norm(s.f - A @ x[1]) / np.linalg.norm(s.f) <= 1e-10
+    srv.close()
+
+
+def test_admission_refuses_before_allocating(elp, meshes):
+    """A model whose resident arrays alone exceed the budget is refused
+    before anything is allocated for it: it is never assembled (its system
+    values report ELP_ERR_STATE), and the device's free memory is unchanged."""
+    torch = pytest.importorskip("torch")
+    big = elp.Model(meshes.cube(14))
+    srv = elp.Server(hbm_budget_bytes=4 << 20, max_inflight=1, precision=1, tol=1e-10, omega_batch=4)
+    b = srv.add_model(big)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    x = np.zeros((1, big.n), np.complex128)
+    rid = srv.submit(b, 2 * np.pi * np.array([10.0]), x)
+    r = srv.wait(60000.0)
+    assert r["request_id"] == rid and r["status"] == 3
+    assert torch.cuda.mem_get_info()[0] >= free0 - (2 << 20)  # at most the worker stream's own bookkeeping
+    with pytest.raises(elp.ElpasoError) as e:
+        big.system_values(2 * np.pi * 10.0)
+    assert e.value.code == 7
+    srv.close()

@@ -55,3 +55,32 @@ def test_lifted_system_keeps_pattern_and_solution(elp, meshes, oracle):
     x = s.solve(om, f)
     z = _free_block_solution(s, om, f)
     assert np.linalg.norm(x - z) / np.linalg.norm(z) <= 1e-12
+
+
+def test_multifrontal_adjoint_solve_and_condition_estimate(elp, meshes, oracle):
+    """solve_h (A^H y = c from the factors of A) against dense LAPACK, and the
+    free-block kappa_1 estimate against the dense kappa_1, on a coupled
+    plate-cavity system (fluid, coupling and Dirichlet rows all present)."""
+    s = oracle.System(meshes.plate_cavity(6, 4, 3, 0.3, 0.2, 0.15))
+    om = 2 * np.pi * 120.0
+    A, rhs = s.lifted(om)
+    mf = oracle.multifrontal(s, leaf=24)
+    mf.factor(A)
+    rng = np.random.default_rng(5)
+    c = rng.standard_normal(s.n) + 1j * rng.standard_normal(s.n)
+    Ad = A.toarray()
+    nA = np.linalg.norm(Ad, 2)
+
+    def backward_error(M, z):  # normwise: a wrong solve gives O(1), a stable one O(eps)
+        return np.linalg.norm(M @ z - c) / (nA * np.linalg.norm(z) + np.linalg.norm(c))
+
+    y = mf.solve_h(c)
+    assert backward_error(Ad.conj().T, y) <= 1e-14
+    x = mf.solve(c)
+    assert backward_error(Ad, x) <= 1e-14
+    y_dense = np.linalg.solve(Ad.conj().T, c)
+    assert np.linalg.norm(y - y_dense) / np.linalg.norm(y_dense) <= 1e-15 * np.linalg.cond(Ad)
+    Aff = s.free_block(om)[0].toarray()
+    exact = np.linalg.norm(Aff, 1) * np.linalg.norm(np.linalg.inv(Aff), 1)
+    est = oracle.free_block_cond1(s, om, mf)
+    assert 0.3 * exact <= est <= exact * (1 + 1e-8), (est, exact)

@@ -69,3 +69,36 @@ def test_noalloc_rejects_more_frequencies_than_its_scratch_holds(elp, meshes):
                                   C.c_void_p(buf.data_ptr()), _p(rel), None)
     assert rc == 1
     assert b"ELP_NOALLOC_MAX_OMEGA" in lib.elp_last_error()
+
+
+def test_noalloc_full_scratch_on_an_unanalysed_model(elp, meshes):
+    """ELP_NOALLOC_MAX_OMEGA frequencies at once (every row of the scratch
+    array in use) on a model that is assembled but not analysed (the
+    residual needs only the value arrays): each relative residual of random
+    solutions equals the host's ||f - A x|| / ||f|| with A from
+    elp_model_system_values, on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    import scipy.sparse as sp
+    m = elp.Model(meshes.plate(10, 8, 0.3, 0.2, 0.002)).assemble()
+    n = m.n
+    lib = elp.load_library()
+    S = 64  # ELP_NOALLOC_MAX_OMEGA
+    oms = np.ascontiguousarray(2 * np.pi * np.linspace(5.0, 495.0, S))
+    rng = np.random.default_rng(11)
+    xh = rng.standard_normal((S, n)) + 1j * rng.standard_normal((S, n))
+    fh = np.stack([m.rhs(om) for om in oms]) + 1e-3 * (rng.standard_normal((S, n)) + 1j * rng.standard_normal((S, n)))
+    rp, ci = m.pattern()
+    want = np.empty(S)
+    for k, om in enumerate(oms):
+        A = sp.csr_matrix((m.system_values(om), ci, rp), shape=(n, n))
+        want[k] = np.linalg.norm(fh[k] - A @ xh[k]) / np.linalg.norm(fh[k])
+    f = torch.from_numpy(np.ascontiguousarray(fh).view(np.float64).copy()).cuda()
+    x = torch.from_numpy(np.ascontiguousarray(xh).view(np.float64).copy()).cuda()
+    r = torch.zeros_like(f)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for call in range(2):
+        rel = np.zeros(S)
+        rc = lib.elp_residual_noalloc(m.handle, _p(oms), S, C.c_void_p(f.data_ptr()), C.c_void_p(x.data_ptr()),
+                                      C.c_void_p(r.data_ptr()), _p(rel), stream)
+        assert rc == 0, lib.elp_last_error()
+        assert np.all(np.abs(rel - want) <= 1e-12 * want), (call, np.max(np.abs(rel - want) / want))
