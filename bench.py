@@ -427,7 +427,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     prof = elp.profile_read()
     elp.profile(False)
-    top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    # the tensor-core front updates (Crout and Schur from the fronts, packed
+    # Schur, its pack pass) are one class of work: the factorisation's GEMMs
+    groups = {k: v for k, v in prof.items() if k not in ("gemm_tc", "schur_tc", "pack")}
+    groups["gemm_tc"] = {"ms": sum(prof[k]["ms"] for k in ("gemm_tc", "schur_tc", "pack")),
+                         "launches": sum(prof[k]["launches"] for k in ("gemm_tc", "schur_tc", "pack"))}
+    top = max(groups.items(), key=lambda kv: kv[1]["ms"])
     hbm, bf16, src = peaks()
     roof = None
     if top[0] == "gemm" or top[0] == "gemm_tc":

@@ -111,7 +111,8 @@ class _Info(C.Structure):
     _fields_ = [("n_dofs", C.c_int64), ("nnz", C.c_int64), ("n_elements", C.c_int64), ("n_fronts", C.c_int64),
                 ("factor_entries", C.c_int64), ("factor_flops", C.c_double), ("n_levels", C.c_int),
                 ("max_front", C.c_int), ("n_struct_groups", C.c_int), ("gemm_flops", C.c_double),
-                ("factor_bytes", C.c_double), ("n_nonpositive_jacobians", C.c_int64), ("factor_stored", C.c_int64)]
+                ("factor_bytes", C.c_double), ("n_nonpositive_jacobians", C.c_int64), ("factor_stored", C.c_int64),
+                ("front_pool_peak", C.c_int64), ("front_pool", C.c_int64)]
 
 
 class SolveInfo(C.Structure):
@@ -145,7 +146,7 @@ EXPORTS = [
 ]
 KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
                   "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc", "spmv", "fwd_border",
-                  "bwd_u12", "krylov"]
+                  "bwd_u12", "krylov", "schur_tc", "pack"]
 
 _lib = None
 
@@ -413,6 +414,9 @@ class Model:
               raise_on_noconv: bool = True, out: np.ndarray | None = None):
         """Solves A(w) u = f for each angular frequency; returns (x[n_omega, n], infos).
 
+        raise_on_noconv=False returns the solutions and infos when some
+        frequency missed the tolerance (status 6) or hit zero pivots (5).
+
         f and out may be host buffers the caller owns (pinned ones copy at
         full link speed); out must be C-contiguous complex128 [n_omega, n]."""
         om = np.ascontiguousarray(np.atleast_1d(omegas), dtype=np.float64)
@@ -430,7 +434,9 @@ class Model:
             fp = _ptr(f)
         rc = self.lib.elp_solve(self.handle, _ptr(om), len(om), int(precision), fp, _ptr(x),
                                 C.cast(infos, C.c_void_p), float(tol))
-        if rc != 0 and (rc != 6 or raise_on_noconv):
+        # 6: a frequency short of the tolerance; 5: the same with zero pivots
+        # (singular); both still return every solution and info
+        if rc != 0 and (rc not in (5, 6) or raise_on_noconv):
             _check(rc)
         return x, [infos[i].as_dict() for i in range(len(om))]
 

@@ -161,9 +161,9 @@ int elp_model_get_info(const elp_model* h, elp_model_info* info) {
     info->factor_bytes = m.sym->factor_bytes;
     info->n_levels = m.sym->n_levels;
     info->max_front = m.sym->max_front;
-    int64_t stored = 0;
-    for (const FrontInfo& F : m.sym->fronts) stored += (int64_t)F.p * F.p + 2 * (int64_t)F.p * F.b;
-    info->factor_stored = stored;
+    info->factor_stored = m.sym->factor_stored;
+    info->front_pool_peak = m.sym->pool_peak;
+    info->front_pool = m.sym->pool;
   }
   if (m.dev) info->n_nonpositive_jacobians = m.dev->bad_jacobians_3d;
   return ELP_OK;

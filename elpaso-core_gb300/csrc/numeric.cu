@@ -105,33 +105,68 @@ __global__ void k_values(CombineArgs A, const Coef* __restrict__ coef, double2* 
     out[q] = combine(A, c, q);
 }
 
+// Full fronts starting at a level: zeroed in the front pool (their region
+// may have held fronts that ended at an earlier level).
 template <class V>
-__global__ void k_scatter(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ row_ptr,
-                          const int32_t* __restrict__ col_idx, const int64_t* __restrict__ entry_off,
-                          const double* __restrict__ dscale, int64_t n, V* __restrict__ arena,
-                          int64_t arena_size, unsigned long long* __restrict__ stats) {
+__global__ void k_zero_fronts(const int32_t* __restrict__ list, const int32_t* __restrict__ fp,
+                              const int32_t* __restrict__ fb, const int64_t* __restrict__ foff,
+                              V* __restrict__ pool, int64_t pool_size) {
+  const int f = list[blockIdx.x];
+  const int64_t m = (int64_t)fp[f] + fb[f], mm = m * m;
+  V* F = pool + blockIdx.y * pool_size + foff[f];
+  const V z = cmk<V>(0.0, 0.0);
+  for (int64_t t = blockIdx.z * (int64_t)blockDim.x + threadIdx.x; t < mm; t += (int64_t)gridDim.z * blockDim.x)
+    F[t] = z;
+}
+
+// A(w) entries owned by the fronts starting at a level, scaled by D on both
+// sides, written into those fronts (every entry has one owner slot; entries
+// in Dirichlet columns stay zero: the solve lifts them to the right-hand side)
+template <class V>
+__global__ void k_scatter(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ order,
+                          int64_t count, const int32_t* __restrict__ entry_row, const int32_t* __restrict__ col_idx,
+                          const int64_t* __restrict__ entry_off, const double* __restrict__ dscale, int64_t n,
+                          V* __restrict__ pool, int64_t pool_size, unsigned long long* __restrict__ stats) {
   const int s = blockIdx.y;
   const Coef c = coef[s];
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const double* d = dscale + s * n;
-  V* F = arena + s * arena_size;
+  V* F = pool + s * pool_size;
   double amax = 0.0;
-  for (int64_t i = warp; i < n; i += nwarps) {
-    const double di = d[i];
-    for (int q = row_ptr[i] + lane; q < row_ptr[i + 1]; q += 32) {
-      if (A.cls[q] & CLS_BC_COLUMN) continue;  // lifted to the right-hand side by the solve
-      double2 v = combine(A, c, q);
-      double sc = di * d[col_idx[q]];
-      v.x *= sc;
-      v.y *= sc;
-      amax = fmax(amax, sqrt(v.x * v.x + v.y * v.y));
-      F[entry_off[q]] = cmk<V>(v.x, v.y);
-    }
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t q = order[t];
+    if (A.cls[q] & CLS_BC_COLUMN) continue;
+    double2 v = combine(A, c, q);
+    const double sc = d[entry_row[q]] * d[col_idx[q]];
+    v.x *= sc;
+    v.y *= sc;
+    amax = fmax(amax, sqrt(v.x * v.x + v.y * v.y));
+    F[entry_off[q]] = cmk<V>(v.x, v.y);
   }
   for (int o = 16; o; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-  if (lane == 0) atomicMax(stats + 4 * s + 3, (unsigned long long)__double_as_longlong(amax));
+  if ((threadIdx.x & 31) == 0) atomicMax(stats + 4 * s + 3, (unsigned long long)__double_as_longlong(amax));
+}
+
+// Factors of a level's fronts copied from the front pool into the factor
+// store once the level is done: the m x p panel (contiguous, ld m) and U12
+// (rows 0..p-1 of columns p..m-1) repacked with ld p.
+template <class V>
+__global__ void k_compact(const int32_t* __restrict__ list, const int32_t* __restrict__ fp,
+                          const int32_t* __restrict__ fb, const int64_t* __restrict__ foff,
+                          const int64_t* __restrict__ ffac, const V* __restrict__ pool, int64_t pool_size,
+                          V* __restrict__ fac, int64_t fac_size) {
+  const int f = list[blockIdx.x];
+  const int64_t p = fp[f], b = fb[f], m = p + b;
+  const V* src = pool + blockIdx.y * pool_size + foff[f];
+  V* dst = fac + blockIdx.y * fac_size + ffac[f];
+  const int64_t np = p * m, total = np + p * b;
+  for (int64_t t = blockIdx.z * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.z * blockDim.x) {
+    if (t < np) {
+      dst[t] = src[t];
+    } else {
+      const int64_t u = t - np, i = u / p, r = u - i * p;
+      dst[t] = src[(p + i) * m + r];
+    }
+  }
 }
 
 // ------------------------------------------------------------- panel
@@ -809,17 +844,17 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   const int r = blockIdx.z * 32 + lane;
   V t = cmk<V>(0.0, 0.0);
   if (r < p) {
-    const V* row = F + (int64_t)p * m + r;
+    const V* row = F + (int64_t)p * m + r;  // U12 in the factor store: after the panel, ld p
     const int i_lo = (b * wv) / 8, i_hi = (b * (wv + 1)) / 8;
     int i = i_lo;
     for (; i + 16 <= i_hi; i += 16) {  // 16 independent loads in flight per thread
       V a[16];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) a[q] = row[(int64_t)(i + q) * m];
+      for (int q = 0; q < 16; ++q) a[q] = row[(int64_t)(i + q) * p];
 #pragma unroll
       for (int q = 0; q < 16; ++q) t = cfma(a[q], xb[i + q], t);
     }
-    for (; i < i_hi; ++i) t = cfma(row[(int64_t)i * m], xb[i], t);
+    for (; i < i_hi; ++i) t = cfma(row[(int64_t)i * p], xb[i], t);
   }
   part[wv][lane] = t;
   __syncthreads();
@@ -1227,12 +1262,19 @@ int device_upload_symbolic(Model& m) {
   ELP_CUDA(D.f_cb_off.upload(co));
   ELP_CUDA(D.f_piv_off.upload(po));
   ELP_CUDA(D.f_off.upload(off));
+  {
+    std::vector<int64_t> fo(T);
+    for (int t = 0; t < T; ++t) fo[t] = S.fronts[t].fac_off;
+    ELP_CUDA(D.f_fac.upload(fo));
+  }
+  ELP_CUDA(D.scatter_order.upload(S.scatter_order));
+  ELP_CUDA(D.entry_row.upload(S.entry_row));
   ELP_CUDA(D.front_dofs.upload(S.front_dofs));
   ELP_CUDA(D.parent_map.upload(S.parent_map));
   ELP_CUDA(D.child_ptr.upload(cptr));
   ELP_CUDA(D.child_list.upload(clist));
   ELP_CUDA(D.entry_off.upload(S.entry_off));
-  std::vector<int32_t> ll, ea;
+  std::vector<int32_t> ll, ea, nl;
   D.levels.assign(S.n_levels, DeviceSymbolic::Level());
   int maxc = std::max(1, S.max_children);
   for (int l = 0; l < S.n_levels; ++l) {
@@ -1244,7 +1286,16 @@ int device_upload_symbolic(Model& m) {
       L.max_p = std::max(L.max_p, p[t]);
       L.max_b = std::max(L.max_b, b[t]);
       L.max_m = std::max(L.max_m, p[t] + b[t]);
+      L.fac_max = std::max<int64_t>(L.fac_max, (int64_t)p[t] * p[t] + 2 * (int64_t)p[t] * b[t]);
     }
+    L.new_start = (int)nl.size();
+    L.new_count = (int)S.level_new[l].size();
+    for (int t : S.level_new[l]) {
+      nl.push_back(t);
+      L.new_max_m2 = std::max<int64_t>(L.new_max_m2, (int64_t)(p[t] + b[t]) * (p[t] + b[t]));
+    }
+    L.ent_start = S.level_entry_start[l];
+    L.ent_count = S.level_entry_start[l + 1] - S.level_entry_start[l];
     L.ea_start.assign(maxc, 0);
     L.ea_count.assign(maxc, 0);
     for (int k = 0; k < maxc; ++k) {
@@ -1276,10 +1327,12 @@ int device_upload_symbolic(Model& m) {
   }
   D.pack_max = workspace_plan(S).pack_max;
   ELP_CUDA(D.pack_base.upload(pbase));
+  ELP_CUDA(D.new_list.upload(nl));
   ELP_CUDA(D.level_list.upload(ll));
   ELP_CUDA(D.ea_list.upload(ea));
   D.n_fronts = T;
-  D.arena = S.arena;
+  D.arena = S.pool;
+  D.fac = S.factor_stored;
   D.cb_total = S.cb_total;
   D.max_front = S.max_front;
   return ELP_OK;
@@ -1322,7 +1375,8 @@ constexpr int kGmresRestart = 24;  // GMRES(24) of the mixed path
 
 WorkspacePlan workspace_plan(const Symbolic& S) {
   WorkspacePlan P;
-  P.arena = S.arena;
+  P.arena = S.pool;
+  P.fac = S.factor_stored;
   P.cb_total = S.cb_total;
   static const bool pack_all_levels = getenv("ELP_TC_PACK") && std::string(getenv("ELP_TC_PACK")) == "all";
   for (int l = 0; l < S.n_levels; ++l) {
@@ -1354,7 +1408,7 @@ int64_t workspace_bytes(const Model& m, int precision, int slots) {
   const int64_t elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
   const int64_t nparts = std::min<int64_t>(1024, (n + 255) / 256);
   const int64_t max_count = D.max_count;
-  int64_t b = S * (D.arena + std::max<int64_t>(1, D.cb_total) + 2 * n) * elem;  // arena, cb, z, tb
+  int64_t b = S * (D.arena + D.fac + std::max<int64_t>(1, D.cb_total) + 2 * n) * elem;  // pool, factors, cb, z, tb
   b += S * n * (4 + 8 + 3 * 16);                                               // perm, dscale, x, r, f
   b += S * (int64_t)(sizeof(Coef) + 16 + nparts * 16 + 4 + 32) + 4;            // coef, norms, partials, flags
   b += max_count * S * swapmap_ints<32>() * 4;
@@ -1395,9 +1449,10 @@ static int workspace_alloc(Model& m, Workspace& w, int precision, int slots) {
   const DeviceSymbolic& D = *m.dsym;
   const int64_t n = m.n;
   cudaError_t e = w.arena.alloc((size_t)slots * D.arena * w.elem);
+  if (e == cudaSuccess) e = w.fac.alloc((size_t)slots * D.fac * w.elem);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    set_error("front arena does not fit in device memory");
+    set_error("front pool and factor store do not fit in device memory");
     return ELP_ERR_NOMEM;
   }
   ELP_CUDA(w.cb.alloc((size_t)slots * std::max<int64_t>(1, D.cb_total) * w.elem));
@@ -1489,13 +1544,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 4096), S_used);
     PROF_LAUNCH(KC_DSCALE, st, k_dscale<<<g, 256, 0, st>>>(A, w.coef.p, G.diag_idx.p, n, w.dscale.p));
   }
-  ELP_CUDA(cudaMemsetAsync(w.arena.p, 0, (size_t)S_used * D.arena * sizeof(V), st));
-  {
-    dim3 g((unsigned)std::min<int64_t>((n + 7) / 8, 8192), S_used);
-    PROF_LAUNCH(KC_SCATTER, st, k_scatter<V><<<g, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, D.entry_off.p, w.dscale.p, n, arena,
-                                    D.arena, w.stats.p));
-  }
-  ELP_CUDA(cudaGetLastError());
+  V* fac = reinterpret_cast<V*>(w.fac.p);
   LevelArgs L;
   L.fp = D.f_p.p;
   L.fb = D.f_b.p;
@@ -1560,6 +1609,19 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   };
   for (size_t l = 0; l < D.levels.size(); ++l) {
     const auto& LV = D.levels[l];
+    prof_set_level((int)l);
+    if (LV.new_count > 0) {  // full fronts starting here: zeroed, then their entries of A(w) written
+      dim3 gz(LV.new_count, S_used, (unsigned)std::min<int64_t>(65535, (LV.new_max_m2 + 2047) / 2048));
+      PROF_LAUNCH(KC_SCATTER, st, k_zero_fronts<V><<<gz, 256, 0, st>>>(D.new_list.p + LV.new_start, D.f_p.p, D.f_b.p,
+                                                                        D.f_off.p, arena, D.arena));
+    }
+    if (LV.ent_count > 0) {
+      dim3 gs((unsigned)std::min<int64_t>((LV.ent_count + 255) / 256, 8192), S_used);
+      PROF_LAUNCH(KC_SCATTER, st, k_scatter<V><<<gs, 256, 0, st>>>(A, w.coef.p, D.scatter_order.p + LV.ent_start,
+                                                                    LV.ent_count, D.entry_row.p, G.col_idx.p,
+                                                                    D.entry_off.p, w.dscale.p, n, arena, D.arena,
+                                                                    w.stats.p));
+    }
     L.list = D.level_list.p + LV.start;
     L.count = LV.count;
     const int steps = (LV.max_p + NB - 1) / NB;
@@ -1602,7 +1664,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       uint32_t* pk = reinterpret_cast<uint32_t*>(w.pack.p);
       if (packed) {
         dim3 gp(LV.count, S_used, (unsigned)LV.pack_blocks);
-        PROF_LAUNCH(KC_GEMM_TC, st, k_pack_schur<NB><<<gp, 256, 0, st>>>(L, fa, pk, D.pack_base.p, LV.pack_bytes));
+        PROF_LAUNCH(KC_PACK, st, k_pack_schur<NB><<<gp, 256, 0, st>>>(L, fa, pk, D.pack_base.p, LV.pack_bytes));
       }
       LevelArgs Lc = L;
       Lc.fuse = 1;
@@ -1617,7 +1679,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
           const int64_t gz = std::min<int64_t>(LV.schur_tiles, std::max<int64_t>(1, (2 * num_sms() + pairs - 1) / pairs));
           dim3 gs(Lc.count, S_used, (unsigned)gz);
           const int fault = fault_tc_wait() ? 1 : 0;  // host-side test switch (elp_fault_inject)
-          PROF_LAUNCH(KC_GEMM_TC, st, k_schur_tc<NB><<<gs, kSchurThreads, kSchurSmemBytes, st>>>(
+          PROF_LAUNCH(KC_SCHUR_TC, st, k_schur_tc<NB><<<gs, kSchurThreads, kSchurSmemBytes, st>>>(
                                           Lc, fa, pk, D.pack_base.p, LV.pack_bytes, w.tc_err.p, fault));
         } else {
           gemm(GM_SCHUR, 0, LV.ea_max_b, LV.ea_max_b, Lc);
@@ -1635,7 +1697,13 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
                                                                            D.parent_map.p, arena, D.arena));
       }
     }
+    {  // the level's factors into the factor store; its full fronts are dead from here
+      dim3 gc(LV.count, S_used, (unsigned)std::min<int64_t>(65535, (LV.fac_max + 2047) / 2048));
+      PROF_LAUNCH(KC_SCATTER, st, k_compact<V><<<gc, 256, 0, st>>>(L.list, D.f_p.p, D.f_b.p, D.f_off.p, D.f_fac.p,
+                                                                    arena, D.arena, fac, D.fac));
+    }
   }
+  prof_set_level(-1);
   ELP_CUDA(cudaGetLastError());
   return ELP_OK;
 }
@@ -1658,18 +1726,19 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
   S.piv_off = D.f_piv_off.p;
   S.child_ptr = D.child_ptr.p;
   S.child_list = D.child_list.p;
-  S.foff = D.f_off.p;
+  S.foff = D.f_fac.p;  // the sweeps read the factor store (U12 with ld p, k_bwd_u12)
   S.dofs = D.front_dofs.p;
   S.pmap = D.parent_map.p;
-  S.arena_size = D.arena;
+  S.arena_size = D.fac;
   S.n = m.n;
   S.cb_total = std::max<int64_t>(1, D.cb_total);
   S.active = mask;
-  const V* arena = reinterpret_cast<const V*>(w.arena.p);
+  const V* arena = reinterpret_cast<const V*>(w.fac.p);
   V* z = reinterpret_cast<V*>(w.z.p);
   V* cb = reinterpret_cast<V*>(w.cb.p);
   for (size_t l = 0; l < D.levels.size(); ++l) {
     const auto& LV = D.levels[l];
+    prof_set_level(32 + (int)l);  // solve sweeps: levels 32.. in the per-level table
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
     size_t sm = (size_t)(LV.max_m + LV.max_p) * sizeof(V);  // front vector + permutation buffer
@@ -1683,6 +1752,7 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
   V* tb = reinterpret_cast<V*>(w.tb.p);
   for (int l = (int)D.levels.size() - 1; l >= 0; --l) {
     const auto& LV = D.levels[l];
+    prof_set_level(32 + l);
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
     const unsigned chunks = (unsigned)((LV.max_p + 31) / 32);
@@ -1691,6 +1761,7 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     size_t sm = (size_t)LV.max_p * sizeof(V);
     PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, z, tb));
   }
+  prof_set_level(-1);
   ELP_CUDA(cudaGetLastError());
   return ELP_OK;
 }
@@ -2091,8 +2162,8 @@ int64_t model_array_bytes(const Model& m) {
   b += (int64_t)m.interfaces.size() * (16 * 4 + 8 + 4 * 4);
   if (m.sym) {  // symbolic maps: per-entry arena offsets, front lists, extend-add maps
     const Symbolic& S = *m.sym;
-    b += (int64_t)S.entry_off.size() * 8 + (int64_t)S.front_dofs.size() * 4 + (int64_t)S.parent_map.size() * 4;
-    b += (int64_t)S.fronts.size() * (8 * 4 + 8 + 8 + 4 * 4);
+    b += (int64_t)S.entry_off.size() * (8 + 4 + 4) + (int64_t)S.front_dofs.size() * 4 + (int64_t)S.parent_map.size() * 4;
+    b += (int64_t)S.fronts.size() * (8 * 4 + 8 + 8 + 8 + 4 * 4);
   }
   return b;
 }

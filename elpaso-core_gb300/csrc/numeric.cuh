@@ -117,7 +117,11 @@ __device__ __forceinline__ double dd_residual(double f, const DD& a) {
 
 struct DeviceSymbolic {
   DevBuf<int32_t> f_p, f_b, f_parent, f_idx_off, f_map_off, f_cb_off, f_piv_off;
-  DevBuf<int64_t> f_off;
+  DevBuf<int64_t> f_off;          // per front: offset of its full m x m front in the front pool
+  DevBuf<int64_t> f_fac;          // per front: offset of its factors in the factor store
+  DevBuf<int32_t> new_list;       // per level: fronts whose full front starts there (zeroed, scattered)
+  DevBuf<int32_t> scatter_order;  // CSR entries by the start level of their owner front
+  DevBuf<int32_t> entry_row;      // per CSR entry: its row
   DevBuf<int32_t> front_dofs, parent_map, child_ptr, child_list;
   DevBuf<int64_t> entry_off;
   DevBuf<int32_t> level_list;     // fronts grouped by level
@@ -130,10 +134,15 @@ struct DeviceSymbolic {
     int64_t pack_bytes = 0;   // packed Schur operands of the level, per frequency slot
     int pack_blocks = 0;      // most packed blocks of one front of the level
     int schur_tiles = 0;      // most 128 x 128 Schur tiles of one front of the level
+    int new_start = 0, new_count = 0;   // fronts starting at this level (in new_list)
+    int64_t new_max_m2 = 0;             // their largest m^2
+    int64_t ent_start = 0, ent_count = 0;  // their CSR entries (in scatter_order)
+    int64_t fac_max = 0;                // largest p^2 + 2 p b of the level's fronts
   };
   std::vector<Level> levels;
   int n_fronts = 0;
-  int64_t arena = 0, cb_total = 0;
+  int64_t arena = 0, cb_total = 0;  // arena: entries of the front pool per frequency
+  int64_t fac = 0;                  // entries of the factor store per frequency
   int max_front = 0;
   DevBuf<int64_t> pack_base;      // per front: byte offset of its packed Schur operands within its level
   int64_t pack_max = 0;           // largest pack_bytes of a level that uses the packed Schur update
@@ -154,7 +163,8 @@ struct Workspace {
   int precision = 0;              // ELP_FP64_PLAIN / ELP_MIXED
   int slots = 0;                  // capacity in frequencies
   size_t elem = 0;                // bytes of one complex front entry
-  DevBuf<char> arena;             // slots x arena complex entries
+  DevBuf<char> arena;             // slots x front pool: full fronts while they are factorised
+  DevBuf<char> fac;               // slots x factor store: L and U of every front, for the solves
   DevBuf<char> cb;                // slots x cb_total complex (solve contributions)
   DevBuf<char> z;                 // slots x n complex (solve vector, front precision)
   DevBuf<char> tb;                // slots x n complex (backward pivot-row buffer)
@@ -192,7 +202,7 @@ struct Workspace {
 
 // Sizes a workspace depends on, from the host symbolic phase alone.
 struct WorkspacePlan {
-  int64_t arena = 0, cb_total = 0, max_count = 1, pack_max = 0;
+  int64_t arena = 0, fac = 0, cb_total = 0, max_count = 1, pack_max = 0;  // arena: the front pool
 };
 WorkspacePlan workspace_plan(const Symbolic& S);
 

@@ -1,4 +1,6 @@
 // Launch counting and per-kernel-class device timing (see prof.cuh).
+#include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -11,7 +13,15 @@ namespace {
 struct Pending {
   cudaEvent_t a, b;
   int cls;
+  int level;
 };
+constexpr int kMaxLevels = 64;
+thread_local int t_level = -1;
+double g_level_ms[kMaxLevels][KC_COUNT];
+bool levels_on() {
+  static const bool v = getenv("ELP_PROF_LEVELS") != nullptr;
+  return v;
+}
 std::atomic<int64_t> g_count[KC_COUNT];
 std::atomic<bool> g_on{false};
 std::mutex g_mu;
@@ -33,11 +43,12 @@ cudaEvent_t take_event() {
 }  // namespace
 
 void prof_count(int cls) { g_count[cls].fetch_add(1, std::memory_order_relaxed); }
+void prof_set_level(int level) { t_level = levels_on() ? level : -1; }
 bool prof_on() { return g_on.load(std::memory_order_relaxed); }
 
 void prof_begin(cudaStream_t s, int cls, void** token) {
   std::lock_guard<std::mutex> lk(g_mu);
-  Pending* p = new Pending{take_event(), take_event(), cls};
+  Pending* p = new Pending{take_event(), take_event(), cls, t_level};
   cudaEventRecord(p->a, s);
   *token = p;
 }
@@ -58,6 +69,7 @@ void prof_resolve() {
     if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
       g_ms[p.cls] += ms;
       g_timed[p.cls] += 1;
+      if (p.level >= 0 && p.level < kMaxLevels) g_level_ms[p.level][p.cls] += ms;
     }
     g_pool.push_back(p.a);
     g_pool.push_back(p.b);
@@ -79,6 +91,8 @@ int elp_profile(int enable) {
     g_ms[i] = 0.0;
     g_timed[i] = 0;
   }
+  for (int l = 0; l < kMaxLevels; ++l)
+    for (int i = 0; i < KC_COUNT; ++i) g_level_ms[l][i] = 0.0;
   g_on.store(enable != 0);
   return ELP_OK;
 }
@@ -92,6 +106,17 @@ int elp_profile_read(double* ms, int64_t* launches, int64_t* timed, int* n_class
     if (timed) timed[i] = g_timed[i];
   }
   if (n_classes) *n_classes = KC_COUNT;
+  if (levels_on()) {
+    for (int l = 0; l < kMaxLevels; ++l) {
+      double tot = 0.0;
+      for (int i = 0; i < KC_COUNT; ++i) tot += g_level_ms[l][i];
+      if (tot == 0.0) continue;
+      fprintf(stderr, "[elp levels] level %2d total %8.3f ms:", l, tot);
+      for (int i = 0; i < KC_COUNT; ++i)
+        if (g_level_ms[l][i] > 0.0) fprintf(stderr, " c%d=%.3f", i, g_level_ms[l][i]);
+      fprintf(stderr, "\n");
+    }
+  }
   return ELP_OK;
 }
 

@@ -16,7 +16,7 @@ namespace elp {
 enum KernelClass {
   KC_ASSEMBLE = 0, KC_DSCALE, KC_SCATTER, KC_PANEL, KC_BORDER, KC_UROW, KC_GEMM, KC_EXTEND_ADD,
   KC_FORWARD, KC_BACKWARD, KC_RESIDUAL, KC_NORMS, KC_RHS, KC_UPDATE, KC_VALUES, KC_GEMM_TC,
-  KC_SPMV, KC_FWD_BORDER, KC_BWD_U12, KC_KRYLOV,
+  KC_SPMV, KC_FWD_BORDER, KC_BWD_U12, KC_KRYLOV, KC_SCHUR_TC, KC_PACK,
   KC_COUNT
 };
 
@@ -25,6 +25,10 @@ bool prof_on();
 void prof_begin(cudaStream_t s, int cls, void** token);
 void prof_end(cudaStream_t s, void* token);
 void prof_resolve();
+// Tree level the calling thread's next launches belong to (-1: none). With
+// ELP_PROF_LEVELS set and profiling on, prof_resolve also sums the device
+// time per (level, class) and elp_profile_read prints that table to stderr.
+void prof_set_level(int level);
 
 struct ProfScope {
   void* tok = nullptr;

@@ -14,7 +14,7 @@
 //  3. fronts in postorder; front s holds its pivots (the separator's DOFs)
 //     followed by its border: every later-eliminated DOF adjacent to a pivot
 //     or in a child's border, sorted by elimination position;
-//  4. per CSR entry, the arena offset of its slot in the front that owns it
+//  4. per CSR entry, the pool offset of its slot in the front that owns it
 //     (the front of whichever of row/column is eliminated first);
 //  5. per border DOF, its position in the parent front (extend-add map).
 #include "symbolic.hpp"
@@ -240,7 +240,6 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
     F.b = b;
     F.piv_off = piv;
     piv += p;
-    F.off = arena;
     const int64_t mm = (int64_t)p + b;
     arena += mm * mm;
     F.cb_off = (int32_t)cbt;
@@ -308,6 +307,7 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
   std::vector<int32_t> list_pos(S.front_dofs.size());
   for (size_t k = 0; k < S.front_dofs.size(); ++k) list_pos[k] = dof_pos[S.front_dofs[k]];
   S.entry_off.assign(nnz, -1);
+  std::vector<int32_t> entry_owner(nnz, -1);
   int outside = 0;
 #pragma omp parallel for schedule(dynamic, 1024) reduction(| : outside)
   for (int64_t r = 0; r < n; ++r) {
@@ -326,7 +326,8 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
       }
       const int32_t loc_first = first - F.piv_off;
       const int32_t lr = pr == first ? loc_first : loc_later, lc = pr == first ? loc_later : loc_first;
-      S.entry_off[q] = F.off + (int64_t)lc * (F.p + F.b) + lr;
+      S.entry_off[q] = (int64_t)lc * (F.p + F.b) + lr;  // local: the front's pool offset is added below
+      entry_owner[q] = front_of_pos[first];
     }
   }
   if (outside) { set_error("entry outside its owner front"); return ELP_ERR_ARG; }
@@ -337,6 +338,118 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
   S.n_levels = L;
   S.level_fronts.assign(L, {});
   for (int t = 0; t < T; ++t) S.level_fronts[level[t]].push_back(t);
+  // ---- factor-only storage. The factors of every front (its m x p panel and
+  // U12) stay in the factor store for the solves; the full m x m front lives
+  // in the front pool only while it is assembled and factorised: from the
+  // level of its first child (or its own, for a leaf) to its own level. Pool
+  // offsets are assigned first-fit, level by level, largest fronts first;
+  // regions of fronts that ended at level l - 1 are free for level l.
+  {
+    std::vector<int> first(T);
+    for (int t = 0; t < T; ++t) first[t] = level[t];
+    for (int t = 0; t < T; ++t)
+      if (parent[t] >= 0) first[parent[t]] = std::min(first[parent[t]], level[t]);
+    std::vector<int64_t> delta(L + 1, 0);
+    S.factor_stored = 0;
+    S.level_new.assign(L, {});
+    for (int t = 0; t < T; ++t) {
+      FrontInfo& F = S.fronts[t];
+      const int64_t p = F.p, b = F.b, mm = p + b;
+      F.fac_off = S.factor_stored;
+      S.factor_stored += p * p + 2 * p * b;
+      F.start_level = first[t];
+      S.level_new[first[t]].push_back(t);
+      delta[first[t]] += mm * mm;
+      delta[level[t] + 1] -= mm * mm;
+    }
+    int64_t live = 0;
+    S.pool_peak = 0;
+    for (int l = 0; l < L; ++l) {
+      live += delta[l];
+      S.pool_peak = std::max(S.pool_peak, live);
+    }
+    // first-fit over free intervals [off, off + len), kept sorted and merged
+    std::vector<std::pair<int64_t, int64_t>> free_list;
+    int64_t top = 0;
+    auto release = [&](int64_t off, int64_t len) {
+      auto it = std::lower_bound(free_list.begin(), free_list.end(), std::make_pair(off, (int64_t)0));
+      it = free_list.insert(it, {off, len});
+      size_t i = it - free_list.begin();
+      if (i + 1 < free_list.size() && free_list[i].first + free_list[i].second == free_list[i + 1].first) {
+        free_list[i].second += free_list[i + 1].second;
+        free_list.erase(free_list.begin() + i + 1);
+      }
+      if (i > 0 && free_list[i - 1].first + free_list[i - 1].second == free_list[i].first) {
+        free_list[i - 1].second += free_list[i].second;
+        free_list.erase(free_list.begin() + i);
+      }
+    };
+    for (int l = 0; l < L; ++l) {
+      if (l > 0)
+        for (int t : S.level_fronts[l - 1]) {
+          const int64_t mm = (int64_t)S.fronts[t].p + S.fronts[t].b;
+          release(S.fronts[t].off, mm * mm);
+        }
+      std::vector<int32_t> order = S.level_new[l];
+      std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t c) {
+        return (int64_t)S.fronts[a].p + S.fronts[a].b > (int64_t)S.fronts[c].p + S.fronts[c].b;
+      });
+      for (int t : order) {
+        const int64_t mm = (int64_t)S.fronts[t].p + S.fronts[t].b, need = mm * mm;
+        int64_t off = -1;
+        for (size_t i = 0; i < free_list.size(); ++i)
+          if (free_list[i].second >= need) {
+            off = free_list[i].first;
+            free_list[i].first += need;
+            free_list[i].second -= need;
+            if (free_list[i].second == 0) free_list.erase(free_list.begin() + i);
+            break;
+          }
+        if (off < 0) {  // grow the pool (a free interval at its end is extended)
+          if (!free_list.empty() && free_list.back().first + free_list.back().second == top) {
+            off = free_list.back().first;
+            free_list.pop_back();
+          } else {
+            off = top;
+          }
+          top = off + need;
+        }
+        S.fronts[t].off = off;
+      }
+    }
+    S.pool = std::max<int64_t>(top, 1);
+    // check: the fronts alive at each level occupy disjoint pool regions
+    std::vector<std::pair<int64_t, int64_t>> alive;
+    for (int l = 0; l < L; ++l) {
+      alive.clear();
+      for (int t = 0; t < T; ++t)
+        if (S.fronts[t].start_level <= l && l <= level[t]) {
+          const int64_t mm = (int64_t)S.fronts[t].p + S.fronts[t].b;
+          alive.push_back({S.fronts[t].off, S.fronts[t].off + mm * mm});
+        }
+      std::sort(alive.begin(), alive.end());
+      for (size_t i = 0; i < alive.size(); ++i)
+        if (alive[i].first < 0 || alive[i].second > S.pool || (i > 0 && alive[i].first < alive[i - 1].second)) {
+          set_error("front pool regions overlap");
+          return ELP_ERR_ARG;
+        }
+    }
+  }
+  // ---- per entry: pool offset; entries grouped by the start level of their
+  // owner (the scatter of a level writes them before its fronts are used)
+  S.entry_row.resize(nnz);
+  std::vector<int64_t> cnt(L + 1, 0);
+  for (int64_t r = 0; r < n; ++r)
+    for (int32_t q = m.row_ptr[r]; q < m.row_ptr[r + 1]; ++q) {
+      const FrontInfo& F = S.fronts[entry_owner[q]];
+      S.entry_off[q] += F.off;
+      S.entry_row[q] = (int32_t)r;
+      cnt[F.start_level + 1]++;
+    }
+  for (int l = 0; l < L; ++l) cnt[l + 1] += cnt[l];
+  S.level_entry_start = cnt;
+  S.scatter_order.resize(nnz);
+  for (int64_t q = 0; q < nnz; ++q) S.scatter_order[cnt[S.fronts[entry_owner[q]].start_level]++] = (int32_t)q;
   return ELP_OK;
 }
 

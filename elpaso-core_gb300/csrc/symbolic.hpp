@@ -17,7 +17,10 @@ struct FrontInfo {
   int32_t map_off = 0;    // offset into parent_map (b entries)
   int32_t piv_off = 0;    // offset of the first pivot in elimination order
   int32_t cb_off = 0;     // offset of the contribution vector (b entries) in solve buffers
-  int64_t off = 0;        // offset (complex entries) of the m x m front in the arena
+  int64_t off = 0;        // offset (complex entries) of the full m x m front in the front pool
+  int64_t fac_off = 0;    // offset of its factors in the factor store: the m x p panel (L11\U11
+                          // and L21, column-major, ld m), then U12 (p x b, column-major, ld p)
+  int32_t start_level = 0;  // first level the full front is alive (its first child's, or its own)
 };
 
 struct Symbolic {
@@ -36,6 +39,15 @@ struct Symbolic {
   double flops = 0.0;                  // real flops of one complex factorisation
   double gemm_flops = 0.0;             // of which trailing (Schur) updates
   double factor_bytes = 0.0;           // factor bytes read per forward + backward sweep (FP32)
+  int64_t factor_stored = 0;           // sum of p^2 + 2 p b: the L and U parts of every front
+  int64_t pool_peak = 0;               // most m^2 entries of full fronts alive at once when levels
+                                       // run in order (a front lives from its first child's level
+                                       // to its own)
+  int64_t pool = 0;                    // entries of the front pool (>= pool_peak: first-fit offsets)
+  std::vector<std::vector<int32_t>> level_new;  // per level: fronts whose full front starts there
+  std::vector<int32_t> scatter_order;  // CSR entries grouped by the start level of their owner front
+  std::vector<int64_t> level_entry_start;  // per level + 1: range of scatter_order
+  std::vector<int32_t> entry_row;      // per CSR entry: its row
 };
 
 // Geometric nested dissection on the node graph; leaf_dofs bounds leaf size.

@@ -198,6 +198,11 @@ typedef struct {
                                reference throws (setupJacobian2D, elementfem.cpp:97-100) */
   int64_t factor_stored;    /* complex entries of the factors kept per frequency (L and U:
                                p^2 + 2 p b per front)                                        */
+  int64_t front_pool_peak;  /* most complex entries of full m x m fronts alive at once when the
+                               tree levels are factorised in order                           */
+  int64_t front_pool;       /* complex entries of the front pool per frequency (first-fit
+                               regions, >= front_pool_peak); the workspace per frequency is the
+                               pool plus the factors (factor_stored), not the sum of all m^2  */
 } elp_model_info;
 
 /* precision of the numeric factorisation */
@@ -371,14 +376,16 @@ int elp_front_update_test(int kernel, int p, int b, int step, int slots, float* 
 /* Kernel classes, in the order of the arrays below:
  *  0 assemble, 1 dscale, 2 scatter, 3 panel, 4 border, 5 urow, 6 gemm,
  *  7 extend_add, 8 forward, 9 backward, 10 residual, 11 norms, 12 rhs,
- *  13 update, 14 values, 15 gemm_tc, 16 spmv, 17 fwd_border, 18 bwd_u12,
- *  19 krylov (GMRES vector kernels).
+ *  13 update, 14 values, 15 gemm_tc (tensor-core Crout and Schur updates
+ *  from the fronts), 16 spmv, 17 fwd_border, 18 bwd_u12, 19 krylov (GMRES
+ *  vector kernels), 20 schur_tc (tensor-core Schur update from packed
+ *  operands), 21 pack (TF32 split of the packed operands).
  * No reference counterpart (the reference times whole phases with
  * cStopwatch, basics/watch/stopwatch.cpp:35-64). elp_profile(1) resets the
  * counters and records a CUDA event pair around every launch on its stream;
  * elp_profile(0) resets and counts launches only. */
 int elp_profile(int enable);
-#define ELP_PROFILE_CLASSES 20
+#define ELP_PROFILE_CLASSES 22
 int elp_profile_read(double* ms /* [ELP_PROFILE_CLASSES] */, int64_t* launches, int64_t* timed,
                      int* n_classes);
 

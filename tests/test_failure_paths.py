@@ -150,7 +150,9 @@ def test_every_device_allocation_failure_of_a_solve(elp, meshes, oracle, prec):
         x, info = m.solve([om], precision=prec)
         assert np.linalg.norm(s.f - A @ x[0]) / np.linalg.norm(s.f) <= 1e-10, k
         m.close()
-    assert hits >= 20  # allocations of a first solve: the C API's 1, workspace ~20, Krylov 10
+    # allocations of a first solve: the C API's buffer, ~17 of the workspace, and
+    # the mixed path's 10 Krylov buffers
+    assert hits >= (15 if prec == 0 else 25), hits
 
 
 PROBE = r"""

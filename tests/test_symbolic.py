@@ -105,3 +105,18 @@ def test_front_statistics_are_consistent_and_deterministic(elp, meshes, make):
     assert i["n_levels"] >= (2 if i["n_fronts"] > 1 else 1)
     _, again = analysed(elp, d)
     assert again == i
+
+
+@pytest.mark.parametrize("name", ["plate_cavity", "cube", "solid_cube", "plate", "two_plates"])
+def test_factor_store_and_front_pool_sizes(elp, meshes, name):
+    """Factor-only storage: the factors kept are sum p^2 + 2 p b, and the
+    pool of full fronts (first-fit regions, checked disjoint per level by
+    the symbolic phase itself) holds at least the most fronts alive at once
+    and at most every front at once."""
+    d = {"plate_cavity": meshes.plate_cavity(16, 12, 8, 0.6, 0.4, 0.3), "cube": meshes.cube(12),
+         "solid_cube": meshes.solid_cube(9), "plate": meshes.plate(40, 30, 0.6, 0.4, 0.002),
+         "two_plates": two_bodies(meshes.plate(12, 9, 0.3, 0.2, 0.002))}[name]
+    m, i = analysed(elp, d)
+    assert 0 < i["factor_stored"] < i["factor_entries"]
+    assert i["front_pool_peak"] <= i["front_pool"] <= i["factor_entries"]
+    assert i["front_pool"] <= 1.25 * i["front_pool_peak"]  # first-fit wastes little on these trees
