@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <new>
 
@@ -33,6 +34,29 @@ int model_symbolic_host(Model& m) {
   }();
   int rc = symbolic_analyse(m, *s, leaf);
   if (rc) return rc;
+  if (getenv("ELP_PROF_LEVELS")) {  // per-level work, beside the per-level device times of the profiler
+    const Symbolic& S = *s;
+    for (int l = 0; l < S.n_levels; ++l) {
+      double crout = 0.0, schur = 0.0, m2 = 0.0, fac = 0.0;
+      int maxp = 0, maxb = 0;
+      for (int t : S.level_fronts[l]) {
+        const int p = S.fronts[t].p, b = S.fronts[t].b;
+        const double pp = p, bb = b, mm = pp + bb;
+        maxp = std::max(maxp, p);
+        maxb = std::max(maxb, b);
+        schur += 8.0 * bb * bb * pp;
+        for (int k0 = 0; k0 < p; k0 += 32) {
+          const double w = std::min(32, p - k0), tt = mm - k0 - w;
+          crout += 8.0 * (tt * tt - bb * bb) * w;  // trailing updates of the pivot rows and columns
+        }
+        m2 += mm * mm;
+        fac += pp * pp + 2.0 * pp * bb;
+      }
+      fprintf(stderr, "[elp levels] level %2d fronts %5zu max p %5d max b %5d: crout %8.2f GF, schur %8.2f GF, "
+              "sum m^2 %8.1f M, factor %8.1f M entries\n", l, S.level_fronts[l].size(), maxp, maxb, crout / 1e9,
+              schur / 1e9, m2 / 1e6, fac / 1e6);
+    }
+  }
   m.sym = std::move(s);
   return ELP_OK;
 }
@@ -277,9 +301,14 @@ int elp_solve_device(elp_model* h, const double* omegas, int n_omega, int precis
   size_t freeb = 0, totb = 0;
   ELP_CUDA(cudaMemGetInfo(&freeb, &totb));
   freeb += (size_t)workspace_held(m, precision);
-  const size_t per_slot = (size_t)workspace_bytes(m, precision, 1);
+  // whole fronts when the batch fits half the free memory that way (no factor
+  // copy); the compact factor store when it does not (about 2/3 of the bytes)
+  const int want = std::min(kMaxSlots, std::max(1, n_omega));
+  const int store = choose_store(m, precision, want, (int64_t)(freeb / 2));
+  const size_t per_slot = (size_t)workspace_bytes(m, precision, 1, store);
   int slots = (int)std::min<size_t>((size_t)kMaxSlots, std::max<size_t>(1, (freeb / 2) / std::max<size_t>(1, per_slot)));
-  if (m.ws[precision] && m.ws[precision]->slots > 0) slots = std::max(slots, std::min(m.ws[precision]->slots, kMaxSlots));
+  if (m.ws[precision] && m.ws[precision]->slots > 0 && m.ws[precision]->store == store)
+    slots = std::max(slots, std::min(m.ws[precision]->slots, kMaxSlots));
   slots = std::min(slots, std::max(1, n_omega));
   // equal chunks when the batch must be split (48 over 46 slots: 2 x 24, not
   // 46 + 2, whose small remainder would cost nearly a whole factorisation pass)
@@ -293,7 +322,7 @@ int elp_solve_device(elp_model* h, const double* omegas, int n_omega, int precis
     rc = numeric_solve_batch(m, precision, omegas + s0, cnt,
                              f_dev ? reinterpret_cast<const double2*>(f_dev) + (size_t)s0 * n : nullptr,
                              reinterpret_cast<double2*>(x_dev) + (size_t)s0 * n, info ? info + s0 : nullptr, tol,
-                             (cudaStream_t)stream);
+                             (cudaStream_t)stream, 4, store);
     if (rc == ELP_ERR_SINGULAR || (rc == ELP_ERR_NOCONV && worst != ELP_ERR_SINGULAR)) worst = rc;
     else if (rc && rc != ELP_ERR_NOCONV) return rc;
   }

@@ -114,9 +114,19 @@ __global__ void k_zero_fronts(const int32_t* __restrict__ list, const int32_t* _
   const int f = list[blockIdx.x];
   const int64_t m = (int64_t)fp[f] + fb[f], mm = m * m;
   V* F = pool + blockIdx.y * pool_size + foff[f];
-  const V z = cmk<V>(0.0, 0.0);
-  for (int64_t t = blockIdx.z * (int64_t)blockDim.x + threadIdx.x; t < mm; t += (int64_t)gridDim.z * blockDim.x)
-    F[t] = z;
+  const int64_t t0 = blockIdx.z * (int64_t)blockDim.x + threadIdx.x, nt = (int64_t)gridDim.z * blockDim.x;
+  // 16-byte stores: one 8-byte entry first when the front starts between 16-byte
+  // boundaries (FP32 complex), the last one alone when an odd count remains
+  const int64_t head = (sizeof(V) == 8 && (reinterpret_cast<uintptr_t>(F) & 15)) ? 1 : 0;
+  const int64_t per16 = 16 / sizeof(V);
+  const int64_t nq = (mm - head) / per16;
+  float4* Q = reinterpret_cast<float4*>(F + head);
+  for (int64_t t = t0; t < nq; t += nt) Q[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (t0 == 0) {
+    const V z = cmk<V>(0.0, 0.0);
+    if (head && mm > 0) F[0] = z;
+    for (int64_t k = head + nq * per16; k < mm; ++k) F[k] = z;
+  }
 }
 
 // A(w) entries owned by the fronts starting at a level, scaled by D on both
@@ -125,7 +135,8 @@ __global__ void k_zero_fronts(const int32_t* __restrict__ list, const int32_t* _
 template <class V>
 __global__ void k_scatter(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ order,
                           int64_t count, const int32_t* __restrict__ entry_row, const int32_t* __restrict__ col_idx,
-                          const int64_t* __restrict__ entry_off, const double* __restrict__ dscale, int64_t n,
+                          const int32_t* __restrict__ entry_owner, const int64_t* __restrict__ entry_local,
+                          const int64_t* __restrict__ foff, const double* __restrict__ dscale, int64_t n,
                           V* __restrict__ pool, int64_t pool_size, unsigned long long* __restrict__ stats) {
   const int s = blockIdx.y;
   const Coef c = coef[s];
@@ -140,7 +151,7 @@ __global__ void k_scatter(CombineArgs A, const Coef* __restrict__ coef, const in
     v.x *= sc;
     v.y *= sc;
     amax = fmax(amax, sqrt(v.x * v.x + v.y * v.y));
-    F[entry_off[q]] = cmk<V>(v.x, v.y);
+    F[foff[entry_owner[q]] + entry_local[q]] = cmk<V>(v.x, v.y);
   }
   for (int o = 16; o; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
   if ((threadIdx.x & 31) == 0) atomicMax(stats + 4 * s + 3, (unsigned long long)__double_as_longlong(amax));
@@ -663,6 +674,7 @@ struct SolveArgs {
   const int32_t* pmap;
   int64_t arena_size, n, cb_total;
   const int* active;
+  int u12_ld_p;  // U12 after the m x p panel with ld p (factor store), else in place with ld m
 };
 
 // dst[k] = src[idx[k]] for k < count: every thread issues the index loads of
@@ -844,17 +856,20 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   const int r = blockIdx.z * 32 + lane;
   V t = cmk<V>(0.0, 0.0);
   if (r < p) {
-    const V* row = F + (int64_t)p * m + r;  // U12 in the factor store: after the panel, ld p
+    // U12 in place (row r of columns p..m-1, ld m), or in the factor store right
+    // after the m x p panel with ld p: both start at F + p m + r
+    const V* row = F + (int64_t)p * m + r;
+    const int64_t ld = S.u12_ld_p ? p : m;
     const int i_lo = (b * wv) / 8, i_hi = (b * (wv + 1)) / 8;
     int i = i_lo;
     for (; i + 16 <= i_hi; i += 16) {  // 16 independent loads in flight per thread
       V a[16];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) a[q] = row[(int64_t)(i + q) * p];
+      for (int q = 0; q < 16; ++q) a[q] = row[(int64_t)(i + q) * ld];
 #pragma unroll
       for (int q = 0; q < 16; ++q) t = cfma(a[q], xb[i + q], t);
     }
-    for (; i < i_hi; ++i) t = cfma(row[(int64_t)i * p], xb[i], t);
+    for (; i < i_hi; ++i) t = cfma(row[(int64_t)i * ld], xb[i], t);
   }
   part[wv][lane] = t;
   __syncthreads();
@@ -1263,9 +1278,13 @@ int device_upload_symbolic(Model& m) {
   ELP_CUDA(D.f_piv_off.upload(po));
   ELP_CUDA(D.f_off.upload(off));
   {
-    std::vector<int64_t> fo(T);
-    for (int t = 0; t < T; ++t) fo[t] = S.fronts[t].fac_off;
+    std::vector<int64_t> fo(T), ff(T);
+    for (int t = 0; t < T; ++t) {
+      fo[t] = S.fronts[t].fac_off;
+      ff[t] = S.fronts[t].off_full;
+    }
     ELP_CUDA(D.f_fac.upload(fo));
+    ELP_CUDA(D.f_off_full.upload(ff));
   }
   ELP_CUDA(D.scatter_order.upload(S.scatter_order));
   ELP_CUDA(D.entry_row.upload(S.entry_row));
@@ -1273,7 +1292,8 @@ int device_upload_symbolic(Model& m) {
   ELP_CUDA(D.parent_map.upload(S.parent_map));
   ELP_CUDA(D.child_ptr.upload(cptr));
   ELP_CUDA(D.child_list.upload(clist));
-  ELP_CUDA(D.entry_off.upload(S.entry_off));
+  ELP_CUDA(D.entry_local.upload(S.entry_local));
+  ELP_CUDA(D.entry_owner.upload(S.entry_owner));
   std::vector<int32_t> ll, ea, nl;
   D.levels.assign(S.n_levels, DeviceSymbolic::Level());
   int maxc = std::max(1, S.max_children);
@@ -1332,6 +1352,7 @@ int device_upload_symbolic(Model& m) {
   ELP_CUDA(D.ea_list.upload(ea));
   D.n_fronts = T;
   D.arena = S.pool;
+  D.arena_full = S.arena;
   D.fac = S.factor_stored;
   D.cb_total = S.cb_total;
   D.max_front = S.max_front;
@@ -1376,6 +1397,7 @@ constexpr int kGmresRestart = 24;  // GMRES(24) of the mixed path
 WorkspacePlan workspace_plan(const Symbolic& S) {
   WorkspacePlan P;
   P.arena = S.pool;
+  P.arena_full = S.arena;
   P.fac = S.factor_stored;
   P.cb_total = S.cb_total;
   static const bool pack_all_levels = getenv("ELP_TC_PACK") && std::string(getenv("ELP_TC_PACK")) == "all";
@@ -1401,14 +1423,15 @@ WorkspacePlan workspace_plan(const Symbolic& S) {
 // mixed path) allocates for `slots` frequencies; the serving loop admits
 // models against this figure, so it mirrors those allocations. Needs only the
 // host symbolic phase (no device allocation has to happen first).
-int64_t workspace_bytes(const Model& m, int precision, int slots) {
+int64_t workspace_bytes(const Model& m, int precision, int slots, int store) {
   if (!m.sym) return 0;
   const WorkspacePlan D = workspace_plan(*m.sym);
   const int64_t n = m.n, S = slots;
   const int64_t elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
   const int64_t nparts = std::min<int64_t>(1024, (n + 255) / 256);
   const int64_t max_count = D.max_count;
-  int64_t b = S * (D.arena + D.fac + std::max<int64_t>(1, D.cb_total) + 2 * n) * elem;  // pool, factors, cb, z, tb
+  const int64_t fronts = store == STORE_COMPACT ? D.arena + D.fac : D.arena_full;  // pool + factors, or whole fronts
+  int64_t b = S * (fronts + std::max<int64_t>(1, D.cb_total) + 2 * n) * elem;          // fronts, cb, z, tb
   b += S * n * (4 + 8 + 3 * 16);                                               // perm, dscale, x, r, f
   b += S * (int64_t)(sizeof(Coef) + 16 + nparts * 16 + 4 + 32) + 4;            // coef, norms, partials, flags
   b += max_count * S * swapmap_ints<32>() * 4;
@@ -1422,34 +1445,53 @@ int64_t workspace_bytes(const Model& m, int precision, int slots) {
 
 int64_t workspace_held(const Model& m, int precision) {
   int64_t b = 0;
-  if (m.ws[precision]) b += workspace_bytes(m, precision, m.ws[precision]->slots);
+  if (m.ws[precision]) b += workspace_bytes(m, precision, m.ws[precision]->slots, m.ws[precision]->store);
   for (const auto& w : m.ws_b[precision])
-    if (w) b += workspace_bytes(m, precision, w->slots);
+    if (w) b += workspace_bytes(m, precision, w->slots, w->store);
   return b;
 }
 
-static int workspace_alloc(Model& m, Workspace& w, int precision, int slots);
+static int workspace_alloc(Model& m, Workspace& w, int precision, int slots, int store);
 
-int workspace_ensure(Model& m, int precision, int slots, int lane) {
+int forced_store() {
+  static const int v = [] {
+    const char* e = getenv("ELP_FACTOR_STORE");
+    if (e && std::string(e) == "full") return (int)STORE_FULL;
+    if (e && std::string(e) == "compact") return (int)STORE_COMPACT;
+    return -1;
+  }();
+  return v;
+}
+
+int choose_store(const Model& m, int precision, int slots, int64_t budget) {
+  const int f = forced_store();
+  if (f >= 0) return f;
+  return workspace_bytes(m, precision, slots, STORE_FULL) <= budget ? STORE_FULL : STORE_COMPACT;
+}
+
+int workspace_ensure(Model& m, int precision, int slots, int lane, int store) {
   std::unique_ptr<Workspace>& W = lane ? m.ws_b[precision][lane - 1] : m.ws[precision];
-  if (W && W->slots >= slots) return ELP_OK;
+  if (W && W->slots >= slots && W->store == store) return ELP_OK;
   W.reset();  // the old workspace goes before the new one is made
   // built aside and kept only when every allocation succeeded
   std::unique_ptr<Workspace> fresh(new Workspace());
-  int rc = workspace_alloc(m, *fresh, precision, slots);
+  int rc = workspace_alloc(m, *fresh, precision, slots, store);
   if (rc) return rc;
   W = std::move(fresh);
   return ELP_OK;
 }
 
-static int workspace_alloc(Model& m, Workspace& w, int precision, int slots) {
+static int workspace_alloc(Model& m, Workspace& w, int precision, int slots, int store) {
   w.precision = precision;
   w.slots = slots;
+  w.store = store;
   w.elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
   const DeviceSymbolic& D = *m.dsym;
   const int64_t n = m.n;
-  cudaError_t e = w.arena.alloc((size_t)slots * D.arena * w.elem);
-  if (e == cudaSuccess) e = w.fac.alloc((size_t)slots * D.fac * w.elem);
+  w.arena_stride = store == STORE_COMPACT ? D.arena : D.arena_full;
+  w.foff = store == STORE_COMPACT ? D.f_off.p : D.f_off_full.p;
+  cudaError_t e = w.arena.alloc((size_t)slots * w.arena_stride * w.elem);
+  if (e == cudaSuccess && store == STORE_COMPACT) e = w.fac.alloc((size_t)slots * D.fac * w.elem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     set_error("front pool and factor store do not fit in device memory");
@@ -1549,8 +1591,8 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   L.fp = D.f_p.p;
   L.fb = D.f_b.p;
   L.piv_off = D.f_piv_off.p;
-  L.foff = D.f_off.p;
-  L.arena_size = D.arena;
+  L.foff = w.foff;
+  L.arena_size = w.arena_stride;
   L.n = n;
   L.fparent = D.f_parent.p;
   L.map_off = D.f_map_off.p;
@@ -1611,16 +1653,16 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
     const auto& LV = D.levels[l];
     prof_set_level((int)l);
     if (LV.new_count > 0) {  // full fronts starting here: zeroed, then their entries of A(w) written
-      dim3 gz(LV.new_count, S_used, (unsigned)std::min<int64_t>(65535, (LV.new_max_m2 + 2047) / 2048));
+      dim3 gz(LV.new_count, S_used, (unsigned)std::min<int64_t>(65535, (LV.new_max_m2 + 4095) / 4096));
       PROF_LAUNCH(KC_SCATTER, st, k_zero_fronts<V><<<gz, 256, 0, st>>>(D.new_list.p + LV.new_start, D.f_p.p, D.f_b.p,
-                                                                        D.f_off.p, arena, D.arena));
+                                                                        w.foff, arena, w.arena_stride));
     }
     if (LV.ent_count > 0) {
       dim3 gs((unsigned)std::min<int64_t>((LV.ent_count + 255) / 256, 8192), S_used);
       PROF_LAUNCH(KC_SCATTER, st, k_scatter<V><<<gs, 256, 0, st>>>(A, w.coef.p, D.scatter_order.p + LV.ent_start,
                                                                     LV.ent_count, D.entry_row.p, G.col_idx.p,
-                                                                    D.entry_off.p, w.dscale.p, n, arena, D.arena,
-                                                                    w.stats.p));
+                                                                    D.entry_owner.p, D.entry_local.p, w.foff,
+                                                                    w.dscale.p, n, arena, w.arena_stride, w.stats.p));
     }
     L.list = D.level_list.p + LV.start;
     L.count = LV.count;
@@ -1693,14 +1735,14 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
         if (!LV.ea_count[k]) continue;
         dim3 g5(LV.ea_count[k], S_used, (unsigned)std::min(65535, (LV.ea_max_b + 3) / 4));  // 4 columns per pass
         PROF_LAUNCH(KC_EXTEND_ADD, st, k_extend_add<R><<<g5, 256, 0, st>>>(D.ea_list.p + LV.ea_start[k], D.f_p.p, D.f_b.p,
-                                                                           D.f_parent.p, D.f_map_off.p, D.f_off.p,
-                                                                           D.parent_map.p, arena, D.arena));
+                                                                           D.f_parent.p, D.f_map_off.p, w.foff,
+                                                                           D.parent_map.p, arena, w.arena_stride));
       }
     }
-    {  // the level's factors into the factor store; its full fronts are dead from here
+    if (w.store == STORE_COMPACT) {  // the level's factors into the factor store; its full fronts are dead from here
       dim3 gc(LV.count, S_used, (unsigned)std::min<int64_t>(65535, (LV.fac_max + 2047) / 2048));
-      PROF_LAUNCH(KC_SCATTER, st, k_compact<V><<<gc, 256, 0, st>>>(L.list, D.f_p.p, D.f_b.p, D.f_off.p, D.f_fac.p,
-                                                                    arena, D.arena, fac, D.fac));
+      PROF_LAUNCH(KC_SCATTER, st, k_compact<V><<<gc, 256, 0, st>>>(L.list, D.f_p.p, D.f_b.p, w.foff, D.f_fac.p,
+                                                                    arena, w.arena_stride, fac, D.fac));
     }
   }
   prof_set_level(-1);
@@ -1726,14 +1768,16 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
   S.piv_off = D.f_piv_off.p;
   S.child_ptr = D.child_ptr.p;
   S.child_list = D.child_list.p;
-  S.foff = D.f_fac.p;  // the sweeps read the factor store (U12 with ld p, k_bwd_u12)
+  const bool compact = w.store == STORE_COMPACT;
+  S.foff = compact ? D.f_fac.p : w.foff;  // the factor store (U12 with ld p), or the fronts in place
+  S.u12_ld_p = compact ? 1 : 0;
   S.dofs = D.front_dofs.p;
   S.pmap = D.parent_map.p;
-  S.arena_size = D.fac;
+  S.arena_size = compact ? D.fac : w.arena_stride;
   S.n = m.n;
   S.cb_total = std::max<int64_t>(1, D.cb_total);
   S.active = mask;
-  const V* arena = reinterpret_cast<const V*>(w.fac.p);
+  const V* arena = reinterpret_cast<const V*>(compact ? w.fac.p : w.arena.p);
   V* z = reinterpret_cast<V*>(w.z.p);
   V* cb = reinterpret_cast<V*>(w.cb.p);
   for (size_t l = 0; l < D.levels.size(); ++l) {
@@ -2066,8 +2110,8 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
 
 // One batch on one workspace lane (0 or 1), on `stream` (its own when null).
 static int solve_lane(Model& m, int precision, int lane, const double* omegas, int n_omega, const double2* f_dev,
-                      double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream) {
-  int rc = workspace_ensure(m, precision, n_omega, lane);
+                      double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream, int store) {
+  int rc = workspace_ensure(m, precision, n_omega, lane, store);
   if (rc) return rc;
   Workspace& w = lane ? *m.ws_b[precision][lane - 1] : *m.ws[precision];
   cudaStream_t st = stream ? stream : w.stream;
@@ -2139,13 +2183,13 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
 }
 
 int numeric_solve_lane(Model& m, int precision, int lane, const double* omegas, int n_omega, const double2* f_dev,
-                       double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream) {
+                       double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream, int store) {
   if (n_omega <= 0) return ELP_OK;
   if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
   if (lane < 0 || lane > 3) { set_error("workspace lane out of range"); return ELP_ERR_ARG; }
   for (int s = 0; s < n_omega; ++s)
     if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
-  return solve_lane(m, precision, lane, omegas, n_omega, f_dev, x_dev, info, tol, stream);
+  return solve_lane(m, precision, lane, omegas, n_omega, f_dev, x_dev, info, tol, stream, store);
 }
 
 const double2* lane_solution(const Model& m, int precision, int lane) {
@@ -2162,8 +2206,10 @@ int64_t model_array_bytes(const Model& m) {
   b += (int64_t)m.interfaces.size() * (16 * 4 + 8 + 4 * 4);
   if (m.sym) {  // symbolic maps: per-entry arena offsets, front lists, extend-add maps
     const Symbolic& S = *m.sym;
-    b += (int64_t)S.entry_off.size() * (8 + 4 + 4) + (int64_t)S.front_dofs.size() * 4 + (int64_t)S.parent_map.size() * 4;
-    b += (int64_t)S.fronts.size() * (8 * 4 + 8 + 8 + 8 + 4 * 4);
+    // per entry: local offset, owner front, row, scatter order
+    b += (int64_t)S.entry_local.size() * (8 + 4 + 4 + 4) + (int64_t)S.front_dofs.size() * 4 +
+         (int64_t)S.parent_map.size() * 4;
+    b += (int64_t)S.fronts.size() * (8 * 4 + 8 * 4 + 4 * 4);
   }
   return b;
 }
@@ -2180,7 +2226,7 @@ constexpr int kSplitMin = 16;
 
 int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega, const double2* f_dev,
                         double2* x_dev, elp_solve_info* info, double tol, cudaStream_t user_stream,
-                        int max_lanes) {
+                        int max_lanes, int store) {
   if (n_omega <= 0) return ELP_OK;
   if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
   for (int s = 0; s < n_omega; ++s)
@@ -2192,13 +2238,13 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
   }();
   const int lanes = std::min({lanes_env, max_lanes, std::max(1, n_omega / (kSplitMin / 2))});
   if (lanes < 2 || n_omega < kSplitMin || prof_on())
-    return solve_lane(m, precision, 0, omegas, n_omega, f_dev, x_dev, info, tol, user_stream);
+    return solve_lane(m, precision, 0, omegas, n_omega, f_dev, x_dev, info, tol, user_stream, store);
   const int64_t n = m.n;
   int first[5];
   for (int l = 0; l <= lanes; ++l) first[l] = (int)((int64_t)n_omega * l / lanes);
   const int part_max = first[1] - first[0] + 1;
   for (int l = 0; l < lanes; ++l) {
-    int rc = workspace_ensure(m, precision, part_max, l);
+    int rc = workspace_ensure(m, precision, part_max, l, store);
     if (rc) return rc;
   }
   // every lane starts after the work already queued on the caller's stream
@@ -2218,7 +2264,7 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
       cudaSetDevice(dev);
       const int a = first[l], c = first[l + 1] - first[l];
       rcs[l] = solve_lane(m, precision, l, omegas + a, c, f_dev ? f_dev + (size_t)a * n : nullptr,
-                          x_dev + (size_t)a * n, info ? info + a : nullptr, tol, nullptr);
+                          x_dev + (size_t)a * n, info ? info + a : nullptr, tol, nullptr, store);
     } catch (const std::exception& e) {
       rcs[l] = ELP_ERR_CUDA;
       set_error(std::string("solve lane: ") + e.what());

@@ -115,15 +115,27 @@ __device__ __forceinline__ double dd_residual(double f, const DD& a) {
 }
 #endif  // __CUDACC__
 
+// How a workspace stores the fronts of a factorisation:
+//  STORE_FULL    every front whole (sum of m^2 entries per frequency); the
+//                solves read the factors in place;
+//  STORE_COMPACT full fronts only while they are assembled and factorised, in
+//                a pool whose regions later fronts reuse; each level's factors
+//                (the m x p panel and U12) are then copied into a factor store
+//                that the solves read (about 2/3 of the memory on the
+//                plate-cavity model, at the price of that copy).
+enum FrontStore { STORE_FULL = 0, STORE_COMPACT = 1 };
+
 struct DeviceSymbolic {
   DevBuf<int32_t> f_p, f_b, f_parent, f_idx_off, f_map_off, f_cb_off, f_piv_off;
   DevBuf<int64_t> f_off;          // per front: offset of its full m x m front in the front pool
+  DevBuf<int64_t> f_off_full;     // per front: offset when every front is kept whole
   DevBuf<int64_t> f_fac;          // per front: offset of its factors in the factor store
   DevBuf<int32_t> new_list;       // per level: fronts whose full front starts there (zeroed, scattered)
   DevBuf<int32_t> scatter_order;  // CSR entries by the start level of their owner front
   DevBuf<int32_t> entry_row;      // per CSR entry: its row
   DevBuf<int32_t> front_dofs, parent_map, child_ptr, child_list;
-  DevBuf<int64_t> entry_off;
+  DevBuf<int64_t> entry_local;    // per CSR entry: offset inside its owner front
+  DevBuf<int32_t> entry_owner;    // per CSR entry: its owner front
   DevBuf<int32_t> level_list;     // fronts grouped by level
   DevBuf<int32_t> ea_list;        // per (level, child slot): fronts to extend-add
   struct Level {
@@ -142,6 +154,7 @@ struct DeviceSymbolic {
   std::vector<Level> levels;
   int n_fronts = 0;
   int64_t arena = 0, cb_total = 0;  // arena: entries of the front pool per frequency
+  int64_t arena_full = 0;           // entries of every front whole (sum of m^2) per frequency
   int64_t fac = 0;                  // entries of the factor store per frequency
   int max_front = 0;
   DevBuf<int64_t> pack_base;      // per front: byte offset of its packed Schur operands within its level
@@ -161,10 +174,13 @@ inline bool packed_schur_level(const DeviceSymbolic::Level& L) {
 
 struct Workspace {
   int precision = 0;              // ELP_FP64_PLAIN / ELP_MIXED
+  int store = STORE_FULL;         // FrontStore of the arena (and of fac)
+  int64_t arena_stride = 0;       // complex entries of the arena per frequency slot
+  const int64_t* foff = nullptr;  // device front offsets into the arena (f_off_full or f_off)
   int slots = 0;                  // capacity in frequencies
   size_t elem = 0;                // bytes of one complex front entry
-  DevBuf<char> arena;             // slots x front pool: full fronts while they are factorised
-  DevBuf<char> fac;               // slots x factor store: L and U of every front, for the solves
+  DevBuf<char> arena;             // slots x fronts: all whole (STORE_FULL) or the pool (STORE_COMPACT)
+  DevBuf<char> fac;               // STORE_COMPACT: slots x factor store (L and U of every front)
   DevBuf<char> cb;                // slots x cb_total complex (solve contributions)
   DevBuf<char> z;                 // slots x n complex (solve vector, front precision)
   DevBuf<char> tb;                // slots x n complex (backward pivot-row buffer)
@@ -202,13 +218,18 @@ struct Workspace {
 
 // Sizes a workspace depends on, from the host symbolic phase alone.
 struct WorkspacePlan {
-  int64_t arena = 0, fac = 0, cb_total = 0, max_count = 1, pack_max = 0;  // arena: the front pool
+  int64_t arena = 0, arena_full = 0, fac = 0, cb_total = 0, max_count = 1, pack_max = 0;  // arena: the pool
 };
 WorkspacePlan workspace_plan(const Symbolic& S);
 
 int device_upload_symbolic(Model& m);
-int workspace_ensure(Model& m, int precision, int slots, int lane = 0);
-int64_t workspace_bytes(const Model& m, int precision, int slots);
+int workspace_ensure(Model& m, int precision, int slots, int lane, int store);
+int64_t workspace_bytes(const Model& m, int precision, int slots, int store);
+// The store a batch of `slots` frequencies uses when `budget` bytes are
+// available for it: STORE_FULL when the whole batch fits that way (or
+// ELP_FACTOR_STORE=full), else STORE_COMPACT (or ELP_FACTOR_STORE=compact).
+int choose_store(const Model& m, int precision, int slots, int64_t budget);
+int forced_store();  // ELP_FACTOR_STORE: STORE_FULL / STORE_COMPACT, or -1 (choose by memory)
 // Device bytes of a model's resident arrays (pattern, value arrays, per-row
 // data, element lists, symbolic maps), from host data alone.
 int64_t model_array_bytes(const Model& m);
@@ -218,7 +239,7 @@ int model_symbolic_host(Model& m);
 // lane's own when null). Distinct lanes of one model may run on different
 // host threads at the same time.
 int numeric_solve_lane(Model& m, int precision, int lane, const double* omegas, int n_omega, const double2* f_dev,
-                       double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream);
+                       double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream, int store);
 // The FP64 solution vectors of a lane's last batch (slot s at + s * n).
 const double2* lane_solution(const Model& m, int precision, int lane);
 // One front update kernel on caller-given FP32 complex fronts (elp_front_update_test).
@@ -232,7 +253,7 @@ int64_t workspace_held(const Model& m, int precision);
 // loop, pass 1).
 int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_omega,
                         const double2* f_dev, double2* x_dev, elp_solve_info* info, double tol,
-                        cudaStream_t user_stream, int max_lanes = 4);
+                        cudaStream_t user_stream, int max_lanes, int store);
 int numeric_system_values(Model& m, double omega, double2* out_dev);
 void make_coef(const Model& m, double w, Coef& c);
 

@@ -72,6 +72,7 @@ struct ModelSlot {
   int64_t array_bytes = 0;       // charged once, when the model is first prepared
   int64_t ws_bytes[kLanesPerModel] = {0, 0};  // charged per lane workspace
   int ws_slots[kLanesPerModel] = {0, 0};      // frequencies the lane's workspace holds
+  int ws_store[kLanesPerModel] = {0, 0};      // its front store (FrontStore)
   std::deque<int64_t> queue;     // requests with unscheduled frequencies
 };
 
@@ -149,26 +150,35 @@ struct elp_server {
         resident -= o.ws_bytes[l];
         o.ws_bytes[l] = 0;
         o.ws_slots[l] = 0;
+        o.ws_store[l] = STORE_FULL;
       }
     }
     return resident + need <= cfg.hbm_budget_bytes;
   }
 
   // frequencies a batch of model `mi` on `lane` may take (<= want), with the
-  // lane's workspace charged for them; 0 when no room is left now
-  int admit_batch(int mi, int lane, int want) {
+  // lane's workspace charged for them (whole fronts where they fit, else the
+  // compact factor store); 0 when no room is left now
+  int admit_batch(int mi, int lane, int want, int& store) {
     ModelSlot& s = *models[mi];
     const Model& m = s.h->m;
+    store = s.ws_store[lane];
     if (s.ws_slots[lane] >= want) return want;  // the lane's workspace already holds them
+    const int forced = forced_store();
     for (int S = want; S >= 1; S = S > 4 ? S / 2 : S - 1) {
       if (S <= s.ws_slots[lane]) return S;
-      const int64_t bytes = workspace_bytes(m, cfg.precision, S);
-      const int64_t extra = bytes - s.ws_bytes[lane];  // the old workspace is freed before the new one is made
-      if (make_room(extra, mi)) {
-        resident += extra;
-        s.ws_bytes[lane] = bytes;
-        s.ws_slots[lane] = S;
-        return S;
+      for (int st = STORE_FULL; st <= STORE_COMPACT; ++st) {
+        if (forced >= 0 && st != forced) continue;
+        const int64_t bytes = workspace_bytes(m, cfg.precision, S, st);
+        const int64_t extra = bytes - s.ws_bytes[lane];  // the old workspace is freed before the new one is made
+        if (make_room(extra, mi)) {
+          resident += extra;
+          s.ws_bytes[lane] = bytes;
+          s.ws_slots[lane] = S;
+          s.ws_store[lane] = st;
+          store = st;
+          return S;
+        }
       }
     }
     return 0;
@@ -194,7 +204,7 @@ struct elp_server {
     lk.lock();
     if (!rc) {
       const int64_t arrays = model_array_bytes(h->m);
-      const int64_t one = workspace_bytes(h->m, cfg.precision, 1);
+      const int64_t one = workspace_bytes(h->m, cfg.precision, 1, forced_store() >= 0 ? forced_store() : STORE_COMPACT);
       if (arrays + one > cfg.hbm_budget_bytes || !make_room(arrays, mi)) {
         rc = ELP_ERR_NOMEM;
       } else {
@@ -212,7 +222,8 @@ struct elp_server {
           if (!W) continue;
           if (prec != cfg.precision || l >= kLanesPerModel) { W.reset(); continue; }
           s.ws_slots[l] = W->slots;
-          s.ws_bytes[l] = workspace_bytes(m, prec, W->slots);
+          s.ws_store[l] = W->store;
+          s.ws_bytes[l] = workspace_bytes(m, prec, W->slots, W->store);
           resident += s.ws_bytes[l];
         }
     }
@@ -256,7 +267,8 @@ struct elp_server {
         waiting += (int)r.omegas.size() - r.next;
         if (waiting >= cfg.omega_batch) break;
       }
-      const int S = admit_batch(mi, lane, std::min(waiting, cfg.omega_batch));
+      int store = STORE_FULL;
+      const int S = admit_batch(mi, lane, std::min(waiting, cfg.omega_batch), store);
       if (S == 0) {
         if (running == 0) {  // nothing will free memory: the model cannot run at all
           set_error("model does not fit the HBM budget");
@@ -289,7 +301,7 @@ struct elp_server {
       int rc;
       try {
         rc = numeric_solve_lane(m, cfg.precision, lane, oms.data(), (int)oms.size(), nullptr, nullptr, info.data(),
-                                cfg.tol, st);
+                                cfg.tol, st, store);
       } catch (const std::bad_alloc&) {
         set_error("host allocation failed");
         rc = ELP_ERR_NOMEM;

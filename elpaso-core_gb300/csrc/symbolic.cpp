@@ -240,6 +240,7 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
     F.b = b;
     F.piv_off = piv;
     piv += p;
+    F.off_full = arena;
     const int64_t mm = (int64_t)p + b;
     arena += mm * mm;
     F.cb_off = (int32_t)cbt;
@@ -306,8 +307,8 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
     for (int k = 0; k < S.fronts[t].p; ++k) front_of_pos[S.fronts[t].piv_off + k] = t;
   std::vector<int32_t> list_pos(S.front_dofs.size());
   for (size_t k = 0; k < S.front_dofs.size(); ++k) list_pos[k] = dof_pos[S.front_dofs[k]];
-  S.entry_off.assign(nnz, -1);
-  std::vector<int32_t> entry_owner(nnz, -1);
+  S.entry_local.assign(nnz, -1);
+  S.entry_owner.assign(nnz, -1);
   int outside = 0;
 #pragma omp parallel for schedule(dynamic, 1024) reduction(| : outside)
   for (int64_t r = 0; r < n; ++r) {
@@ -326,8 +327,8 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
       }
       const int32_t loc_first = first - F.piv_off;
       const int32_t lr = pr == first ? loc_first : loc_later, lc = pr == first ? loc_later : loc_first;
-      S.entry_off[q] = (int64_t)lc * (F.p + F.b) + lr;  // local: the front's pool offset is added below
-      entry_owner[q] = front_of_pos[first];
+      S.entry_local[q] = (int64_t)lc * (F.p + F.b) + lr;
+      S.entry_owner[q] = front_of_pos[first];
     }
   }
   if (outside) { set_error("entry outside its owner front"); return ELP_ERR_ARG; }
@@ -435,21 +436,19 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
         }
     }
   }
-  // ---- per entry: pool offset; entries grouped by the start level of their
-  // owner (the scatter of a level writes them before its fronts are used)
+  // ---- entries grouped by the start level of their owner (the scatter of a
+  // level writes them before its fronts are used)
   S.entry_row.resize(nnz);
   std::vector<int64_t> cnt(L + 1, 0);
   for (int64_t r = 0; r < n; ++r)
     for (int32_t q = m.row_ptr[r]; q < m.row_ptr[r + 1]; ++q) {
-      const FrontInfo& F = S.fronts[entry_owner[q]];
-      S.entry_off[q] += F.off;
       S.entry_row[q] = (int32_t)r;
-      cnt[F.start_level + 1]++;
+      cnt[S.fronts[S.entry_owner[q]].start_level + 1]++;
     }
   for (int l = 0; l < L; ++l) cnt[l + 1] += cnt[l];
   S.level_entry_start = cnt;
   S.scatter_order.resize(nnz);
-  for (int64_t q = 0; q < nnz; ++q) S.scatter_order[cnt[S.fronts[entry_owner[q]].start_level]++] = (int32_t)q;
+  for (int64_t q = 0; q < nnz; ++q) S.scatter_order[cnt[S.fronts[S.entry_owner[q]].start_level]++] = (int32_t)q;
   return ELP_OK;
 }
 

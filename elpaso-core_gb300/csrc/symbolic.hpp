@@ -18,6 +18,7 @@ struct FrontInfo {
   int32_t piv_off = 0;    // offset of the first pivot in elimination order
   int32_t cb_off = 0;     // offset of the contribution vector (b entries) in solve buffers
   int64_t off = 0;        // offset (complex entries) of the full m x m front in the front pool
+  int64_t off_full = 0;   // its offset when every front is kept whole (sum of the earlier m^2)
   int64_t fac_off = 0;    // offset of its factors in the factor store: the m x p panel (L11\U11
                           // and L21, column-major, ld m), then U12 (p x b, column-major, ld p)
   int32_t start_level = 0;  // first level the full front is alive (its first child's, or its own)
@@ -27,7 +28,8 @@ struct Symbolic {
   std::vector<FrontInfo> fronts;       // postorder: children before parents
   std::vector<int32_t> front_dofs;     // per front: pivots then border (global rows)
   std::vector<int32_t> parent_map;     // per front: position of each border dof in the parent's list
-  std::vector<int64_t> entry_off;      // per CSR entry: arena offset inside its owner front
+  std::vector<int64_t> entry_local;    // per CSR entry: offset inside its owner front (column-major)
+  std::vector<int32_t> entry_owner;    // per CSR entry: the front that owns it
   std::vector<int32_t> elim_dof;       // elimination position -> dof
   std::vector<std::vector<int32_t>> level_fronts;
   std::vector<std::vector<int32_t>> level_children;  // per level: fronts whose parent is in a later level
