@@ -1466,7 +1466,10 @@ int forced_store() {
 int choose_store(const Model& m, int precision, int slots, int64_t budget) {
   const int f = forced_store();
   if (f >= 0) return f;
-  return workspace_bytes(m, precision, slots, STORE_FULL) <= budget ? STORE_FULL : STORE_COMPACT;
+  const int64_t full = workspace_bytes(m, precision, slots, STORE_FULL);
+  // small trees: the pool holds most fronts at once and the compact store saves nothing
+  if (full <= budget || workspace_bytes(m, precision, slots, STORE_COMPACT) >= full) return STORE_FULL;
+  return STORE_COMPACT;
 }
 
 int workspace_ensure(Model& m, int precision, int slots, int lane, int store) {

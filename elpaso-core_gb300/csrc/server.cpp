@@ -167,9 +167,11 @@ struct elp_server {
     const int forced = forced_store();
     for (int S = want; S >= 1; S = S > 4 ? S / 2 : S - 1) {
       if (S <= s.ws_slots[lane]) return S;
+      const int64_t full_bytes = workspace_bytes(m, cfg.precision, S, STORE_FULL);
       for (int st = STORE_FULL; st <= STORE_COMPACT; ++st) {
         if (forced >= 0 && st != forced) continue;
-        const int64_t bytes = workspace_bytes(m, cfg.precision, S, st);
+        const int64_t bytes = st == STORE_FULL ? full_bytes : workspace_bytes(m, cfg.precision, S, st);
+        if (st == STORE_COMPACT && forced < 0 && bytes >= full_bytes) continue;  // no saving on small trees
         const int64_t extra = bytes - s.ws_bytes[lane];  // the old workspace is freed before the new one is made
         if (make_room(extra, mi)) {
           resident += extra;
