@@ -302,6 +302,45 @@ def serving_measurement(elp, meshes, n_stream=96, n_probe=48):
             "server": "max_inflight 4, omega_batch 16, HBM budget 160 GiB, mixed precision"}
 
 
+def grouped_plates_measurement(elp, meshes, count=256, n_omega=32, repeats=2):
+    """The batched-plates workload through ONE group (elp_group_*): the 256
+    plates are one system whose tree levels are factorised by launches over
+    the fronts of all plates, every element integrated in one pass, each
+    plate at its own 32 frequencies from U(10, 400) Hz. Group creation and
+    the first solve (assembly, symbolic upload, workspaces) are outside the
+    timed region; the timed region solves all 8,192 (plate, frequency) pairs
+    `repeats` times (new frequencies each time), host buffers in and out."""
+    descs = meshes.batched_plates(count)
+    models = [elp.Model(d) for d in descs]
+    t0 = time.perf_counter()
+    g = elp.Group(models)
+    t_create = time.perf_counter() - t0
+    info = g.info()
+    rng = np.random.default_rng(20260101 + 4)
+    oms = [2 * np.pi * rng.uniform(10.0, 400.0, (count, n_omega)) for _ in range(repeats + 1)]
+    t0 = time.perf_counter()
+    g.solve(oms[0], precision=elp.MIXED, raise_on_noconv=False)  # assembly, symbolic upload, workspaces
+    t_first = time.perf_counter() - t0
+    worst, notconv = 0.0, 0
+    t0 = time.perf_counter()
+    for r in range(repeats):
+        _, infos = g.solve(oms[r + 1], precision=elp.MIXED, raise_on_noconv=False)
+        for row in infos:
+            for i in row:
+                worst = max(worst, i["rel_residual"])
+                notconv += i["converged"] == 0
+    t = time.perf_counter() - t0
+    g.close()
+    for m in models:
+        m.close()
+    return {"models": count, "dofs_total": info["n_dofs"], "fronts": info["n_fronts"], "levels": info["n_levels"],
+            "solves": count * n_omega * repeats, "seconds": t, "solves_s": count * n_omega * repeats / t,
+            "max_rel_residual": worst, "not_converged": notconv, "group_create_s": t_create,
+            "first_solve_s": t_first, "factor_gflop_per_slot": info["factor_flops"] / 1e9,
+            "note": "status of a frequency short of 1e-10 is reported, not hidden (its FP64 floor "
+                    "eps |||A| |x||| / ||f|| can exceed 1e-10); timed through elp_group_solve with host buffers"}
+
+
 def batched_plates_measurement(elp, meshes, count=256, n_omega=32):
     """The batched-plates workload: `count` simply supported DSG4 plates m x m,
     m ~ U{10..80} (363-19,683 DOFs), t ~ U(1, 5) mm, each with n_omega
@@ -479,7 +518,8 @@ def run_ours(args):
     serving = plates = None
     if rank == 0 and not args.no_serving:
         serving = serving_measurement(elp, meshes)
-        plates = batched_plates_measurement(elp, meshes)
+        plates = {"grouped": grouped_plates_measurement(elp, meshes),
+                  "serving_loop": batched_plates_measurement(elp, meshes)}
     cpu = None
     err_vs_oracle = None
     if rank == 0 and world == 1 and not args.no_cpu:

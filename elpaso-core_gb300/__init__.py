@@ -20,7 +20,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 __all__ = [
-    "ElpasoError", "ModelDesc", "Model", "Server", "load_library", "library_path",
+    "ElpasoError", "ModelDesc", "Model", "Group", "Server", "load_library", "library_path",
     "BRICK8", "DSG4", "FLUID8", "STR_LIN_ELA_ISO_DIR", "STR_LIN_VIS_ISO_DIR",
     "AF_LIN_UAF_ISO_DIR", "FP64_PLAIN", "MIXED", "DOF",
 ]
@@ -142,7 +142,7 @@ EXPORTS = [
     "elp_solve", "elp_model_destroy", "elp_last_error", "elp_solve_device", "elp_model_time_assembly",
     "elp_server_create", "elp_server_add_model", "elp_server_submit", "elp_server_wait",
     "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc", "elp_fault_inject",
-    "elp_front_update_test",
+    "elp_front_update_test", "elp_group_create", "elp_group_info", "elp_group_solve", "elp_group_destroy",
 ]
 KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
                   "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc", "spmv", "fwd_border",
@@ -184,6 +184,10 @@ def load_library(path: str | None = None):
     lib.elp_server_destroy.argtypes = [P]
     lib.elp_residual_noalloc.argtypes = [P, P, C.c_int, P, P, P, P, P]
     lib.elp_fault_inject.argtypes = [C.c_int, C.c_int]
+    lib.elp_group_create.argtypes = [P, C.c_int, C.POINTER(P)]
+    lib.elp_group_info.argtypes = [P, C.POINTER(_Info)]
+    lib.elp_group_solve.argtypes = [P, P, C.c_int, C.c_int, P, P, C.c_double]
+    lib.elp_group_destroy.argtypes = [P]
     lib.elp_front_update_test.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P, P]
     lib.elp_profile.argtypes = [C.c_int]
     lib.elp_profile_read.argtypes = [P, P, P, C.POINTER(C.c_int)]
@@ -439,6 +443,55 @@ class Model:
         if rc != 0 and (rc not in (5, 6) or raise_on_noconv):
             _check(rc)
         return x, [infos[i].as_dict() for i in range(len(om))]
+
+
+class Group:
+    """Several models solved together as one system (elp_group_*): every tree
+    level is one launch over the fronts of all members, each member with its
+    own frequencies, right-hand side and numbering. The members are copied:
+    the group does not refer to the Model objects afterwards."""
+
+    def __init__(self, models):
+        self.lib = load_library()
+        arr = (C.c_void_p * len(models))(*[m.handle.value for m in models])
+        self.ns = [m.n for m in models]
+        self.handle = C.c_void_p()
+        _check(self.lib.elp_group_create(C.cast(arr, C.c_void_p), len(models), C.byref(self.handle)))
+
+    def info(self) -> dict:
+        i = _Info()
+        _check(self.lib.elp_group_info(self.handle, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def solve(self, omegas, precision: int = MIXED, tol: float = 1e-10, raise_on_noconv: bool = True):
+        """omegas: [n_models, n_omega] angular frequencies (each member its own).
+        Returns ([x_k of shape (n_omega, n_k)], [[info] per frequency] per member)."""
+        om = np.ascontiguousarray(np.asarray(omegas, np.float64))
+        if om.ndim != 2 or om.shape[0] != len(self.ns):
+            raise ValueError("omegas must be [n_models, n_omega]")
+        nw = om.shape[1]
+        x = np.zeros(sum(self.ns) * nw, np.complex128)
+        infos = (SolveInfo * max(1, len(self.ns) * nw))()
+        rc = self.lib.elp_group_solve(self.handle, _ptr(om), nw, int(precision), _ptr(x), C.cast(infos, C.c_void_p),
+                                      float(tol))
+        if rc != 0 and (rc not in (5, 6) or raise_on_noconv):
+            _check(rc)
+        xs, off = [], 0
+        for n in self.ns:
+            xs.append(x[off:off + nw * n].reshape(nw, n))
+            off += nw * n
+        return xs, [[infos[k * nw + j].as_dict() for j in range(nw)] for k in range(len(self.ns))]
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.elp_group_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def profile(enable: bool = True):

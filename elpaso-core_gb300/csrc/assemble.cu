@@ -542,6 +542,10 @@ int device_upload_model(Model& m) {
   ELP_CUDA(D.col_idx.upload(m.col_idx));
   ELP_CUDA(D.diag_idx.upload(m.diag_idx));
   ELP_CUDA(D.cls.upload(m.cls));
+  if (m.n_members > 1) {
+    ELP_CUDA(D.row_model.upload(m.row_model));
+    ELP_CUDA(D.member_off.upload(m.member_row_off));
+  }
   std::vector<double> rhs(2 * m.n);
   for (int64_t i = 0; i < m.n; ++i) { rhs[2 * i] = m.rhs[i].real(); rhs[2 * i + 1] = m.rhs[i].imag(); }
   ELP_CUDA(D.rhs.upload(rhs));

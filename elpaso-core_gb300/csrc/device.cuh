@@ -89,6 +89,8 @@ struct DeviceModel {
   DevBuf<int32_t> iface_rows;      // per quad: 12 structure rows + 4 fluid rows
   DevBuf<double> iface_scale;      // per quad: -ori
   DevBuf<int32_t> iface_geom;      // per quad: 4 fluid node indices (geometry)
+  DevBuf<int32_t> row_model;       // a group: each row's member
+  DevBuf<int64_t> member_off;      // a group: first row of each member (n_members + 1)
   DevBuf<int> flags;               // [0] 3D non-positive detJ count, [1] 2D count
   int64_t bad_jacobians_3d = 0;    // flags[0] of the last assembly
   int64_t n_brick = 0, n_plate = 0, n_fluid = 0, n_iface = 0;

@@ -162,6 +162,14 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err) {
   m.materials.assign(d->materials, d->materials + d->n_materials);
   // frequency tables: copied here, the caller's pointers are not kept
   std::vector<StructGroup> tables(m.materials.size());
+  m.E_tables.assign(m.materials.size(), {});
+  m.eta_tables.assign(m.materials.size(), {});
+  for (size_t i = 0; i < m.materials.size(); ++i) {
+    const elp_material& mt = m.materials[i];
+    if (mt.n_E_table > 0 && mt.E_table) m.E_tables[i].assign(mt.E_table, mt.E_table + 2 * (size_t)mt.n_E_table);
+    if (mt.n_eta_table > 0 && mt.eta_table)
+      m.eta_tables[i].assign(mt.eta_table, mt.eta_table + 2 * (size_t)mt.n_eta_table);
+  }
   for (size_t i = 0; i < m.materials.size(); ++i) {
     elp_material& mt = m.materials[i];
     const bool any = mt.n_E_table > 0 || mt.n_eta_table > 0;

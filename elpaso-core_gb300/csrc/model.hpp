@@ -69,6 +69,7 @@ struct Model {
   std::vector<int64_t> node_ids;
   std::vector<double> coords;
   std::vector<elp_material> materials;
+  std::vector<std::vector<double>> E_tables, eta_tables;  // per material: the rows as given (f, value)
   std::vector<Block> blocks;
   std::vector<elp_interface_quad> interfaces;
   std::vector<elp_fixed_dof> fixed;
@@ -103,6 +104,14 @@ struct Model {
   // ---- structure loss-factor groups
   std::vector<StructGroup> groups;   // groups[0] -> VK, groups[g>0] -> VKg[g-1]
   std::vector<int> material_group;   // per material, -1 for fluid
+
+  // ---- a group of models solved together (elp_group): the member of each
+  // row and the first row of each member (a member's rows are contiguous and
+  // in its own order); empty for a single model
+  std::vector<int32_t> row_model;
+  std::vector<int64_t> member_row_off;  // n_members + 1
+  std::vector<double> member_f;         // per member: ||F||^2, 2 Re<F, G>, ||G||^2 of F(w) = F + G / w
+  int n_members = 1;
 
   int64_t n_elements_total = 0;
   bool assembled = false;

@@ -87,12 +87,61 @@ __global__ void k_add_vn(const double2* __restrict__ g, const Coef* __restrict__
   }
 }
 
+// A group's right-hand sides: F(w) = F + G / w of each member at its own
+// frequency of the slot, scaled to unit norm (fscale) so that the group's
+// residual bounds every member's relative residual (G may be null)
+__global__ void k_group_rhs(CombineArgs A, const double2* __restrict__ rhs, const double2* __restrict__ g,
+                            const Coef* __restrict__ coef, int64_t n, double2* __restrict__ f) {
+  const int s = blockIdx.y;
+  double2* fs = f + s * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const Coef& c = row_coef(A, coef, s, i);
+    double2 v = rhs[i];
+    if (g) {
+      const double2 t = g[i];
+      if (t.x != 0.0 || t.y != 0.0) v = make_double2(v.x + t.x * c.inv_w, v.y + t.y * c.inv_w);
+    }
+    fs[i] = make_double2(v.x * c.fscale, v.y * c.fscale);
+  }
+}
+
+// x of each group member back to its own right-hand side's scale
+__global__ void k_group_unscale(CombineArgs A, const Coef* __restrict__ coef, int64_t n, double2* __restrict__ x) {
+  const int s = blockIdx.y;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = 1.0 / row_coef(A, coef, s, i).fscale;
+    const double2 v = x[s * n + i];
+    x[s * n + i] = make_double2(v.x * d, v.y * d);
+  }
+}
+
+// ||r||^2 and ||f||^2 of each group member in each slot (its rows are
+// contiguous: [off[k], off[k + 1])), summed in a fixed order
+__global__ void k_member_norms(const int64_t* __restrict__ off, int nm, int64_t n, const double2* __restrict__ r,
+                               const double2* __restrict__ f, double* __restrict__ out) {
+  const int k = blockIdx.x, s = blockIdx.y;
+  double rr = 0.0, ff = 0.0;
+  for (int64_t i = off[k] + threadIdx.x; i < off[k + 1]; i += blockDim.x) {
+    const double2 a = r[s * n + i], b = f[s * n + i];
+    rr += a.x * a.x + a.y * a.y;
+    ff += b.x * b.x + b.y * b.y;
+  }
+  __shared__ double sr[256], sf[256];
+  sr[threadIdx.x] = rr;
+  sf[threadIdx.x] = ff;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o; o >>= 1) {
+    if ((int)threadIdx.x < o) { sr[threadIdx.x] += sr[threadIdx.x + o]; sf[threadIdx.x] += sf[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[2 * ((int64_t)s * nm + k)] = sr[0]; out[2 * ((int64_t)s * nm + k) + 1] = sf[0]; }
+}
+
 __global__ void k_dscale(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ diag,
                          int64_t n, double* __restrict__ dscale) {
   const int s = blockIdx.y;
-  const Coef c = coef[s];
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double2 v = combine(A, c, diag[i]);
+    double2 v = combine(A, row_coef(A, coef, s, i), diag[i]);
     double a = sqrt(v.x * v.x + v.y * v.y);
     dscale[s * n + i] = a > 0.0 ? 1.0 / sqrt(a) : 1.0;
   }
@@ -139,15 +188,15 @@ __global__ void k_scatter(CombineArgs A, const Coef* __restrict__ coef, const in
                           const int64_t* __restrict__ foff, const double* __restrict__ dscale, int64_t n,
                           V* __restrict__ pool, int64_t pool_size, unsigned long long* __restrict__ stats) {
   const int s = blockIdx.y;
-  const Coef c = coef[s];
   const double* d = dscale + s * n;
   V* F = pool + s * pool_size;
   double amax = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
     const int32_t q = order[t];
     if (A.cls[q] & CLS_BC_COLUMN) continue;
-    double2 v = combine(A, c, q);
-    const double sc = d[entry_row[q]] * d[col_idx[q]];
+    const int32_t i = entry_row[q];
+    double2 v = combine(A, row_coef(A, coef, s, i), q);
+    const double sc = d[i] * d[col_idx[q]];
     v.x *= sc;
     v.y *= sc;
     amax = fmax(amax, sqrt(v.x * v.x + v.y * v.y));
@@ -947,7 +996,6 @@ __global__ void k_residual(CombineArgs A, const Coef* __restrict__ coef, const i
                            int nparts, const int* __restrict__ active, int x_zero) {
   const int s = blockIdx.y;
   if (!active[s]) return;
-  const Coef c = coef[s];
   const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
   const double2* xs = x + s * n;
   double rr = 0.0, ff = 0.0;
@@ -957,7 +1005,8 @@ __global__ void k_residual(CombineArgs A, const Coef* __restrict__ coef, const i
   for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
     const int64_t i = base + lane / kRowLanes;
     DD sx{0.0, 0.0}, sy{0.0, 0.0};
-    if (i < n && !x_zero)
+    if (i < n && !x_zero) {
+      const Coef& c = row_coef(A, coef, s, i);
       for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
         double2 a = combine(A, c, q);
         double2 v = xs[col_idx[q]];
@@ -966,6 +1015,7 @@ __global__ void k_residual(CombineArgs A, const Coef* __restrict__ coef, const i
         dd_fma(sy, a.x, v.y);
         dd_fma(sy, a.y, v.x);
       }
+    }
     if (!x_zero) {
       sx = row_sum(sx);
       sy = row_sum(sy);
@@ -1038,7 +1088,7 @@ __global__ void k_rhs(CombineArgs A, const Coef* __restrict__ coef, const int32_
       for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
         if (!(A.cls[q] & CLS_BC_COLUMN)) continue;
         lift = true;
-        double2 a = combine(A, coef[s], q);
+        double2 a = combine(A, row_coef(A, coef, s, i), q);
         double2 v = rs[col_idx[q]];
         sx += a.x * v.x - a.y * v.y;
         sy += a.x * v.y + a.y * v.x;
@@ -1084,7 +1134,6 @@ __global__ void k_spmv(CombineArgs A, const Coef* __restrict__ coef, const int32
                        double2* __restrict__ w, const int* __restrict__ active) {
   const int s = blockIdx.y;
   if (!active[s]) return;
-  const Coef c = coef[s];
   const int lane = threadIdx.x & 31, sub = lane & (kRowLanes - 1);
   const double2* us = u + s * ustride;
   constexpr int RPW = 32 / kRowLanes;
@@ -1093,13 +1142,15 @@ __global__ void k_spmv(CombineArgs A, const Coef* __restrict__ coef, const int32
   for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
     const int64_t i = base + lane / kRowLanes;
     double sx = 0.0, sy = 0.0;
-    if (i < n)
+    if (i < n) {
+      const Coef& c = row_coef(A, coef, s, i);
       for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
         double2 a = combine(A, c, q);
         double2 v = us[col_idx[q]];
         sx += a.x * v.x - a.y * v.y;
         sy += a.x * v.y + a.y * v.x;
       }
+    }
     sx = row_sum(sx);
     sy = row_sum(sy);
     if (i < n && sub == 0) w[s * n + i] = make_double2(sx, sy);
@@ -1224,6 +1275,7 @@ Workspace::~Workspace() {
   if (h_active) cudaFreeHost(h_active);
   if (h_stats) cudaFreeHost(h_stats);
   if (h_flag) cudaFreeHost(h_flag);
+  if (h_mnorms) cudaFreeHost(h_mnorms);
   if (h_h) cudaFreeHost(h_h);
   if (h_y) cudaFreeHost(h_y);
   if (h_scal) cudaFreeHost(h_scal);
@@ -1236,6 +1288,7 @@ Workspace::~Workspace() {
 void make_coef(const Model& m, double w, Coef& c) {
   memset(&c, 0, sizeof(c));
   c.inv_w = 1.0 / w;
+  c.fscale = 1.0;
   cplx c0 = group_coefficient(m.groups[0], w);
   c.a[CLS_STRUCT] = make_double2(c0.real(), c0.imag());
   c.b[CLS_STRUCT] = -w * w;
@@ -1433,7 +1486,8 @@ int64_t workspace_bytes(const Model& m, int precision, int slots, int store) {
   const int64_t fronts = store == STORE_COMPACT ? D.arena + D.fac : D.arena_full;  // pool + factors, or whole fronts
   int64_t b = S * (fronts + std::max<int64_t>(1, D.cb_total) + 2 * n) * elem;          // fronts, cb, z, tb
   b += S * n * (4 + 8 + 3 * 16);                                               // perm, dscale, x, r, f
-  b += S * (int64_t)(sizeof(Coef) + 16 + nparts * 16 + 4 + 32) + 4;            // coef, norms, partials, flags
+  b += S * (int64_t)(sizeof(Coef) * m.n_members + 16 + nparts * 16 + 4 + 32) + 4;  // coef, norms, partials, flags
+  if (m.n_members > 1) b += S * m.n_members * 16;                                   // member norms
   b += max_count * S * swapmap_ints<32>() * 4;
   if (precision == ELP_MIXED) {
     b += S * D.pack_max;
@@ -1508,7 +1562,9 @@ static int workspace_alloc(Model& m, Workspace& w, int precision, int slots, int
   ELP_CUDA(w.x.alloc((size_t)slots * n));
   ELP_CUDA(w.r.alloc((size_t)slots * n));
   ELP_CUDA(w.f.alloc((size_t)slots * n));
-  ELP_CUDA(w.coef.alloc(slots));
+  const int nm = m.n_members;
+  ELP_CUDA(w.coef.alloc((size_t)slots * nm));
+  if (nm > 1) ELP_CUDA(w.mnorms.alloc((size_t)slots * nm * 2));
   ELP_CUDA(w.norms.alloc(2 * (size_t)slots));
   w.nparts = (int)std::min<int64_t>(1024, (n + 255) / 256);
   ELP_CUDA(w.partial.alloc((size_t)slots * w.nparts * 2));
@@ -1522,7 +1578,8 @@ static int workspace_alloc(Model& m, Workspace& w, int precision, int slots, int
   ELP_CUDA(w.tc_err.alloc(1));
   ELP_CUDA(cudaMemset(w.tc_err.p, 0, sizeof(int)));
   if (precision == ELP_MIXED && D.pack_max > 0) ELP_CUDA(w.pack.alloc((size_t)slots * D.pack_max));
-  ELP_CUDA(cudaMallocHost((void**)&w.h_coef, sizeof(Coef) * slots));
+  ELP_CUDA(cudaMallocHost((void**)&w.h_coef, sizeof(Coef) * slots * nm));
+  if (nm > 1) ELP_CUDA(cudaMallocHost((void**)&w.h_mnorms, sizeof(double) * 2 * slots * nm));
   ELP_CUDA(cudaMallocHost((void**)&w.h_norms, sizeof(double) * 2 * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_active, sizeof(int) * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_stats, sizeof(unsigned long long) * 4 * slots));
@@ -1540,6 +1597,8 @@ CombineArgs combine_args(const Model& m) {
   A.cls = m.dev->cls.p;
   A.nnz = m.nnz;
   A.ngroups = (int)std::min<size_t>(m.groups.size(), kMaxGroups);
+  A.row_model = m.n_members > 1 ? m.dev->row_model.p : nullptr;
+  A.n_members = m.n_members;
   return A;
 }
 
@@ -2119,17 +2178,43 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
   Workspace& w = lane ? *m.ws_b[precision][lane - 1] : *m.ws[precision];
   cudaStream_t st = stream ? stream : w.stream;
   const int64_t n = m.n;
-  for (int s = 0; s < n_omega; ++s) make_coef(m, omegas[s], w.h_coef[s]);
-  ELP_CUDA(cudaMemcpyAsync(w.coef.p, w.h_coef, sizeof(Coef) * n_omega, cudaMemcpyHostToDevice, st));
-  for (int s = 0; s < n_omega; ++s) {
-    const double2* src = f_dev ? f_dev + (size_t)s * n : reinterpret_cast<const double2*>(m.dev->rhs.p);
-    ELP_CUDA(cudaMemcpyAsync(w.f.p + (size_t)s * n, src, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
-  }
-  if (!f_dev && m.has_vn) {  // the model's F(w) = F + G / w
+  const int nm = m.n_members;  // a group: one coefficient table (and frequency) per member and slot
+  const bool group = nm > 1;
+  if (group && f_dev) { set_error("a group solves its members' own right-hand sides"); return ELP_ERR_ARG; }
+  int nonzero = 0;  // group members with a nonzero right-hand side
+  for (int s = 0; s < n_omega; ++s)
+    for (int k = 0; k < nm; ++k) {
+      const double om = omegas[(int64_t)s * nm + k];
+      Coef& c = w.h_coef[(int64_t)s * nm + k];
+      make_coef(m, om, c);
+      if (group) {  // F_k(w) to unit norm: the group's residual then bounds each member's
+        const double* q = &m.member_f[3 * k];
+        const double f2 = q[0] + q[1] / om + q[2] / (om * om);
+        c.fscale = f2 > 0.0 ? 1.0 / std::sqrt(f2) : 1.0;
+        if (s == 0 && f2 > 0.0) ++nonzero;
+      }
+    }
+  ELP_CUDA(cudaMemcpyAsync(w.coef.p, w.h_coef, sizeof(Coef) * n_omega * nm, cudaMemcpyHostToDevice, st));
+  if (group) {
     const dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 1024), n_omega);
-    PROF_LAUNCH(KC_RHS, st, k_add_vn<<<g, 256, 0, st>>>(reinterpret_cast<const double2*>(m.dev->rhs_vn.p), w.coef.p, n,
-                                                        w.f.p));
+    PROF_LAUNCH(KC_RHS, st, k_group_rhs<<<g, 256, 0, st>>>(
+                                combine_args(m), reinterpret_cast<const double2*>(m.dev->rhs.p),
+                                m.has_vn ? reinterpret_cast<const double2*>(m.dev->rhs_vn.p) : nullptr, w.coef.p, n,
+                                w.f.p));
+    // ||r|| <= tol / sqrt(K) over the group bounds every member's ||r_k|| / ||f_k|| by tol
+    tol /= std::sqrt((double)std::max(1, nonzero));
+  } else {
+    for (int s = 0; s < n_omega; ++s) {
+      const double2* src = f_dev ? f_dev + (size_t)s * n : reinterpret_cast<const double2*>(m.dev->rhs.p);
+      ELP_CUDA(cudaMemcpyAsync(w.f.p + (size_t)s * n, src, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+    }
+    if (!f_dev && m.has_vn) {  // the model's F(w) = F + G / w
+      const dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 1024), n_omega);
+      PROF_LAUNCH(KC_RHS, st, k_add_vn<<<g, 256, 0, st>>>(reinterpret_cast<const double2*>(m.dev->rhs_vn.p), w.coef.p,
+                                                          n, w.f.p));
+    }
   }
+  const double tol_member = group ? tol * std::sqrt((double)std::max(1, nonzero)) : tol;
   // the tensor-core timeout flag reports this batch only
   ELP_CUDA(cudaMemsetAsync(w.tc_err.p, 0, sizeof(int), st));
   int iters = 0;
@@ -2137,6 +2222,14 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
   if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 12, st, ms);
   else rc = run_batch<double>(m, w, n_omega, tol, 8, st, &iters, ms);
   if (rc) return rc;
+  if (group) {  // each member's own residual, then its solution at its own scale
+    PROF_LAUNCH(KC_NORMS, st, k_member_norms<<<dim3(nm, n_omega), 256, 0, st>>>(m.dev->member_off.p, nm, n, w.r.p,
+                                                                                  w.f.p, w.mnorms.p));
+    const dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 1024), n_omega);
+    PROF_LAUNCH(KC_UPDATE, st, k_group_unscale<<<g, 256, 0, st>>>(combine_args(m), w.coef.p, n, w.x.p));
+    ELP_CUDA(cudaMemcpyAsync(w.h_mnorms, w.mnorms.p, sizeof(double) * 2 * n_omega * nm, cudaMemcpyDeviceToHost, st));
+    tol = tol_member;
+  }
   if (x_dev) ELP_CUDA(cudaMemcpyAsync(x_dev, w.x.p, sizeof(double2) * n * n_omega, cudaMemcpyDeviceToDevice, st));
   ELP_CUDA(cudaMemcpyAsync(w.h_stats, w.stats.p, sizeof(unsigned long long) * 4 * n_omega, cudaMemcpyDeviceToHost, st));
   int tcerr = 0;
@@ -2148,16 +2241,18 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
     return ELP_ERR_CUDA;
   }
   bool ok = true, singular = false;
-  for (int s = 0; s < n_omega; ++s) {
-    double fn = w.h_norms[2 * s + 1];
-    double rel = fn > 0 ? std::sqrt(w.h_norms[2 * s] / fn) : std::sqrt(w.h_norms[2 * s]);
+  for (int sk = 0; sk < n_omega * nm; ++sk) {
+    const int s = sk / nm;  // slot; a group reports each member (info[s * nm + k])
+    const double* nr = group ? w.h_mnorms + 2 * sk : w.h_norms + 2 * s;
+    double fn = nr[1];
+    double rel = fn > 0 ? std::sqrt(nr[0] / fn) : std::sqrt(nr[0]);
     if (!(rel <= tol)) {
       ok = false;
       // a zero pivot the static-pivot floor stood in for, and the refinement could not recover
       if (w.h_stats[4 * s + 0] > 0) singular = true;
     }
     if (info) {
-      elp_solve_info& I = info[s];
+      elp_solve_info& I = info[sk];
       I.rel_residual = rel;
       double umax, amax;
       unsigned long long b1 = w.h_stats[4 * s + 1], b3 = w.h_stats[4 * s + 3];
@@ -2190,7 +2285,7 @@ int numeric_solve_lane(Model& m, int precision, int lane, const double* omegas, 
   if (n_omega <= 0) return ELP_OK;
   if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
   if (lane < 0 || lane > 3) { set_error("workspace lane out of range"); return ELP_ERR_ARG; }
-  for (int s = 0; s < n_omega; ++s)
+  for (int64_t s = 0; s < (int64_t)n_omega * m.n_members; ++s)
     if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
   return solve_lane(m, precision, lane, omegas, n_omega, f_dev, x_dev, info, tol, stream, store);
 }
@@ -2232,7 +2327,8 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
                         int max_lanes, int store) {
   if (n_omega <= 0) return ELP_OK;
   if (n_omega > kMaxSlots) { set_error("batch larger than the slot limit"); return ELP_ERR_ARG; }
-  for (int s = 0; s < n_omega; ++s)
+  const int nm = m.n_members;  // a group: omegas and info hold one entry per member and slot
+  for (int64_t s = 0; s < (int64_t)n_omega * nm; ++s)
     if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
   static const int lanes_env = [] {
     const char* e = getenv("ELP_LANES");
@@ -2266,8 +2362,8 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
     try {
       cudaSetDevice(dev);
       const int a = first[l], c = first[l + 1] - first[l];
-      rcs[l] = solve_lane(m, precision, l, omegas + a, c, f_dev ? f_dev + (size_t)a * n : nullptr,
-                          x_dev + (size_t)a * n, info ? info + a : nullptr, tol, nullptr, store);
+      rcs[l] = solve_lane(m, precision, l, omegas + (size_t)a * nm, c, f_dev ? f_dev + (size_t)a * n : nullptr,
+                          x_dev + (size_t)a * n, info ? info + (size_t)a * nm : nullptr, tol, nullptr, store);
     } catch (const std::exception& e) {
       rcs[l] = ELP_ERR_CUDA;
       set_error(std::string("solve lane: ") + e.what());

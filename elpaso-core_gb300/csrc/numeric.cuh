@@ -18,6 +18,7 @@ struct Coef {
   double b[3];                   // coefficient of VM
   double2 g[kMaxGroups];         // coefficient of VKg[g - 1] (g >= 1) on structure entries
   double inv_w;                  // 1 / w: weight of the normal-velocity loads in F(w)
+  double fscale;                 // a group member's right-hand side is scaled by this (1 / ||F(w)||); 1 otherwise
 };
 
 // the w-independent value arrays of a model and the per-w combine
@@ -28,11 +29,21 @@ struct CombineArgs {
   const uint8_t* cls;
   int64_t nnz;
   int ngroups;
+  // a group of models (elp_group): each row's member; the coefficient table of
+  // slot s and member k is coef[s * n_members + k]. Null for a single model.
+  const int32_t* row_model;
+  int n_members;
 };
 
 CombineArgs combine_args(const Model& m);
 
 #ifdef __CUDACC__
+// the coefficients of slot s that apply to row i
+__device__ __forceinline__ const Coef& row_coef(const CombineArgs& A, const Coef* __restrict__ coef, int s,
+                                                int64_t i) {
+  return A.row_model ? coef[(int64_t)s * A.n_members + A.row_model[i]] : coef[s];
+}
+
 // A(w) at CSR entry q, Dirichlet rows included (MatZeroRows, diag = 1)
 __device__ __forceinline__ double2 combine(const CombineArgs& A, const Coef& c, int64_t q) {
   const uint8_t k = A.cls[q] & CLS_MASK;
@@ -200,6 +211,8 @@ struct Workspace {
   int* h_active = nullptr;
   unsigned long long* h_stats = nullptr;
   int* h_flag = nullptr;          // pinned: tc_err read back after the factorisation
+  DevBuf<double> mnorms;          // a group: slots x members x (||r||^2, ||f||^2)
+  double* h_mnorms = nullptr;     // pinned copy
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   int nparts = 0;

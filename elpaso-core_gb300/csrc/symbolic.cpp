@@ -162,15 +162,33 @@ int symbolic_analyse(const Model& m, Symbolic& S, int leaf_dofs) {
     std::vector<int32_t>().swap(nb[v]);
   }
 
-  // ---- nested dissection
+  // ---- nested dissection, per connected component of the node graph (the
+  // members of a group, disconnected bodies): each gets its own subtree, so
+  // no separator front mixes unconnected parts however their coordinates lie
   Builder B(m, g, leaf_dofs);
   B.first_row = first_row;
   B.ndof = ndof;
   B.mark.assign(N, 0);
-  std::vector<int32_t> all;
-  for (int64_t v = 0; v < N; ++v)
-    if (ndof[v] > 0) all.push_back((int32_t)v);
-  std::vector<int32_t> roots = B.nd(all);
+  {
+    std::vector<int32_t> comp(N, -1), stack;
+    int nc = 0;
+    for (int64_t v0 = 0; v0 < N; ++v0) {
+      if (ndof[v0] == 0 || comp[v0] >= 0) continue;
+      comp[v0] = nc;
+      stack.assign(1, (int32_t)v0);
+      while (!stack.empty()) {
+        const int32_t v = stack.back();
+        stack.pop_back();
+        for (int64_t q = g.ptr[v]; q < g.ptr[v + 1]; ++q)
+          if (comp[g.adj[q]] < 0) { comp[g.adj[q]] = nc; stack.push_back(g.adj[q]); }
+      }
+      ++nc;
+    }
+    std::vector<std::vector<int32_t>> parts(nc);
+    for (int64_t v = 0; v < N; ++v)
+      if (ndof[v] > 0) parts[comp[v]].push_back((int32_t)v);
+    for (auto& part : parts) B.nd(part);
+  }
   const int T = (int)B.tnodes.size();
 
   // ---- elimination order

@@ -325,6 +325,34 @@ int elp_model_time_assembly(elp_model* m, int repeats, double* ms_per_assembly,
 int elp_residual_noalloc(elp_model* m, const double* omegas, int n_omega, const double* f_dev,
                          const double* x_dev, double* r_dev, double* rel_residual_out, void* stream);
 
+/* ---- groups of models: frontal updates grouped across models ----------- */
+
+/* No reference counterpart (elpasoC solves one model per process). A group
+ * solves several models together as ONE system, their disjoint union, so
+ * that each tree level of the multifrontal factorisation is one launch over
+ * the fronts of every member, and every member's elements are integrated in
+ * one pass: many small models keep the GPU busy instead of leaving it idle
+ * between their own small launches. Each member keeps its own frequencies,
+ * its own right-hand side (its F(w), as elp_solve with f == NULL) and its own
+ * numbering; results and infos are reported per member. The members are
+ * copied at creation (the group does not refer to them later); their
+ * loss-factor groups are merged by value, at most 8 distinct in a group.
+ * Refinement runs the group to ||r|| / ||f|| <= tol / sqrt(K) with every
+ * member's load scaled to unit norm (K members with a nonzero load), which
+ * bounds each member's own relative residual by tol; that residual is
+ * measured on the member's own rows and reported in its info. */
+typedef struct elp_group elp_group;
+int elp_group_create(elp_model* const* models, int n_models, elp_group** out);
+/* Sizes of the combined system (n_dofs, nnz, fronts, ... of all members). */
+int elp_group_info(const elp_group* g, elp_model_info* info);
+/* omegas: n_models x n_omega angular frequencies, member-major (member k's
+ * at omegas[k * n_omega + j]); x_out: member k's n_omega x n_k solutions
+ * (complex interleaved) after the earlier members' blocks; info (may be
+ * NULL): n_models x n_omega, member-major. Status as elp_solve. */
+int elp_group_solve(elp_group* g, const double* omegas, int n_omega, int precision, double* x_out,
+                    elp_solve_info* info, double tol);
+int elp_group_destroy(elp_group* g);
+
 /* ---- fault injection for failure-path tests ---------------------------- */
 
 /* No counterpart in the reference. Arms one host-side fault, made on the host

@@ -1,11 +1,13 @@
-"""The two front stores of a factorisation give the same solutions, bit for
-bit: whole fronts (STORE_FULL, the solves read the factors in place) and the
+"""The two front stores of a factorisation give the same solutions: whole fronts (STORE_FULL, the solves read the factors in place) and the
 compact store (STORE_COMPACT: full fronts only while a level is factorised,
 in reused pool regions; each level's m x p panel and U12 copied into a
 factor store the solves read, U12 with leading dimension p). The arithmetic
 and its order are the same, only the factors' addresses differ. The store
 is chosen by memory unless ELP_FACTOR_STORE forces one; it is read once per
-process, so each store runs in its own process. Models: the coupled
+process, so each store runs in its own process -- and two processes assemble
+A(w) with FP64 atomic additions in different orders, which moves its values
+by ~1e-16 relative and the solutions by ~1e-13. The bar is therefore
+rounding level: max |x_full - x_compact| <= 1e-11 max |x_full| per solution. Models: the coupled
 plate-cavity (fluid, coupling, Dirichlet rows; the packed tensor-core Schur
 levels forced on every level with ELP_TC_PACK=all) and a Brick8 cube, both
 precisions."""
@@ -56,4 +58,5 @@ def test_compact_factor_store_equals_whole_fronts(pack):
         xf, resf = full[key]
         xc, resc = compact[key]
         assert max(resf) <= 1e-10 and max(resc) <= 1e-10, key
-        assert np.array_equal(np.asarray(xf), np.asarray(xc)), key
+        xf, xc = np.asarray(xf), np.asarray(xc)
+        assert np.max(np.abs(xf - xc)) <= 1e-11 * np.max(np.abs(xf)), key

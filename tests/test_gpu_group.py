@@ -1,0 +1,70 @@
+"""Groups of models solved together (elp_group_*), against the oracle.
+
+A group is its members' disjoint union: one launch per tree level over the
+fronts of all members, each member at its own frequencies. Bars, per member
+and frequency, as for single models: ||f - A x||_2 / ||f||_2 <= 1e-10 with
+the oracle's matrix of that member, the error against the oracle's FP64
+solve within 3 kappa_1(A_ff) (res_1 + res_ref_1), and the reported residual
+equal to the one measured here. A group of one model takes the single-model
+path and equals the model solved alone bit for bit.
+"""
+import numpy as np
+import pytest
+
+from test_gpu_solve import cond1
+
+pytestmark = pytest.mark.gpu
+
+
+def _members(meshes):
+    return [meshes.plate(12, 9, 0.3, 0.2, 0.002), meshes.plate(30, 22, 0.6, 0.4, 0.003, seed=7),
+            meshes.cube(5), meshes.plate_cavity(8, 6, 4, 0.6, 0.4, 0.3), meshes.solid_plate(8, 6, 2)]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_group_members_match_the_oracle(elp, meshes, oracle, prec):
+    ds = _members(meshes)
+    g = elp.Group([elp.Model(d) for d in ds])
+    rng = np.random.default_rng(31 + prec)
+    oms = 2 * np.pi * rng.uniform(5.0, 480.0, size=(len(ds), 4))
+    xs, infos = g.solve(oms, precision=prec)
+    for k, d in enumerate(ds):
+        s = oracle.System(d)
+        for j, om in enumerate(oms[k]):
+            A, f = s.matrix(om), s.rhs(om)
+            x = xs[k][j]
+            res = np.linalg.norm(f - A @ x) / np.linalg.norm(f)
+            assert res <= 1e-10, (k, j, res)
+            assert abs(infos[k][j]["rel_residual"] - res) <= 1e-11 + 1e-3 * res, (k, j, infos[k][j], res)
+            assert infos[k][j]["converged"] == 1
+            xr = s.solve(om)
+            n1 = np.linalg.norm(f, 1)
+            res1 = np.linalg.norm(f - A @ x, 1) / n1
+            res_ref1 = np.linalg.norm(f - A @ xr, 1) / n1
+            err = np.linalg.norm(x - xr, 1) / np.linalg.norm(xr, 1)
+            assert err <= max(1e-13, 3.0 * cond1(s.free_block(om)[0]) * (res1 + res_ref1)), (k, j, err)
+
+
+def test_group_of_one_equals_the_model_alone(elp, meshes):
+    d = meshes.plate(16, 12, 0.6, 0.4, 0.002)
+    oms = 2 * np.pi * np.array([13.0, 170.0, 333.0])
+    xa, _ = elp.Model(d).assemble().analyse().solve(oms, precision=1)
+    xg, _ = elp.Group([elp.Model(d)]).solve(oms[None, :], precision=1)
+    assert np.array_equal(xa, xg[0])
+
+
+def test_group_of_many_plates(elp, meshes, oracle):
+    """Forty plates of 363-3,468 DOFs, 8 frequencies each: the grouped launch
+    covers fronts of many sizes; a sample of members is checked against the
+    oracle."""
+    ds = meshes.batched_plates(40, lo=10, hi=33)
+    g = elp.Group([elp.Model(d) for d in ds])
+    rng = np.random.default_rng(4)
+    oms = 2 * np.pi * rng.uniform(10.0, 400.0, size=(len(ds), 8))
+    xs, infos = g.solve(oms, precision=1, raise_on_noconv=False)
+    assert all(i["converged"] == 1 for row in infos for i in row)
+    for k in (0, 7, 23, 39):
+        s = oracle.System(ds[k])
+        for j in (0, 5):
+            A, f = s.matrix(oms[k][j]), s.rhs(oms[k][j])
+            assert np.linalg.norm(f - A @ xs[k][j]) / np.linalg.norm(f) <= 1e-10

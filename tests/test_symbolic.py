@@ -120,3 +120,20 @@ def test_factor_store_and_front_pool_sizes(elp, meshes, name):
     assert 0 < i["factor_stored"] < i["factor_entries"]
     assert i["front_pool_peak"] <= i["front_pool"] <= i["factor_entries"]
     assert i["front_pool"] <= 1.25 * i["front_pool_peak"]  # first-fit wastes little on these trees
+
+
+def test_group_keeps_each_members_tree(elp, meshes):
+    """A group is the disjoint union of its members: the symbolic phase splits
+    it into connected components first, so its fronts, factor entries and
+    flops are exactly the sums of the members' own, whatever the members'
+    coordinates (here all overlap at the origin)."""
+    ds = [meshes.plate(12, 9, 0.3, 0.2, 0.002), meshes.plate(20, 15, 0.6, 0.4, 0.003), meshes.cube(4),
+          meshes.plate_cavity(6, 4, 3, 0.3, 0.2, 0.15)]
+    infos = [analysed(elp, d)[1] for d in ds]
+    ms = [elp.Model(d) for d in ds]
+    g = elp.Group(ms)
+    gi = g.info()
+    for key in ("n_dofs", "nnz", "n_elements", "n_fronts", "factor_entries", "factor_stored"):
+        assert gi[key] == sum(i[key] for i in infos), key
+    assert gi["factor_flops"] == pytest.approx(sum(i["factor_flops"] for i in infos), rel=1e-12)
+    assert gi["n_levels"] == max(i["n_levels"] for i in infos)
