@@ -129,6 +129,15 @@ class ServerConfig(C.Structure):
                 ("tol", C.c_double), ("omega_batch", C.c_int)]
 
 
+class Tuning(C.Structure):
+    """elp_tuning: leaf, schur_tile, pack_count, pack_min_border, lanes (0 / negative: default)."""
+    _fields_ = [("leaf", C.c_int), ("schur_tile", C.c_int), ("pack_count", C.c_int),
+                ("pack_min_border", C.c_int), ("lanes", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class RequestResult(C.Structure):
     _fields_ = [("request_id", C.c_int64), ("status", C.c_int), ("n_omega", C.c_int),
                 ("latency_ms", C.c_double), ("max_rel_residual", C.c_double)]
@@ -143,6 +152,8 @@ EXPORTS = [
     "elp_server_create", "elp_server_add_model", "elp_server_submit", "elp_server_wait",
     "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc", "elp_fault_inject",
     "elp_front_update_test", "elp_group_create", "elp_group_info", "elp_group_solve", "elp_group_destroy",
+    "elp_model_set_tuning", "elp_model_get_tuning", "elp_model_autotune", "elp_group_set_tuning",
+    "elp_group_autotune",
 ]
 KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
                   "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc", "spmv", "fwd_border",
@@ -188,6 +199,13 @@ def load_library(path: str | None = None):
     lib.elp_group_info.argtypes = [P, C.POINTER(_Info)]
     lib.elp_group_solve.argtypes = [P, P, C.c_int, C.c_int, P, P, C.c_double]
     lib.elp_group_destroy.argtypes = [P]
+    lib.elp_model_set_tuning.argtypes = [P, C.POINTER(Tuning)]
+    lib.elp_model_get_tuning.argtypes = [P, C.POINTER(Tuning)]
+    lib.elp_model_autotune.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_int)]
+    lib.elp_group_set_tuning.argtypes = [P, C.POINTER(Tuning)]
+    lib.elp_group_autotune.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_int)]
     lib.elp_front_update_test.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P, P]
     lib.elp_profile.argtypes = [C.c_int]
     lib.elp_profile_read.argtypes = [P, P, P, C.POINTER(C.c_int)]
@@ -409,6 +427,25 @@ class Model:
         _check(self.lib.elp_node_stresses(self.handle, float(omega), _ptr(xs), _ptr(out)))
         return out
 
+    def set_tuning(self, **knobs):
+        """leaf, schur_tile, pack_count, pack_min_border, lanes (unset: default)."""
+        t = Tuning(**{k: int(v) for k, v in knobs.items()})
+        _check(self.lib.elp_model_set_tuning(self.handle, C.byref(t)))
+        return self
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        _check(self.lib.elp_model_get_tuning(self.handle, C.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, omegas, precision: int = MIXED):
+        """(chosen tuning, seconds of its timed solve, trials)."""
+        om = np.ascontiguousarray(np.atleast_1d(omegas), dtype=np.float64)
+        t, sec, n = Tuning(), C.c_double(), C.c_int()
+        _check(self.lib.elp_model_autotune(self.handle, _ptr(om), len(om), int(precision), C.byref(t), C.byref(sec),
+                                           C.byref(n)))
+        return t.as_dict(), sec.value, n.value
+
     def time_assembly(self, repeats: int = 3):
         a, b = C.c_double(), C.c_double()
         _check(self.lib.elp_model_time_assembly(self.handle, repeats, C.byref(a), C.byref(b)))
@@ -462,6 +499,19 @@ class Group:
         i = _Info()
         _check(self.lib.elp_group_info(self.handle, C.byref(i)))
         return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def set_tuning(self, **knobs):
+        t = Tuning(**{k: int(v) for k, v in knobs.items()})
+        _check(self.lib.elp_group_set_tuning(self.handle, C.byref(t)))
+        return self
+
+    def autotune(self, omegas, precision: int = MIXED):
+        """(chosen tuning, seconds of its timed solve, trials); omegas as for solve."""
+        om = np.ascontiguousarray(np.asarray(omegas, np.float64))
+        t, sec, n = Tuning(), C.c_double(), C.c_int()
+        _check(self.lib.elp_group_autotune(self.handle, _ptr(om), om.shape[1], int(precision), C.byref(t),
+                                           C.byref(sec), C.byref(n)))
+        return t.as_dict(), sec.value, n.value
 
     def solve(self, omegas, precision: int = MIXED, tol: float = 1e-10, raise_on_noconv: bool = True):
         """omegas: [n_models, n_omega] angular frequencies (each member its own).

@@ -25,14 +25,9 @@ int model_symbolic_host(Model& m) {
   if (m.sym) return ELP_OK;
   fault_host_alloc_point();
   std::unique_ptr<Symbolic> s(new Symbolic());
-  // leaves of the nested dissection: subsets of at most this many DOFs
-  // (ELP_LEAF, default 128)
-  static const int leaf = [] {
-    const char* e = getenv("ELP_LEAF");
-    const int v = e ? atoi(e) : 128;
-    return v < 8 ? 8 : v;
-  }();
-  int rc = symbolic_analyse(m, *s, leaf);
+  // leaves of the nested dissection: subsets of at most this many DOFs (the
+  // model's tuning; ELP_LEAF, default 128)
+  int rc = symbolic_analyse(m, *s, resolved_tuning(m).leaf);
   if (rc) return rc;
   if (getenv("ELP_PROF_LEVELS")) {  // per-level work, beside the per-level device times of the profiler
     const Symbolic& S = *s;

@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_gemm_tc(LevelArgs L, float2* 
                   if (jb8 + q < NC) cv[q] = dst0[(int64_t)q * m];
 #pragma unroll
                 for (int q = 0; q < 8; ++q) cv[q] = make_float2(cv[q].x - re[q], cv[q].y - im[q]);
-                if (NT == 64 && mode == GM_SCHUR && L.fuse) {  // only the 64-wide tiles run GM_SCHUR
+                if (mode == GM_SCHUR && L.fuse) {  // the Schur complement goes into the parent
                   add_into_parent<8>(L, arena, f, s, i, jb8, NC, cv);  // border (i, j) of the Schur complement
                 } else {
 #pragma unroll

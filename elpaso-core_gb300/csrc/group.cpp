@@ -165,6 +165,10 @@ int build_group(elp_model* const* models, int count, elp_group& g, std::string& 
 
 }  // namespace
 
+namespace elp {
+Model& group_model(elp_group* g) { return g->combined.m; }
+}  // namespace elp
+
 #define GUARD_BEGIN try {
 #define GUARD_END                                      \
   }                                                    \

@@ -51,6 +51,18 @@ int dofs_per_node(int type);
 // reference getDofs(): Brick8 {x1,x2,x3}, DSG4 {x3,w1,w2}, Fluid8 {fluid}
 const int* element_dofs(int type);
 
+// Tuning of a model's factorisation (elp_model_set_tuning, elp_model_autotune).
+// A negative value (0 for the tile) takes the process default: the ELP_*
+// environment variable if set, else the built-in value measured best on the
+// coupled plate-cavity sweep.
+struct Tuning {
+  int leaf = -1;        // nested-dissection leaf size in DOFs (ELP_LEAF, 128)
+  int schur_tile = 0;   // columns of a converter-kernel Schur tile, 32 or 64 (64)
+  int pack_count = -1;  // packed Schur kernel on levels of at most this many fronts (ELP_PACK_COUNT, 300)
+  int pack_minb = -1;   // ... whose largest border has at least this many rows (ELP_PACK_MINB, 300)
+  int lanes = -1;       // workspace lanes a batch of 16+ frequencies is split over (ELP_LANES, 4)
+};
+
 struct Block {
   int type = 0;
   int material = 0;
@@ -112,6 +124,8 @@ struct Model {
   std::vector<int64_t> member_row_off;  // n_members + 1
   std::vector<double> member_f;         // per member: ||F||^2, 2 Re<F, G>, ||G||^2 of F(w) = F + G / w
   int n_members = 1;
+
+  Tuning tune;
 
   int64_t n_elements_total = 0;
   bool assembled = false;

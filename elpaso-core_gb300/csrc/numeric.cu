@@ -137,6 +137,17 @@ __global__ void k_member_norms(const int64_t* __restrict__ off, int nm, int64_t 
   if (threadIdx.x == 0) { out[2 * ((int64_t)s * nm + k)] = sr[0]; out[2 * ((int64_t)s * nm + k) + 1] = sf[0]; }
 }
 
+// residual rows of the group members that reached the tolerance set to zero:
+// A and the preconditioner are block diagonal, so those members' solutions
+// stop changing while the others go on
+__global__ void k_mask_members(const int32_t* __restrict__ row_model, const int* __restrict__ done, int nm,
+                               int64_t n, double2* __restrict__ r, const int* __restrict__ active) {
+  const int s = blockIdx.y;
+  if (!active[s]) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (done[(int64_t)s * nm + row_model[i]]) r[s * n + i] = make_double2(0.0, 0.0);
+}
+
 __global__ void k_dscale(CombineArgs A, const Coef* __restrict__ coef, const int32_t* __restrict__ diag,
                          int64_t n, double* __restrict__ dscale) {
   const int s = blockIdx.y;
@@ -1276,6 +1287,7 @@ Workspace::~Workspace() {
   if (h_stats) cudaFreeHost(h_stats);
   if (h_flag) cudaFreeHost(h_flag);
   if (h_mnorms) cudaFreeHost(h_mnorms);
+  if (h_mdone) cudaFreeHost(h_mdone);
   if (h_h) cudaFreeHost(h_h);
   if (h_y) cudaFreeHost(h_y);
   if (h_scal) cudaFreeHost(h_scal);
@@ -1398,7 +1410,7 @@ int device_upload_symbolic(Model& m) {
     }
     L.pack_bytes = off;
   }
-  D.pack_max = workspace_plan(S).pack_max;
+  D.pack_max = workspace_plan(m).pack_max;
   ELP_CUDA(D.pack_base.upload(pbase));
   ELP_CUDA(D.new_list.upload(nl));
   ELP_CUDA(D.level_list.upload(ll));
@@ -1447,7 +1459,31 @@ int pack_min_border() {
 
 constexpr int kGmresRestart = 24;  // GMRES(24) of the mixed path
 
-WorkspacePlan workspace_plan(const Symbolic& S) {
+Tuning resolved_tuning(const Model& m) {
+  static const int leaf_env = [] {
+    const char* e = getenv("ELP_LEAF");
+    const int v = e ? atoi(e) : 128;
+    return v < 8 ? 8 : v;
+  }();
+  static const int lanes_env = [] {
+    const char* e = getenv("ELP_LANES");
+    int v = e ? atoi(e) : 4;
+    return v < 1 ? 1 : v > 4 ? 4 : v;
+  }();
+  Tuning t = m.tune;
+  if (t.leaf < 0) t.leaf = leaf_env;
+  t.leaf = std::max(8, t.leaf);
+  if (t.schur_tile != 32) t.schur_tile = 64;
+  if (t.pack_count < 0) t.pack_count = pack_max_count();
+  if (t.pack_minb < 0) t.pack_minb = pack_min_border();
+  if (t.lanes < 1) t.lanes = lanes_env;
+  t.lanes = std::min(4, t.lanes);
+  return t;
+}
+
+WorkspacePlan workspace_plan(const Model& m) {
+  const Symbolic& S = *m.sym;
+  const Tuning tn = resolved_tuning(m);
   WorkspacePlan P;
   P.arena = S.pool;
   P.arena_full = S.arena;
@@ -1467,7 +1503,7 @@ WorkspacePlan workspace_plan(const Symbolic& S) {
       }
     }
     P.max_count = std::max<int64_t>(P.max_count, L.count);
-    if (pack_all_levels || packed_schur_level(L)) P.pack_max = std::max(P.pack_max, off);
+    if (pack_all_levels || packed_schur_level(L, tn)) P.pack_max = std::max(P.pack_max, off);
   }
   return P;
 }
@@ -1478,7 +1514,7 @@ WorkspacePlan workspace_plan(const Symbolic& S) {
 // host symbolic phase (no device allocation has to happen first).
 int64_t workspace_bytes(const Model& m, int precision, int slots, int store) {
   if (!m.sym) return 0;
-  const WorkspacePlan D = workspace_plan(*m.sym);
+  const WorkspacePlan D = workspace_plan(m);
   const int64_t n = m.n, S = slots;
   const int64_t elem = precision == ELP_MIXED ? sizeof(float2) : sizeof(double2);
   const int64_t nparts = std::min<int64_t>(1024, (n + 255) / 256);
@@ -1487,7 +1523,7 @@ int64_t workspace_bytes(const Model& m, int precision, int slots, int store) {
   int64_t b = S * (fronts + std::max<int64_t>(1, D.cb_total) + 2 * n) * elem;          // fronts, cb, z, tb
   b += S * n * (4 + 8 + 3 * 16);                                               // perm, dscale, x, r, f
   b += S * (int64_t)(sizeof(Coef) * m.n_members + 16 + nparts * 16 + 4 + 32) + 4;  // coef, norms, partials, flags
-  if (m.n_members > 1) b += S * m.n_members * 16;                                   // member norms
+  if (m.n_members > 1) b += S * m.n_members * 20;                                   // member norms, flags
   b += max_count * S * swapmap_ints<32>() * 4;
   if (precision == ELP_MIXED) {
     b += S * D.pack_max;
@@ -1564,7 +1600,10 @@ static int workspace_alloc(Model& m, Workspace& w, int precision, int slots, int
   ELP_CUDA(w.f.alloc((size_t)slots * n));
   const int nm = m.n_members;
   ELP_CUDA(w.coef.alloc((size_t)slots * nm));
-  if (nm > 1) ELP_CUDA(w.mnorms.alloc((size_t)slots * nm * 2));
+  if (nm > 1) {
+    ELP_CUDA(w.mnorms.alloc((size_t)slots * nm * 2));
+    ELP_CUDA(w.mdone.alloc((size_t)slots * nm));
+  }
   ELP_CUDA(w.norms.alloc(2 * (size_t)slots));
   w.nparts = (int)std::min<int64_t>(1024, (n + 255) / 256);
   ELP_CUDA(w.partial.alloc((size_t)slots * w.nparts * 2));
@@ -1579,7 +1618,10 @@ static int workspace_alloc(Model& m, Workspace& w, int precision, int slots, int
   ELP_CUDA(cudaMemset(w.tc_err.p, 0, sizeof(int)));
   if (precision == ELP_MIXED && D.pack_max > 0) ELP_CUDA(w.pack.alloc((size_t)slots * D.pack_max));
   ELP_CUDA(cudaMallocHost((void**)&w.h_coef, sizeof(Coef) * slots * nm));
-  if (nm > 1) ELP_CUDA(cudaMallocHost((void**)&w.h_mnorms, sizeof(double) * 2 * slots * nm));
+  if (nm > 1) {
+    ELP_CUDA(cudaMallocHost((void**)&w.h_mnorms, sizeof(double) * 2 * slots * nm));
+    ELP_CUDA(cudaMallocHost((void**)&w.h_mdone, sizeof(int) * slots * nm));
+  }
   ELP_CUDA(cudaMallocHost((void**)&w.h_norms, sizeof(double) * 2 * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_active, sizeof(int) * slots));
   ELP_CUDA(cudaMallocHost((void**)&w.h_stats, sizeof(unsigned long long) * 4 * slots));
@@ -1643,6 +1685,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   const int64_t n = m.n;
   V* arena = reinterpret_cast<V*>(w.arena.p);
   CombineArgs A = combine_args(m);
+  const Tuning tn = resolved_tuning(m);
   ELP_CUDA(cudaMemsetAsync(w.stats.p, 0, sizeof(unsigned long long) * 4 * S_used, st));
   {
     dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 4096), S_used);
@@ -1686,7 +1729,11 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
   auto gemm = [&](int mode, int k, int rows_c, int cols_c, const LevelArgs& L) {
     if (tc) {
       float2* fa = reinterpret_cast<float2*>(arena);
-      if (mode == GM_SCHUR) {
+      if (mode == GM_SCHUR && tn.schur_tile == 32) {  // narrower tiles: more CTAs on short borders
+        const int t = ((rows_c + 127) / 128) * ((cols_c + 31) / 32);
+        dim3 g(L.count, S_used, (unsigned)std::min(65535, t));
+        PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 32, false><<<g, kTcThreads, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
+      } else if (mode == GM_SCHUR) {
         const int t = ((rows_c + 127) / 128) * ((cols_c + 63) / 64);
         dim3 g(L.count, S_used, (unsigned)std::min(65535, t));
         PROF_LAUNCH(KC_GEMM_TC, st, k_gemm_tc<NB, 64, false><<<g, kTcThreads, kTcSmemBytes, st>>>(L, fa, k, mode, w.tc_err.p));
@@ -1763,7 +1810,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       // few, large fronts (the top of the tree): operands split into TF32 planes once,
       // then bulk-copied by the MMA kernel (k_schur_tc); below, the converter kernel wins
       // (128-wide tiles waste work on short borders and the pack pass does not pay off)
-      const bool packed = use_pack && w.pack.p && (pack_all || packed_schur_level(LV));
+      const bool packed = use_pack && w.pack.p && (pack_all || packed_schur_level(LV, tn));
       float2* fa = reinterpret_cast<float2*>(arena);
       uint32_t* pk = reinterpret_cast<uint32_t*>(w.pack.p);
       if (packed) {
@@ -1905,6 +1952,36 @@ static int solve_smem(const Model& m) {
   return rc;
 }
 
+// A group: each member's residual in the active slots; members at their
+// tolerance (w.tol_member) have their residual rows zeroed. rel[s] becomes the
+// norm of the rows still open relative to ||f|| of the slot, exactly 0 once
+// every member is done.
+static int group_mask(Model& m, Workspace& w, int S_used, cudaStream_t st, double* rel) {
+  const int nm = m.n_members;
+  const int64_t n = m.n;
+  PROF_LAUNCH(KC_NORMS, st, k_member_norms<<<dim3(nm, S_used), 256, 0, st>>>(m.dev->member_off.p, nm, n, w.r.p,
+                                                                                w.f.p, w.mnorms.p));
+  ELP_CUDA(cudaMemcpyAsync(w.h_mnorms, w.mnorms.p, sizeof(double) * 2 * S_used * nm, cudaMemcpyDeviceToHost, st));
+  ELP_CUDA(cudaStreamSynchronize(st));
+  for (int s = 0; s < S_used; ++s) {
+    double open = 0.0, ff = 0.0;
+    for (int k = 0; k < nm; ++k) {
+      const double rr = w.h_mnorms[2 * (s * nm + k)], fk = w.h_mnorms[2 * (s * nm + k) + 1];
+      const double mrel = fk > 0 ? std::sqrt(rr / fk) : std::sqrt(rr);
+      const int done = mrel <= w.tol_member ? 1 : 0;
+      w.h_mdone[s * nm + k] = done;
+      if (!done) open += rr;
+      ff += fk;
+    }
+    if (w.h_active[s]) rel[s] = open == 0.0 ? 0.0 : (ff > 0 ? std::sqrt(open / ff) : std::sqrt(open));
+  }
+  ELP_CUDA(cudaMemcpyAsync(w.mdone.p, w.h_mdone, sizeof(int) * S_used * nm, cudaMemcpyHostToDevice, st));
+  const dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 1024), S_used);
+  PROF_LAUNCH(KC_KRYLOV, st, k_mask_members<<<g, 256, 0, st>>>(m.dev->row_model.p, w.mdone.p, nm, n, w.r.p,
+                                                                w.active.p));
+  return ELP_OK;
+}
+
 template <class R>
 static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_iter, cudaStream_t st,
                      int* iters, float* ms) {
@@ -1948,11 +2025,17 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
     refine_ms += b;
     bool all = true, changed = false;
     static const bool trace = getenv("ELP_TRACE") != nullptr;
+    std::vector<double> grel(S_used, 0.0);
+    if (m.n_members > 1) {  // a group: members at their tolerance stop changing
+      rc = group_mask(m, w, S_used, st, grel.data());
+      if (rc) return rc;
+    }
     for (int s = 0; s < S_used; ++s) {
       if (!w.h_active[s]) continue;
       w.iters[s]++;
       double fn = w.h_norms[2 * s + 1];
       double rel = fn > 0 ? std::sqrt(w.h_norms[2 * s] / fn) : std::sqrt(w.h_norms[2 * s]);
+      if (m.n_members > 1) rel = grel[s];
       if (trace) fprintf(stderr, "[elp] it %d slot %d rel_residual %.3e\n", it, s, rel);
       if (rel <= tol || !std::isfinite(rel)) { w.h_active[s] = 0; changed = true; }
       else all = false;
@@ -2034,6 +2117,8 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
       fn[s] = std::sqrt(w.h_norms[2 * s + 1]);
       rel[s] = fn[s] > 0 ? std::sqrt(w.h_norms[2 * s]) / fn[s] : std::sqrt(w.h_norms[2 * s]);
     }
+    // a group: members at their tolerance stop changing; rel is the open rows' residual
+    if (m.n_members > 1) return group_mask(m, w, S_used, st, rel.data());
     return ELP_OK;
   };
   auto precond = [&](const double2* src, int64_t sstride, const int* mask) -> int {
@@ -2190,7 +2275,8 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
       if (group) {  // F_k(w) to unit norm: the group's residual then bounds each member's
         const double* q = &m.member_f[3 * k];
         const double f2 = q[0] + q[1] / om + q[2] / (om * om);
-        c.fscale = f2 > 0.0 ? 1.0 / std::sqrt(f2) : 1.0;
+        // a power of two near 1 / ||F_k(w)||: scaling and unscaling are exact
+        c.fscale = f2 > 0.0 ? std::exp2(-std::round(std::log2(std::sqrt(f2)))) : 1.0;
         if (s == 0 && f2 > 0.0) ++nonzero;
       }
     }
@@ -2201,8 +2287,11 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
                                 combine_args(m), reinterpret_cast<const double2*>(m.dev->rhs.p),
                                 m.has_vn ? reinterpret_cast<const double2*>(m.dev->rhs_vn.p) : nullptr, w.coef.p, n,
                                 w.f.p));
-    // ||r|| <= tol / sqrt(K) over the group bounds every member's ||r_k|| / ||f_k|| by tol
-    tol /= std::sqrt((double)std::max(1, nonzero));
+    // every scaled ||f_k|| lies in [1/sqrt 2, sqrt 2], so ||r|| / ||f|| <= tol / (2 sqrt K)
+    // over the group bounds each member's ||r_k|| / ||f_k|| by tol; members that
+    // reach tol on their own are frozen on the way (group_mask)
+    w.tol_member = tol;
+    tol /= 2.0 * std::sqrt((double)std::max(1, nonzero));
   } else {
     for (int s = 0; s < n_omega; ++s) {
       const double2* src = f_dev ? f_dev + (size_t)s * n : reinterpret_cast<const double2*>(m.dev->rhs.p);
@@ -2214,7 +2303,7 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
                                                           n, w.f.p));
     }
   }
-  const double tol_member = group ? tol * std::sqrt((double)std::max(1, nonzero)) : tol;
+  const double tol_member = group ? w.tol_member : tol;
   // the tensor-core timeout flag reports this batch only
   ELP_CUDA(cudaMemsetAsync(w.tc_err.p, 0, sizeof(int), st));
   int iters = 0;
@@ -2222,7 +2311,13 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
   if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 12, st, ms);
   else rc = run_batch<double>(m, w, n_omega, tol, 8, st, &iters, ms);
   if (rc) return rc;
-  if (group) {  // each member's own residual, then its solution at its own scale
+  if (group) {  // each member's own true residual (no rows masked), then its solution at its own scale
+    for (int s = 0; s < n_omega; ++s) w.h_active[s] = 1;
+    ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * n_omega, cudaMemcpyHostToDevice, st));
+    const CombineArgs Ag = combine_args(m);
+    PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<dim3((unsigned)w.nparts, n_omega), 256, 0, st>>>(
+                                     Ag, w.coef.p, m.dev->row_ptr.p, m.dev->col_idx.p, n, w.x.p, w.f.p, w.r.p,
+                                     w.partial.p, w.nparts, w.active.p, 0));
     PROF_LAUNCH(KC_NORMS, st, k_member_norms<<<dim3(nm, n_omega), 256, 0, st>>>(m.dev->member_off.p, nm, n, w.r.p,
                                                                                   w.f.p, w.mnorms.p));
     const dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 1024), n_omega);
@@ -2330,12 +2425,7 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
   const int nm = m.n_members;  // a group: omegas and info hold one entry per member and slot
   for (int64_t s = 0; s < (int64_t)n_omega * nm; ++s)
     if (!(omegas[s] > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
-  static const int lanes_env = [] {
-    const char* e = getenv("ELP_LANES");
-    int v = e ? atoi(e) : 4;
-    return v < 1 ? 1 : v > 4 ? 4 : v;
-  }();
-  const int lanes = std::min({lanes_env, max_lanes, std::max(1, n_omega / (kSplitMin / 2))});
+  const int lanes = std::min({resolved_tuning(m).lanes, max_lanes, std::max(1, n_omega / (kSplitMin / 2))});
   if (lanes < 2 || n_omega < kSplitMin || prof_on())
     return solve_lane(m, precision, 0, omegas, n_omega, f_dev, x_dev, info, tol, user_stream, store);
   const int64_t n = m.n;
@@ -2396,7 +2486,7 @@ int numeric_solve_batch(Model& m, int precision, const double* omegas, int n_ome
 int front_update_test(int kernel, int p, int b, int step, int slots, float* fronts, int parent_m,
                       const int32_t* pmap, float* parents) {
   constexpr int NB = 32;
-  if (kernel < 0 || kernel > 3 || p < 1 || b < 0 || slots < 1 || slots > kMaxSlots || !fronts || step < 0) {
+  if (kernel < 0 || kernel > 4 || p < 1 || b < 0 || slots < 1 || slots > kMaxSlots || !fronts || step < 0) {
     set_error("bad front update test arguments");
     return ELP_ERR_ARG;
   }
@@ -2461,6 +2551,9 @@ int front_update_test(int kernel, int p, int b, int step, int slots, float* fron
   } else if (kernel == 2) {
     dim3 g(1, slots, (unsigned)(((b + 127) / 128) * ((b + 63) / 64)));
     if (b > 0) k_gemm_tc<NB, 64, false><<<g, kTcThreads, kTcSmemBytes, st>>>(L, arena.p, 0, GM_SCHUR, err.p);
+  } else if (kernel == 4) {  // the same with 128 x 32 tiles
+    dim3 g(1, slots, (unsigned)(((b + 127) / 128) * ((b + 31) / 32)));
+    if (b > 0) k_gemm_tc<NB, 32, false><<<g, kTcThreads, kTcSmemBytes, st>>>(L, arena.p, 0, GM_SCHUR, err.p);
   } else {
     const int64_t tiles = (b + kSchurTile - 1) / kSchurTile, nch = (p + kTcKC - 1) / kTcKC;
     const int64_t pack_bytes = tiles * nch * (kSchurABlock + kSchurBBlock);

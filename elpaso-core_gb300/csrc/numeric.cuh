@@ -179,8 +179,10 @@ struct DeviceSymbolic {
 // default 300).
 int pack_max_count();
 int pack_min_border();
-inline bool packed_schur_level(const DeviceSymbolic::Level& L) {
-  return L.count <= pack_max_count() && L.max_b >= pack_min_border();
+// the model's tuning with its defaults resolved
+Tuning resolved_tuning(const Model& m);
+inline bool packed_schur_level(const DeviceSymbolic::Level& L, const Tuning& t) {
+  return L.count <= t.pack_count && L.max_b >= t.pack_minb;
 }
 
 struct Workspace {
@@ -213,6 +215,9 @@ struct Workspace {
   int* h_flag = nullptr;          // pinned: tc_err read back after the factorisation
   DevBuf<double> mnorms;          // a group: slots x members x (||r||^2, ||f||^2)
   double* h_mnorms = nullptr;     // pinned copy
+  DevBuf<int> mdone;              // a group: slots x members, 1 when the member reached the tolerance
+  int* h_mdone = nullptr;         // pinned copy
+  double tol_member = 0.0;        // a group: the members' own tolerance (the group runs to a smaller one)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   int nparts = 0;
@@ -233,7 +238,7 @@ struct Workspace {
 struct WorkspacePlan {
   int64_t arena = 0, arena_full = 0, fac = 0, cb_total = 0, max_count = 1, pack_max = 0;  // arena: the pool
 };
-WorkspacePlan workspace_plan(const Symbolic& S);
+WorkspacePlan workspace_plan(const Model& m);
 
 int device_upload_symbolic(Model& m);
 int workspace_ensure(Model& m, int precision, int slots, int lane, int store);
@@ -255,6 +260,10 @@ int numeric_solve_lane(Model& m, int precision, int lane, const double* omegas, 
                        double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream, int store);
 // The FP64 solution vectors of a lane's last batch (slot s at + s * n).
 const double2* lane_solution(const Model& m, int precision, int lane);
+// A changed tuning drops what it invalidates (tune.cpp).
+void apply_tuning(Model& m, const Tuning& t);
+// The combined model of a group (group.cpp).
+Model& group_model(elp_group* g);
 // One front update kernel on caller-given FP32 complex fronts (elp_front_update_test).
 int front_update_test(int kernel, int p, int b, int step, int slots, float* fronts, int parent_m,
                       const int32_t* pmap, float* parents);

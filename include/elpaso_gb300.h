@@ -325,6 +325,38 @@ int elp_model_time_assembly(elp_model* m, int repeats, double* ms_per_assembly,
 int elp_residual_noalloc(elp_model* m, const double* omegas, int n_omega, const double* f_dev,
                          const double* x_dev, double* r_dev, double* rel_residual_out, void* stream);
 
+/* ---- tuning and the autotuner ------------------------------------------ */
+
+/* No reference counterpart (MUMPS and PETSc take their own parameters).
+ * How a model is factorised, never what is computed; 0 or a negative value
+ * takes the default (the ELP_* environment variable if set, else the value
+ * measured best on the coupled plate-cavity sweep):
+ *   leaf            nested-dissection leaf size in DOFs (128)
+ *   schur_tile      columns of a converter-kernel Schur tile: 32 or 64 (64)
+ *   pack_count      packed tensor-core Schur kernel on levels of at most this
+ *                   many fronts (300; 0: never) ...
+ *   pack_min_border ... whose largest border has at least this many rows (300)
+ *   lanes           workspace lanes a batch of 16+ frequencies is split over (4)
+ * A new leaf size redoes the symbolic phase at the next solve; the other
+ * knobs rebuild the workspaces. */
+typedef struct {
+  int leaf;
+  int schur_tile;
+  int pack_count;
+  int pack_min_border;
+  int lanes;
+} elp_tuning;
+int elp_model_set_tuning(elp_model* m, const elp_tuning* t);
+/* The tuning in effect, defaults resolved. */
+int elp_model_get_tuning(const elp_model* m, elp_tuning* t);
+/* Project-written autotuner: times solves of the caller's frequencies (at
+ * most 64) while it tries each knob in turn (leaf 64/128/256, tile 32/64,
+ * packed levels on/off, lanes 1/2/4 for 16+ frequencies), keeps whatever
+ * was fastest, leaves the model tuned so and reports the choice, the
+ * seconds of its timed solve and the number of trials. */
+int elp_model_autotune(elp_model* m, const double* omegas, int n_omega, int precision, elp_tuning* chosen,
+                       double* seconds, int* trials);
+
 /* ---- groups of models: frontal updates grouped across models ----------- */
 
 /* No reference counterpart (elpasoC solves one model per process). A group
@@ -352,6 +384,11 @@ int elp_group_info(const elp_group* g, elp_model_info* info);
 int elp_group_solve(elp_group* g, const double* omegas, int n_omega, int precision, double* x_out,
                     elp_solve_info* info, double tol);
 int elp_group_destroy(elp_group* g);
+/* Tuning of a group's combined system, and its autotuner (as for a model;
+ * omegas as for elp_group_solve). */
+int elp_group_set_tuning(elp_group* g, const elp_tuning* t);
+int elp_group_autotune(elp_group* g, const double* omegas, int n_omega, int precision, elp_tuning* chosen,
+                       double* seconds, int* trials);
 
 /* ---- fault injection for failure-path tests ---------------------------- */
 
@@ -389,13 +426,16 @@ int elp_fault_inject(int kind, int countdown);
  *     into parent[pmap[i], pmap[j]] instead (the extend-add fused into the
  *     update), F left as it was;
  *   ELP_KERNEL_PACKED_SCHUR: S added into the parents through the packed
- *     operands (split once into TF32 planes, bulk-copied by the MMA kernel).
+ *     operands (split once into TF32 planes, bulk-copied by the MMA kernel);
+ *   ELP_KERNEL_GEMM_SCHUR_32: as ELP_KERNEL_GEMM_SCHUR with 128 x 32 tiles
+ *     (the narrow tile the tuning may select).
  * pmap: b distinct parent positions. Returns ELP_ERR_ARG for inconsistent
  * sizes. */
 #define ELP_KERNEL_GEMM_COL 0
 #define ELP_KERNEL_GEMM_ROW 1
 #define ELP_KERNEL_GEMM_SCHUR 2
 #define ELP_KERNEL_PACKED_SCHUR 3
+#define ELP_KERNEL_GEMM_SCHUR_32 4
 int elp_front_update_test(int kernel, int p, int b, int step, int slots, float* fronts, int parent_m,
                           const int32_t* pmap, float* parents);
 

@@ -68,3 +68,33 @@ def test_group_of_many_plates(elp, meshes, oracle):
         for j in (0, 5):
             A, f = s.matrix(oms[k][j]), s.rhs(oms[k][j])
             assert np.linalg.norm(f - A @ xs[k][j]) / np.linalg.norm(f) <= 1e-10
+
+
+def test_autotune_leaves_a_working_tuning(elp, meshes, oracle):
+    """The autotuner times real solves while it varies leaf size, Schur tile,
+    packed levels and lanes, keeps the fastest, and leaves the model tuned
+    so: the tuning reported is the one in effect, and the next solve meets
+    the residual bar against the oracle."""
+    d = meshes.plate_cavity(12, 8, 6, 0.6, 0.4, 0.3)
+    m = elp.Model(d).assemble().analyse()
+    oms = 2 * np.pi * np.array([20.0, 140.0, 333.0, 470.0])
+    chosen, sec, trials = m.autotune(oms)
+    assert trials >= 5 and sec > 0
+    assert chosen["leaf"] in (64, 128, 256) and chosen["schur_tile"] in (32, 64)
+    assert m.tuning() == chosen
+    x, info = m.solve(oms, precision=1)
+    s = oracle.System(d)
+    for j, om in enumerate(oms):
+        A, f = s.matrix(om), s.rhs(om)
+        assert np.linalg.norm(f - A @ x[j]) / np.linalg.norm(f) <= 1e-10
+
+
+def test_group_autotune(elp, meshes):
+    ds = meshes.batched_plates(12, lo=10, hi=30)
+    g = elp.Group([elp.Model(d) for d in ds])
+    rng = np.random.default_rng(9)
+    oms = 2 * np.pi * rng.uniform(10.0, 400.0, size=(len(ds), 16))
+    chosen, sec, trials = g.autotune(oms)
+    assert trials >= 7 and sec > 0 and chosen["lanes"] in (1, 2, 4)
+    xs, infos = g.solve(oms, precision=1)
+    assert all(i["rel_residual"] <= 1e-10 for row in infos for i in row)

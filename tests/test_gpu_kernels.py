@@ -23,7 +23,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-GEMM_COL, GEMM_ROW, GEMM_SCHUR, PACKED_SCHUR = 0, 1, 2, 3
+GEMM_COL, GEMM_ROW, GEMM_SCHUR, PACKED_SCHUR, GEMM_SCHUR_32 = 0, 1, 2, 3, 4
 
 
 def _fronts(rng, slots, m):
@@ -95,12 +95,13 @@ def test_crout_row_update(elp, p, b, step):
         assert np.array_equal(G[s][mask], F[s][mask])
 
 
+@pytest.mark.parametrize("kernel", [GEMM_SCHUR, GEMM_SCHUR_32])
 @pytest.mark.parametrize("p,b", [(200, 300), (45, 77)])
-def test_schur_update_in_place(elp, p, b):
+def test_schur_update_in_place(elp, kernel, p, b):
     rng = np.random.default_rng(300 + p)
     m = p + b
     F = _fronts(rng, 2, m)
-    G, _ = _run(elp, GEMM_SCHUR, p, b, 0, F)
+    G, _ = _run(elp, kernel, p, b, 0, F)
     for s in range(2):
         A, B, Cb = F[s][p:, :p], F[s][:p, p:], F[s][p:, p:]
         want = Cb.astype(np.complex128) - A.astype(np.complex128) @ B.astype(np.complex128)
@@ -108,7 +109,7 @@ def test_schur_update_in_place(elp, p, b):
         assert np.array_equal(G[s][:p, :], F[s][:p, :]) and np.array_equal(G[s][:, :p], F[s][:, :p])
 
 
-@pytest.mark.parametrize("kernel", [GEMM_SCHUR, PACKED_SCHUR])
+@pytest.mark.parametrize("kernel", [GEMM_SCHUR, PACKED_SCHUR, GEMM_SCHUR_32])
 @pytest.mark.parametrize("p,b", [(200, 300), (300, 129), (40, 20)])
 def test_schur_update_into_parent(elp, kernel, p, b):
     """The extend-add fused into the update: parent[pmap[i], pmap[j]] +=

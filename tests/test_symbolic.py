@@ -137,3 +137,31 @@ def test_group_keeps_each_members_tree(elp, meshes):
         assert gi[key] == sum(i[key] for i in infos), key
     assert gi["factor_flops"] == pytest.approx(sum(i["factor_flops"] for i in infos), rel=1e-12)
     assert gi["n_levels"] == max(i["n_levels"] for i in infos)
+
+
+def test_tuning_is_per_model(elp, meshes):
+    """The leaf size of one model's tuning changes its tree (and nothing of
+    another model's); get_tuning reports the values in effect, defaults
+    resolved; bad values are refused."""
+    d = meshes.plate(40, 30, 0.6, 0.4, 0.002)
+    a = elp.Model(d).set_tuning(leaf=64)
+    b = elp.Model(d)
+    ia, ib = analysed(elp, d)[1], None
+    for m in (a, b):
+        try:
+            m.analyse()
+        except elp.ElpasoError as e:
+            assert e.code == 2
+    ia, ib = a.info(), b.info()
+    assert ia["n_fronts"] > ib["n_fronts"]
+    ta, tb = a.tuning(), b.tuning()
+    assert ta["leaf"] == 64 and tb["leaf"] == 128
+    assert tb["schur_tile"] == 64 and tb["lanes"] == 4 and tb["pack_count"] == 300
+    a.set_tuning(leaf=128)  # the symbolic phase is redone with the new leaf size
+    try:
+        a.analyse()
+    except elp.ElpasoError:
+        pass
+    assert a.info()["n_fronts"] == ib["n_fronts"]
+    with pytest.raises(elp.ElpasoError):
+        b.set_tuning(schur_tile=48)
