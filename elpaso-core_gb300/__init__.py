@@ -153,7 +153,7 @@ EXPORTS = [
     "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc", "elp_fault_inject",
     "elp_front_update_test", "elp_group_create", "elp_group_info", "elp_group_solve", "elp_group_destroy",
     "elp_model_set_tuning", "elp_model_get_tuning", "elp_model_autotune", "elp_group_set_tuning",
-    "elp_group_autotune",
+    "elp_group_autotune", "elp_peak_fp64",
 ]
 KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
                   "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc", "spmv", "fwd_border",
@@ -204,6 +204,7 @@ def load_library(path: str | None = None):
     lib.elp_model_autotune.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_double),
                                        C.POINTER(C.c_int)]
     lib.elp_group_set_tuning.argtypes = [P, C.POINTER(Tuning)]
+    lib.elp_peak_fp64.argtypes = [C.POINTER(C.c_double)]
     lib.elp_group_autotune.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_double),
                                        C.POINTER(C.c_int)]
     lib.elp_front_update_test.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, P, P]
@@ -542,6 +543,13 @@ class Group:
             self.close()
         except Exception:
             pass
+
+
+def peak_fp64() -> float:
+    """Measured FP64 FMA rate of the current device, TFLOP/s."""
+    v = C.c_double()
+    _check(load_library().elp_peak_fp64(C.byref(v)))
+    return v.value
 
 
 def profile(enable: bool = True):

@@ -457,6 +457,11 @@ int elp_profile(int enable);
 int elp_profile_read(double* ms /* [ELP_PROFILE_CLASSES] */, int64_t* launches, int64_t* timed,
                      int* n_classes);
 
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (a chain of
+ * independent FMAs on every SM, timed with CUDA events; no reference
+ * counterpart): the roofline of the FP64 kernels (plain path, assembly). */
+int elp_peak_fp64(double* tflops);
+
 /* ---- serving loop (continuous batching over resident models) ------------ */
 
 typedef struct elp_server elp_server;
