@@ -16,11 +16,12 @@
 //  - assembly is one pass over the elements of all members;
 //  - each member keeps its own frequencies: the kernels that form A(w) look up
 //    the coefficients of a row's member (coef[slot * members + member]);
-//  - the right-hand side of each member is scaled to unit norm and the
-//    refinement runs to ||r|| / ||f|| <= tol / sqrt(K) over the group (K
-//    members with a nonzero load), which bounds every member's own relative
-//    residual by tol; each member's residual is then measured on its own rows
-//    and reported per member and frequency.
+//  - the right-hand side of each member is scaled by a power of two to about
+//    unit norm (exact, so it changes no rounding); convergence is per member:
+//    the mixed path runs one Krylov process per (member, frequency) pair on
+//    the shared launches (numeric.cu run_gmres_group), the plain path's
+//    refinement freezes members that reached tol; each member's residual is
+//    measured on its own rows and reported per member and frequency.
 // The members' loss-factor groups are merged by value, at most 8 in a group.
 #include <cuda_runtime.h>
 

@@ -1266,6 +1266,90 @@ __global__ void k_combo(const double2* __restrict__ basis, int64_t sstride, int6
   }
 }
 
+// ---- GMRES per group member: the same vector kernels, with one set of
+// coefficients per (slot, member) pair p = s * nm + k (rows of member k are
+// off[k] .. off[k + 1] - 1)
+
+// out[p * kMaxBasis + i] = sum over member k's rows of conj(V_i) w, one CTA per pair (fixed order)
+__global__ void k_dots_seg(const double2* __restrict__ basis, int64_t sstride, int64_t vstride, int nv,
+                           const double2* __restrict__ w, int64_t wstride, const int64_t* __restrict__ off, int nm,
+                           double2* __restrict__ out, const int* __restrict__ pact) {
+  const int k = blockIdx.x, s = blockIdx.y;
+  const int64_t p = (int64_t)s * nm + k;
+  if (!pact[p]) return;
+  __shared__ double red[2][256];
+  const double2* ws = w + s * wstride;
+  for (int i = 0; i < nv; ++i) {
+    const double2* v = basis + s * sstride + (int64_t)i * vstride;
+    double ax = 0.0, ay = 0.0;
+    for (int64_t r = off[k] + threadIdx.x; r < off[k + 1]; r += blockDim.x) {
+      const double2 a = v[r], b = ws[r];
+      ax += a.x * b.x + a.y * b.y;
+      ay += a.x * b.y - a.y * b.x;
+    }
+    red[0][threadIdx.x] = ax;
+    red[1][threadIdx.x] = ay;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o; o >>= 1) {
+      if ((int)threadIdx.x < o) {
+        red[0][threadIdx.x] += red[0][threadIdx.x + o];
+        red[1][threadIdx.x] += red[1][threadIdx.x + o];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[p * kMaxBasis + i] = make_double2(red[0][0], red[1][0]);
+    __syncthreads();
+  }
+}
+
+// w -= sum_i h_{p,i} V_i on every row (its pair's coefficients)
+__global__ void k_gs_seg(const double2* __restrict__ basis, int64_t sstride, int64_t vstride, int nv,
+                         const double2* __restrict__ h, double2* __restrict__ w, int64_t n,
+                         const int32_t* __restrict__ row_model, int nm, const int* __restrict__ pact) {
+  const int s = blockIdx.y;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = (int64_t)s * nm + row_model[r];
+    if (!pact[p]) continue;
+    double2 t = w[s * n + r];
+    for (int i = 0; i < nv; ++i) {
+      const double2 c = h[p * kMaxBasis + i], v = basis[s * sstride + (int64_t)i * vstride + r];
+      t.x -= c.x * v.x - c.y * v.y;
+      t.y -= c.x * v.y + c.y * v.x;
+    }
+    w[s * n + r] = t;
+  }
+}
+
+// dst = src * scale_p (0 for the pairs that are done: their block of the basis is zero)
+__global__ void k_vscale_seg(const double2* __restrict__ src, int64_t sstride_src, double2* __restrict__ dst,
+                             int64_t sstride_dst, const double* __restrict__ scale, int64_t n,
+                             const int32_t* __restrict__ row_model, int nm) {
+  const int s = blockIdx.y;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double a = scale[(int64_t)s * nm + row_model[r]];
+    const double2 v = src[s * sstride_src + r];
+    dst[s * sstride_dst + r] = make_double2(v.x * a, v.y * a);
+  }
+}
+
+// t += sum_i y_{p,i} Z_i
+__global__ void k_combo_seg(const double2* __restrict__ basis, int64_t sstride, int64_t vstride, int nv,
+                            const double2* __restrict__ y, double2* __restrict__ t, int64_t n,
+                            const int32_t* __restrict__ row_model, int nm, const int* __restrict__ pact) {
+  const int s = blockIdx.y;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = (int64_t)s * nm + row_model[r];
+    if (!pact[p]) continue;
+    double ax = t[s * n + r].x, ay = t[s * n + r].y;
+    for (int i = 0; i < nv; ++i) {
+      const double2 c = y[p * kMaxBasis + i], v = basis[s * sstride + (int64_t)i * vstride + r];
+      ax += c.x * v.x - c.y * v.y;
+      ay += c.x * v.y + c.y * v.x;
+    }
+    t[s * n + r] = make_double2(ax, ay);
+  }
+}
+
 // u = D z (front precision -> FP64), u of slot s at u + s * sstride
 template <class V>
 __global__ void k_unscale(const V* __restrict__ z, const double* __restrict__ dscale, int64_t n, double2* __restrict__ u,
@@ -1288,6 +1372,10 @@ Workspace::~Workspace() {
   if (h_flag) cudaFreeHost(h_flag);
   if (h_mnorms) cudaFreeHost(h_mnorms);
   if (h_mdone) cudaFreeHost(h_mdone);
+  if (h_ph) cudaFreeHost(h_ph);
+  if (h_py) cudaFreeHost(h_py);
+  if (h_pscal) cudaFreeHost(h_pscal);
+  if (h_pact) cudaFreeHost(h_pact);
   if (h_h) cudaFreeHost(h_h);
   if (h_y) cudaFreeHost(h_y);
   if (h_scal) cudaFreeHost(h_scal);
@@ -1529,6 +1617,7 @@ int64_t workspace_bytes(const Model& m, int precision, int slots, int store) {
     b += S * D.pack_max;
     const int64_t rst = kGmresRestart;
     b += S * ((2 * rst + 2) * n * 16 + (int64_t)kMaxBasis * 16 * (4 + nparts) + 8 + 4);  // Vb, Zb, wv, Hessenberg
+    if (m.n_members > 1) b += S * m.n_members * ((int64_t)kMaxBasis * 16 * 4 + 12);        // per-member GMRES
   }
   return b;
 }
@@ -2052,9 +2141,22 @@ static int run_batch(Model& m, Workspace& w, int S_used, double tol, int max_ite
   return ELP_OK;
 }
 
-static int gmres_alloc(Workspace& w, int64_t n, int S, int rst) {
+static int gmres_alloc(Workspace& w, int64_t n, int S, int rst, int nm = 1) {
   if (w.rst == rst) return ELP_OK;
   w.rst = 0;  // set once every buffer below exists, so a failed call is retried in full
+  if (nm > 1) {  // a group: one Krylov process per (slot, member) pair
+    const size_t P = (size_t)S * nm;
+    ELP_CUDA(w.ph1.alloc(P * kMaxBasis));
+    ELP_CUDA(w.ph2.alloc(P * kMaxBasis));
+    ELP_CUDA(w.phn.alloc(P * kMaxBasis));
+    ELP_CUDA(w.py.alloc(P * kMaxBasis));
+    ELP_CUDA(w.pscal.alloc(P));
+    ELP_CUDA(w.pact.alloc(P));
+    if (!w.h_ph) ELP_CUDA(cudaMallocHost((void**)&w.h_ph, sizeof(double2) * 3 * P * kMaxBasis));
+    if (!w.h_py) ELP_CUDA(cudaMallocHost((void**)&w.h_py, sizeof(double2) * P * kMaxBasis));
+    if (!w.h_pscal) ELP_CUDA(cudaMallocHost((void**)&w.h_pscal, sizeof(double) * P));
+    if (!w.h_pact) ELP_CUDA(cudaMallocHost((void**)&w.h_pact, sizeof(int) * P));
+  }
   ELP_CUDA(w.Vb.alloc((size_t)S * (rst + 1) * n));
   ELP_CUDA(w.Zb.alloc((size_t)S * rst * n));
   ELP_CUDA(w.wv.alloc((size_t)S * n));
@@ -2255,6 +2357,202 @@ static int run_gmres(Model& m, Workspace& w, int S_used, double tol, int max_cyc
   return ELP_OK;
 }
 
+// GMRES-IR for a group: the factorisation and the preconditioner sweeps run
+// over the whole group (one launch per tree level for all members), but each
+// (slot, member) pair p = s * nm + k has its own Krylov process -- its own dot
+// products over its rows, Hessenberg matrix, rotations and update -- exactly
+// the process the member would run alone, with its own stopping test
+// ||r_k|| / ||f_k|| <= tol. A and the preconditioner are block diagonal, so
+// the pairs only share launches: a member whose frequency is hard (or that sits
+// at its FP64 floor) slows and fails no other member.
+template <class R>
+static int run_gmres_group(Model& m, Workspace& w, int S_used, double tol, int max_cycles, cudaStream_t st, float* ms) {
+  using V = typename Vec2<R>::T;
+  typedef std::complex<double> cd;
+  const int64_t n = m.n;
+  const int nm = m.n_members;
+  const int64_t P = (int64_t)S_used * nm;
+  DeviceModel& G = *m.dev;
+  CombineArgs A = combine_args(m);
+  int rc = solve_smem<R>(m);
+  if (rc) return rc;
+  const int RST = kGmresRestart;
+  rc = gmres_alloc(w, n, w.slots, RST, nm);
+  if (rc) return rc;
+  const int64_t vst = (int64_t)(RST + 1) * n, zst = (int64_t)RST * n;
+  for (int s = 0; s < S_used; ++s) { w.h_active[s] = 1; w.iters[s] = 0; }
+  ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+  ELP_CUDA(cudaEventRecord(w.ev[0], st));
+  rc = factor_and_setup<R>(m, w, S_used, st);
+  if (rc) return rc;
+  ELP_CUDA(cudaEventRecord(w.ev[1], st));
+  ELP_CUDA(cudaMemsetAsync(w.x.p, 0, sizeof(double2) * S_used * n, st));
+  const dim3 gv((unsigned)std::min<int64_t>((n + 255) / 256, 4096), S_used);
+  const dim3 gr((unsigned)w.nparts, S_used);
+  const dim3 gp((unsigned)nm, S_used);
+  V* z = reinterpret_cast<V*>(w.z.p);
+  const int64_t* off = G.member_off.p;
+  const int32_t* rmod = G.row_model.p;
+  std::vector<double> fn(P), rel(P);
+  auto residual = [&](int x_zero) -> int {
+    PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p,
+                                                                   w.r.p, w.partial.p, w.nparts, w.active.p, x_zero));
+    PROF_LAUNCH(KC_NORMS, st, k_member_norms<<<gp, 256, 0, st>>>(off, nm, n, w.r.p, w.f.p, w.mnorms.p));
+    ELP_CUDA(cudaMemcpyAsync(w.h_mnorms, w.mnorms.p, sizeof(double) * 2 * P, cudaMemcpyDeviceToHost, st));
+    ELP_CUDA(cudaStreamSynchronize(st));
+    for (int64_t q = 0; q < P; ++q) {
+      const double rr = w.h_mnorms[2 * q], ff = w.h_mnorms[2 * q + 1];
+      fn[q] = std::sqrt(ff);
+      rel[q] = ff > 0 ? std::sqrt(rr / ff) : std::sqrt(rr);
+    }
+    return ELP_OK;
+  };
+  auto precond = [&](const double2* src, int64_t sstride, const int* mask) -> int {
+    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, src, sstride, w.dscale.p, n, z, mask));
+    return solve_sweep<R>(m, w, S_used, st, mask);
+  };
+  // a tensor-core wait that ran out left the factors incomplete (read with the first residual)
+  ELP_CUDA(cudaMemcpyAsync(w.h_flag, w.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  rc = residual(1);
+  if (rc) return rc;
+  if (*w.h_flag) {
+    set_error("a tensor-core Schur update gave up waiting for its MMAs");
+    return ELP_ERR_CUDA;
+  }
+  std::vector<std::vector<cd>> H(P, std::vector<cd>((RST + 1) * RST)), g(P, std::vector<cd>(RST + 1)),
+      sn(P, std::vector<cd>(RST));
+  std::vector<std::vector<double>> cs(P, std::vector<double>(RST));
+  std::vector<int> ncol(P), open(P);
+  float solve_ms = 0.f;
+  auto upload_pairs = [&]() -> int {
+    ELP_CUDA(cudaMemcpyAsync(w.pact.p, w.h_pact, sizeof(int) * P, cudaMemcpyHostToDevice, st));
+    ELP_CUDA(cudaMemcpyAsync(w.pscal.p, w.h_pscal, sizeof(double) * P, cudaMemcpyHostToDevice, st));
+    ELP_CUDA(cudaMemcpyAsync(w.inner.p, w.h_inner, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+    return ELP_OK;
+  };
+  for (int cycle = 0; cycle < max_cycles; ++cycle) {
+    bool any = false;
+    for (int s = 0; s < S_used; ++s) w.h_inner[s] = 0;
+    for (int64_t q = 0; q < P; ++q) {
+      open[q] = rel[q] > tol && std::isfinite(rel[q]);
+      w.h_pact[q] = open[q];
+      w.h_pscal[q] = open[q] ? 1.0 / (rel[q] * fn[q]) : 0.0;
+      ncol[q] = 0;
+      if (open[q]) {
+        std::fill(g[q].begin(), g[q].end(), cd(0));
+        g[q][0] = rel[q] * fn[q];
+        w.h_inner[q / nm] = 1;
+        any = true;
+      }
+    }
+    if (!any) break;
+    for (int s = 0; s < S_used; ++s) w.h_active[s] = w.h_inner[s];
+    ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * S_used, cudaMemcpyHostToDevice, st));
+    rc = upload_pairs();
+    if (rc) return rc;
+    PROF_LAUNCH(KC_KRYLOV, st, k_vscale_seg<<<gv, 256, 0, st>>>(w.r.p, n, w.Vb.p, vst, w.pscal.p, n, rmod, nm));
+    for (int j = 0; j < RST; ++j) {
+      ELP_CUDA(cudaEventRecord(w.ev[2], st));
+      rc = precond(w.Vb.p + (int64_t)j * n, vst, w.inner.p);
+      if (rc) return rc;
+      ELP_CUDA(cudaEventRecord(w.ev[3], st));
+      PROF_LAUNCH(KC_KRYLOV, st, k_unscale<V><<<gv, 256, 0, st>>>(z, w.dscale.p, n, w.Zb.p + (int64_t)j * n, zst, w.inner.p));
+      PROF_LAUNCH(KC_SPMV, st, k_spmv<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n,
+                                                                 w.Zb.p + (int64_t)j * n, zst, w.wv.p, w.inner.p));
+      const int nv = j + 1;
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_seg<<<gp, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, off, nm, w.ph1.p, w.pact.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_gs_seg<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.ph1.p, w.wv.p, n, rmod, nm, w.pact.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_seg<<<gp, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, off, nm, w.ph2.p, w.pact.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_gs_seg<<<gv, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.ph2.p, w.wv.p, n, rmod, nm, w.pact.p));
+      PROF_LAUNCH(KC_KRYLOV, st, k_dots_seg<<<gp, 256, 0, st>>>(w.wv.p, n, 0, 1, w.wv.p, n, off, nm, w.phn.p, w.pact.p));
+      ELP_CUDA(cudaMemcpyAsync(w.h_ph, w.ph1.p, sizeof(double2) * P * kMaxBasis, cudaMemcpyDeviceToHost, st));
+      ELP_CUDA(cudaMemcpyAsync(w.h_ph + P * kMaxBasis, w.ph2.p, sizeof(double2) * P * kMaxBasis,
+                               cudaMemcpyDeviceToHost, st));
+      ELP_CUDA(cudaMemcpyAsync(w.h_ph + 2 * P * kMaxBasis, w.phn.p, sizeof(double2) * P * kMaxBasis,
+                               cudaMemcpyDeviceToHost, st));
+      ELP_CUDA(cudaStreamSynchronize(st));
+      float a = 0.f;
+      cudaEventElapsedTime(&a, w.ev[2], w.ev[3]);
+      solve_ms += a;
+      for (int s = 0; s < S_used; ++s)
+        if (w.h_inner[s]) w.iters[s]++;
+      bool more = false;
+      for (int s = 0; s < S_used; ++s) w.h_inner[s] = 0;
+      for (int64_t q = 0; q < P; ++q) {
+        if (!w.h_pact[q]) { w.h_pscal[q] = 0.0; continue; }
+        cd* Hs = H[q].data();  // column-major (RST + 1) x RST
+        for (int i = 0; i <= j; ++i) {
+          const double2 h1 = w.h_ph[q * kMaxBasis + i], h2 = w.h_ph[(P + q) * kMaxBasis + i];
+          Hs[j * (RST + 1) + i] = cd(h1.x + h2.x, h1.y + h2.y);
+        }
+        const double hn = std::sqrt(std::max(0.0, w.h_ph[(2 * P + q) * kMaxBasis].x));
+        Hs[j * (RST + 1) + j + 1] = cd(hn, 0.0);
+        for (int i = 0; i < j; ++i) {  // previous rotations
+          const cd a0 = Hs[j * (RST + 1) + i], b0 = Hs[j * (RST + 1) + i + 1];
+          Hs[j * (RST + 1) + i] = cs[q][i] * a0 + sn[q][i] * b0;
+          Hs[j * (RST + 1) + i + 1] = -std::conj(sn[q][i]) * a0 + cs[q][i] * b0;
+        }
+        const cd a0 = Hs[j * (RST + 1) + j], b0 = Hs[j * (RST + 1) + j + 1];
+        const double rho = std::sqrt(std::norm(a0) + std::norm(b0));
+        if (std::abs(a0) == 0.0) { cs[q][j] = 0.0; sn[q][j] = cd(1.0, 0.0); }
+        else {
+          cs[q][j] = std::abs(a0) / rho;
+          sn[q][j] = (a0 / std::abs(a0)) * std::conj(b0) / rho;
+        }
+        Hs[j * (RST + 1) + j] = cs[q][j] * a0 + sn[q][j] * b0;
+        Hs[j * (RST + 1) + j + 1] = 0.0;
+        g[q][j + 1] = -std::conj(sn[q][j]) * g[q][j];
+        g[q][j] = cs[q][j] * g[q][j];
+        ncol[q] = j + 1;
+        const double est = std::abs(g[q][j + 1]) / fn[q];
+        if (est <= 0.5 * tol || hn <= 1e-300 || j == RST - 1 || !std::isfinite(est)) {
+          w.h_pact[q] = 0;
+          w.h_pscal[q] = 0.0;
+        } else {
+          more = true;
+          w.h_inner[q / nm] = 1;
+          w.h_pscal[q] = hn > 0 ? 1.0 / hn : 0.0;
+        }
+      }
+      rc = upload_pairs();
+      if (rc) return rc;
+      PROF_LAUNCH(KC_KRYLOV, st, k_vscale_seg<<<gv, 256, 0, st>>>(w.wv.p, n, w.Vb.p + (int64_t)(j + 1) * n, vst,
+                                                                   w.pscal.p, n, rmod, nm));
+      if (!more) break;
+    }
+    // x += Z y for every pair that ran this cycle
+    int nvmax = 0;
+    for (int64_t q = 0; q < P; ++q) {
+      for (int i = 0; i < kMaxBasis; ++i) w.h_py[q * kMaxBasis + i] = make_double2(0, 0);
+      w.h_pact[q] = open[q];
+      if (!open[q]) continue;
+      const int k = ncol[q];
+      nvmax = std::max(nvmax, k);
+      std::vector<cd> y(k);
+      const cd* Hs = H[q].data();
+      for (int i = k - 1; i >= 0; --i) {
+        cd t = g[q][i];
+        for (int c = i + 1; c < k; ++c) t -= Hs[c * (RST + 1) + i] * y[c];
+        y[i] = t / Hs[i * (RST + 1) + i];
+      }
+      for (int i = 0; i < k; ++i) w.h_py[q * kMaxBasis + i] = make_double2(y[i].real(), y[i].imag());
+    }
+    ELP_CUDA(cudaMemcpyAsync(w.py.p, w.h_py, sizeof(double2) * P * kMaxBasis, cudaMemcpyHostToDevice, st));
+    ELP_CUDA(cudaMemcpyAsync(w.pact.p, w.h_pact, sizeof(int) * P, cudaMemcpyHostToDevice, st));
+    PROF_LAUNCH(KC_UPDATE, st, k_combo_seg<<<gv, 256, 0, st>>>(w.Zb.p, zst, n, nvmax, w.py.p, w.x.p, n, rmod, nm,
+                                                                w.pact.p));
+    rc = residual(0);
+    if (rc) return rc;
+  }
+  ELP_CUDA(cudaGetLastError());
+  float fms = 0.f;
+  cudaEventElapsedTime(&fms, w.ev[0], w.ev[1]);
+  ms[0] = fms;
+  ms[1] = solve_ms;
+  ms[2] = 0.f;
+  return ELP_OK;
+}
+
 // One batch on one workspace lane (0 or 1), on `stream` (its own when null).
 static int solve_lane(Model& m, int precision, int lane, const double* omegas, int n_omega, const double2* f_dev,
                       double2* x_dev, elp_solve_info* info, double tol, cudaStream_t stream, int store) {
@@ -2308,7 +2606,8 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
   ELP_CUDA(cudaMemsetAsync(w.tc_err.p, 0, sizeof(int), st));
   int iters = 0;
   float ms[3] = {0, 0, 0};
-  if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 12, st, ms);
+  if (precision == ELP_MIXED && group) rc = run_gmres_group<float>(m, w, n_omega, w.tol_member, 12, st, ms);
+  else if (precision == ELP_MIXED) rc = run_gmres<float>(m, w, n_omega, tol, 12, st, ms);
   else rc = run_batch<double>(m, w, n_omega, tol, 8, st, &iters, ms);
   if (rc) return rc;
   if (group) {  // each member's own true residual (no rows masked), then its solution at its own scale

@@ -216,6 +216,15 @@ struct Workspace {
   DevBuf<double> mnorms;          // a group: slots x members x (||r||^2, ||f||^2)
   double* h_mnorms = nullptr;     // pinned copy
   DevBuf<int> mdone;              // a group: slots x members, 1 when the member reached the tolerance
+  // a group's GMRES, one process per (slot, member) pair: Hessenberg columns,
+  // least-squares coefficients, scales, pair activity
+  DevBuf<double2> ph1, ph2, phn, py;
+  DevBuf<double> pscal;
+  DevBuf<int> pact;
+  double2* h_ph = nullptr;        // pinned: 3 x pairs x 32
+  double2* h_py = nullptr;        // pinned: pairs x 32
+  double* h_pscal = nullptr;      // pinned: pairs
+  int* h_pact = nullptr;          // pinned: pairs
   int* h_mdone = nullptr;         // pinned copy
   double tol_member = 0.0;        // a group: the members' own tolerance (the group runs to a smaller one)
   cudaStream_t stream = nullptr;

@@ -369,10 +369,11 @@ int elp_model_autotune(elp_model* m, const double* omegas, int n_omega, int prec
  * numbering; results and infos are reported per member. The members are
  * copied at creation (the group does not refer to them later); their
  * loss-factor groups are merged by value, at most 8 distinct in a group.
- * Refinement runs the group to ||r|| / ||f|| <= tol / sqrt(K) with every
- * member's load scaled to unit norm (K members with a nonzero load), which
- * bounds each member's own relative residual by tol; that residual is
- * measured on the member's own rows and reported in its info. */
+ * Convergence is per member: the mixed path runs one Krylov process per
+ * (member, frequency) with its own stopping test; the plain path's
+ * refinement freezes each member once it reaches tol. A hard member fails
+ * only itself. Each member's residual is measured on its own rows and
+ * reported in its info. */
 typedef struct elp_group elp_group;
 int elp_group_create(elp_model* const* models, int n_models, elp_group** out);
 /* Sizes of the combined system (n_dofs, nnz, fronts, ... of all members). */
