@@ -5,7 +5,7 @@ fronts of all members, each member at its own frequencies. Bars, per member
 and frequency, as for single models: ||f - A x||_2 / ||f||_2 <= 1e-10 with
 the oracle's matrix of that member, the error against the oracle's FP64
 solve within 3 kappa_1(A_ff) (res_1 + res_ref_1), and the reported residual
-equal to the one measured here. A group of one model takes the single-model
+within 1e-10 of the one measured here. A group of one model takes the single-model
 path and equals the model solved alone up to assembly rounding.
 """
 import numpy as np
@@ -37,7 +37,9 @@ def test_group_members_match_the_oracle(elp, meshes, oracle, prec):
             x = xs[k][j]
             res = np.linalg.norm(f - A @ x) / np.linalg.norm(f)
             assert res <= 1e-10, (k, j, res)
-            assert abs(infos[k][j]["rel_residual"] - res) <= 1e-11 + 1e-3 * res, (k, j, infos[k][j], res)
+            # the library's residual is double-double; this one is plain FP64, good to ~1e-10 on the
+            # clamped plate (|| |A| |x| || / ||f|| ~ 1e6): the bar of the single-model solve tests
+            assert abs(infos[k][j]["rel_residual"] - res) <= 1e-10, (k, j, infos[k][j], res)
             assert infos[k][j]["converged"] == 1
             xr = s.solve(om)
             n1 = np.linalg.norm(f, 1)
