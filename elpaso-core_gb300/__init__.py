@@ -28,6 +28,8 @@ __all__ = [
 BRICK8, DSG4, FLUID8 = 1, 2, 3
 STR_LIN_ELA_ISO_DIR, STR_LIN_VIS_ISO_DIR, AF_LIN_UAF_ISO_DIR = 1, 2, 3
 FP64_PLAIN, MIXED = 0, 1
+# arithmetic of the Brick8 / Fluid8 element contractions (elp_model_set_assembly)
+ASSEMBLY_FP64, ASSEMBLY_DOUBLE_FLOAT = 0, 1
 NODES_PER_ELEMENT = {BRICK8: 8, DSG4: 4, FLUID8: 8}
 # fedata/basics_dof.h:24-60
 DOF = {"disp_x1": 0, "disp_x2": 1, "disp_x3": 2, "disp_w1": 3, "disp_w2": 4, "fluid": 16}
@@ -153,7 +155,7 @@ EXPORTS = [
     "elp_server_destroy", "elp_profile", "elp_profile_read", "elp_residual_noalloc", "elp_fault_inject",
     "elp_front_update_test", "elp_group_create", "elp_group_info", "elp_group_solve", "elp_group_destroy",
     "elp_model_set_tuning", "elp_model_get_tuning", "elp_model_autotune", "elp_group_set_tuning",
-    "elp_group_autotune", "elp_peak_fp64",
+    "elp_group_autotune", "elp_peak_fp64", "elp_model_set_assembly",
 ]
 KERNEL_CLASSES = ["assemble", "dscale", "scatter", "panel", "border", "urow", "gemm", "extend_add", "forward",
                   "backward", "residual", "norms", "rhs", "update", "values", "gemm_tc", "spmv", "fwd_border",
@@ -200,6 +202,7 @@ def load_library(path: str | None = None):
     lib.elp_group_solve.argtypes = [P, P, C.c_int, C.c_int, P, P, C.c_double]
     lib.elp_group_destroy.argtypes = [P]
     lib.elp_model_set_tuning.argtypes = [P, C.POINTER(Tuning)]
+    lib.elp_model_set_assembly.argtypes = [P, C.c_int]
     lib.elp_model_get_tuning.argtypes = [P, C.POINTER(Tuning)]
     lib.elp_model_autotune.argtypes = [P, P, C.c_int, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_double),
                                        C.POINTER(C.c_int)]
@@ -427,6 +430,12 @@ class Model:
         out = np.zeros((self.desc.n_nodes, 9), np.complex128)
         _check(self.lib.elp_node_stresses(self.handle, float(omega), _ptr(xs), _ptr(out)))
         return out
+
+    def set_assembly(self, arithmetic: int):
+        """ASSEMBLY_FP64 (default) or ASSEMBLY_DOUBLE_FLOAT for the Brick8 /
+        Fluid8 contractions; an assembled model is assembled again."""
+        _check(self.lib.elp_model_set_assembly(self.handle, int(arithmetic)))
+        return self
 
     def set_tuning(self, **knobs):
         """leaf, schur_tile, pack_count, pack_min_border, lanes (unset: default)."""

@@ -26,6 +26,7 @@
 // shape/shapehex8.cpp:49-90, shape/shapequad4.cpp:48-73, misc/gausspoints.h:27-43;
 // 3D Gauss points are numbered x fastest, 2D points y fastest
 // (misc/gausspoints.cpp:76-87, 165-195).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
@@ -38,6 +39,46 @@ namespace elp {
 __constant__ double c_hex[4][8][8];    // [fun, xi, eta, zeta][node][gp]
 __constant__ double c_quad[3][4][4];   // [fun, xi, eta][node][gp]
 __constant__ unsigned char c_pair_a[36], c_pair_b[36];
+// the same tables split into FP32 pairs (hi + lo = the FP64 value to ~2^-48):
+// shape derivatives [xi, eta, zeta][node][gp] and node-pair products
+// N_a N_b [pair][gp], for the double-float contractions below
+__constant__ float2 c_hexd[3][8][8];
+__constant__ float2 c_mass[36][8];
+__constant__ double c_massd[36][8];  // N_a N_b [pair][gp] in FP64
+
+// ---------------------------------------------------------------- double-float
+// Opt-in (ELP_ASSEMBLY_DOUBLE_FLOAT): the Brick8 / Fluid8 contractions
+// (gradients J^-T grad N and the node-pair sums P_ab = sum_gp w g_a g_b^T) in
+// FP32 pairs. FP64 executes at about 1/64 of the FP32 rate on this part, and
+// these sums are most of the assembly's FP64 work. A value is hi + lo (two
+// floats); a product keeps the FMA error of hi * hi plus the two cross terms
+// (relative error ~2^-46), a sum adds the high parts error-free (two-sum) and
+// collects every error in lo. Results are formed in FP64 as hi + lo; against
+// the FP64 sums they differ by ~1e-14 of the sum of the magnitudes of their
+// terms. J, det J and J^-1 stay FP64.
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF df_split(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return {p, e};
+}
+__device__ __forceinline__ void df_acc(DF& s, DF x) {
+  const float t = s.h + x.h;
+  const float bb = t - s.h;
+  const float err = (s.h - (t - bb)) + (x.h - bb);
+  s.h = t;
+  s.l += err + x.l;
+}
+__device__ __forceinline__ double df_value(DF s) { return (double)s.h + (double)s.l; }
+__device__ __forceinline__ DF df_of(float2 v) { return {v.x, v.y}; }
 
 static const double kGp2 = 0.577350269189626;  // misc/gausspoints.h gp4[1]
 
@@ -148,23 +189,62 @@ __device__ __forceinline__ double jac3(const double* x, int gp, double inv[3][3]
   double det = J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] +
                J[0][2] * J[1][0] * J[2][1] - J[0][2] * J[1][1] * J[2][0] -
                J[0][0] * J[1][2] * J[2][1] - J[0][1] * J[1][0] * J[2][2];
-  inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
-  inv[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) / det;
-  inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
-  inv[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) / det;
-  inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
-  inv[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) / det;
-  inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
-  inv[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) / det;
-  inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+  const double id = 1.0 / det;  // one FP64 division instead of nine
+  inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * id;
+  inv[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) * id;
+  inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * id;
+  inv[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * id;
+  inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+  inv[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * id;
+  inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+  inv[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) * id;
+  inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
   return det;
 }
 
 // ---------------------------------------------------------------- hex items
-// kind 0 = Brick8, 1 = Fluid8
-template <int kKind>
-__device__ void hex_item(const AsmArgs& A, int64_t item, double (*sg)[8][8][3], double (*sw)[8],
-                         int (*srow)[8], int* smat) {
+// Arithmetic of the Brick8 / Fluid8 contractions: FP64 (the default, the
+// drop-in) or double-float (elp_model_set_assembly). Shared-memory values are
+// 8 bytes in both: a double, or a float pair hi + lo.
+template <bool kDF>
+struct HexArith;
+template <>
+struct HexArith<false> {
+  using V = double;
+  __device__ static V zero() { return 0.0; }
+  __device__ static V of(double s) { return s; }
+  __device__ static double store(V v) { return v; }
+  __device__ static V split(double x) { return x; }
+  __device__ static V mul(V a, V b) { return a * b; }
+  __device__ static void fma(V& s, V a, V b) { s = ::fma(a, b, s); }
+  __device__ static double value(V v) { return v; }
+  __device__ static V dshape(int dv, int k, int gp) { return c_hex[dv + 1][k][gp]; }
+  __device__ static V mass(int pr, int gp) { return c_massd[pr][gp]; }
+};
+template <>
+struct HexArith<true> {
+  using V = DF;
+  __device__ static V zero() { return {0.f, 0.f}; }
+  __device__ static V of(double s) { return {__int_as_float(__double2loint(s)), __int_as_float(__double2hiint(s))}; }
+  __device__ static double store(V v) { return __hiloint2double(__float_as_int(v.l), __float_as_int(v.h)); }
+  __device__ static V split(double x) { return df_split(x); }
+  __device__ static V mul(V a, V b) { return df_mul(a, b); }
+  __device__ static void fma(V& s, V a, V b) { df_acc(s, df_mul(a, b)); }
+  __device__ static double value(V v) { return df_value(v); }
+  __device__ static V dshape(int dv, int k, int gp) { return df_of(c_hexd[dv][k][gp]); }
+  __device__ static V mass(int pr, int gp) { return df_of(c_mass[pr][gp]); }
+};
+
+// kind 0 = Brick8, 1 = Fluid8. Per item of 8 elements: 64 threads form
+// J, det J and J^-1 (FP64) at one Gauss point each and store g_k = J^-T grad N_k
+// and w g_k for the 8 nodes; then one thread per node pair (a <= b) sums
+// P_ab = sum_gp (w g_a) g_b^T (and the mass term) and adds the 3 x 3 block
+// (and its transpose) into the CSR value arrays.
+template <int kKind, bool kDF>
+__device__ void hex_item(const AsmArgs& A, int64_t item, double (*sg)[8][8][3], double (*swg)[8][8][3],
+                         double (*sw)[8], int (*srow)[8], int* smat) {
+  using H = HexArith<kDF>;
+  using V = typename H::V;
   const int t = threadIdx.x;
   const int64_t e0 = item * kHexPerItem;
   const int64_t ne = kKind == 0 ? A.n_brick : A.n_fluid;
@@ -184,14 +264,25 @@ __device__ void hex_item(const AsmArgs& A, int64_t item, double (*sg)[8][8][3], 
       double inv[3][3];
       double det = jac3(x, gp, inv);
       if (det <= 0.0) atomicAdd(A.flags + 0, 1);
+      V iv[3][3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) iv[d][j] = H::split(inv[d][j]);
+      const V w = H::split(det);  // level-2 weights are 1 x 1 x 1
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        double a = c_hex[1][k][gp], b = c_hex[2][k][gp], c = c_hex[3][k][gp];
-        sg[el][gp][k][0] = inv[0][0] * a + inv[0][1] * b + inv[0][2] * c;
-        sg[el][gp][k][1] = inv[1][0] * a + inv[1][1] * b + inv[1][2] * c;
-        sg[el][gp][k][2] = inv[2][0] * a + inv[2][1] * b + inv[2][2] * c;
+        const V a = H::dshape(0, k, gp), b = H::dshape(1, k, gp), c = H::dshape(2, k, gp);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          V g = H::mul(iv[d][0], a);
+          H::fma(g, iv[d][1], b);
+          H::fma(g, iv[d][2], c);
+          sg[el][gp][k][d] = H::store(g);
+          swg[el][gp][k][d] = H::store(H::mul(w, g));
+        }
       }
-      sw[el][gp] = 1.0 * det;  // level-2 weights are 1 x 1 x 1
+      sw[el][gp] = H::store(w);
     }
   } else if (t < 128) {
     int el = (t - 64) >> 3, k = (t - 64) & 7;
@@ -211,18 +302,31 @@ __device__ void hex_item(const AsmArgs& A, int64_t item, double (*sg)[8][8][3], 
       const ElemMaterial& mt = A.mats[smat[el]];
       const int ra = srow[el][a], rb = srow[el][b];
       if (kKind == 0) {
-        double P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        double mm = 0.0;
+        V Pv[3][3], mv_ = H::zero();
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) Pv[i][j] = H::zero();
 #pragma unroll
         for (int gp = 0; gp < 8; ++gp) {
-          double w = sw[el][gp];
-          double wa0 = w * sg[el][gp][a][0], wa1 = w * sg[el][gp][a][1], wa2 = w * sg[el][gp][a][2];
-          double gb0 = sg[el][gp][b][0], gb1 = sg[el][gp][b][1], gb2 = sg[el][gp][b][2];
-          P[0][0] += wa0 * gb0; P[0][1] += wa0 * gb1; P[0][2] += wa0 * gb2;
-          P[1][0] += wa1 * gb0; P[1][1] += wa1 * gb1; P[1][2] += wa1 * gb2;
-          P[2][0] += wa2 * gb0; P[2][1] += wa2 * gb1; P[2][2] += wa2 * gb2;
-          mm += w * c_hex[0][a][gp] * c_hex[0][b][gp];
+          V wa[3], gb[3];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            wa[d] = H::of(swg[el][gp][a][d]);
+            gb[d] = H::of(sg[el][gp][b][d]);
+          }
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) H::fma(Pv[i][j], wa[i], gb[j]);
+          H::fma(mv_, H::of(sw[el][gp]), H::mass(pr, gp));
         }
+        double P[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) P[i][j] = H::value(Pv[i][j]);
+        const double mm = H::value(mv_);
         const double tr = P[0][0] + P[1][1] + P[2][2];
         double Kb[3][3];
 #pragma unroll
@@ -250,14 +354,14 @@ __device__ void hex_item(const AsmArgs& A, int64_t item, double (*sg)[8][8][3], 
           }
         }
       } else {
-        double kk = 0.0, mm = 0.0;
+        V kv = H::zero(), mv_ = H::zero();
 #pragma unroll
         for (int gp = 0; gp < 8; ++gp) {
-          double w = sw[el][gp];
-          kk += w * (sg[el][gp][a][0] * sg[el][gp][b][0] + sg[el][gp][a][1] * sg[el][gp][b][1] +
-                     sg[el][gp][a][2] * sg[el][gp][b][2]);
-          mm += mt.inv_c2 * c_hex[0][a][gp] * c_hex[0][b][gp] * w;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) H::fma(kv, H::of(swg[el][gp][a][d]), H::of(sg[el][gp][b][d]));
+          H::fma(mv_, H::of(sw[el][gp]), H::mass(pr, gp));
         }
+        const double kk = H::value(kv), mm = mt.inv_c2 * H::value(mv_);
         const double ir = 1.0 / mt.rho;
         int p = find_col(A.row_ptr, A.col_idx, ra, rb);
         add_at(A.VK, p, kk * ir);
@@ -484,15 +588,17 @@ __device__ void interface_quad(const AsmArgs& A, int64_t q) {
 // ---------------------------------------------------------------- kernel
 // Brick8 / Fluid8 items (8 elements per CTA); register-light, so three CTAs
 // share an SM.
+template <bool kDF>
 __global__ void __launch_bounds__(kThreads, 3) assemble_hex_kernel(AsmArgs A) {
   __shared__ double sg[kHexPerItem][8][8][3];
+  __shared__ double swg[kHexPerItem][8][8][3];
   __shared__ double sw[kHexPerItem][8];
   __shared__ int srow[kHexPerItem][8];
   __shared__ int smat[kHexPerItem];
   const int64_t total = A.items_brick + A.items_fluid;
   for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
-    if (it < A.items_brick) hex_item<0>(A, it, sg, sw, srow, smat);
-    else hex_item<1>(A, it - A.items_brick, sg, sw, srow, smat);
+    if (it < A.items_brick) hex_item<0, kDF>(A, it, sg, swg, sw, srow, smat);
+    else hex_item<1, kDF>(A, it - A.items_brick, sg, swg, sw, srow, smat);
   }
 }
 
@@ -527,6 +633,22 @@ static int upload_tables(int dev) {
   ELP_CUDA(cudaMemcpyToSymbol(c_quad, quad, sizeof(quad)));
   ELP_CUDA(cudaMemcpyToSymbol(c_pair_a, pa, sizeof(pa)));
   ELP_CUDA(cudaMemcpyToSymbol(c_pair_b, pb, sizeof(pb)));
+  auto split = [](double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+  };
+  float2 hd[3][8][8], ms[36][8];
+  for (int dv = 0; dv < 3; ++dv)
+    for (int n = 0; n < 8; ++n)
+      for (int g = 0; g < 8; ++g) hd[dv][n][g] = split(hex[dv + 1][n][g]);
+  for (int q = 0; q < 36; ++q)
+    for (int g = 0; g < 8; ++g) ms[q][g] = split(hex[0][pa[q]][g] * hex[0][pb[q]][g]);
+  ELP_CUDA(cudaMemcpyToSymbol(c_hexd, hd, sizeof(hd)));
+  ELP_CUDA(cudaMemcpyToSymbol(c_mass, ms, sizeof(ms)));
+  double md[36][8];
+  for (int q = 0; q < 36; ++q)
+    for (int g = 0; g < 8; ++g) md[q][g] = hex[0][pa[q]][g] * hex[0][pb[q]][g];
+  ELP_CUDA(cudaMemcpyToSymbol(c_massd, md, sizeof(md)));
   g_tables_done[dev] = true;
   return ELP_OK;
 }
@@ -564,6 +686,36 @@ int device_upload_model(Model& m) {
     mm->insert(mm->end(), blk.n_elements, (int16_t)blk.material);
   }
   if (m.materials.size() > 32767) { set_error("too many materials"); return ELP_ERR_ARG; }
+  // Each element kind is launched in order of its lowest node (a stable
+  // counting sort): the CTAs in flight then add into a narrow band of CSR
+  // rows that stays in L2 until its last element. Block by block order
+  // sweeps the whole matrix once per material block (four times over on a
+  // cube with four randomly assigned materials).
+  auto locality_sort = [&](std::vector<int32_t>& conn, std::vector<int16_t>& mat, int per) {
+    const size_t ne = mat.size();
+    if (ne < 2) return;
+    std::vector<int64_t> start((size_t)m.n_nodes + 1, 0);
+    std::vector<int32_t> key(ne);
+    for (size_t e = 0; e < ne; ++e) {
+      int32_t k = conn[e * per];
+      for (int a = 1; a < per; ++a) k = std::min(k, conn[e * per + a]);
+      key[e] = k;
+      ++start[(size_t)k + 1];
+    }
+    for (int64_t v = 0; v < m.n_nodes; ++v) start[v + 1] += start[v];
+    std::vector<int32_t> c2(conn.size());
+    std::vector<int16_t> m2(ne);
+    for (size_t e = 0; e < ne; ++e) {
+      const int64_t d = start[key[e]]++;
+      std::copy(conn.begin() + e * per, conn.begin() + (e + 1) * per, c2.begin() + d * per);
+      m2[d] = mat[e];
+    }
+    conn.swap(c2);
+    mat.swap(m2);
+  };
+  locality_sort(bc, bm, 8);
+  locality_sort(pc, pm, 4);
+  locality_sort(fc, fm, 8);
   D.n_brick = (int64_t)bm.size();
   D.n_plate = (int64_t)pm.size();
   D.n_fluid = (int64_t)fm.size();
@@ -684,7 +836,9 @@ int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms) {
   A.flags = D.flags.p;
   int sms = 0, per_hex = 0, per_quad = 0;
   ELP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D.device));
-  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_hex, assemble_hex_kernel, kThreads, 0));
+  const bool df = m.assembly == ELP_ASSEMBLY_DOUBLE_FLOAT;
+  auto hex_kernel = df ? assemble_hex_kernel<true> : assemble_hex_kernel<false>;
+  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_hex, hex_kernel, kThreads, 0));
   ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_quad, assemble_quad_kernel, kThreads, 0));
   // persistent grids: one resident wave over the items of each kernel
   const int64_t g_hex = std::min<int64_t>((int64_t)sms * std::max(1, per_hex), A.items_brick + A.items_fluid);
@@ -693,7 +847,7 @@ int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms) {
   ELP_CUDA(cudaEventCreate(&e0));
   ELP_CUDA(cudaEventCreate(&e1));
   ELP_CUDA(cudaEventRecord(e0, stream));
-  if (g_hex > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, assemble_hex_kernel<<<(unsigned)g_hex, kThreads, 0, stream>>>(A));
+  if (g_hex > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, hex_kernel<<<(unsigned)g_hex, kThreads, 0, stream>>>(A));
   if (g_quad > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, assemble_quad_kernel<<<(unsigned)g_quad, kThreads, 0, stream>>>(A));
   ELP_CUDA(cudaGetLastError());
   ELP_CUDA(cudaEventRecord(e1, stream));

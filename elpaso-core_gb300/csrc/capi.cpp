@@ -129,6 +129,28 @@ int elp_model_assemble(elp_model* h) {
   GUARD_END
 }
 
+int elp_model_set_assembly(elp_model* h, int arithmetic) {
+  GUARD_BEGIN
+  if (!h) { set_error("null model"); return ELP_ERR_ARG; }
+  if (arithmetic != ELP_ASSEMBLY_FP64 && arithmetic != ELP_ASSEMBLY_DOUBLE_FLOAT) {
+    set_error("assembly arithmetic must be ELP_ASSEMBLY_FP64 or ELP_ASSEMBLY_DOUBLE_FLOAT");
+    return ELP_ERR_ARG;
+  }
+  Model& m = h->m;
+  if (m.n_members > 1) { set_error("groups assemble in FP64"); return ELP_ERR_ARG; }
+  const bool again = m.assembled && m.assembly != arithmetic;
+  m.assembly = arithmetic;
+  if (again) {
+    float ms = 0.f;
+    m.assembled = false;
+    int rc = device_assemble(m, 0, &ms);
+    if (rc) return rc;
+    m.assembled = true;
+  }
+  return ELP_OK;
+  GUARD_END
+}
+
 int elp_model_time_assembly(elp_model* h, int repeats, double* ms_per_assembly, double* ms_kernel_only) {
   GUARD_BEGIN
   if (!h || !h->m.assembled) { set_error("assemble the model first"); return ELP_ERR_STATE; }

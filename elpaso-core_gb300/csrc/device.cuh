@@ -16,7 +16,7 @@ namespace elp {
   do {                                                                            \
     cudaError_t e_ = (call);                                                      \
     if (e_ != cudaSuccess) {                                                      \
-      set_error(std::string("CUDA: ") + cudaGetErrorString(e_) + " at " __FILE__); \
+      set_error(std::string("CUDA: ") + cudaGetErrorString(e_) + " at " __FILE__ ":" + std::to_string(__LINE__)); \
       if (e_ == cudaErrorMemoryAllocation) {                                      \
         cudaGetLastError();                                                       \
         return ELP_ERR_NOMEM;                                                     \

@@ -572,12 +572,13 @@ __global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* _
   if (p == 0 || b == 0) return;
   const int tiles = (b + kSchurTile - 1) / kSchurTile, nch = (p + kTcKC - 1) / kTcKC;
   const int nA = tiles * nch;
-  int blk = blockIdx.z;
-  if (blk >= 2 * nA) return;
   const float2* F = arena + s * L.arena_size + L.foff[f];
   char* base = reinterpret_cast<char*>(pack) + s * slot_bytes + pack_base[f];
   // word of (row, k) within a plane, k = 4 kq + (0..3) stored contiguously
   auto row16 = [](int row, int kq) { return ((row >> 3) * (kTcKC >> 2) + kq) * 32 + (row & 7) * 4; };
+  // blocks z, z + gridDim.z, ...: the largest fronts have more than 65,535
+  for (int blk0 = blockIdx.z; blk0 < 2 * nA; blk0 += gridDim.z) {
+  int blk = blk0;
   if (blk < nA) {
     const int tr = blk / nch, c = blk % nch;
     uint32_t* P = reinterpret_cast<uint32_t*>(base + (int64_t)blk * kSchurABlock);
@@ -621,6 +622,7 @@ __global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* _
       *reinterpret_cast<uint4*>(&P[0 * PL + w_im]) = ih;
       *reinterpret_cast<uint4*>(&P[1 * PL + w_im]) = il;
     }
+  }
   }
 }
 

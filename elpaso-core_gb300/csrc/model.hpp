@@ -126,6 +126,7 @@ struct Model {
   int n_members = 1;
 
   Tuning tune;
+  int assembly = 0;  // ELP_ASSEMBLY_FP64 or ELP_ASSEMBLY_DOUBLE_FLOAT
 
   int64_t n_elements_total = 0;
   bool assembled = false;

@@ -735,7 +735,18 @@ struct SolveArgs {
   int64_t arena_size, n, cb_total;
   const int* active;
   int u12_ld_p;  // U12 after the m x p panel with ld p (factor store), else in place with ld m
+  // levels whose front vector does not fit shared memory: one global slice of
+  // gvec_stride entries per (front of the level, slot), else null
+  void* gvec;
+  int64_t gvec_stride;
 };
+
+// the sweep kernels' working vector: the CTA's global slice, or shared memory
+template <class V>
+__device__ __forceinline__ V* solve_buf(const SolveArgs& S, unsigned char* smraw) {
+  return S.gvec ? reinterpret_cast<V*>(S.gvec) + ((int64_t)blockIdx.y * S.count + blockIdx.x) * S.gvec_stride
+                : reinterpret_cast<V*>(smraw);
+}
 
 // dst[k] = src[idx[k]] for k < count: every thread issues the index loads of
 // four entries, then their value loads, so the dependent pairs of loads
@@ -764,7 +775,7 @@ __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec
                                                  typename Vec2<R>::T* __restrict__ cb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
-  V* w = reinterpret_cast<V*>(smraw);
+  V* w = solve_buf<V>(S, smraw);
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
   if (!S.active[s]) return;
@@ -852,7 +863,8 @@ __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename 
                                                     typename Vec2<R>::T* __restrict__ cb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
-  V* y = reinterpret_cast<V*>(smraw);
+  // global slices: the forward launch of this level left y_p in its first p entries
+  V* y = solve_buf<V>(S, smraw);
   __shared__ V part[8][32];
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -862,7 +874,7 @@ __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename 
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   const V* zs = z + s * S.n;
-  gather_rows(y, zs, I, p);
+  if (!S.gvec) gather_rows(y, zs, I, p);
   __syncthreads();
   const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
   const int i = blockIdx.z * 32 + lane;
@@ -900,7 +912,8 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
                                                  typename Vec2<R>::T* __restrict__ tb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
-  V* xb = reinterpret_cast<V*>(smraw);
+  // global slices: k_gather_border filled the first b entries with x_b
+  V* xb = solve_buf<V>(S, smraw);
   __shared__ V part[8][32];
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -910,7 +923,7 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   const V* zs = z + s * S.n;
-  gather_rows(xb, zs, I + p, b);
+  if (!S.gvec) gather_rows(xb, zs, I + p, b);
   __syncthreads();
   const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
   const int r = blockIdx.z * 32 + lane;
@@ -941,13 +954,26 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   }
 }
 
+// global slices only: x_b of each (front, slot) into the first b entries of
+// its slice, once, for the k_bwd_u12 CTAs that share it
+template <class R>
+__global__ void __launch_bounds__(256) k_gather_border(SolveArgs S, const typename Vec2<R>::T* __restrict__ z) {
+  using V = typename Vec2<R>::T;
+  const int f = S.list[blockIdx.x];
+  const int s = blockIdx.y;
+  if (!S.active[s]) return;
+  const int p = S.fp[f], b = S.fb[f];
+  V* xb = reinterpret_cast<V*>(S.gvec) + ((int64_t)blockIdx.y * S.count + blockIdx.x) * S.gvec_stride;
+  gather_rows(xb, z + s * S.n, S.dofs + S.idx_off[f] + p, b);
+}
+
 template <class R>
 __global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                   typename Vec2<R>::T* __restrict__ z,
                                                   const typename Vec2<R>::T* __restrict__ tb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
-  V* w = reinterpret_cast<V*>(smraw);
+  V* w = solve_buf<V>(S, smraw);
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
   if (!S.active[s]) return;
@@ -1569,6 +1595,11 @@ Tuning resolved_tuning(const Model& m) {
   return t;
 }
 
+bool solve_global_forced() {
+  static const bool v = getenv("ELP_SOLVE_GLOBAL") && std::string(getenv("ELP_SOLVE_GLOBAL")) == "1";
+  return v;
+}
+
 WorkspacePlan workspace_plan(const Model& m) {
   const Symbolic& S = *m.sym;
   const Tuning tn = resolved_tuning(m);
@@ -1585,6 +1616,8 @@ WorkspacePlan workspace_plan(const Model& m) {
     for (int t : S.level_fronts[l]) {
       const FrontInfo& F = S.fronts[t];
       L.max_b = std::max(L.max_b, F.b);
+      L.max_p = std::max(L.max_p, F.p);
+      L.max_m = std::max(L.max_m, F.p + F.b);
       if (F.p > 0 && F.b > 0) {
         const int64_t tiles = (F.b + kSchurTile - 1) / kSchurTile, nch = (F.p + kTcKC - 1) / kTcKC;
         off += tiles * nch * (kSchurABlock + kSchurBBlock);
@@ -1592,6 +1625,11 @@ WorkspacePlan workspace_plan(const Model& m) {
     }
     P.max_count = std::max<int64_t>(P.max_count, L.count);
     if (pack_all_levels || packed_schur_level(L, tn)) P.pack_max = std::max(P.pack_max, off);
+    for (int prec = 0; prec < 2; ++prec) {
+      const int64_t elem = prec == ELP_MIXED ? sizeof(float2) : sizeof(double2);
+      if (solve_level_global(L.max_m, L.max_p, elem))
+        P.gvec[prec] = std::max<int64_t>(P.gvec[prec], (int64_t)L.count * (L.max_m + L.max_p));
+    }
   }
   return P;
 }
@@ -1613,6 +1651,7 @@ int64_t workspace_bytes(const Model& m, int precision, int slots, int store) {
   b += S * (int64_t)(sizeof(Coef) * m.n_members + 16 + nparts * 16 + 4 + 32) + 4;  // coef, norms, partials, flags
   if (m.n_members > 1) b += S * m.n_members * 20;                                   // member norms, flags
   b += max_count * S * swapmap_ints<32>() * 4;
+  b += S * D.gvec[precision == ELP_MIXED ? 1 : 0] * elem;                    // global solve vectors
   if (precision == ELP_MIXED) {
     b += S * D.pack_max;
     const int64_t rst = kGmresRestart;
@@ -1682,6 +1721,10 @@ static int workspace_alloc(Model& m, Workspace& w, int precision, int slots, int
   ELP_CUDA(w.cb.alloc((size_t)slots * std::max<int64_t>(1, D.cb_total) * w.elem));
   ELP_CUDA(w.z.alloc((size_t)slots * n * w.elem));
   ELP_CUDA(w.tb.alloc((size_t)slots * n * w.elem));
+  {
+    const int64_t gv = workspace_plan(m).gvec[precision == ELP_MIXED ? 1 : 0];
+    if (gv > 0) ELP_CUDA(w.gvec.alloc((size_t)slots * gv * w.elem));
+  }
   ELP_CUDA(w.perm.alloc((size_t)slots * n));
   ELP_CUDA(w.dscale.alloc((size_t)slots * n));
   ELP_CUDA(w.x.alloc((size_t)slots * n));
@@ -1903,7 +1946,7 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
       float2* fa = reinterpret_cast<float2*>(arena);
       uint32_t* pk = reinterpret_cast<uint32_t*>(w.pack.p);
       if (packed) {
-        dim3 gp(LV.count, S_used, (unsigned)LV.pack_blocks);
+        dim3 gp(LV.count, S_used, (unsigned)std::min(65535, LV.pack_blocks));
         PROF_LAUNCH(KC_PACK, st, k_pack_schur<NB><<<gp, 256, 0, st>>>(L, fa, pk, D.pack_base.p, LV.pack_bytes));
       }
       LevelArgs Lc = L;
@@ -1975,7 +2018,16 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
   S.n = m.n;
   S.cb_total = std::max<int64_t>(1, D.cb_total);
   S.active = mask;
+  S.gvec = nullptr;
+  S.gvec_stride = 0;
   const V* arena = reinterpret_cast<const V*>(compact ? w.fac.p : w.arena.p);
+  // levels whose front vector exceeds shared memory work on global slices
+  auto level_buffers = [&](const DeviceSymbolic::Level& LV) -> bool {
+    const bool glob = solve_level_global(LV.max_m, LV.max_p, sizeof(V));
+    S.gvec = glob ? (void*)w.gvec.p : nullptr;
+    S.gvec_stride = LV.max_m + LV.max_p;
+    return glob;
+  };
   V* z = reinterpret_cast<V*>(w.z.p);
   V* cb = reinterpret_cast<V*>(w.cb.p);
   for (size_t l = 0; l < D.levels.size(); ++l) {
@@ -1983,11 +2035,14 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     prof_set_level(32 + (int)l);  // solve sweeps: levels 32.. in the per-level table
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
-    size_t sm = (size_t)(LV.max_m + LV.max_p) * sizeof(V);  // front vector + permutation buffer
+    const bool glob = level_buffers(LV);
+    if (glob && !w.gvec.p) { set_error("solve workspace lacks its global front vectors"); return ELP_ERR_STATE; }
+    // front vector + permutation buffer
+    size_t sm = glob ? 0 : (size_t)(LV.max_m + LV.max_p) * sizeof(V);
     PROF_LAUNCH(KC_FORWARD, st, k_forward<R><<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, w.perm.p, z, cb));
     if (LV.max_b > 0) {
       const unsigned chunks = (unsigned)((LV.max_b + 31) / 32);
-      PROF_LAUNCH(KC_FWD_BORDER, st, k_fwd_border<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)LV.max_p * sizeof(V), st>>>(
+      PROF_LAUNCH(KC_FWD_BORDER, st, k_fwd_border<R><<<dim3(LV.count, S_used, chunks), 256, glob ? 0 : (size_t)LV.max_p * sizeof(V), st>>>(
                                       S, arena, z, cb));
     }
   }
@@ -1997,10 +2052,14 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     prof_set_level(32 + l);
     S.list = D.level_list.p + LV.start;
     S.count = LV.count;
+    const bool glob = level_buffers(LV);
+    if (glob && !w.gvec.p) { set_error("solve workspace lacks its global front vectors"); return ELP_ERR_STATE; }
     const unsigned chunks = (unsigned)((LV.max_p + 31) / 32);
-    PROF_LAUNCH(KC_BWD_U12, st, k_bwd_u12<R><<<dim3(LV.count, S_used, chunks), 256, (size_t)std::max(1, LV.max_b) * sizeof(V), st>>>(
-                                     S, arena, z, tb));
-    size_t sm = (size_t)LV.max_p * sizeof(V);
+    if (glob && LV.max_b > 0)
+      PROF_LAUNCH(KC_BWD_U12, st, k_gather_border<R><<<dim3(LV.count, S_used), 256, 0, st>>>(S, z));
+    PROF_LAUNCH(KC_BWD_U12, st, k_bwd_u12<R><<<dim3(LV.count, S_used, chunks), 256,
+                                                glob ? 0 : (size_t)std::max(1, LV.max_b) * sizeof(V), st>>>(S, arena, z, tb));
+    size_t sm = glob ? 0 : (size_t)LV.max_p * sizeof(V);
     PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, z, tb));
   }
   prof_set_level(-1);
@@ -2010,12 +2069,7 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
 
 template <class R>
 static int solve_smem(const Model& m) {
-  using V = typename Vec2<R>::T;
-  const size_t smem_need = 2 * (size_t)m.dsym->max_front * sizeof(V);  // k_forward: front + permutation buffer
-  if (smem_need > 227 * 1024) {
-    set_error("front larger than the shared-memory solve buffer (max 227 KB)");
-    return ELP_ERR_NOMEM;
-  }
+  (void)m;  // levels beyond solve_smem_cap run on global slices (solve_sweep)
   // The limit is raised once per process to what the device allows: solves of
   // different models run concurrently (server workers), and a per-model value
   // set by one thread could lower the limit under another thread's launch.
@@ -2025,6 +2079,10 @@ static int solve_smem(const Model& m) {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (optin < kSolveSmemOptin) {
+      rc = ELP_ERR_CUDA;
+      return;
+    }
     const void* fns[4] = {(const void*)k_forward<R>, (const void*)k_backward<R>, (const void*)k_fwd_border<R>,
                           (const void*)k_bwd_u12<R>};
     for (const void* fn : fns) {
@@ -2861,7 +2919,8 @@ int front_update_test(int kernel, int p, int b, int step, int slots, float* fron
     DevBuf<char> pack;
     ELP_CUDA(pack.alloc((size_t)slots * pack_bytes));
     uint32_t* pk = reinterpret_cast<uint32_t*>(pack.p);
-    k_pack_schur<NB><<<dim3(1, slots, (unsigned)(2 * tiles * nch)), 256, 0, st>>>(L, arena.p, pk, pbase.p, pack_bytes);
+    k_pack_schur<NB><<<dim3(1, slots, (unsigned)std::min<int64_t>(65535, 2 * tiles * nch)), 256, 0, st>>>(L, arena.p, pk, pbase.p,
+                                                                                               pack_bytes);
     const int64_t gz = std::min<int64_t>(tiles * tiles, std::max<int64_t>(1, (2 * num_sms() + slots - 1) / slots));
     k_schur_tc<NB><<<dim3(1, slots, (unsigned)gz), kSchurThreads, kSchurSmemBytes, st>>>(L, arena.p, pk, pbase.p,
                                                                                          pack_bytes, err.p, 0);

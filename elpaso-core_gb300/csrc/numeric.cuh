@@ -197,6 +197,7 @@ struct Workspace {
   DevBuf<char> cb;                // slots x cb_total complex (solve contributions)
   DevBuf<char> z;                 // slots x n complex (solve vector, front precision)
   DevBuf<char> tb;                // slots x n complex (backward pivot-row buffer)
+  DevBuf<char> gvec;              // slots x WorkspacePlan::gvec complex (global solve vectors), or empty
   DevBuf<int32_t> perm;           // slots x n local pivot rows
   DevBuf<double> dscale;          // slots x n symmetric diagonal scaling
   DevBuf<double2> x, r, f;        // slots x n FP64 solution, residual, rhs
@@ -246,7 +247,21 @@ struct Workspace {
 // Sizes a workspace depends on, from the host symbolic phase alone.
 struct WorkspacePlan {
   int64_t arena = 0, arena_full = 0, fac = 0, cb_total = 0, max_count = 1, pack_max = 0;  // arena: the pool
+  // complex entries per frequency slot of the solve sweeps' global front
+  // vectors, [0] FP64 plain, [1] FP32 mixed: levels whose front vector does
+  // not fit shared memory keep it in global memory (solve_level_global)
+  int64_t gvec[2] = {0, 0};
 };
+// Dynamic shared memory the solve sweeps may take per CTA (227 KB opt-in less
+// the kernels' static buffers of at most 1,056 complex entries), and whether a
+// level with these largest front / pivot counts runs them on global buffers.
+// ELP_SOLVE_GLOBAL=1 puts every level on global buffers (same arithmetic).
+constexpr int64_t kSolveSmemOptin = 227 * 1024;
+inline int64_t solve_smem_cap(int64_t elem) { return kSolveSmemOptin - 1056 * elem; }
+bool solve_global_forced();
+inline bool solve_level_global(int64_t max_m, int64_t max_p, int64_t elem) {
+  return solve_global_forced() || (max_m + max_p) * elem > solve_smem_cap(elem);
+}
 WorkspacePlan workspace_plan(const Model& m);
 
 int device_upload_symbolic(Model& m);

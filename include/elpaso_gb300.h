@@ -233,6 +233,22 @@ int elp_model_create(const elp_model_desc* desc, elp_model** out);
  * element loop analysisfrequencybasic.cpp:281-304. */
 int elp_model_assemble(elp_model* m);
 
+/* Arithmetic of the Brick8 / Fluid8 element contractions (no counterpart in
+ * the reference, whose element code is FP64):
+ *   ELP_ASSEMBLY_FP64 (default): FP64 throughout, the drop-in;
+ *   ELP_ASSEMBLY_DOUBLE_FLOAT: the shape gradients and the Gauss-point sums
+ *     in FP32 pairs (error-free products and sums, ~48 significant bits);
+ *     J, det J and J^-1 in FP64. Entries differ from the FP64 ones by
+ *     ~1e-14 of the sum of the magnitudes of their terms (well inside the
+ *     1e-12 parity bar), but a residual measured against an FP64-assembled
+ *     matrix then carries ~1e-14 || |A| |x| || / ||f||: keep FP64 for
+ *     models whose || |A| |x| || is far above ||f|| (clamped stiff plates).
+ * DSG4 plates and interface quads are FP64 in both. Setting it on an
+ * assembled model re-runs the assembly. */
+#define ELP_ASSEMBLY_FP64 0
+#define ELP_ASSEMBLY_DOUBLE_FLOAT 1
+int elp_model_set_assembly(elp_model* m, int arithmetic);
+
 /* Symbolic phase: nested-dissection ordering, assembly tree, front index
  * maps (once per model; the reference leaves this to MUMPS's analysis). */
 int elp_model_analyse(elp_model* m);

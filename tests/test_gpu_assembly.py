@@ -75,3 +75,35 @@ def test_full_size_clamped_plate_matches_oracle(elp, meshes, oracle):
     assert m.info()["n_dofs"] == 3969 and m.info()["nnz"] == 234423
     om = 2 * np.pi * 100.0
     assert row_rel(s.row_ptr, m.system_values(om), s.values(om)) <= TOL
+
+
+@pytest.mark.parametrize("name", ["solid_plate", "plate_cavity", "solid_cube_3mat"])
+def test_double_float_assembly_matches_oracle(elp, meshes, oracle, name):
+    """ELP_ASSEMBLY_DOUBLE_FLOAT: Brick8 / Fluid8 contractions in FP32 pairs.
+    The same 1e-12 per-row bar against the oracle; the values are not the
+    FP64 assembly's bits (the other arithmetic ran) but within 1e-13 per row
+    of them."""
+    d = models(meshes)[name]
+    m64 = elp.Model(d).assemble()
+    mdf = elp.Model(d).set_assembly(elp.ASSEMBLY_DOUBLE_FLOAT).assemble()
+    s = oracle.System(d)
+    for f_hz in (1.0, 437.0):
+        om = 2 * np.pi * f_hz
+        a = mdf.system_values(om)
+        assert row_rel(s.row_ptr, a, s.values(om)) <= TOL
+        b = m64.system_values(om)
+        assert row_rel(s.row_ptr, a, b) <= 1e-13
+        assert np.any(a != b)
+
+
+def test_set_assembly_on_an_assembled_model_assembles_again(elp, meshes):
+    d = meshes.solid_cube(3, n_materials=2)
+    m = elp.Model(d).assemble()
+    a64 = m.system_values(2 * np.pi * 50.0)
+    m.set_assembly(elp.ASSEMBLY_DOUBLE_FLOAT)
+    adf = m.system_values(2 * np.pi * 50.0)
+    m.set_assembly(elp.ASSEMBLY_FP64)
+    assert np.any(adf != a64)
+    assert row_rel(m.pattern()[0], m.system_values(2 * np.pi * 50.0), a64) <= 1e-15
+    with pytest.raises(elp.ElpasoError):
+        m.set_assembly(7)

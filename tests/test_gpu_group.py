@@ -3,15 +3,18 @@
 A group is its members' disjoint union: one launch per tree level over the
 fronts of all members, each member at its own frequencies. Bars, per member
 and frequency, as for single models: ||f - A x||_2 / ||f||_2 <= 1e-10 with
-the oracle's matrix of that member, the error against the oracle's FP64
-solve within 3 kappa_1(A_ff) (res_1 + res_ref_1), and the reported residual
-within 1e-10 of the one measured here. A group of one model takes the single-model
+the oracle's matrix of that member, plus the FP64 floor 4 eps || |A| |x| || /
+||f|| of measuring it with a matrix summed in another order (1.4e6 eps on the
+clamped solid plate at 451 Hz, whose oracle solution itself has residual
+1.4e-10), the error against the oracle's FP64 solve within
+3 kappa_1(A_ff) (res_1 + res_ref_1), and the reported residual within the
+same bar of the one measured here. A group of one model takes the single-model
 path and equals the model solved alone up to assembly rounding.
 """
 import numpy as np
 import pytest
 
-from test_gpu_solve import cond1
+from test_gpu_solve import cond1, residual_floor
 
 pytestmark = pytest.mark.gpu
 
@@ -36,10 +39,11 @@ def test_group_members_match_the_oracle(elp, meshes, oracle, prec):
             A, f = s.matrix(om), s.rhs(om)
             x = xs[k][j]
             res = np.linalg.norm(f - A @ x) / np.linalg.norm(f)
-            assert res <= 1e-10, (k, j, res)
-            # the library's residual is double-double; this one is plain FP64, good to ~1e-10 on the
-            # clamped plate (|| |A| |x| || / ||f|| ~ 1e6): the bar of the single-model solve tests
-            assert abs(infos[k][j]["rel_residual"] - res) <= 1e-10, (k, j, infos[k][j], res)
+            bar = 1e-10 + residual_floor(A, x, f)
+            assert res <= bar, (k, j, res, bar)
+            # the library's residual is double-double with its own matrix; this one is plain FP64
+            # with the oracle's
+            assert abs(infos[k][j]["rel_residual"] - res) <= bar, (k, j, infos[k][j], res)
             assert infos[k][j]["converged"] == 1
             xr = s.solve(om)
             n1 = np.linalg.norm(f, 1)

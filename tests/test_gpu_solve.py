@@ -24,6 +24,13 @@ def cond1(A):
     return sla.onenormest(A) * sla.onenormest(inv)
 
 
+def residual_floor(A, x, f, unit=2.0 ** -53):
+    """4 u || |A| |x| || / ||f||: how far ||f - A x|| / ||f|| can move when A's
+    entries move by a few units of roundoff u (another summation order of the
+    assembly, or the FP64 product that measures it)."""
+    return 4.0 * unit * np.linalg.norm(abs(A) @ np.abs(x)) / np.linalg.norm(f)
+
+
 def check(elp, oracle, d, f_list, prec):
     m = elp.Model(d).assemble().analyse()
     s = oracle.System(d)
@@ -132,3 +139,21 @@ def test_brick_face_tractions(elp, meshes, oracle, prec):
     force: the right-hand side built at model creation reaches the solve."""
     from test_loads import traction_brick
     check(elp, oracle, traction_brick(meshes, nx=20, ny=20, count=40), [100.0], prec)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_double_float_assembled_models_solve(elp, meshes, oracle, prec):
+    """Models assembled with the double-float element contractions solve to
+    the residual bar against the oracle's FP64 matrix, plus the floor that
+    ~2^-46 entry differences allow (4 2^-46 || |A| |x| || / ||f||, below
+    1e-11 on these two models)."""
+    for d in (meshes.cube(5), meshes.plate_cavity(8, 6, 4, 0.6, 0.4, 0.3)):
+        m = elp.Model(d).set_assembly(elp.ASSEMBLY_DOUBLE_FLOAT).assemble().analyse()
+        s = oracle.System(d)
+        oms = 2 * np.pi * np.array([7.0, 180.0, 455.0])
+        x, infos = m.solve(oms, precision=prec)
+        for k, om in enumerate(oms):
+            A, f = s.matrix(om), s.rhs(om)
+            res = np.linalg.norm(f - A @ x[k]) / np.linalg.norm(f)
+            assert infos[k]["converged"] == 1
+            assert res <= RES_TOL + residual_floor(A, x[k], f, unit=2.0 ** -46), (d.name, k, res)
