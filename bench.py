@@ -274,7 +274,7 @@ def serving_measurement(elp, meshes, n_stream=300, n_probe=40):
     """Latency under load through the C-ABI serving loop (elp_server_*), the
     serving workload's shape: 8 resident models with DOF counts log-uniform
     in 5k-500k (seeded, stratified), alternately DSG4 shell plates and Brick8
-    solid plates, each request 1-64 frequencies from U(1, 500) Hz on a
+    steel slabs, each request 1-64 frequencies from U(1, 500) Hz on a
     uniformly chosen model. Capacity = requests/s of a saturating burst of
     `n_probe` requests; then a Poisson stream of `n_stream` requests at 80%
     of that capacity (the serving workload names 10,000; 300 keep the bench

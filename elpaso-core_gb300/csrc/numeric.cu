@@ -741,11 +741,13 @@ struct SolveArgs {
   int64_t gvec_stride;
 };
 
-// the sweep kernels' working vector: the CTA's global slice, or shared memory
-template <class V>
+// the sweep kernels' working vector: the CTA's global slice (G), or shared
+// memory; a compile-time choice, so that the shared-memory variants address
+// shared memory directly instead of through generic pointers
+template <class V, bool G>
 __device__ __forceinline__ V* solve_buf(const SolveArgs& S, unsigned char* smraw) {
-  return S.gvec ? reinterpret_cast<V*>(S.gvec) + ((int64_t)blockIdx.y * S.count + blockIdx.x) * S.gvec_stride
-                : reinterpret_cast<V*>(smraw);
+  if (G) return reinterpret_cast<V*>(S.gvec) + ((int64_t)blockIdx.y * S.count + blockIdx.x) * S.gvec_stride;
+  return reinterpret_cast<V*>(smraw);
 }
 
 // dst[k] = src[idx[k]] for k < count: every thread issues the index loads of
@@ -769,13 +771,13 @@ __device__ __forceinline__ void gather_rows(V* dst, const V* __restrict__ src, c
   }
 }
 
-template <class R>
+template <class R, bool G>
 __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                  const int32_t* __restrict__ perm, typename Vec2<R>::T* __restrict__ z,
                                                  typename Vec2<R>::T* __restrict__ cb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
-  V* w = solve_buf<V>(S, smraw);
+  V* w = solve_buf<V, G>(S, smraw);
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
   if (!S.active[s]) return;
@@ -857,14 +859,14 @@ __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec
 // border rows of the forward step: cb -= L21 y_p. A CTA takes 32 border rows
 // (lane = row, loads coalesced along the column); its 8 warps split the p
 // columns and their partial sums are added in a fixed order.
-template <class R>
+template <class R, bool G>
 __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                     const typename Vec2<R>::T* __restrict__ z,
                                                     typename Vec2<R>::T* __restrict__ cb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
   // global slices: the forward launch of this level left y_p in its first p entries
-  V* y = solve_buf<V>(S, smraw);
+  V* y = solve_buf<V, G>(S, smraw);
   __shared__ V part[8][32];
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -874,7 +876,7 @@ __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename 
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   const V* zs = z + s * S.n;
-  if (!S.gvec) gather_rows(y, zs, I, p);
+  if (!G) gather_rows(y, zs, I, p);
   __syncthreads();
   const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
   const int i = blockIdx.z * 32 + lane;
@@ -906,14 +908,14 @@ __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename 
 // pivot rows of the backward step: t = y_p - U12 x_b. A CTA takes 32 pivot
 // rows (lane = row); its 8 warps split the b border columns, partial sums
 // added in a fixed order.
-template <class R>
+template <class R, bool G>
 __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                  const typename Vec2<R>::T* __restrict__ z,
                                                  typename Vec2<R>::T* __restrict__ tb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
   // global slices: k_gather_border filled the first b entries with x_b
-  V* xb = solve_buf<V>(S, smraw);
+  V* xb = solve_buf<V, G>(S, smraw);
   __shared__ V part[8][32];
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
@@ -923,7 +925,7 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
   const V* zs = z + s * S.n;
-  if (!S.gvec) gather_rows(xb, zs, I + p, b);
+  if (!G) gather_rows(xb, zs, I + p, b);
   __syncthreads();
   const int lane = threadIdx.x & 31, wv = threadIdx.x >> 5;
   const int r = blockIdx.z * 32 + lane;
@@ -967,13 +969,13 @@ __global__ void __launch_bounds__(256) k_gather_border(SolveArgs S, const typena
   gather_rows(xb, z + s * S.n, S.dofs + S.idx_off[f] + p, b);
 }
 
-template <class R>
+template <class R, bool G>
 __global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                   typename Vec2<R>::T* __restrict__ z,
                                                   const typename Vec2<R>::T* __restrict__ tb) {
   using V = typename Vec2<R>::T;
   extern __shared__ unsigned char smraw[];
-  V* w = solve_buf<V>(S, smraw);
+  V* w = solve_buf<V, G>(S, smraw);
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
   if (!S.active[s]) return;
@@ -2039,10 +2041,12 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     if (glob && !w.gvec.p) { set_error("solve workspace lacks its global front vectors"); return ELP_ERR_STATE; }
     // front vector + permutation buffer
     size_t sm = glob ? 0 : (size_t)(LV.max_m + LV.max_p) * sizeof(V);
-    PROF_LAUNCH(KC_FORWARD, st, k_forward<R><<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, w.perm.p, z, cb));
+    auto fwd = glob ? k_forward<R, true> : k_forward<R, false>;
+    PROF_LAUNCH(KC_FORWARD, st, fwd<<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, w.perm.p, z, cb));
     if (LV.max_b > 0) {
       const unsigned chunks = (unsigned)((LV.max_b + 31) / 32);
-      PROF_LAUNCH(KC_FWD_BORDER, st, k_fwd_border<R><<<dim3(LV.count, S_used, chunks), 256, glob ? 0 : (size_t)LV.max_p * sizeof(V), st>>>(
+      auto fb = glob ? k_fwd_border<R, true> : k_fwd_border<R, false>;
+      PROF_LAUNCH(KC_FWD_BORDER, st, fb<<<dim3(LV.count, S_used, chunks), 256, glob ? 0 : (size_t)LV.max_p * sizeof(V), st>>>(
                                       S, arena, z, cb));
     }
   }
@@ -2057,10 +2061,12 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
     const unsigned chunks = (unsigned)((LV.max_p + 31) / 32);
     if (glob && LV.max_b > 0)
       PROF_LAUNCH(KC_BWD_U12, st, k_gather_border<R><<<dim3(LV.count, S_used), 256, 0, st>>>(S, z));
-    PROF_LAUNCH(KC_BWD_U12, st, k_bwd_u12<R><<<dim3(LV.count, S_used, chunks), 256,
-                                                glob ? 0 : (size_t)std::max(1, LV.max_b) * sizeof(V), st>>>(S, arena, z, tb));
+    auto bu = glob ? k_bwd_u12<R, true> : k_bwd_u12<R, false>;
+    PROF_LAUNCH(KC_BWD_U12, st, bu<<<dim3(LV.count, S_used, chunks), 256,
+                                     glob ? 0 : (size_t)std::max(1, LV.max_b) * sizeof(V), st>>>(S, arena, z, tb));
     size_t sm = glob ? 0 : (size_t)LV.max_p * sizeof(V);
-    PROF_LAUNCH(KC_BACKWARD, st, k_backward<R><<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, z, tb));
+    auto bwd = glob ? k_backward<R, true> : k_backward<R, false>;
+    PROF_LAUNCH(KC_BACKWARD, st, bwd<<<dim3(LV.count, S_used), solve_threads(LV.max_p), sm, st>>>(S, arena, z, tb));
   }
   prof_set_level(-1);
   ELP_CUDA(cudaGetLastError());
@@ -2083,11 +2089,12 @@ static int solve_smem(const Model& m) {
       rc = ELP_ERR_CUDA;
       return;
     }
-    const void* fns[4] = {(const void*)k_forward<R>, (const void*)k_backward<R>, (const void*)k_fwd_border<R>,
-                          (const void*)k_bwd_u12<R>};
+    const void* fns[4] = {(const void*)k_forward<R, false>, (const void*)k_backward<R, false>,
+                          (const void*)k_fwd_border<R, false>, (const void*)k_bwd_u12<R, false>};
     for (const void* fn : fns) {
       cudaFuncAttributes a;
       if (cudaFuncGetAttributes(&a, fn) != cudaSuccess ||
+          optin - (int64_t)a.sharedSizeBytes < solve_smem_cap(sizeof(typename Vec2<R>::T)) ||
           cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes) !=
               cudaSuccess) {
         cudaGetLastError();

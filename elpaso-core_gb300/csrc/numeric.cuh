@@ -253,11 +253,12 @@ struct WorkspacePlan {
   int64_t gvec[2] = {0, 0};
 };
 // Dynamic shared memory the solve sweeps may take per CTA (227 KB opt-in less
-// the kernels' static buffers of at most 1,056 complex entries), and whether a
+// 2,048 complex entries for the kernels' static buffers, which hold at most
+// 1,152; solve_smem checks it against the compiled kernels), and whether a
 // level with these largest front / pivot counts runs them on global buffers.
 // ELP_SOLVE_GLOBAL=1 puts every level on global buffers (same arithmetic).
 constexpr int64_t kSolveSmemOptin = 227 * 1024;
-inline int64_t solve_smem_cap(int64_t elem) { return kSolveSmemOptin - 1056 * elem; }
+inline int64_t solve_smem_cap(int64_t elem) { return kSolveSmemOptin - 2048 * elem; }
 bool solve_global_forced();
 inline bool solve_level_global(int64_t max_m, int64_t max_p, int64_t elem) {
   return solve_global_forced() || (max_m + max_p) * elem > solve_smem_cap(elem);
