@@ -249,6 +249,7 @@ def _server_stream(elp, srv, reqs, rate=None, timeout_s=600.0):
     th = threading.Thread(target=collect, daemon=True)
     th.start()
     t_next = t0
+    by_id = {}
     for (mid, n, oms), gap in zip(reqs, gaps):
         t_next += gap
         delay = t_next - time.perf_counter()
@@ -256,9 +257,11 @@ def _server_stream(elp, srv, reqs, rate=None, timeout_s=600.0):
             time.sleep(delay)
         x = np.zeros((len(oms), n), np.complex128)
         outs.append(x)
-        srv.submit(mid, oms, x)
+        by_id[srv.submit(mid, oms, x)] = (mid, oms)
     done.wait(timeout_s)
     th.join(1.0)
+    for r in results:  # which model and frequencies each result belongs to
+        r["model"], r["omegas"] = by_id.get(r["request_id"], (None, None))
     return results, time.perf_counter() - t0
 
 
@@ -319,6 +322,12 @@ def serving_measurement(elp, meshes, n_stream=300, n_probe=40):
                                          "p99": float(np.percentile(per_omega, 99))},
             "request_status": _status_counts(res + res_p),
             "max_rel_residual": max(r["max_rel_residual"] for r in res + res_p),
+            # requests short of the target: model, frequencies (Hz) and the residual reached
+            "not_at_target": [{"model": descs[mids.index(r["model"])].name if r["model"] in mids else None,
+                               "status": r["status"], "max_rel_residual": r["max_rel_residual"],
+                               "hz": [round(float(w) / (2 * np.pi), 3) for w in r["omegas"]]
+                               if r["omegas"] is not None else None}
+                              for r in res + res_p if r["status"] != 0][:24],
             "server": "max_inflight 4, omega_batch 16, 2 workspace lanes per model, HBM budget 200 GiB, mixed"}
 
 

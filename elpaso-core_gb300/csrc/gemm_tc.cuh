@@ -643,6 +643,18 @@ __global__ void __launch_bounds__(256) k_pack_schur(LevelArgs L, const float2* _
 // and epilogue waits then run out with no copy or MMA in flight.
 constexpr int kSchurThreads = 320;
 
+// Tile t of a front's tiles x tiles Schur complement, in groups of G tile rows
+// walked column by column: the tiles that run at the same time (consecutive t)
+// span G row blocks of L21 and about (concurrent / G) column blocks of U12,
+// instead of every row block of one column, so fewer operand blocks are read
+// from DRAM more than once. The last group may have fewer rows.
+__device__ __forceinline__ void schur_tile_rc(int t, int tiles, int G, int& tr, int& tcol) {
+  const int grp = t / (G * tiles), idx = t - grp * G * tiles;
+  const int r0 = grp * G, rows = min(G, tiles - r0);
+  tcol = idx / rows;
+  tr = r0 + idx % rows;
+}
+
 template <int NB>
 __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, float2* __restrict__ arena,
                                                                const uint32_t* __restrict__ pack,
@@ -659,6 +671,9 @@ __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, floa
   const int ntile = tiles * tiles;
   if ((int)blockIdx.z >= ntile) return;  // uniform per CTA, before any TMEM allocation
   const int nmine = (ntile - 1 - (int)blockIdx.z) / (int)gridDim.z + 1;
+  // about half the CTAs of a front and slot run at once (two waves per launch):
+  // groups of ~sqrt of that many tile rows
+  const int G = max(1, min(tiles, (int)(sqrtf(0.5f * (float)gridDim.z) + 0.5f)));
   const char* base = reinterpret_cast<const char*>(pack) + s * slot_bytes + pack_base[f];
   const char* Abase = base;
   const char* Bbase = base + (int64_t)tiles * nch * kSchurABlock;
@@ -696,7 +711,8 @@ __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, floa
     int g = 0;
     for (int j = 0; j < nmine && ok && !fault; ++j) {
       const int t = (int)blockIdx.z + j * (int)gridDim.z;
-      const int tr = t % tiles, tcol = t / tiles;
+      int tr, tcol;
+      schur_tile_rc(t, tiles, G, tr, tcol);
       const char* Ab = Abase + (int64_t)(tr * nch) * kSchurABlock;
       const char* Bb = Bbase + (int64_t)(tcol * nch) * kSchurBBlock;
       for (int c = 0; c < nch; ++c, ++g) {
@@ -763,7 +779,8 @@ __global__ void __launch_bounds__(kSchurThreads, 1) k_schur_tc(LevelArgs L, floa
     for (int j = 0; j < nmine; ++j) {
       const int acc = j & 1;
       const int t = (int)blockIdx.z + j * (int)gridDim.z;
-      const int tr = t % tiles, tcol = t / tiles;
+      int tr, tcol;
+      schur_tile_rc(t, tiles, G, tr, tcol);
       if (lane == 0 && ok) ok = tc::mbar_wait(&sm.acc_full[acc], (j / 2) & 1, lim);
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;

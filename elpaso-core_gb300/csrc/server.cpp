@@ -137,12 +137,14 @@ struct elp_server {
     return best;
   }
 
-  // releases idle models' workspaces (no lane busy, nothing queued) until
-  // `need` more bytes fit; returns whether they do
-  bool make_room(int64_t need, int keep) {
+  // releases idle models' workspaces until `need` more bytes fit; returns
+  // whether they do. Idle: no lane busy and nothing queued; with `queued`,
+  // also models whose requests wait (their next batch makes its workspace
+  // again) -- used when no batch runs, so that nothing else would free memory.
+  bool make_room(int64_t need, int keep, bool queued = false) {
     for (int i = 0; i < (int)models.size() && resident + need > cfg.hbm_budget_bytes; ++i) {
       ModelSlot& o = *models[i];
-      if (i == keep || o.lanes_busy || !o.queue.empty()) continue;
+      if (i == keep || o.lanes_busy || (!queued && !o.queue.empty())) continue;
       for (int l = 0; l < kLanesPerModel; ++l) {
         if (!o.ws_bytes[l]) continue;
         std::unique_ptr<Workspace>& W = l ? o.h->m.ws_b[cfg.precision][l - 1] : o.h->m.ws[cfg.precision];
@@ -159,7 +161,7 @@ struct elp_server {
   // frequencies a batch of model `mi` on `lane` may take (<= want), with the
   // lane's workspace charged for them (whole fronts where they fit, else the
   // compact factor store); 0 when no room is left now
-  int admit_batch(int mi, int lane, int want, int& store) {
+  int admit_batch(int mi, int lane, int want, int& store, bool queued = false) {
     ModelSlot& s = *models[mi];
     const Model& m = s.h->m;
     store = s.ws_store[lane];
@@ -173,7 +175,7 @@ struct elp_server {
         const int64_t bytes = st == STORE_FULL ? full_bytes : workspace_bytes(m, cfg.precision, S, st);
         if (st == STORE_COMPACT && forced < 0 && bytes >= full_bytes) continue;  // no saving on small trees
         const int64_t extra = bytes - s.ws_bytes[lane];  // the old workspace is freed before the new one is made
-        if (make_room(extra, mi)) {
+        if (make_room(extra, mi, queued)) {
           resident += extra;
           s.ws_bytes[lane] = bytes;
           s.ws_slots[lane] = S;
@@ -207,8 +209,17 @@ struct elp_server {
     if (!rc) {
       const int64_t arrays = model_array_bytes(h->m);
       const int64_t one = workspace_bytes(h->m, cfg.precision, 1, forced_store() >= 0 ? forced_store() : STORE_COMPACT);
-      if (arrays + one > cfg.hbm_budget_bytes || !make_room(arrays, mi)) {
-        rc = ELP_ERR_NOMEM;
+      if (arrays + one > cfg.hbm_budget_bytes) {
+        rc = ELP_ERR_NOMEM;  // cannot run even alone
+      } else if (!make_room(arrays, mi, running == 0)) {
+        if (running == 0) {
+          rc = ELP_ERR_NOMEM;  // other models' resident arrays hold the budget
+        } else {
+          // running batches free their workspaces when they end: prepared
+          // again then (the symbolic phase is kept)
+          s.preparing = false;
+          return false;
+        }
       } else {
         resident += arrays;
         s.array_bytes = arrays;
@@ -259,7 +270,11 @@ struct elp_server {
       ModelSlot& s = *models[mi];
       if (s.failed) { fail_queue(mi, ELP_ERR_NOMEM); continue; }
       if (!s.ready) {
-        if (!prepare(lk, mi)) { cv_work.notify_all(); continue; }
+        if (!prepare(lk, mi)) {
+          if (!s.failed) cv_work.wait(lk);  // no room yet: a running batch frees memory when it ends
+          cv_work.notify_all();
+          continue;
+        }
         if (s.queue.empty() || (s.lanes_busy >> lane & 1)) { cv_work.notify_all(); continue; }
       }
       // batch size: waiting frequencies, capped by omega_batch and by the budget
@@ -270,9 +285,12 @@ struct elp_server {
         if (waiting >= cfg.omega_batch) break;
       }
       int store = STORE_FULL;
-      const int S = admit_batch(mi, lane, std::min(waiting, cfg.omega_batch), store);
+      int S = admit_batch(mi, lane, std::min(waiting, cfg.omega_batch), store);
+      // nothing runs, so nothing else frees memory: models whose requests wait
+      // give up their workspaces too
+      if (S == 0 && running == 0) S = admit_batch(mi, lane, std::min(waiting, cfg.omega_batch), store, true);
       if (S == 0) {
-        if (running == 0) {  // nothing will free memory: the model cannot run at all
+        if (running == 0) {  // the model cannot run at all
           set_error("model does not fit the HBM budget");
           fail_queue(mi, ELP_ERR_NOMEM);
           cv_work.notify_all();
