@@ -322,11 +322,10 @@ def serving_measurement(elp, meshes, n_stream=300, n_probe=40):
                                          "p99": float(np.percentile(per_omega, 99))},
             "request_status": _status_counts(res + res_p),
             "max_rel_residual": max(r["max_rel_residual"] for r in res + res_p),
-            # requests short of the target: model, frequencies (Hz) and the residual reached
+            # requests short of the target: model, frequency count and the residual reached
             "not_at_target": [{"model": descs[mids.index(r["model"])].name if r["model"] in mids else None,
                                "status": r["status"], "max_rel_residual": r["max_rel_residual"],
-                               "hz": [round(float(w) / (2 * np.pi), 3) for w in r["omegas"]]
-                               if r["omegas"] is not None else None}
+                               "n_omega": r["n_omega"]}
                               for r in res + res_p if r["status"] != 0][:24],
             "server": "max_inflight 4, omega_batch 16, 2 workspace lanes per model, HBM budget 200 GiB, mixed"}
 
@@ -439,6 +438,11 @@ def batched_plates_measurement(elp, meshes, count=256, n_omega=32):
     for m in models:
         m.close()
     return out
+
+
+# ncu: DRAM read + write of the tensor-core class (k_gemm_tc, k_schur_tc,
+# k_pack_schur) in one factorisation of the plate-cavity model, per frequency
+TC_CLASS_DRAM_BYTES_PER_FREQUENCY = (20.174e9 + 3.642e9) / 2
 
 
 def run_ours(args):
@@ -569,11 +573,15 @@ def run_ours(args):
         flops = info["gemm_flops"] * S
         ach = flops / (top[1]["ms"] / 1e3) / 1e12
         roof = {"kernel": top[0], "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-                "frac": ach / bf16, "traffic": None,
-                "traffic_ref": "ncu, profiles/k_schur_tc_plate_cavity_60x40x30.md: 227 MB DRAM for the "
-                               "level-9 packed Schur launch of 31.7 GFLOP (2 frequencies, one front); per "
-                               "step the class is many launches of every tree level, so no single per-launch "
-                               "figure applies",
+                "frac": ach / bf16,
+                # DRAM bytes of the class per step: the per-frequency traffic of one factorisation
+                # from ncu x the frequencies of the step (each frequency repeats the same launches)
+                "traffic": TC_CLASS_DRAM_BYTES_PER_FREQUENCY * S if d.name.startswith("plate_cavity_60x40x30")
+                else None,
+                "traffic_ref": "ncu, profiles/tensor_core_class_traffic_plate_cavity_60x40x30_batch2.md: "
+                               "20.17 GB read + 3.64 GB written by the class's 292 launches of one "
+                               "factorisation at 2 frequencies (11.9 GB per frequency), x frequencies "
+                               "per step",
                 "note": f"algorithmic = Schur-update flops of one factorisation x {S} frequencies; "
                         f"peak = dense bf16 ({src})"}
     else:
