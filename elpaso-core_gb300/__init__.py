@@ -109,12 +109,18 @@ class _Desc(C.Structure):
                 ("n_face_tractions", C.c_int64), ("face_tractions", C.POINTER(_FaceTraction))]
 
 
+def _plain(v):
+    """ctypes arrays (nested) as lists, other values unchanged."""
+    return [_plain(e) for e in v] if isinstance(v, C.Array) else v
+
+
 class _Info(C.Structure):
     _fields_ = [("n_dofs", C.c_int64), ("nnz", C.c_int64), ("n_elements", C.c_int64), ("n_fronts", C.c_int64),
                 ("factor_entries", C.c_int64), ("factor_flops", C.c_double), ("n_levels", C.c_int),
                 ("max_front", C.c_int), ("n_struct_groups", C.c_int), ("gemm_flops", C.c_double),
                 ("factor_bytes", C.c_double), ("n_nonpositive_jacobians", C.c_int64), ("factor_stored", C.c_int64),
-                ("front_pool_peak", C.c_int64), ("front_pool", C.c_int64)]
+                ("front_pool_peak", C.c_int64), ("front_pool", C.c_int64), ("device_array_bytes", C.c_int64),
+                ("workspace_bytes_per_frequency", (C.c_int64 * 2) * 2)]
 
 
 class SolveInfo(C.Structure):
@@ -375,7 +381,7 @@ class Model:
     def info(self) -> dict:
         i = _Info()
         _check(self.lib.elp_model_get_info(self.handle, C.byref(i)))
-        return {k: getattr(i, k) for k, _ in i._fields_}
+        return {k: _plain(getattr(i, k)) for k, _ in i._fields_}
 
     @property
     def n(self) -> int:
@@ -508,7 +514,7 @@ class Group:
     def info(self) -> dict:
         i = _Info()
         _check(self.lib.elp_group_info(self.handle, C.byref(i)))
-        return {k: getattr(i, k) for k, _ in i._fields_}
+        return {k: _plain(getattr(i, k)) for k, _ in i._fields_}
 
     def set_tuning(self, **knobs):
         t = Tuning(**{k: int(v) for k, v in knobs.items()})

@@ -205,7 +205,12 @@ int elp_model_get_info(const elp_model* h, elp_model_info* info) {
     info->factor_stored = m.sym->factor_stored;
     info->front_pool_peak = m.sym->pool_peak;
     info->front_pool = m.sym->pool;
+    for (int prec = 0; prec < 2; ++prec)
+      for (int st = 0; st < 2; ++st)
+        info->workspace_bytes_per_frequency[prec][st] =
+            workspace_bytes(m, prec, 1, st == 0 ? STORE_FULL : STORE_COMPACT);
   }
+  info->device_array_bytes = model_array_bytes(m);
   if (m.dev) info->n_nonpositive_jacobians = m.dev->bad_jacobians_3d;
   return ELP_OK;
   GUARD_END

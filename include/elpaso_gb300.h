@@ -203,6 +203,14 @@ typedef struct {
   int64_t front_pool;       /* complex entries of the front pool per frequency (first-fit
                                regions, >= front_pool_peak); the workspace per frequency is the
                                pool plus the factors (factor_stored), not the sum of all m^2  */
+  /* Device memory, for capacity planning (and what the serving loop charges
+   * against its budget): the model's resident arrays (value arrays, pattern,
+   * right-hand side, element lists, symbolic maps), and the workspace of ONE
+   * frequency slot per precision [ELP_FP64_PLAIN, ELP_MIXED] and front store
+   * [whole fronts, compact factor store]; a batch of S frequencies takes S
+   * times that. Workspace figures are 0 before the symbolic phase.          */
+  int64_t device_array_bytes;
+  int64_t workspace_bytes_per_frequency[2][2];
 } elp_model_info;
 
 /* precision of the numeric factorisation */

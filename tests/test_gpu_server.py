@@ -137,3 +137,32 @@ def test_admission_refuses_before_allocating(elp, meshes):
         big.system_values(2 * np.pi * 10.0)
     assert e.value.code == 7
     srv.close()
+
+
+def test_a_model_waits_for_room_instead_of_failing(elp, meshes):
+    """The budget holds both models' resident arrays but only one of them
+    with an 8-frequency workspace. While model A's 64 frequencies run, B's
+    arrays do not fit: B waits for A's workspace to be released (or takes it
+    once nothing runs) instead of failing its requests with ELP_ERR_NOMEM."""
+    import time
+    ma = elp.Model(meshes.plate_cavity(12, 8, 6, 0.6, 0.4, 0.3)).assemble().analyse()
+    mb = elp.Model(meshes.plate(30, 22, 0.6, 0.4, 0.003, seed=7)).assemble().analyse()
+    ia, ib = ma.info(), mb.info()
+    A, B = ia["device_array_bytes"], ib["device_array_bytes"]
+    W = ia["workspace_bytes_per_frequency"][1][0]
+    Wb = ib["workspace_bytes_per_frequency"][1][0]
+    budget = A + 8 * W + B // 2
+    assert B + Wb <= budget  # B alone fits: a NOMEM would be the bug
+    srv = elp.Server(hbm_budget_bytes=budget, max_inflight=2, precision=1, tol=1e-10, omega_batch=8)
+    a, b = srv.add_model(ma), srv.add_model(mb)
+    xa = np.zeros((64, ma.n), np.complex128)
+    ra = srv.submit(a, 2 * np.pi * np.linspace(10.0, 490.0, 64), xa)
+    time.sleep(0.2)  # A's first batch holds its workspace
+    xb = [np.zeros((4, mb.n), np.complex128) for _ in range(3)]
+    rb = [srv.submit(b, 2 * np.pi * np.array([21.0, 140.0, 260.0, 377.0]) + k, x) for k, x in enumerate(xb)]
+    got = {}
+    for _ in range(4):
+        r = srv.wait(300000.0)
+        got[r["request_id"]] = r
+    assert all(got[r]["status"] == 0 and got[r]["max_rel_residual"] <= 1e-10 for r in [ra] + rb), got
+    srv.close()

@@ -165,3 +165,19 @@ def test_tuning_is_per_model(elp, meshes):
     assert a.info()["n_fronts"] == ib["n_fronts"]
     with pytest.raises(elp.ElpasoError):
         b.set_tuning(schur_tile=48)
+
+
+def test_device_footprint_in_model_info(elp, meshes):
+    """elp_model_info reports the resident arrays and one frequency's
+    workspace per precision and front store: FP64 fronts take more than FP32
+    ones, the whole fronts at least 8 B per front entry, and the compact store
+    no more than the whole fronts plus its factor copy."""
+    d = meshes.plate_cavity(16, 12, 8, 0.6, 0.4, 0.3)
+    m, i = analysed(elp, d)
+    assert i["device_array_bytes"] >= i["nnz"] * 21
+    w = i["workspace_bytes_per_frequency"]
+    assert w[1][0] >= 8 * i["factor_entries"] and w[0][0] >= 16 * i["factor_entries"]
+    assert w[0][0] > w[1][0] and w[0][1] > w[1][1]
+    assert w[1][1] <= w[1][0] + 8 * i["factor_stored"]
+    fresh = elp.Model(d).info()  # no symbolic phase yet
+    assert fresh["device_array_bytes"] > 0 and fresh["workspace_bytes_per_frequency"] == [[0, 0], [0, 0]]
