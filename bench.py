@@ -617,7 +617,7 @@ def run_ours(args):
         asm100 = assembly_measurement(elp, meshes, n_cube=args.assembly_n, fp64_peak=fp64_peak)
     serving = plates = large = None
     if rank == 0 and not args.no_serving:
-        serving = serving_measurement(elp, meshes)
+        serving = serving_measurement(elp, meshes, n_stream=args.serving_requests)
         plates = {"grouped": grouped_plates_measurement(elp, meshes),
                   "serving_loop": batched_plates_measurement(elp, meshes)}
         large = large_models_measurement(elp, meshes)
@@ -700,6 +700,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--assembly-n", type=int, default=100, help="edge of the Brick8 cube of the assembly measurement")
     ap.add_argument("--cpu-budget-s", type=float, default=90.0)
+    ap.add_argument("--serving-requests", type=int, default=300,
+                    help="requests of the Poisson stream of the serving measurement")
     ap.add_argument("--tuning", default="",
                     help="leaf=..,schur_tile=..,pack_count=..,pack_min_border=..,lanes=.. instead of the autotuner")
     args = ap.parse_args()

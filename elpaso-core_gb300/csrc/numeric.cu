@@ -739,7 +739,16 @@ struct SolveArgs {
   // gvec_stride entries per (front of the level, slot), else null
   void* gvec;
   int64_t gvec_stride;
+  // groups: fronts of (member, slot) pairs whose input rows are zero (pact 0)
+  // are skipped -- their exact output is zero, which k_rhs already wrote
+  const int32_t* fmember;
+  const int* pact;
+  int nm;
 };
+
+__device__ __forceinline__ bool front_skipped(const SolveArgs& S, int f, int s) {
+  return S.pact && !S.pact[(int64_t)s * S.nm + S.fmember[f]];
+}
 
 // the sweep kernels' working vector: the CTA's global slice (G), or shared
 // memory; a compile-time choice, so that the shared-memory variants address
@@ -780,7 +789,7 @@ __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec
   V* w = solve_buf<V, G>(S, smraw);
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
-  if (!S.active[s]) return;
+  if (!S.active[s] || front_skipped(S, f, s)) return;
   const int p = S.fp[f], b = S.fb[f], m = p + b;
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
@@ -870,7 +879,7 @@ __global__ void __launch_bounds__(256) k_fwd_border(SolveArgs S, const typename 
   __shared__ V part[8][32];
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
-  if (!S.active[s]) return;
+  if (!S.active[s] || front_skipped(S, f, s)) return;
   const int p = S.fp[f], b = S.fb[f], m = p + b;
   if ((int)blockIdx.z * 32 >= b) return;
   const V* F = arena + s * S.arena_size + S.foff[f];
@@ -919,7 +928,7 @@ __global__ void __launch_bounds__(256) k_bwd_u12(SolveArgs S, const typename Vec
   __shared__ V part[8][32];
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
-  if (!S.active[s]) return;
+  if (!S.active[s] || front_skipped(S, f, s)) return;
   const int p = S.fp[f], b = S.fb[f], m = p + b;
   if ((int)blockIdx.z * 32 >= p) return;
   const V* F = arena + s * S.arena_size + S.foff[f];
@@ -963,7 +972,7 @@ __global__ void __launch_bounds__(256) k_gather_border(SolveArgs S, const typena
   using V = typename Vec2<R>::T;
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
-  if (!S.active[s]) return;
+  if (!S.active[s] || front_skipped(S, f, s)) return;
   const int p = S.fp[f], b = S.fb[f];
   V* xb = reinterpret_cast<V*>(S.gvec) + ((int64_t)blockIdx.y * S.count + blockIdx.x) * S.gvec_stride;
   gather_rows(xb, z + s * S.n, S.dofs + S.idx_off[f] + p, b);
@@ -978,7 +987,7 @@ __global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Ve
   V* w = solve_buf<V, G>(S, smraw);
   const int f = S.list[blockIdx.x];
   const int s = blockIdx.y;
-  if (!S.active[s]) return;
+  if (!S.active[s] || front_skipped(S, f, s)) return;
   const int p = S.fp[f], m = p + S.fb[f];
   const V* F = arena + s * S.arena_size + S.foff[f];
   const int32_t* I = S.dofs + S.idx_off[f];
@@ -1470,6 +1479,12 @@ int device_upload_symbolic(Model& m) {
   ELP_CUDA(D.scatter_order.upload(S.scatter_order));
   ELP_CUDA(D.entry_row.upload(S.entry_row));
   ELP_CUDA(D.front_dofs.upload(S.front_dofs));
+  if (m.n_members > 1) {  // a front's DOFs all belong to one member (members share no node)
+    std::vector<int32_t> fm(T, 0);
+    for (int t = 0; t < T; ++t)
+      if (S.fronts[t].p + S.fronts[t].b > 0) fm[t] = m.row_model[S.front_dofs[S.fronts[t].idx_off]];
+    ELP_CUDA(D.f_member.upload(fm));
+  }
   ELP_CUDA(D.parent_map.upload(S.parent_map));
   ELP_CUDA(D.child_ptr.upload(cptr));
   ELP_CUDA(D.child_list.upload(clist));
@@ -1999,7 +2014,8 @@ static int factor_and_setup(Model& m, Workspace& w, int S_used, cudaStream_t st)
 static int solve_threads(int max_p) { return max_p <= 128 ? 128 : max_p >= 512 ? 512 : 256; }
 
 template <class R>
-static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, const int* mask) {
+static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, const int* mask,
+                       const int* pact = nullptr) {
   using V = typename Vec2<R>::T;
   DeviceSymbolic& D = *m.dsym;
   SolveArgs S;
@@ -2022,6 +2038,9 @@ static int solve_sweep(Model& m, Workspace& w, int S_used, cudaStream_t st, cons
   S.active = mask;
   S.gvec = nullptr;
   S.gvec_stride = 0;
+  S.fmember = D.f_member.p;
+  S.pact = pact;
+  S.nm = m.n_members;
   const V* arena = reinterpret_cast<const V*>(compact ? w.fac.p : w.arena.p);
   // levels whose front vector exceeds shared memory work on global slices
   auto level_buffers = [&](const DeviceSymbolic::Level& LV) -> bool {
@@ -2474,7 +2493,9 @@ static int run_gmres_group(Model& m, Workspace& w, int S_used, double tol, int m
   };
   auto precond = [&](const double2* src, int64_t sstride, const int* mask) -> int {
     PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, src, sstride, w.dscale.p, n, z, mask));
-    return solve_sweep<R>(m, w, S_used, st, mask);
+    // pairs that are done have zero rows in src (the basis scale of their block is 0): their
+    // fronts are skipped
+    return solve_sweep<R>(m, w, S_used, st, mask, w.pact.p);
   };
   // a tensor-core wait that ran out left the factors incomplete (read with the first residual)
   ELP_CUDA(cudaMemcpyAsync(w.h_flag, w.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));

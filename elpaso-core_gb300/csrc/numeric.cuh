@@ -145,6 +145,7 @@ struct DeviceSymbolic {
   DevBuf<int32_t> scatter_order;  // CSR entries by the start level of their owner front
   DevBuf<int32_t> entry_row;      // per CSR entry: its row
   DevBuf<int32_t> front_dofs, parent_map, child_ptr, child_list;
+  DevBuf<int32_t> f_member;  // groups: the member each front belongs to (empty for one model)
   DevBuf<int64_t> entry_local;    // per CSR entry: offset inside its owner front
   DevBuf<int32_t> entry_owner;    // per CSR entry: its owner front
   DevBuf<int32_t> level_list;     // fronts grouped by level
