@@ -1130,9 +1130,10 @@ __global__ void k_rhs(CombineArgs A, const Coef* __restrict__ coef, const int32_
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
     const int64_t i = base + lane / kRowLanes;
+    const bool on = i < n && row_on(A, s, i);
     double sx = 0.0, sy = 0.0;
     bool lift = false;  // entries in Dirichlet columns: lifted to the right-hand side
-    if (i < n)
+    if (on)
       for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
         if (!(A.cls[q] & CLS_BC_COLUMN)) continue;
         lift = true;
@@ -1145,7 +1146,7 @@ __global__ void k_rhs(CombineArgs A, const Coef* __restrict__ coef, const int32_
       sx = row_sum(sx);
       sy = row_sum(sy);
     }
-    if (i < n && sub == 0) {
+    if (on && sub == 0) {
       const double d = dscale[s * n + i];
       const double2 v = rs[i];
       z[s * n + i] = cmk<V>((v.x - sx) * d, (v.y - sy) * d);
@@ -1189,8 +1190,9 @@ __global__ void k_spmv(CombineArgs A, const Coef* __restrict__ coef, const int32
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
     const int64_t i = base + lane / kRowLanes;
+    const bool on = i < n && row_on(A, s, i);
     double sx = 0.0, sy = 0.0;
-    if (i < n) {
+    if (on) {
       const Coef& c = row_coef(A, coef, s, i);
       for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
         double2 a = combine(A, c, q);
@@ -1201,7 +1203,7 @@ __global__ void k_spmv(CombineArgs A, const Coef* __restrict__ coef, const int32
     }
     sx = row_sum(sx);
     sy = row_sum(sy);
-    if (i < n && sub == 0) w[s * n + i] = make_double2(sx, sy);
+    if (on && sub == 0) w[s * n + i] = make_double2(sx, sy);
   }
 }
 
@@ -2491,10 +2493,18 @@ static int run_gmres_group(Model& m, Workspace& w, int S_used, double tol, int m
     }
     return ELP_OK;
   };
+  // the pairs that are done have zero rows in every later basis vector (the basis scale of
+  // their block is 0); the products and the preconditioner skip their rows and fronts, and
+  // the kernels that read those rows (segmented dots, Gram-Schmidt, combination) skip them
+  // too, so what the skipped rows hold never reaches an open pair. The buffers start zeroed.
+  CombineArgs Am = A;
+  Am.pact = w.pact.p;
+  ELP_CUDA(cudaMemsetAsync(w.Vb.p, 0, sizeof(double2) * (size_t)w.slots * (RST + 1) * n, st));
+  ELP_CUDA(cudaMemsetAsync(w.Zb.p, 0, sizeof(double2) * (size_t)w.slots * RST * n, st));
+  ELP_CUDA(cudaMemsetAsync(w.wv.p, 0, sizeof(double2) * (size_t)w.slots * n, st));
+  ELP_CUDA(cudaMemsetAsync(w.z.p, 0, w.elem * (size_t)w.slots * n, st));
   auto precond = [&](const double2* src, int64_t sstride, const int* mask) -> int {
-    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, src, sstride, w.dscale.p, n, z, mask));
-    // pairs that are done have zero rows in src (the basis scale of their block is 0): their
-    // fronts are skipped
+    PROF_LAUNCH(KC_RHS, st, k_rhs<V><<<gv, 256, 0, st>>>(Am, w.coef.p, G.row_ptr.p, G.col_idx.p, src, sstride, w.dscale.p, n, z, mask));
     return solve_sweep<R>(m, w, S_used, st, mask, w.pact.p);
   };
   // a tensor-core wait that ran out left the factors incomplete (read with the first residual)
@@ -2543,7 +2553,7 @@ static int run_gmres_group(Model& m, Workspace& w, int S_used, double tol, int m
       if (rc) return rc;
       ELP_CUDA(cudaEventRecord(w.ev[3], st));
       PROF_LAUNCH(KC_KRYLOV, st, k_unscale<V><<<gv, 256, 0, st>>>(z, w.dscale.p, n, w.Zb.p + (int64_t)j * n, zst, w.inner.p));
-      PROF_LAUNCH(KC_SPMV, st, k_spmv<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n,
+      PROF_LAUNCH(KC_SPMV, st, k_spmv<<<gr, 256, 0, st>>>(Am, w.coef.p, G.row_ptr.p, G.col_idx.p, n,
                                                                  w.Zb.p + (int64_t)j * n, zst, w.wv.p, w.inner.p));
       const int nv = j + 1;
       PROF_LAUNCH(KC_KRYLOV, st, k_dots_seg<<<gp, 256, 0, st>>>(w.Vb.p, vst, n, nv, w.wv.p, n, off, nm, w.ph1.p, w.pact.p));

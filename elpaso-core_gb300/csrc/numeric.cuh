@@ -33,6 +33,9 @@ struct CombineArgs {
   // slot s and member k is coef[s * n_members + k]. Null for a single model.
   const int32_t* row_model;
   int n_members;
+  // a group's GMRES steps: the (slot, member) pairs still iterating; rows of
+  // the others are skipped by k_spmv and k_rhs (null: every row)
+  const int* pact = nullptr;
 };
 
 CombineArgs combine_args(const Model& m);
@@ -42,6 +45,9 @@ CombineArgs combine_args(const Model& m);
 __device__ __forceinline__ const Coef& row_coef(const CombineArgs& A, const Coef* __restrict__ coef, int s,
                                                 int64_t i) {
   return A.row_model ? coef[(int64_t)s * A.n_members + A.row_model[i]] : coef[s];
+}
+__device__ __forceinline__ bool row_on(const CombineArgs& A, int s, int64_t i) {
+  return !A.pact || A.pact[(int64_t)s * A.n_members + A.row_model[i]];
 }
 
 // A(w) at CSR entry q, Dirichlet rows included (MatZeroRows, diag = 1)
