@@ -138,12 +138,20 @@ class ServerConfig(C.Structure):
 
 
 class Tuning(C.Structure):
-    """elp_tuning: leaf, schur_tile, pack_count, pack_min_border, lanes (0 / negative: default)."""
+    """elp_tuning: leaf, schur_tile, pack_count, pack_min_border, lanes (0 / negative: default;
+    pack_count 0: never)."""
     _fields_ = [("leaf", C.c_int), ("schur_tile", C.c_int), ("pack_count", C.c_int),
                 ("pack_min_border", C.c_int), ("lanes", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+    @classmethod
+    def of(cls, knobs: dict):
+        """The knobs given; every other field -1 (its default)."""
+        vals = {k: -1 for k, _ in cls._fields_}
+        vals.update({k: int(v) for k, v in knobs.items()})
+        return cls(**vals)
 
 
 class RequestResult(C.Structure):
@@ -445,7 +453,7 @@ class Model:
 
     def set_tuning(self, **knobs):
         """leaf, schur_tile, pack_count, pack_min_border, lanes (unset: default)."""
-        t = Tuning(**{k: int(v) for k, v in knobs.items()})
+        t = Tuning.of(knobs)
         _check(self.lib.elp_model_set_tuning(self.handle, C.byref(t)))
         return self
 
@@ -517,7 +525,7 @@ class Group:
         return {k: _plain(getattr(i, k)) for k, _ in i._fields_}
 
     def set_tuning(self, **knobs):
-        t = Tuning(**{k: int(v) for k, v in knobs.items()})
+        t = Tuning.of(knobs)
         _check(self.lib.elp_group_set_tuning(self.handle, C.byref(t)))
         return self
 

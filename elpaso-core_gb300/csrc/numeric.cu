@@ -1603,12 +1603,13 @@ Tuning resolved_tuning(const Model& m) {
     int v = e ? atoi(e) : 4;
     return v < 1 ? 1 : v > 4 ? 4 : v;
   }();
+  // 0 or negative: the default, except pack_count, where 0 means never
   Tuning t = m.tune;
-  if (t.leaf < 0) t.leaf = leaf_env;
+  if (t.leaf <= 0) t.leaf = leaf_env;
   t.leaf = std::max(8, t.leaf);
   if (t.schur_tile != 32) t.schur_tile = 64;
   if (t.pack_count < 0) t.pack_count = pack_max_count();
-  if (t.pack_minb < 0) t.pack_minb = pack_min_border();
+  if (t.pack_minb <= 0) t.pack_minb = pack_min_border();
   if (t.lanes < 1) t.lanes = lanes_env;
   t.lanes = std::min(4, t.lanes);
   return t;

@@ -137,8 +137,8 @@ extern "C" {
 int elp_model_set_tuning(elp_model* h, const elp_tuning* t) {
   GUARD_BEGIN
   if (!h || !t) { set_error("null argument"); return ELP_ERR_ARG; }
-  if (t->schur_tile != 0 && t->schur_tile != 32 && t->schur_tile != 64) {
-    set_error("schur_tile must be 32 or 64 (0: default)");
+  if (t->schur_tile > 0 && t->schur_tile != 32 && t->schur_tile != 64) {
+    set_error("schur_tile must be 32 or 64 (0 or negative: default)");
     return ELP_ERR_ARG;
   }
   if (t->lanes > 4) { set_error("at most 4 lanes"); return ELP_ERR_ARG; }

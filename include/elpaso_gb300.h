@@ -354,7 +354,8 @@ int elp_residual_noalloc(elp_model* m, const double* omegas, int n_omega, const 
 /* No reference counterpart (MUMPS and PETSc take their own parameters).
  * How a model is factorised, never what is computed; 0 or a negative value
  * takes the default (the ELP_* environment variable if set, else the value
- * measured best on the coupled plate-cavity sweep):
+ * measured best on the coupled plate-cavity sweep), except pack_count, where 0
+ * means never and a negative value the default:
  *   leaf            nested-dissection leaf size in DOFs (128)
  *   schur_tile      columns of a converter-kernel Schur tile: 32 or 64 (64)
  *   pack_count      packed tensor-core Schur kernel on levels of at most this

@@ -165,6 +165,11 @@ def test_tuning_is_per_model(elp, meshes):
     assert a.info()["n_fronts"] == ib["n_fronts"]
     with pytest.raises(elp.ElpasoError):
         b.set_tuning(schur_tile=48)
+    # unspecified knobs keep their defaults; 0 takes the default too, except pack_count (0: never)
+    assert a.set_tuning(leaf=64).tuning()["pack_count"] == 300
+    t = elp.Model(d).set_tuning(leaf=0, pack_min_border=0, lanes=0).tuning()
+    assert (t["leaf"], t["pack_min_border"], t["lanes"]) == (128, 300, 4)
+    assert elp.Model(d).set_tuning(pack_count=0).tuning()["pack_count"] == 0
 
 
 def test_device_footprint_in_model_info(elp, meshes):
