@@ -378,134 +378,183 @@ __device__ void hex_item(const AsmArgs& A, int64_t item, double (*sg)[8][8][3], 
 }
 
 // ---------------------------------------------------------------- DSG4 plate
-__device__ void plate_element(const AsmArgs& A, int64_t e) {
-  double x[4], y[4], z[4];
-  int rows[4];
+// 28 plates per CTA item: 112 threads form one Gauss point each (J, det J,
+// dN/dx, dN/dy and the DSG shear rows Bs), then one thread per node pair
+// (a <= b, 10 per plate) sums its 3 x 3 block of K = sum_gp (Bb^T Cb Bb +
+// tau Cs Bs^T Bs) w det J and the mass term, and adds the block (and its
+// transpose) into the CSR value arrays.
+constexpr int kPlatesPerItem = 28;  // x 10 node pairs = 280 of the 288 threads
+__constant__ unsigned char c_qpair_a[10] = {0, 0, 0, 0, 1, 1, 1, 2, 2, 3};
+__constant__ unsigned char c_qpair_b[10] = {0, 1, 2, 3, 1, 2, 3, 2, 3, 3};
+
+struct PlateShared {
+  double dx[kPlatesPerItem][4][4], dy[kPlatesPerItem][4][4];  // [plate][gp][node] dN/dx, dN/dy
+  double bs[kPlatesPerItem][4][2][12];                          // [plate][gp] DSG shear rows, / det J
+  double wd[kPlatesPerItem][4];                                 // w det J (weights 1 x 1)
+  double cst[kPlatesPerItem][6];                                // Cb00, Cb01, Cb22, tau Cs, m1, m2
+  int row[kPlatesPerItem][4];
+  int grp[kPlatesPerItem];
+};
+
+__device__ void plate_item(const AsmArgs& A, int64_t item, PlateShared& ps) {
+  const int t = threadIdx.x;
+  const int64_t e0 = item * kPlatesPerItem;
+  if (t < kPlatesPerItem * 4) {
+    const int el = t >> 2, n = t & 3;
+    const int64_t e = e0 + el;
+    if (e < A.n_plate) {
+      double x[4], y[4], z[4];
+      int vv[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    int v = __ldg(A.plate_conn + e * 4 + k);
-    x[k] = A.coords[3 * (int64_t)v + 0];
-    y[k] = A.coords[3 * (int64_t)v + 1];
-    z[k] = A.coords[3 * (int64_t)v + 2];
-    rows[k] = A.nr_plate[v];
-  }
-  const ElemMaterial& mt = A.mats[A.plate_mat[e]];
-  const double thick = mt.t;
-  // Lyly-Stenberg: hk = max edge over the pairs (1,0), (2,1), (3,2)
-  double hk = 0.0;
-  const int seq[5] = {0, 1, 2, 3, 0};
-#pragma unroll
-  for (int i = 1; i < 4; ++i) {
-    int p = seq[i], q = seq[i - 1];
-    double dx = x[p] - x[q], dy = y[p] - y[q], dz = z[p] - z[q];
-    double dd = sqrt(dx * dx + dy * dy + dz * dz);
-    hk = hk > dd ? hk : dd;
-  }
-  const double tau = 1.0 / (1.0 + 0.12 * hk * hk / (thick * thick));
-  const double Bm = mt.Db;                 // E t^3 / (12 (1 - nu^2))
-  const double Cb00 = Bm, Cb01 = Bm * mt.nu, Cb22 = mt.Gt;  // Gt holds G t^3 / 12
-  const double Cs = mt.lam * tau;          // lam holds G t Ks for plates
-  const double m1 = mt.rho * thick, m2 = mt.rho * (thick * thick * thick / 12.0);
-  double K[78];
-  double M[16];
-#pragma unroll
-  for (int i = 0; i < 78; ++i) K[i] = 0.0;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) M[i] = 0.0;
-  for (int n = 0; n < 4; ++n) {
-    double J00 = 0, J01 = 0, J10 = 0, J11 = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      J00 += c_quad[1][k][n] * x[k];
-      J01 += c_quad[1][k][n] * y[k];
-      J10 += c_quad[2][k][n] * x[k];
-      J11 += c_quad[2][k][n] * y[k];
-    }
-    const double det = J00 * J11 - J01 * J10;
-    if (det <= 0.0) atomicAdd(A.flags + 1, 1);
-    const double a = J00, b = J01, d = J10, c = J11;
-    const double wdJ = 1.0 * det;
-    double Bb[3][12], Bs[2][12];
-#pragma unroll
-    for (int i = 0; i < 12; ++i) { Bb[0][i] = Bb[1][i] = Bb[2][i] = 0.0; }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      double dNdx = (c * c_quad[1][k][n] - b * c_quad[2][k][n]) / det;
-      double dNdy = (-d * c_quad[1][k][n] + a * c_quad[2][k][n]) / det;
-      Bb[0][k * 3 + 2] = dNdx;
-      Bb[1][k * 3 + 1] = -dNdy;
-      Bb[2][k * 3 + 2] = dNdy;
-      Bb[2][k * 3 + 1] = -dNdx;
-    }
-    const double Nx1 = c_quad[1][1][n], Nx2 = c_quad[1][2][n];
-    const double Ne2 = c_quad[2][2][n], Ne3 = c_quad[2][3][n];
-    Bs[0][0] = -c * Nx1 + b * Ne3;
-    Bs[0][1] = -b * c * Nx1 + b * c * Ne3;
-    Bs[0][2] = a * c * Nx1 - b * d * Ne3;
-    Bs[1][0] = d * Nx1 - a * Ne3;
-    Bs[1][1] = -a * c * Ne3 + b * d * Nx1;
-    Bs[1][2] = a * d * Ne3 - a * d * Nx1;
-    Bs[0][3] = c * Nx1 + b * Ne2;
-    Bs[0][4] = -b * c * Nx1 + b * c * Ne2;
-    Bs[0][5] = a * c * Nx1 - b * d * Ne2;
-    Bs[1][3] = -a * Ne2 - d * Nx1;
-    Bs[1][4] = -a * c * Ne2 + b * d * Nx1;
-    Bs[1][5] = a * d * Ne2 - a * d * Nx1;
-    Bs[0][6] = c * Nx2 - b * Ne2;
-    Bs[0][7] = -b * c * Nx2 + b * c * Ne2;
-    Bs[0][8] = a * c * Nx2 - b * d * Ne2;
-    Bs[1][6] = a * Ne2 - d * Nx2;
-    Bs[1][7] = -a * c * Ne2 + b * d * Nx2;
-    Bs[1][8] = a * d * Ne2 - a * d * Nx2;
-    Bs[0][9] = -c * Nx2 - b * Ne3;
-    Bs[0][10] = -b * c * Nx2 + b * c * Ne3;
-    Bs[0][11] = a * c * Nx2 - b * d * Ne3;
-    Bs[1][9] = a * Ne3 + d * Nx2;
-    Bs[1][10] = -a * c * Ne3 + b * d * Nx2;
-    Bs[1][11] = a * d * Ne3 - a * d * Nx2;
-    const double idet = 1. / det;
-#pragma unroll
-    for (int i = 0; i < 12; ++i) { Bs[0][i] *= idet; Bs[1][i] *= idet; }
-    // K += Bb^T Cb Bb wdJ + Bs^T (tau Cs) Bs wdJ (upper triangle)
-    double CB[3][12];
-#pragma unroll
-    for (int j = 0; j < 12; ++j) {
-      CB[0][j] = Cb00 * Bb[0][j] + Cb01 * Bb[1][j];
-      CB[1][j] = Cb01 * Bb[0][j] + Cb00 * Bb[1][j];
-      CB[2][j] = Cb22 * Bb[2][j];
-    }
-    int idx = 0;
-#pragma unroll
-    for (int i = 0; i < 12; ++i)
-#pragma unroll
-      for (int j = i; j < 12; ++j) {
-        double s = Bb[0][i] * CB[0][j] + Bb[1][i] * CB[1][j] + Bb[2][i] * CB[2][j];
-        s += Cs * (Bs[0][i] * Bs[0][j] + Bs[1][i] * Bs[1][j]);
-        K[idx++] += s * wdJ;
+      for (int k = 0; k < 4; ++k) {
+        const int v = __ldg(A.plate_conn + e * 4 + k);
+        vv[k] = v;
+        x[k] = A.coords[3 * (int64_t)v + 0];
+        y[k] = A.coords[3 * (int64_t)v + 1];
+        z[k] = A.coords[3 * (int64_t)v + 2];
       }
+      double J00 = 0, J01 = 0, J10 = 0, J11 = 0;
 #pragma unroll
-    for (int zz = 0; zz < 4; ++zz)
+      for (int k = 0; k < 4; ++k) {
+        J00 += c_quad[1][k][n] * x[k];
+        J01 += c_quad[1][k][n] * y[k];
+        J10 += c_quad[2][k][n] * x[k];
+        J11 += c_quad[2][k][n] * y[k];
+      }
+      const double det = J00 * J11 - J01 * J10;
+      if (det <= 0.0) atomicAdd(A.flags + 1, 1);
+      const double a = J00, b = J01, d = J10, c = J11;
 #pragma unroll
-      for (int ss = 0; ss < 4; ++ss) M[zz * 4 + ss] += c_quad[0][zz][n] * c_quad[0][ss][n] * wdJ;
-  }
-  double* VKt = mt.group == 0 ? A.VK : A.VKg + (int64_t)(mt.group - 1) * A.nnz;
-  // scatter: row (node zz, dof i), col (node ss, dof j)
-  for (int zz = 0; zz < 4; ++zz)
-    for (int i = 0; i < 3; ++i) {
-      const int gi = zz * 3 + i;
-      const int r = rows[zz] + i;
-      for (int ss = 0; ss < 4; ++ss) {
-        int p = find_col(A.row_ptr, A.col_idx, r, rows[ss]);
-        for (int j = 0; j < 3; ++j) {
-          const int gj = ss * 3 + j;
-          const int lo = gi < gj ? gi : gj, hi = gi < gj ? gj : gi;
-          const int u = lo * 12 - (lo * (lo - 1)) / 2 + (hi - lo);
-          add_at(VKt, p + j, K[u]);
+      for (int k = 0; k < 4; ++k) {
+        ps.dx[el][n][k] = (c * c_quad[1][k][n] - b * c_quad[2][k][n]) / det;
+        ps.dy[el][n][k] = (-d * c_quad[1][k][n] + a * c_quad[2][k][n]) / det;
+      }
+      // DSG shear strains of the edge-based interpolation (elementstructuremindlindsg4.cpp)
+      const double Nx1 = c_quad[1][1][n], Nx2 = c_quad[1][2][n];
+      const double Ne2 = c_quad[2][2][n], Ne3 = c_quad[2][3][n];
+      double Bs[2][12];
+      Bs[0][0] = -c * Nx1 + b * Ne3;
+      Bs[0][1] = -b * c * Nx1 + b * c * Ne3;
+      Bs[0][2] = a * c * Nx1 - b * d * Ne3;
+      Bs[1][0] = d * Nx1 - a * Ne3;
+      Bs[1][1] = -a * c * Ne3 + b * d * Nx1;
+      Bs[1][2] = a * d * Ne3 - a * d * Nx1;
+      Bs[0][3] = c * Nx1 + b * Ne2;
+      Bs[0][4] = -b * c * Nx1 + b * c * Ne2;
+      Bs[0][5] = a * c * Nx1 - b * d * Ne2;
+      Bs[1][3] = -a * Ne2 - d * Nx1;
+      Bs[1][4] = -a * c * Ne2 + b * d * Nx1;
+      Bs[1][5] = a * d * Ne2 - a * d * Nx1;
+      Bs[0][6] = c * Nx2 - b * Ne2;
+      Bs[0][7] = -b * c * Nx2 + b * c * Ne2;
+      Bs[0][8] = a * c * Nx2 - b * d * Ne2;
+      Bs[1][6] = a * Ne2 - d * Nx2;
+      Bs[1][7] = -a * c * Ne2 + b * d * Nx2;
+      Bs[1][8] = a * d * Ne2 - a * d * Nx2;
+      Bs[0][9] = -c * Nx2 - b * Ne3;
+      Bs[0][10] = -b * c * Nx2 + b * c * Ne3;
+      Bs[0][11] = a * c * Nx2 - b * d * Ne3;
+      Bs[1][9] = a * Ne3 + d * Nx2;
+      Bs[1][10] = -a * c * Ne3 + b * d * Nx2;
+      Bs[1][11] = a * d * Ne3 - a * d * Nx2;
+      const double idet = 1. / det;
+#pragma unroll
+      for (int i = 0; i < 12; ++i) {
+        ps.bs[el][n][0][i] = Bs[0][i] * idet;
+        ps.bs[el][n][1][i] = Bs[1][i] * idet;
+      }
+      ps.wd[el][n] = 1.0 * det;
+      if (n == 0) {
+        const ElemMaterial& mt = A.mats[A.plate_mat[e]];
+        const double thick = mt.t;
+        // Lyly-Stenberg: hk = max edge over the pairs (1,0), (2,1), (3,2)
+        double hk = 0.0;
+        const int seq[5] = {0, 1, 2, 3, 0};
+#pragma unroll
+        for (int i = 1; i < 4; ++i) {
+          const int p = seq[i], q = seq[i - 1];
+          const double ex = x[p] - x[q], ey = y[p] - y[q], ez = z[p] - z[q];
+          const double dd = sqrt(ex * ex + ey * ey + ez * ez);
+          hk = hk > dd ? hk : dd;
         }
-        const double mv = M[zz * 4 + ss] * (i == 0 ? m1 : m2);
-        add_at(A.VM, p + i, mv);
+        const double tau = 1.0 / (1.0 + 0.12 * hk * hk / (thick * thick));
+        ps.cst[el][0] = mt.Db;           // E t^3 / (12 (1 - nu^2))
+        ps.cst[el][1] = mt.Db * mt.nu;
+        ps.cst[el][2] = mt.Gt;           // G t^3 / 12
+        ps.cst[el][3] = mt.lam * tau;    // lam holds G t Ks for plates
+        ps.cst[el][4] = mt.rho * thick;
+        ps.cst[el][5] = mt.rho * (thick * thick * thick / 12.0);
+        ps.grp[el] = mt.group;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) ps.row[el][k] = A.nr_plate[vv[k]];
       }
     }
+  }
+  __syncthreads();
+  if (t < kPlatesPerItem * 10) {
+    const int el = t / 10, pr = t % 10;
+    const int64_t e = e0 + el;
+    if (e < A.n_plate) {
+      const int a = c_qpair_a[pr], b = c_qpair_b[pr];
+      const double Cb00 = ps.cst[el][0], Cb01 = ps.cst[el][1], Cb22 = ps.cst[el][2], Cs = ps.cst[el][3];
+      double Kb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, mab = 0.0;
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        const double wdJ = ps.wd[el][n];
+        // bending rows of the nodes' columns (w, theta_x, theta_y): Bb[r][3k + i]
+        const double xa = ps.dx[el][n][a], ya = ps.dy[el][n][a], xb = ps.dx[el][n][b], yb = ps.dy[el][n][b];
+        const double Ba[3][3] = {{0.0, 0.0, xa}, {0.0, -ya, 0.0}, {0.0, -xa, ya}};
+        const double Bn[3][3] = {{0.0, 0.0, xb}, {0.0, -yb, 0.0}, {0.0, -xb, yb}};
+        double CB[3][3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          CB[0][j] = Cb00 * Bn[0][j] + Cb01 * Bn[1][j];
+          CB[1][j] = Cb01 * Bn[0][j] + Cb00 * Bn[1][j];
+          CB[2][j] = Cb22 * Bn[2][j];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            if (a == b && j < i) continue;  // diagonal block: upper triangle, mirrored below
+            double s = Ba[0][i] * CB[0][j] + Ba[1][i] * CB[1][j] + Ba[2][i] * CB[2][j];
+            s += Cs * (ps.bs[el][n][0][3 * a + i] * ps.bs[el][n][0][3 * b + j] +
+                       ps.bs[el][n][1][3 * a + i] * ps.bs[el][n][1][3 * b + j]);
+            Kb[i][j] += s * wdJ;
+          }
+        mab += c_quad[0][a][n] * c_quad[0][b][n] * wdJ;
+      }
+      if (a == b) {
+        Kb[1][0] = Kb[0][1];
+        Kb[2][0] = Kb[0][2];
+        Kb[2][1] = Kb[1][2];
+      }
+      const double m1 = ps.cst[el][4], m2 = ps.cst[el][5];
+      const int g = ps.grp[el];
+      double* VKt = g == 0 ? A.VK : A.VKg + (int64_t)(g - 1) * A.nnz;
+      const int ra = ps.row[el][a], rb = ps.row[el][b];
+      // rows (node a, dof i), columns (node b, dof j); the mass couples equal dofs
+      const int pa0 = find_col(A.row_ptr, A.col_idx, ra, rb);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const int p = i == 0 ? pa0 : sibling_col(A.row_ptr, A.col_idx, ra, pa0, i, rb);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) add_at(VKt, p + j, Kb[i][j]);
+        add_at(A.VM, p + i, mab * (i == 0 ? m1 : m2));
+      }
+      if (a != b) {
+        const int pb0 = find_col(A.row_ptr, A.col_idx, rb, ra);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int p = j == 0 ? pb0 : sibling_col(A.row_ptr, A.col_idx, rb, pb0, j, ra);
+#pragma unroll
+          for (int i = 0; i < 3; ++i) add_at(VKt, p + i, Kb[i][j]);
+          add_at(A.VM, p + j, mab * (j == 0 ? m1 : m2));
+        }
+      }
+    }
+  }
+  __syncthreads();
 }
 
 // ---------------------------------------------------------------- interface
@@ -602,14 +651,14 @@ __global__ void __launch_bounds__(kThreads, 3) assemble_hex_kernel(AsmArgs A) {
   }
 }
 
-// DSG4 plates and interface quads, one element per thread (the 12 x 12
-// element matrix lives in registers).
+// DSG4 plates (28 per item, a thread per node pair) and interface quads (one
+// per thread).
 __global__ void __launch_bounds__(kThreads) assemble_quad_kernel(AsmArgs A) {
+  __shared__ PlateShared ps;
   const int64_t total = A.items_plate + A.items_iface;
   for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
     if (it < A.items_plate) {
-      int64_t e = it * kThreads + threadIdx.x;
-      if (e < A.n_plate) plate_element(A, e);
+      plate_item(A, it, ps);
     } else {
       int64_t q = (it - A.items_plate) * kThreads + threadIdx.x;
       if (q < A.n_iface) interface_quad(A, q);
@@ -831,7 +880,7 @@ int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms) {
   A.n_iface = D.n_iface;
   A.items_brick = (D.n_brick + kHexPerItem - 1) / kHexPerItem;
   A.items_fluid = (D.n_fluid + kHexPerItem - 1) / kHexPerItem;
-  A.items_plate = (D.n_plate + kThreads - 1) / kThreads;
+  A.items_plate = (D.n_plate + kPlatesPerItem - 1) / kPlatesPerItem;
   A.items_iface = (D.n_iface + kThreads - 1) / kThreads;
   A.flags = D.flags.p;
   int sms = 0, per_hex = 0, per_quad = 0;
