@@ -780,16 +780,12 @@ __device__ __forceinline__ void gather_rows(V* dst, const V* __restrict__ src, c
   }
 }
 
-// Pivot-block triangular solves of the sweeps. Tall pivot blocks (p >=
-// kLookAheadMinP, the top levels, where few CTAs run) use look-ahead: while warps
+// Pivot-block triangular solves of the sweeps, with look-ahead: while warps
 // 1.. apply the solved block b to the rows below block b + 1 (forward) or
 // above it (backward), warp 0 applies it to the 32 rows of block b + 1,
 // stages that block's diagonal and solves it, so the sequential 32-step
 // chain runs beside the bulk update instead of between two of them. Each
 // row sees the same operations in the same order as without look-ahead.
-// Short blocks stage each diagonal block with every thread instead: there
-// the staging, not the bulk update, is the longer part.
-constexpr int kLookAheadMinP = 384;
 
 // warp 0: the jw x jw diagonal block at (j0, j0) of F (ld m) into dblk[row][col]
 template <class V>
@@ -899,24 +895,10 @@ __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec
   const int lane = tid & 31, wid = tid >> 5;
   // L11 solve on the pivot block only (with look-ahead); the border rows
   // (L21) are updated by k_fwd_border across many CTAs
-  __shared__ V dblk[32][33];  // diagonal 32 x 32 block, staged so the warp solve never waits on DRAM
-  if (p < kLookAheadMinP) {  // short pivot blocks: every thread stages, warp 0 solves, every thread updates
-    for (int j0 = 0; j0 < p; j0 += 32) {
-      const int jw = min(32, p - j0);
-      staged_copy<sizeof(R) == 4 ? 8 : 4>(
-          32 * 32, [&](int t) { return (t >> 5) < jw && (t & 31) < jw; },
-          [&](int t) { return F[(int64_t)(j0 + (t >> 5)) * m + j0 + (t & 31)]; },
-          [&](int t, V v) { dblk[t & 31][t >> 5] = v; });
-      __syncthreads();
-      if (wid == 0) solve_lower_warp(dblk, w, j0, jw, lane);
-      __syncthreads();
-      for (int r = j0 + jw + tid; r < p; r += blockDim.x) apply_block_row(F, m, j0, jw, r, w);
-      __syncthreads();
-    }
-  } else {
-  if (wid == 0) {
-    stage_diag_warp(dblk, F, m, 0, 32, lane);
-    solve_lower_warp(dblk, w, 0, 32, lane);
+  __shared__ V dblk[32][33];  // warp 0's diagonal block, staged so its solve never waits on DRAM
+  if (wid == 0 && p > 0) {
+    stage_diag_warp(dblk, F, m, 0, min(32, p), lane);
+    solve_lower_warp(dblk, w, 0, min(32, p), lane);
   }
   __syncthreads();
   for (int j0 = 0; j0 < p; j0 += 32) {  // block [j0, j0 + jw) is solved
@@ -933,7 +915,6 @@ __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec
       for (int r = n0 + max(nw, 0) + tid - 32; r < p; r += blockDim.x - 32) apply_block_row(F, m, j0, jw, r, w);
     }
     __syncthreads();
-  }
   }
   for (int k = tid; k < m; k += blockDim.x) {
     if (k < p) zs[I[k]] = w[k];
@@ -1073,26 +1054,11 @@ __global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Ve
   __syncthreads();
   const int lane = tid & 31, wid = tid >> 5;
   // U11 solve from the last block up, with look-ahead
-  __shared__ V dblk[32][33];  // diagonal 32 x 32 block, staged so the warp solve never waits on DRAM
-  if (p < kLookAheadMinP) {  // short pivot blocks: every thread stages, warp 0 solves, every thread updates
-    for (int jend = p; jend > 0; jend -= 32) {
-      const int j0 = max(0, jend - 32);
-      const int jw = jend - j0;
-      staged_copy<sizeof(R) == 4 ? 8 : 4>(
-          32 * 32, [&](int t) { return (t >> 5) < jw && (t & 31) < jw; },
-          [&](int t) { return F[(int64_t)(j0 + (t >> 5)) * m + j0 + (t & 31)]; },
-          [&](int t, V v) { dblk[t & 31][t >> 5] = v; });
-      __syncthreads();
-      if (wid == 0) solve_upper_warp(dblk, w, j0, jw, lane);
-      __syncthreads();
-      for (int r = tid; r < j0; r += blockDim.x) apply_block_row(F, m, j0, jw, r, w);
-      __syncthreads();
-    }
-  } else {
-  if (wid == 0) {
-    const int j0 = p - 32;
-    stage_diag_warp(dblk, F, m, j0, 32, lane);
-    solve_upper_warp(dblk, w, j0, 32, lane);
+  __shared__ V dblk[32][33];  // warp 0's diagonal block, staged so its solve never waits on DRAM
+  if (wid == 0 && p > 0) {
+    const int j0 = max(0, p - 32);
+    stage_diag_warp(dblk, F, m, j0, p - j0, lane);
+    solve_upper_warp(dblk, w, j0, p - j0, lane);
   }
   __syncthreads();
   for (int jend = p; jend > 0; jend -= 32) {  // block [j0, jend) is solved
@@ -1110,7 +1076,6 @@ __global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Ve
       for (int r = tid - 32; r < n0; r += blockDim.x - 32) apply_block_row(F, m, j0, jw, r, w);
     }
     __syncthreads();
-  }
   }
   for (int k = tid; k < p; k += blockDim.x) zs[I[k]] = w[k];
 }
