@@ -780,73 +780,6 @@ __device__ __forceinline__ void gather_rows(V* dst, const V* __restrict__ src, c
   }
 }
 
-// Pivot-block triangular solves of the sweeps, with look-ahead: while warps
-// 1.. apply the solved block b to the rows below block b + 1 (forward) or
-// above it (backward), warp 0 applies it to the 32 rows of block b + 1,
-// stages that block's diagonal and solves it, so the sequential 32-step
-// chain runs beside the bulk update instead of between two of them. Each
-// row sees the same operations in the same order as without look-ahead.
-
-// warp 0: the jw x jw diagonal block at (j0, j0) of F (ld m) into dblk[row][col]
-template <class V>
-__device__ __forceinline__ void stage_diag_warp(V (*dblk)[33], const V* __restrict__ F, int m, int j0, int jw,
-                                                int lane) {
-#pragma unroll
-  for (int h = 0; h < 32; h += 8) {
-    V v[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-      v[c] = (h + c < jw && lane < jw) ? F[(int64_t)(j0 + h + c) * m + j0 + lane] : cmk<V>(0.0, 0.0);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) dblk[lane][h + c] = v[c];
-  }
-  __syncwarp();
-}
-
-// w[r] -= sum_jj F[j0 + jj, r] w[j0 + jj] (F column-major, ld m): the row's loads first
-template <class V>
-__device__ __forceinline__ void apply_block_row(const V* __restrict__ F, int m, int j0, int jw, int r, V* w) {
-  V a[32];  // all loads of the row first: one memory latency per row, not 32
-#pragma unroll
-  for (int jj = 0; jj < 32; ++jj) a[jj] = jj < jw ? F[(int64_t)(j0 + jj) * m + r] : cmk<V>(0.0, 0.0);
-  V t = w[r];
-#pragma unroll
-  for (int jj = 0; jj < 32; ++jj)
-    if (jj < jw) t = cfms(t, a[jj], w[j0 + jj]);
-  w[r] = t;
-}
-
-// warp 0: unit-lower solve of w[j0 .. j0 + jw) with the staged block
-template <class V>
-__device__ __forceinline__ void solve_lower_warp(V (*dblk)[33], V* w, int j0, int jw, int lane) {
-  V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
-  for (int jj = 0; jj < jw; ++jj) {
-    V x;
-    x.x = __shfl_sync(0xffffffffu, val.x, jj);
-    x.y = __shfl_sync(0xffffffffu, val.y, jj);
-    if (lane > jj && lane < jw) val = cfms(val, dblk[lane][jj], x);
-  }
-  if (lane < jw) w[j0 + lane] = val;
-  __syncwarp();
-}
-
-// warp 0: upper solve of w[j0 .. j0 + jw) with the staged block; every lane
-// inverts its own diagonal entry up front (no division on the sequential chain)
-template <class V>
-__device__ __forceinline__ void solve_upper_warp(V (*dblk)[33], V* w, int j0, int jw, int lane) {
-  V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
-  const V dinv = lane < jw ? cinv(dblk[lane][lane]) : cmk<V>(0.0, 0.0);
-  for (int jj = jw - 1; jj >= 0; --jj) {
-    if (lane == jj) val = cmul(val, dinv);
-    V x;
-    x.x = __shfl_sync(0xffffffffu, val.x, jj);
-    x.y = __shfl_sync(0xffffffffu, val.y, jj);
-    if (lane < jj) val = cfms(val, dblk[lane][jj], x);
-  }
-  if (lane < jw) w[j0 + lane] = val;
-  __syncwarp();
-}
-
 template <class R, bool G>
 __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec2<R>::T* __restrict__ arena,
                                                  const int32_t* __restrict__ perm, typename Vec2<R>::T* __restrict__ z,
@@ -893,26 +826,36 @@ __global__ void __launch_bounds__(512) k_forward(SolveArgs S, const typename Vec
     __syncthreads();
   }
   const int lane = tid & 31, wid = tid >> 5;
-  // L11 solve on the pivot block only (with look-ahead); the border rows
-  // (L21) are updated by k_fwd_border across many CTAs
-  __shared__ V dblk[32][33];  // warp 0's diagonal block, staged so its solve never waits on DRAM
-  if (wid == 0 && p > 0) {
-    stage_diag_warp(dblk, F, m, 0, min(32, p), lane);
-    solve_lower_warp(dblk, w, 0, min(32, p), lane);
-  }
-  __syncthreads();
-  for (int j0 = 0; j0 < p; j0 += 32) {  // block [j0, j0 + jw) is solved
+  // L11 solve on the pivot block only; the border rows (L21) are updated by
+  // k_fwd_border across many CTAs
+  __shared__ V dblk[32][33];  // diagonal 32 x 32 block, staged so the warp solve never waits on DRAM
+  for (int j0 = 0; j0 < p; j0 += 32) {
     const int jw = min(32, p - j0);
-    const int n0 = j0 + jw, nw = min(32, p - n0);  // the next block (nw <= 0: none)
+    staged_copy<sizeof(R) == 4 ? 8 : 4>(
+        32 * 32, [&](int t) { return (t >> 5) < jw && (t & 31) < jw; },
+        [&](int t) { return F[(int64_t)(j0 + (t >> 5)) * m + j0 + (t & 31)]; },
+        [&](int t, V v) { dblk[t & 31][t >> 5] = v; });
+    __syncthreads();
     if (wid == 0) {
-      if (nw > 0) {
-        if (lane < nw) apply_block_row(F, m, j0, jw, n0 + lane, w);
-        __syncwarp();
-        stage_diag_warp(dblk, F, m, n0, nw, lane);
-        solve_lower_warp(dblk, w, n0, nw, lane);
+      V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
+      for (int jj = 0; jj < jw; ++jj) {
+        V x;
+        x.x = __shfl_sync(0xffffffffu, val.x, jj);
+        x.y = __shfl_sync(0xffffffffu, val.y, jj);
+        if (lane > jj && lane < jw) val = cfms(val, dblk[lane][jj], x);
       }
-    } else {
-      for (int r = n0 + max(nw, 0) + tid - 32; r < p; r += blockDim.x - 32) apply_block_row(F, m, j0, jw, r, w);
+      if (lane < jw) w[j0 + lane] = val;
+    }
+    __syncthreads();
+    for (int r = j0 + jw + tid; r < p; r += blockDim.x) {
+      V a[32];  // all loads of the row first: one memory latency per row, not 32
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj) a[jj] = jj < jw ? F[(int64_t)(j0 + jj) * m + r] : cmk<V>(0.0, 0.0);
+      V t = w[r];
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj)
+        if (jj < jw) t = cfms(t, a[jj], w[j0 + jj]);
+      w[r] = t;
     }
     __syncthreads();
   }
@@ -1053,27 +996,38 @@ __global__ void __launch_bounds__(512) k_backward(SolveArgs S, const typename Ve
   for (int k = tid; k < p; k += blockDim.x) w[k] = tb[s * S.n + S.piv_off[f] + k];
   __syncthreads();
   const int lane = tid & 31, wid = tid >> 5;
-  // U11 solve from the last block up, with look-ahead
-  __shared__ V dblk[32][33];  // warp 0's diagonal block, staged so its solve never waits on DRAM
-  if (wid == 0 && p > 0) {
-    const int j0 = max(0, p - 32);
-    stage_diag_warp(dblk, F, m, j0, p - j0, lane);
-    solve_upper_warp(dblk, w, j0, p - j0, lane);
-  }
-  __syncthreads();
-  for (int jend = p; jend > 0; jend -= 32) {  // block [j0, jend) is solved
+  __shared__ V dblk[32][33];  // diagonal 32 x 32 block, staged so the warp solve never waits on DRAM
+  for (int jend = p; jend > 0; jend -= 32) {
     const int j0 = max(0, jend - 32);
     const int jw = jend - j0;
-    const int n0 = max(0, j0 - 32), nw = j0 - n0;  // the next block up (nw == 0: none)
+    staged_copy<sizeof(R) == 4 ? 8 : 4>(
+        32 * 32, [&](int t) { return (t >> 5) < jw && (t & 31) < jw; },
+        [&](int t) { return F[(int64_t)(j0 + (t >> 5)) * m + j0 + (t & 31)]; },
+        [&](int t, V v) { dblk[t & 31][t >> 5] = v; });
+    __syncthreads();
     if (wid == 0) {
-      if (nw > 0) {
-        if (lane < nw) apply_block_row(F, m, j0, jw, n0 + lane, w);
-        __syncwarp();
-        stage_diag_warp(dblk, F, m, n0, nw, lane);
-        solve_upper_warp(dblk, w, n0, nw, lane);
+      V val = lane < jw ? w[j0 + lane] : cmk<V>(0.0, 0.0);
+      // every lane inverts its own diagonal entry up front: no division on the sequential chain
+      const V dinv = lane < jw ? cinv(dblk[lane][lane]) : cmk<V>(0.0, 0.0);
+      for (int jj = jw - 1; jj >= 0; --jj) {
+        if (lane == jj) val = cmul(val, dinv);
+        V x;
+        x.x = __shfl_sync(0xffffffffu, val.x, jj);
+        x.y = __shfl_sync(0xffffffffu, val.y, jj);
+        if (lane < jj) val = cfms(val, dblk[lane][jj], x);
       }
-    } else {
-      for (int r = tid - 32; r < n0; r += blockDim.x - 32) apply_block_row(F, m, j0, jw, r, w);
+      if (lane < jw) w[j0 + lane] = val;
+    }
+    __syncthreads();
+    for (int r = tid; r < j0; r += blockDim.x) {
+      V a[32];  // all loads of the row first: one memory latency per row, not 32
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj) a[jj] = jj < jw ? F[(int64_t)(j0 + jj) * m + r] : cmk<V>(0.0, 0.0);
+      V t = w[r];
+#pragma unroll
+      for (int jj = 0; jj < 32; ++jj)
+        if (jj < jw) t = cfms(t, a[jj], w[j0 + jj]);
+      w[r] = t;
     }
     __syncthreads();
   }
