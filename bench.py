@@ -675,10 +675,13 @@ def run_reference(args):
     meshes_mod = importlib.import_module("elpaso_core_gb300.meshes")
     b, _ = cpu_baseline(meshes_mod, args, n_freq=max(6, args.steps))
     d = workload(meshes_mod, args)
-    line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    # n_gpus: the N this arm was launched with; the work runs on rank 0's host cores only
+    line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * args.batch / b["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
             "dtype": "c128", "impl": "reference", "data": "synthetic",
-            "config": {"workload": workload_label(d),
+            "config": {"workload": workload_label(d), "frequencies_per_step": args.batch, "host_cores_only": True,
                        "note": "the reference (PETSc/MUMPS) cannot be built here; its CPU path is timed "
                                "as the oracle restatement (element loop + multifrontal LU)"},
             "cpu_baseline": b,
