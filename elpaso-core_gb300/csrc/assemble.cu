@@ -726,13 +726,17 @@ int device_upload_model(Model& m) {
   }
   ELP_CUDA(D.bc_rows.upload(m.bc_rows));
   // element lists per type
-  std::vector<int32_t> bc, pc, fc;
+  std::vector<int32_t> bc, pc, fc, be, pe, fe;  // connectivity, descriptor positions
   std::vector<int16_t> bm, pm, fm;
+  int64_t eid = 0;
   for (auto& blk : m.blocks) {
     std::vector<int32_t>* c = blk.type == ELP_BRICK8 ? &bc : blk.type == ELP_DSG4 ? &pc : &fc;
     std::vector<int16_t>* mm = blk.type == ELP_BRICK8 ? &bm : blk.type == ELP_DSG4 ? &pm : &fm;
+    std::vector<int32_t>* ee = blk.type == ELP_BRICK8 ? &be : blk.type == ELP_DSG4 ? &pe : &fe;
     c->insert(c->end(), blk.conn.begin(), blk.conn.end());
     mm->insert(mm->end(), blk.n_elements, (int16_t)blk.material);
+    for (int64_t e = 0; e < blk.n_elements; ++e) ee->push_back((int32_t)(eid + e));
+    eid += blk.n_elements;
   }
   if (m.materials.size() > 32767) { set_error("too many materials"); return ELP_ERR_ARG; }
   // Each element kind is launched in order of its lowest node (a stable
@@ -740,7 +744,8 @@ int device_upload_model(Model& m) {
   // rows that stays in L2 until its last element. Block by block order
   // sweeps the whole matrix once per material block (four times over on a
   // cube with four randomly assigned materials).
-  auto locality_sort = [&](std::vector<int32_t>& conn, std::vector<int16_t>& mat, int per) {
+  auto locality_sort = [&](std::vector<int32_t>& conn, std::vector<int16_t>& mat, std::vector<int32_t>& pos,
+                           int per) {
     const size_t ne = mat.size();
     if (ne < 2) return;
     std::vector<int64_t> start((size_t)m.n_nodes + 1, 0);
@@ -752,19 +757,26 @@ int device_upload_model(Model& m) {
       ++start[(size_t)k + 1];
     }
     for (int64_t v = 0; v < m.n_nodes; ++v) start[v + 1] += start[v];
-    std::vector<int32_t> c2(conn.size());
+    std::vector<int32_t> c2(conn.size()), p2(ne);
     std::vector<int16_t> m2(ne);
     for (size_t e = 0; e < ne; ++e) {
       const int64_t d = start[key[e]]++;
       std::copy(conn.begin() + e * per, conn.begin() + (e + 1) * per, c2.begin() + d * per);
       m2[d] = mat[e];
+      p2[d] = pos[e];
     }
     conn.swap(c2);
     mat.swap(m2);
+    pos.swap(p2);
   };
-  locality_sort(bc, bm, 8);
-  locality_sort(pc, pm, 4);
-  locality_sort(fc, fm, 8);
+  locality_sort(bc, bm, be, 8);
+  locality_sort(pc, pm, pe, 4);
+  locality_sort(fc, fm, fe, 8);
+  D.h_brick_eid = be;
+  D.h_plate_eid = pe;
+  D.h_brick_conn = bc;
+  D.h_fluid_conn = fc;
+  D.stress_ready = false;
   D.n_brick = (int64_t)bm.size();
   D.n_plate = (int64_t)pm.size();
   D.n_fluid = (int64_t)fm.size();
@@ -790,6 +802,8 @@ int device_upload_model(Model& m) {
     ElemMaterial& e = em[i];
     memset(&e, 0, sizeof(e));
     e.rho = mt.rho;
+    e.Es = mt.E;
+    e.nus = mt.nu;
     e.group = m.material_group[i] < 0 ? 0 : m.material_group[i];
     if (mt.kind == ELP_AF_LIN_UAF_ISO_DIR) {
       e.inv_c2 = 1.0 / (mt.c * mt.c);

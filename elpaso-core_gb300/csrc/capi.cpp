@@ -249,7 +249,9 @@ int elp_cell_stresses(const elp_model* h, double omega, const double* x, double*
   if (!h || !x || !sigma) { set_error("null argument"); return ELP_ERR_ARG; }
   if (!(omega > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
   std::string err;
-  const int rc = cell_stresses(h->m, omega, reinterpret_cast<const cplx*>(x), reinterpret_cast<cplx*>(sigma),
+  // the model is logically unchanged; its device copy is made on first use
+  Model& m = const_cast<Model&>(h->m);
+  const int rc = cell_stresses(m, omega, reinterpret_cast<const cplx*>(x), reinterpret_cast<cplx*>(sigma),
                                reinterpret_cast<cplx*>(sigma_lower), err);
   if (rc) set_error(err);
   return rc;
@@ -261,7 +263,8 @@ int elp_node_stresses(const elp_model* h, double omega, const double* x, double*
   if (!h || !x || !sigma_nodes) { set_error("null argument"); return ELP_ERR_ARG; }
   if (!(omega > 0.0)) { set_error("angular frequency must be > 0"); return ELP_ERR_ARG; }
   std::string err;
-  const int rc = node_stresses(h->m, omega, reinterpret_cast<const cplx*>(x), reinterpret_cast<cplx*>(sigma_nodes), err);
+  Model& m = const_cast<Model&>(h->m);
+  const int rc = node_stresses(m, omega, reinterpret_cast<const cplx*>(x), reinterpret_cast<cplx*>(sigma_nodes), err);
   if (rc) set_error(err);
   return rc;
   GUARD_END

@@ -34,6 +34,7 @@ struct ElemMaterial {
   double Db, nu;       // DSG4: E t^3 / (12 (1 - nu^2)), nu
   double Gt, t;        // DSG4: E / (2 (1 + nu)) * t * 5/6 (setupCs), thickness
   double inv_c2;       // Fluid8: 1 / c^2
+  double Es, nus;      // structure: E and nu (the stresses' C(w) and Cm(w))
   int group;           // structure loss-factor group
   int pad;
 };
@@ -95,6 +96,16 @@ struct DeviceModel {
   int64_t bad_jacobians_3d = 0;    // flags[0] of the last assembly
   int64_t n_brick = 0, n_plate = 0, n_fluid = 0, n_iface = 0;
   double assembly_ms = 0.0;
+  // the element lists are in locality order (lowest node first): per element
+  // its position in descriptor order (blocks, then elements), and the host
+  // copies of the Brick8 / Fluid8 connectivity the node lists are built from
+  std::vector<int32_t> h_brick_eid, h_plate_eid, h_brick_conn, h_fluid_conn;
+  // stresses (stress.cu), built on first use: descriptor positions, per node
+  // its (element, kind * 8 + corner) entries, element count and output row
+  bool stress_ready = false;
+  DevBuf<int32_t> brick_eid, plate_eid, node_adj_el, node_count, node_seq;
+  DevBuf<int64_t> node_adj_ptr;
+  DevBuf<int8_t> node_adj_kc;
 };
 
 // assemble.cu

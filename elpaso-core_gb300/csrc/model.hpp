@@ -148,11 +148,11 @@ int build_model(const elp_model_desc* d, Model& m, std::string& err);
 // coefficient of group g at angular frequency w
 cplx group_coefficient(const StructGroup& g, double w);
 
-// cell stresses of the solution x at w (stress.cpp): 9 complex per element,
+// cell stresses of the solution x at w (stress.cu, on the device): 9 complex per element,
 // elements in descriptor order; out2 (may be null) the lower plate surface
-int cell_stresses(const Model& m, double w, const cplx* x, cplx* out, cplx* out2, std::string& err);
-// nodal stresses (stress.cpp): 9 complex per node, nodes in ascending id
-int node_stresses(const Model& m, double w, const cplx* x, cplx* out, std::string& err);
+int cell_stresses(Model& m, double w, const cplx* x, cplx* out, cplx* out2, std::string& err);
+// nodal stresses (stress.cu, on the device): 9 complex per node, nodes in ascending id
+int node_stresses(Model& m, double w, const cplx* x, cplx* out, std::string& err);
 
 // thread-local error text
 void set_error(const std::string& s);

@@ -5,8 +5,9 @@ FullRun would through a shim) and prints what the host-side calls return.
 Its output must equal the Python binding's bit for bit on the same model
 (the ctypes mirror and the header agree) and the oracle's restatement
 (numbering, pattern bit-exact; F and stresses to 1e-14 / 1e-13). The header
-also compiles as C++ (the reference is C++). No GPU: elp_model_analyse runs
-the symbolic phase and then reports the missing device."""
+also compiles as C++ (the reference is C++). It runs with or without a GPU:
+elp_model_analyse runs the symbolic phase and then reports a missing device;
+the stresses are computed on the device and compared when one is present."""
 import copy
 import os
 import shutil
@@ -103,10 +104,11 @@ def test_c_host_matches_python_binding(elp, c_host_output):
     om = 2 * np.pi * 120.0
     np.testing.assert_array_equal(_cplx(o["f_omega"]), m.rhs(om))
     x = _cplx(o["x"])
-    up, lo = m.cell_stresses(om, x)
-    np.testing.assert_array_equal(_cplx(o["sigma"]).reshape(up.shape), up)
-    np.testing.assert_array_equal(_cplx(o["sigma_lower"]).reshape(lo.shape), lo)
-    np.testing.assert_array_equal(_cplx(o["sigma_nodes"]).reshape(n_nodes, 9), m.node_stresses(om, x))
+    if "sigma" in o:  # the stresses run on the device (printed only when one answered)
+        up, lo = m.cell_stresses(om, x)
+        np.testing.assert_array_equal(_cplx(o["sigma"]).reshape(up.shape), up)
+        np.testing.assert_array_equal(_cplx(o["sigma_lower"]).reshape(lo.shape), lo)
+        np.testing.assert_array_equal(_cplx(o["sigma_nodes"]).reshape(n_nodes, 9), m.node_stresses(om, x))
     rc, fronts, levels, max_front = (int(v) for v in o["analyse"])
     assert rc in (0, 2) and fronts >= 1 and levels >= 1 and 0 < max_front <= n
 
@@ -124,6 +126,8 @@ def test_c_host_matches_oracle(elp, oracle, c_host_output):
     assert np.abs(f - oracle.System(d0).f).max() > 0.1  # the tractions are in
     om = 2 * np.pi * 120.0
     x = _cplx(o["x"])
+    if "sigma" not in o:  # no device: the stresses were not computed
+        return
     ou, ol = oracle.cell_stresses(s, om, x)
     scale = np.abs(ou).max()
     np.testing.assert_allclose(_cplx(o["sigma"]).reshape(ou.shape), ou, rtol=0, atol=1e-13 * scale)

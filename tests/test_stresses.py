@@ -2,13 +2,15 @@
 computeStressesNodes, analysis.cpp:869-935; Brick8
 elementstructurebrick.cpp:48-270, Mindlin/DSG4 elementstructuremindlin.cpp:51-175,
 Fluid8 grad p elementfluid3d.cpp:380-557), computed by the library
-(`elp_cell_stresses`, `elp_node_stresses`) against the oracle's restatement
-and against closed forms. The stresses are linear in the solution, so arbitrary vectors stand
-in for solutions (no GPU needed)."""
+(`elp_cell_stresses`, `elp_node_stresses`, CUDA kernels) against the
+oracle's restatement and against closed forms. The stresses are linear in
+the solution, so arbitrary vectors stand in for solutions."""
 import copy
 
 import numpy as np
 import pytest
+
+pytestmark = pytest.mark.gpu
 
 
 def test_brick_uniform_strain_closed_form(elp, meshes):
@@ -108,3 +110,14 @@ def test_node_pressure_gradient_closed_form(elp, meshes):
     expect[seq] = nfl[:, None] * (1 + 2j) * g[None, :]
     np.testing.assert_allclose(out[:, 6:], expect, rtol=0, atol=1e-11 * np.abs(expect).max())
 
+
+
+def test_node_stresses_are_deterministic(elp, meshes):
+    """One thread per node sums its elements in a fixed order (no atomics):
+    the same input gives the same bits."""
+    d = meshes.plate_cavity(6, 4, 3, 0.6, 0.4, 0.3)
+    m = elp.Model(d)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(m.n) + 1j * rng.standard_normal(m.n)
+    a, b = m.node_stresses(2 * np.pi * 40.0, x), m.node_stresses(2 * np.pi * 40.0, x)
+    np.testing.assert_array_equal(a, b)
