@@ -142,3 +142,23 @@ def test_python_binding_is_the_same_descriptor(elp):
     d = c_host_desc(elp)
     m1, m2 = elp.Model(d), elp.Model(copy.deepcopy(d))
     np.testing.assert_array_equal(m1.rhs(), m2.rhs())
+
+
+@pytest.mark.gpu
+def test_c_host_stresses_on_the_device(elp, oracle, c_host_output):
+    """With a device the C host computes the stresses too: the same bits as
+    the Python binding (both run the same kernels, which sum in a fixed
+    order), and the oracle's values to 1e-13."""
+    o = c_host_output
+    assert "sigma" in o and "sigma_nodes" in o
+    m = elp.Model(c_host_desc(elp))
+    n_nodes = int(o["sizes"][2])
+    om = 2 * np.pi * 120.0
+    x = _cplx(o["x"])
+    up, lo = m.cell_stresses(om, x)
+    np.testing.assert_array_equal(_cplx(o["sigma"]).reshape(up.shape), up)
+    np.testing.assert_array_equal(_cplx(o["sigma_lower"]).reshape(lo.shape), lo)
+    np.testing.assert_array_equal(_cplx(o["sigma_nodes"]).reshape(n_nodes, 9), m.node_stresses(om, x))
+    s = oracle.System(c_host_desc(elp))
+    ou, _ = oracle.cell_stresses(s, om, x)
+    np.testing.assert_allclose(up, ou, rtol=0, atol=1e-13 * np.abs(ou).max())
