@@ -429,40 +429,36 @@ __device__ void plate_item(const AsmArgs& A, int64_t item, PlateShared& ps) {
         ps.dx[el][n][k] = (c * c_quad[1][k][n] - b * c_quad[2][k][n]) / det;
         ps.dy[el][n][k] = (-d * c_quad[1][k][n] + a * c_quad[2][k][n]) / det;
       }
-      // DSG shear strains of the edge-based interpolation (elementstructuremindlindsg4.cpp)
+      // DSG shear strains of the edge-based interpolation (elementstructuremindlindsg4.cpp),
+      // each row entry / det J stored as it is formed
       const double Nx1 = c_quad[1][1][n], Nx2 = c_quad[1][2][n];
       const double Ne2 = c_quad[2][2][n], Ne3 = c_quad[2][3][n];
-      double Bs[2][12];
-      Bs[0][0] = -c * Nx1 + b * Ne3;
-      Bs[0][1] = -b * c * Nx1 + b * c * Ne3;
-      Bs[0][2] = a * c * Nx1 - b * d * Ne3;
-      Bs[1][0] = d * Nx1 - a * Ne3;
-      Bs[1][1] = -a * c * Ne3 + b * d * Nx1;
-      Bs[1][2] = a * d * Ne3 - a * d * Nx1;
-      Bs[0][3] = c * Nx1 + b * Ne2;
-      Bs[0][4] = -b * c * Nx1 + b * c * Ne2;
-      Bs[0][5] = a * c * Nx1 - b * d * Ne2;
-      Bs[1][3] = -a * Ne2 - d * Nx1;
-      Bs[1][4] = -a * c * Ne2 + b * d * Nx1;
-      Bs[1][5] = a * d * Ne2 - a * d * Nx1;
-      Bs[0][6] = c * Nx2 - b * Ne2;
-      Bs[0][7] = -b * c * Nx2 + b * c * Ne2;
-      Bs[0][8] = a * c * Nx2 - b * d * Ne2;
-      Bs[1][6] = a * Ne2 - d * Nx2;
-      Bs[1][7] = -a * c * Ne2 + b * d * Nx2;
-      Bs[1][8] = a * d * Ne2 - a * d * Nx2;
-      Bs[0][9] = -c * Nx2 - b * Ne3;
-      Bs[0][10] = -b * c * Nx2 + b * c * Ne3;
-      Bs[0][11] = a * c * Nx2 - b * d * Ne3;
-      Bs[1][9] = a * Ne3 + d * Nx2;
-      Bs[1][10] = -a * c * Ne3 + b * d * Nx2;
-      Bs[1][11] = a * d * Ne3 - a * d * Nx2;
       const double idet = 1. / det;
-#pragma unroll
-      for (int i = 0; i < 12; ++i) {
-        ps.bs[el][n][0][i] = Bs[0][i] * idet;
-        ps.bs[el][n][1][i] = Bs[1][i] * idet;
-      }
+      double (*bs)[12] = ps.bs[el][n];
+      bs[0][0] = (-c * Nx1 + b * Ne3) * idet;
+      bs[0][1] = (-b * c * Nx1 + b * c * Ne3) * idet;
+      bs[0][2] = (a * c * Nx1 - b * d * Ne3) * idet;
+      bs[1][0] = (d * Nx1 - a * Ne3) * idet;
+      bs[1][1] = (-a * c * Ne3 + b * d * Nx1) * idet;
+      bs[1][2] = (a * d * Ne3 - a * d * Nx1) * idet;
+      bs[0][3] = (c * Nx1 + b * Ne2) * idet;
+      bs[0][4] = (-b * c * Nx1 + b * c * Ne2) * idet;
+      bs[0][5] = (a * c * Nx1 - b * d * Ne2) * idet;
+      bs[1][3] = (-a * Ne2 - d * Nx1) * idet;
+      bs[1][4] = (-a * c * Ne2 + b * d * Nx1) * idet;
+      bs[1][5] = (a * d * Ne2 - a * d * Nx1) * idet;
+      bs[0][6] = (c * Nx2 - b * Ne2) * idet;
+      bs[0][7] = (-b * c * Nx2 + b * c * Ne2) * idet;
+      bs[0][8] = (a * c * Nx2 - b * d * Ne2) * idet;
+      bs[1][6] = (a * Ne2 - d * Nx2) * idet;
+      bs[1][7] = (-a * c * Ne2 + b * d * Nx2) * idet;
+      bs[1][8] = (a * d * Ne2 - a * d * Nx2) * idet;
+      bs[0][9] = (-c * Nx2 - b * Ne3) * idet;
+      bs[0][10] = (-b * c * Nx2 + b * c * Ne3) * idet;
+      bs[0][11] = (a * c * Nx2 - b * d * Ne3) * idet;
+      bs[1][9] = (a * Ne3 + d * Nx2) * idet;
+      bs[1][10] = (-a * c * Ne3 + b * d * Nx2) * idet;
+      bs[1][11] = (a * d * Ne3 - a * d * Nx2) * idet;
       ps.wd[el][n] = 1.0 * det;
       if (n == 0) {
         const ElemMaterial& mt = A.mats[A.plate_mat[e]];
@@ -637,30 +633,39 @@ __device__ void interface_quad(const AsmArgs& A, int64_t q) {
 // ---------------------------------------------------------------- kernel
 // Brick8 / Fluid8 items (8 elements per CTA); register-light, so three CTAs
 // share an SM.
-template <bool kDF>
-__global__ void __launch_bounds__(kThreads, 3) assemble_hex_kernel(AsmArgs A) {
-  __shared__ double sg[kHexPerItem][8][8][3];
-  __shared__ double swg[kHexPerItem][8][8][3];
-  __shared__ double sw[kHexPerItem][8];
-  __shared__ int srow[kHexPerItem][8];
-  __shared__ int smat[kHexPerItem];
-  const int64_t total = A.items_brick + A.items_fluid;
-  for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
-    if (it < A.items_brick) hex_item<0, kDF>(A, it, sg, swg, sw, srow, smat);
-    else hex_item<1, kDF>(A, it - A.items_brick, sg, swg, sw, srow, smat);
-  }
-}
+// The element integration of every element type in ONE persistent launch:
+// items are Brick8 groups, Fluid8 groups (8 elements each, hex_item), DSG4
+// groups (28 plates each, plate_item) and interface quads (one per thread),
+// in that order; a CTA takes items blockIdx.x, blockIdx.x + gridDim.x, ...,
+// so its items of one kind come before those of the next and the shared
+// memory of the hex and plate items (a union) is never live in both at once
+// (each item ends with a barrier).
+struct HexShared {
+  double sg[kHexPerItem][8][8][3];
+  double swg[kHexPerItem][8][8][3];
+  double sw[kHexPerItem][8];
+  int srow[kHexPerItem][8];
+  int smat[kHexPerItem];
+};
+union AsmShared {
+  HexShared hex;
+  PlateShared plate;
+};
 
-// DSG4 plates (28 per item, a thread per node pair) and interface quads (one
-// per thread).
-__global__ void __launch_bounds__(kThreads) assemble_quad_kernel(AsmArgs A) {
-  __shared__ PlateShared ps;
-  const int64_t total = A.items_plate + A.items_iface;
+template <bool kDF>
+__global__ void __launch_bounds__(kThreads, 3) assemble_kernel(AsmArgs A) {
+  __shared__ AsmShared sh;
+  const int64_t i_fluid = A.items_brick, i_plate = i_fluid + A.items_fluid, i_iface = i_plate + A.items_plate;
+  const int64_t total = i_iface + A.items_iface;
   for (int64_t it = blockIdx.x; it < total; it += gridDim.x) {
-    if (it < A.items_plate) {
-      plate_item(A, it, ps);
+    if (it < i_fluid) {
+      hex_item<0, kDF>(A, it, sh.hex.sg, sh.hex.swg, sh.hex.sw, sh.hex.srow, sh.hex.smat);
+    } else if (it < i_plate) {
+      hex_item<1, kDF>(A, it - i_fluid, sh.hex.sg, sh.hex.swg, sh.hex.sw, sh.hex.srow, sh.hex.smat);
+    } else if (it < i_iface) {
+      plate_item(A, it - i_plate, sh.plate);
     } else {
-      int64_t q = (it - A.items_plate) * kThreads + threadIdx.x;
+      const int64_t q = (it - i_iface) * kThreads + threadIdx.x;
       if (q < A.n_iface) interface_quad(A, q);
     }
   }
@@ -897,21 +902,19 @@ int device_assemble(Model& m, cudaStream_t stream, float* kernel_ms) {
   A.items_plate = (D.n_plate + kPlatesPerItem - 1) / kPlatesPerItem;
   A.items_iface = (D.n_iface + kThreads - 1) / kThreads;
   A.flags = D.flags.p;
-  int sms = 0, per_hex = 0, per_quad = 0;
+  int sms = 0, per_sm = 0;
   ELP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D.device));
   const bool df = m.assembly == ELP_ASSEMBLY_DOUBLE_FLOAT;
-  auto hex_kernel = df ? assemble_hex_kernel<true> : assemble_hex_kernel<false>;
-  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_hex, hex_kernel, kThreads, 0));
-  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_quad, assemble_quad_kernel, kThreads, 0));
-  // persistent grids: one resident wave over the items of each kernel
-  const int64_t g_hex = std::min<int64_t>((int64_t)sms * std::max(1, per_hex), A.items_brick + A.items_fluid);
-  const int64_t g_quad = std::min<int64_t>((int64_t)sms * std::max(1, per_quad), A.items_plate + A.items_iface);
+  auto kernel = df ? assemble_kernel<true> : assemble_kernel<false>;
+  ELP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0));
+  // one persistent launch: one resident wave over the items of every element type
+  const int64_t items = A.items_brick + A.items_fluid + A.items_plate + A.items_iface;
+  const int64_t grid = std::min<int64_t>((int64_t)sms * std::max(1, per_sm), items);
   cudaEvent_t e0, e1;
   ELP_CUDA(cudaEventCreate(&e0));
   ELP_CUDA(cudaEventCreate(&e1));
   ELP_CUDA(cudaEventRecord(e0, stream));
-  if (g_hex > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, hex_kernel<<<(unsigned)g_hex, kThreads, 0, stream>>>(A));
-  if (g_quad > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, assemble_quad_kernel<<<(unsigned)g_quad, kThreads, 0, stream>>>(A));
+  if (grid > 0) PROF_LAUNCH(KC_ASSEMBLE, stream, kernel<<<(unsigned)grid, kThreads, 0, stream>>>(A));
   ELP_CUDA(cudaGetLastError());
   ELP_CUDA(cudaEventRecord(e1, stream));
   ELP_CUDA(cudaEventSynchronize(e1));
