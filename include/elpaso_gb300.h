@@ -289,9 +289,10 @@ int elp_model_rhs_omega(const elp_model* m, double omega, double* f_out);
 int elp_solve(elp_model* m, const double* omegas, int n_omega, int precision,
               const double* f_or_null, double* x_out, elp_solve_info* info, double tol);
 
-/* Cell stresses of a solution x (n complex interleaved, e.g. one frequency of
- * elp_solve's output) at angular frequency omega, as the reference computes
- * them after a solve (cAnalysis::computeStressesCells, analysis.cpp:869-905):
+/* Cell stresses of a solution x (n complex interleaved host buffer, e.g. one
+ * frequency of elp_solve's output) at angular frequency omega, computed on the
+ * device (ELP_ERR_CUDA without one) as the reference computes them after a
+ * solve (cAnalysis::computeStressesCells, analysis.cpp:869-905):
  * 9 complex slots per element, elements in descriptor order (blocks, then
  * elements; the reference orders them by ascending element id, Id0n).
  * Brick8: sigma at the element centre, slots 0..5
@@ -301,7 +302,8 @@ int elp_solve(elp_model* m, const double* omegas, int n_omega, int precision,
  * sigma_lower may be NULL. */
 int elp_cell_stresses(const elp_model* m, double omega, const double* x, double* sigma, double* sigma_lower);
 
-/* Nodal stresses of a solution x at omega (cAnalysis::computeStressesNodes,
+/* Nodal stresses of a solution x at omega, on the device, one thread per
+ * node summing its elements in a fixed order (cAnalysis::computeStressesNodes,
  * analysis.cpp:907-935): 9 complex slots per node, nodes in ascending id
  * (GlobalSeqId). Brick8 adds its centre stress divided by the number of
  * elements at the node to slots 0..5 (elementstructurebrick.cpp:161-270);
