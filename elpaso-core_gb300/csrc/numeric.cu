@@ -1052,8 +1052,10 @@ __global__ void k_residual(CombineArgs A, const Coef* __restrict__ coef, const i
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t base = warp * RPW; base < n; base += nwarps * RPW) {
     const int64_t i = base + lane / kRowLanes;
+    // a group's finished pairs (A.pact) keep their residual rows: their x did not change
+    const bool on = i < n && row_on(A, s, i);
     DD sx{0.0, 0.0}, sy{0.0, 0.0};
-    if (i < n && !x_zero) {
+    if (on && !x_zero) {
       const Coef& c = row_coef(A, coef, s, i);
       for (int q = row_ptr[i] + sub; q < row_ptr[i + 1]; q += kRowLanes) {
         double2 a = combine(A, c, q);
@@ -1068,7 +1070,7 @@ __global__ void k_residual(CombineArgs A, const Coef* __restrict__ coef, const i
       sx = row_sum(sx);
       sy = row_sum(sy);
     }
-    if (i < n && sub == 0) {
+    if (on && sub == 0) {
       double2 fi = f[s * n + i];
       double2 ri = x_zero ? fi : make_double2(dd_residual(fi.x, sx), dd_residual(fi.y, sy));
       r[s * n + i] = ri;
@@ -2481,8 +2483,12 @@ static int run_gmres_group(Model& m, Workspace& w, int S_used, double tol, int m
   const int64_t* off = G.member_off.p;
   const int32_t* rmod = G.row_model.p;
   std::vector<double> fn(P), rel(P);
-  auto residual = [&](int x_zero) -> int {
-    PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(A, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p,
+  // masked: only the rows of the pairs in w.pact (those whose x changed this
+  // cycle) are recomputed; the others keep their residual rows
+  auto residual = [&](int x_zero, bool masked) -> int {
+    CombineArgs Ar = A;
+    if (masked) Ar.pact = w.pact.p;
+    PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<gr, 256, 0, st>>>(Ar, w.coef.p, G.row_ptr.p, G.col_idx.p, n, w.x.p, w.f.p,
                                                                    w.r.p, w.partial.p, w.nparts, w.active.p, x_zero));
     PROF_LAUNCH(KC_NORMS, st, k_member_norms<<<gp, 256, 0, st>>>(off, nm, n, w.r.p, w.f.p, w.mnorms.p));
     ELP_CUDA(cudaMemcpyAsync(w.h_mnorms, w.mnorms.p, sizeof(double) * 2 * P, cudaMemcpyDeviceToHost, st));
@@ -2510,7 +2516,7 @@ static int run_gmres_group(Model& m, Workspace& w, int S_used, double tol, int m
   };
   // a tensor-core wait that ran out left the factors incomplete (read with the first residual)
   ELP_CUDA(cudaMemcpyAsync(w.h_flag, w.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-  rc = residual(1);
+  rc = residual(1, false);
   if (rc) return rc;
   if (*w.h_flag) {
     set_error("a tensor-core Schur update gave up waiting for its MMAs");
@@ -2638,7 +2644,7 @@ static int run_gmres_group(Model& m, Workspace& w, int S_used, double tol, int m
     ELP_CUDA(cudaMemcpyAsync(w.pact.p, w.h_pact, sizeof(int) * P, cudaMemcpyHostToDevice, st));
     PROF_LAUNCH(KC_UPDATE, st, k_combo_seg<<<gv, 256, 0, st>>>(w.Zb.p, zst, n, nvmax, w.py.p, w.x.p, n, rmod, nm,
                                                                 w.pact.p));
-    rc = residual(0);
+    rc = residual(0, true);  // w.pact: the pairs that ran this cycle
     if (rc) return rc;
   }
   ELP_CUDA(cudaGetLastError());
