@@ -2717,9 +2717,13 @@ static int solve_lane(Model& m, int precision, int lane, const double* omegas, i
     for (int s = 0; s < n_omega; ++s) w.h_active[s] = 1;
     ELP_CUDA(cudaMemcpyAsync(w.active.p, w.h_active, sizeof(int) * n_omega, cudaMemcpyHostToDevice, st));
     const CombineArgs Ag = combine_args(m);
-    PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<dim3((unsigned)w.nparts, n_omega), 256, 0, st>>>(
-                                     Ag, w.coef.p, m.dev->row_ptr.p, m.dev->col_idx.p, n, w.x.p, w.f.p, w.r.p,
-                                     w.partial.p, w.nparts, w.active.p, 0));
+    // the mixed path's residual rows are already every pair's true residual (a
+    // pair's rows were last computed after its x last changed); the plain
+    // path's refinement zeroed the rows of the members it froze
+    if (precision != ELP_MIXED)
+      PROF_LAUNCH(KC_RESIDUAL, st, k_residual<<<dim3((unsigned)w.nparts, n_omega), 256, 0, st>>>(
+                                       Ag, w.coef.p, m.dev->row_ptr.p, m.dev->col_idx.p, n, w.x.p, w.f.p, w.r.p,
+                                       w.partial.p, w.nparts, w.active.p, 0));
     PROF_LAUNCH(KC_NORMS, st, k_member_norms<<<dim3(nm, n_omega), 256, 0, st>>>(m.dev->member_off.p, nm, n, w.r.p,
                                                                                   w.f.p, w.mnorms.p));
     const dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 1024), n_omega);
